@@ -1,0 +1,1240 @@
+/*
+ * pdg_oracle.c -- CPU restatement of PDELab's ConvectionDiffusionDG
+ * matrix-free path.  TEST INFRASTRUCTURE ONLY (see pdg_oracle.h).
+ *
+ * Each routine cites the reference file:line it restates.  Paths are
+ * relative to the dune-pdelab source tree (dune/pdelab/...).
+ *
+ * Third-party arithmetic that is not part of dune-pdelab and is restated
+ * here from its published algorithm:
+ *   - dune-geometry (>= 2.10) QuadratureRules, Gauss-Legendre: nodes are
+ *     the roots of P_m found by Newton iteration, weights 2/((1-x^2)P'_m^2)
+ *     (Abramowitz & Stegun 25.4.29), mapped to [0,1].  Order 2k selects
+ *     m = k+1 points per direction.
+ *   - dune-istl (>= 2.10) CGSolver / BiCGSTABSolver: preconditioned CG
+ *     (Hestenes & Stiefel 1952) and BiCGStab (van der Vorst 1992) in the
+ *     form dune-istl uses (defect-based, reduction relative to the
+ *     initial defect two-norm, half-step iteration count for BiCGStab).
+ *   - Eigen PartialPivLU: LU with row partial pivoting (max |a_ij| in
+ *     the column).
+ *   - dune-grid YaspGrid: axis-parallel cells, lexicographic leaf index
+ *     with x fastest, intersections ordered -x,+x,-y,+y,-z,+z.
+ */
+#include "pdg_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define MAXD 3
+#define MAXK 6
+#define MAXN1 (MAXK + 1)
+#define MAXNB (MAXN1 * MAXN1 * MAXN1)
+
+/* ------------------------------------------------------------------ */
+/* 1D building blocks                                                  */
+/* ------------------------------------------------------------------ */
+
+/* QkStuff::p  (finiteelement/qkdglagrange.hh:55-62) */
+double pdgo_lagrange(int k, int i, double x) {
+  double result = 1.0;
+  for (int j = 0; j <= k; j++)
+    if (j != i) result *= (k * x - j) / (i - j);
+  return result;
+}
+
+/* QkStuff::dp  (finiteelement/qkdglagrange.hh:65-79) */
+double pdgo_dlagrange(int k, int i, double x) {
+  double result = 0.0;
+  for (int j = 0; j <= k; j++)
+    if (j != i) {
+      double prod = (k * 1.0) / (i - j);
+      for (int l = 0; l <= k; l++)
+        if (l != i && l != j) prod *= (k * x - l) / (i - l);
+      result += prod;
+    }
+  return result;
+}
+
+/* Gauss-Legendre rule with m points on [0,1] (dune-geometry's default
+   QuadratureType::GaussLegendre, selected by quadratureRule() at
+   common/quadraturerules.hh:110-120).  Newton on P_m in long double. */
+int pdgo_gauss_legendre(int m, double *x, double *w) {
+  if (m < 1 || m > 32) return PDGO_EARG;
+  for (int i = 0; i < m; i++) {
+    long double z = cosl(3.14159265358979323846264338327950288L * (i + 0.75L) / (m + 0.5L));
+    long double dp = 0;
+    for (int it = 0; it < 100; it++) {
+      long double p0 = 1.0L, p1 = 0.0L;
+      for (int j = 1; j <= m; j++) {
+        long double p2 = p1;
+        p1 = p0;
+        p0 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * p2) / j;
+      }
+      dp = m * (z * p0 - p1) / (z * z - 1.0L);
+      long double dz = p0 / dp;
+      z -= dz;
+      if (fabsl(dz) < 1e-19L) break;
+    }
+    /* recompute derivative at the converged root */
+    {
+      long double p0 = 1.0L, p1 = 0.0L;
+      for (int j = 1; j <= m; j++) {
+        long double p2 = p1;
+        p1 = p0;
+        p0 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * p2) / j;
+      }
+      dp = m * (z * p0 - p1) / (z * z - 1.0L);
+    }
+    /* roots z descend with i, so (1 - z)/2 ascends on [0,1] */
+    x[i] = (double)((1.0L - z) * 0.5L);
+    w[i] = (double)(1.0L / ((1.0L - z * z) * dp * dp));
+  }
+  return PDGO_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* geometry and tables                                                 */
+/* ------------------------------------------------------------------ */
+
+typedef struct tables {
+  int d, k, n1, nb, nq, nqv, nqf;
+  double gx[MAXN1], gw[MAXN1];
+  /* volume points: phi [nqv][nb], js [nqv][nb][d], weight [nqv], local [nqv][d] */
+  double *vphi, *vjs, *vw, *vloc;
+  /* face points for face f = 2*dir+hi: phi [2d][nqf][nb], js, weight, local,
+     face-local coordinates mapped into the cell */
+  double *fphi, *fjs, *fw, *floc;
+  double theta;
+} tables;
+
+static int get_theta(int method, double *theta) {
+  /* convectiondiffusiondg.hh:99-101 */
+  if (method == PDGO_NIPG) *theta = 1.0;
+  else if (method == PDGO_SIPG) *theta = -1.0;
+  else if (method == PDGO_IIPG) *theta = 0.0;
+  else return PDGO_EARG;
+  return PDGO_OK;
+}
+
+/* QkLocalBasis::evaluateFunction / evaluateJacobian
+   (qkdglagrange.hh:153-198) with multiindex (qkdglagrange.hh:118-128) */
+static void eval_basis(int d, int k, const double *xi, double *phi, double *js) {
+  int n1 = k + 1, nb = 1;
+  for (int j = 0; j < d; j++) nb *= n1;
+  for (int i = 0; i < nb; i++) {
+    int alpha[MAXD], t = i;
+    for (int j = 0; j < d; j++) { alpha[j] = t % n1; t /= n1; }
+    double v = 1.0;
+    for (int j = 0; j < d; j++) v *= pdgo_lagrange(k, alpha[j], xi[j]);
+    phi[i] = v;
+    for (int j = 0; j < d; j++) {
+      double g = pdgo_dlagrange(k, alpha[j], xi[j]);
+      for (int l = 0; l < d; l++)
+        if (l != j) g *= pdgo_lagrange(k, alpha[l], xi[l]);
+      js[i * d + j] = g;
+    }
+  }
+}
+
+static int tables_init(const pdgo_problem *p, tables *T) {
+  memset(T, 0, sizeof(*T));
+  if (p->dim < 2 || p->dim > 3 || p->k < 1 || p->k > MAXK) return PDGO_EARG;
+  for (int j = 0; j < p->dim; j++)
+    if (p->nc[j] < 1 || !(p->L[j] > 0)) return PDGO_EARG;
+  if (get_theta(p->method, &T->theta)) return PDGO_EARG;
+  int d = T->d = p->dim;
+  int k = T->k = p->k;
+  int n1 = T->n1 = k + 1;
+  T->nb = 1;
+  for (int j = 0; j < d; j++) T->nb *= n1;
+  /* intorder = quadrature_factor * order = 2k (convectiondiffusiondg.hh:139,
+     360, 745, 1061) -> m = k+1 Gauss points per direction */
+  int nq = T->nq = k + 1;
+  pdgo_gauss_legendre(nq, T->gx, T->gw);
+  T->nqv = 1; T->nqf = 1;
+  for (int j = 0; j < d; j++) T->nqv *= nq;
+  for (int j = 0; j < d - 1; j++) T->nqf *= nq;
+  int nb = T->nb, nqv = T->nqv, nqf = T->nqf;
+  T->vphi = malloc(sizeof(double) * nqv * nb);
+  T->vjs = malloc(sizeof(double) * nqv * nb * d);
+  T->vw = malloc(sizeof(double) * nqv);
+  T->vloc = malloc(sizeof(double) * nqv * d);
+  T->fphi = malloc(sizeof(double) * 2 * d * nqf * nb);
+  T->fjs = malloc(sizeof(double) * 2 * d * nqf * nb * d);
+  T->fw = malloc(sizeof(double) * 2 * d * nqf);
+  T->floc = malloc(sizeof(double) * 2 * d * nqf * d);
+  for (int q = 0; q < nqv; q++) {
+    int t = q;
+    double w = 1.0;
+    for (int j = 0; j < d; j++) {
+      int a = t % nq; t /= nq;
+      T->vloc[q * d + j] = T->gx[a];
+      w *= T->gw[a];
+    }
+    T->vw[q] = w;
+    eval_basis(d, k, &T->vloc[q * d], &T->vphi[q * nb], &T->vjs[q * nb * d]);
+  }
+  for (int f = 0; f < 2 * d; f++) {
+    int dir = f / 2, hi = f % 2;
+    for (int q = 0; q < nqf; q++) {
+      int t = q;
+      double w = 1.0;
+      double *loc = &T->floc[(f * nqf + q) * d];
+      /* face-local coordinates map to the remaining directions in order */
+      for (int j = 0; j < d; j++) {
+        if (j == dir) { loc[j] = hi ? 1.0 : 0.0; continue; }
+        int a = t % nq; t /= nq;
+        loc[j] = T->gx[a];
+        w *= T->gw[a];
+      }
+      T->fw[f * nqf + q] = w;
+      eval_basis(d, k, loc, &T->fphi[(f * nqf + q) * nb], &T->fjs[(f * nqf + q) * nb * d]);
+    }
+  }
+  return PDGO_OK;
+}
+
+static void tables_free(tables *T) {
+  free(T->vphi); free(T->vjs); free(T->vw); free(T->vloc);
+  free(T->fphi); free(T->fjs); free(T->fw); free(T->floc);
+}
+
+long pdgo_ncell(const pdgo_problem *p) {
+  long n = 1;
+  for (int j = 0; j < p->dim; j++) n *= p->nc[j];
+  return n;
+}
+int pdgo_nbasis(const pdgo_problem *p) {
+  int n = 1;
+  for (int j = 0; j < p->dim; j++) n *= p->k + 1;
+  return n;
+}
+long pdgo_ndof(const pdgo_problem *p) { return pdgo_ncell(p) * pdgo_nbasis(p); }
+
+long pdgo_nbpts_side(const pdgo_problem *p, int side) {
+  int dir = side / 2;
+  long n = 1;
+  for (int j = 0; j < p->dim; j++)
+    if (j != dir) n *= (long)p->nc[j] * (p->k + 1);
+  return n;
+}
+long pdgo_bpts_offset(const pdgo_problem *p, int side) {
+  long off = 0;
+  for (int s = 0; s < side; s++) off += pdgo_nbpts_side(p, s);
+  return off;
+}
+long pdgo_nbpts_total(const pdgo_problem *p) { return pdgo_bpts_offset(p, 2 * p->dim); }
+
+static void cell_index(const pdgo_problem *p, long e, int *ix) {
+  long t = e;
+  for (int j = 0; j < p->dim; j++) { ix[j] = (int)(t % p->nc[j]); t /= p->nc[j]; }
+}
+static long cell_of(const pdgo_problem *p, const int *ix) {
+  long e = 0;
+  for (int j = p->dim - 1; j >= 0; j--) e = e * p->nc[j] + ix[j];
+  return e;
+}
+static double cell_h(const pdgo_problem *p, int j) { return p->L[j] / p->nc[j]; }
+
+/* index of a boundary face (cell e on side s) among that side's faces */
+static long boundary_face_index(const pdgo_problem *p, const int *ix, int side) {
+  int dir = side / 2;
+  long idx = 0;
+  for (int j = p->dim - 1; j >= 0; j--) {
+    if (j == dir) continue;
+    idx = idx * p->nc[j] + ix[j];
+  }
+  return idx;
+}
+
+static double Kof(const pdgo_problem *p, long e) { return p->K ? p->K[e] : 1.0; }
+
+static void velocity(const pdgo_problem *p, const double *xg, double *b) {
+  for (int j = 0; j < MAXD; j++) b[j] = 0.0;
+  for (int m = 0; m < p->nmodes; m++) {
+    const double *md = &p->modes[7 * m];
+    double arg = md[3];
+    for (int j = 0; j < p->dim; j++) arg += 2.0 * M_PI * md[j] * xg[j];
+    double s = sin(arg);
+    for (int j = 0; j < p->dim; j++) b[j] += md[4 + j] * s;
+  }
+}
+
+int pdgo_volume_points(const pdgo_problem *p, double *xyz) {
+  tables T;
+  if (tables_init(p, &T)) return PDGO_EARG;
+  long nc = pdgo_ncell(p);
+  int d = T.d;
+  for (long e = 0; e < nc; e++) {
+    int ix[MAXD];
+    cell_index(p, e, ix);
+    for (int q = 0; q < T.nqv; q++)
+      for (int j = 0; j < d; j++)
+        xyz[(e * T.nqv + q) * d + j] = (ix[j] + T.vloc[q * d + j]) * cell_h(p, j);
+  }
+  tables_free(&T);
+  return PDGO_OK;
+}
+
+int pdgo_boundary_points(const pdgo_problem *p, double *xyz) {
+  tables T;
+  if (tables_init(p, &T)) return PDGO_EARG;
+  int d = T.d;
+  long nc = pdgo_ncell(p);
+  for (long e = 0; e < nc; e++) {
+    int ix[MAXD];
+    cell_index(p, e, ix);
+    for (int side = 0; side < 2 * d; side++) {
+      int dir = side / 2, hi = side % 2;
+      if (ix[dir] != (hi ? p->nc[dir] - 1 : 0)) continue;
+      long base = pdgo_bpts_offset(p, side) + boundary_face_index(p, ix, side) * T.nqf;
+      for (int q = 0; q < T.nqf; q++)
+        for (int j = 0; j < d; j++)
+          xyz[(base + q) * d + j] = (ix[j] + T.floc[(side * T.nqf + q) * d + j]) * cell_h(p, j);
+    }
+  }
+  tables_free(&T);
+  return PDGO_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* local operator (residual / jacobian_apply form)                     */
+/* ------------------------------------------------------------------ */
+
+typedef struct coef_override {
+  int active;       /* 1: use Ks/Kn below, drop convection + reaction */
+  double Ks, Kn;
+} coef_override;
+
+/* alpha_volume (convectiondiffusiondg.hh:105-188); also
+   jacobian_apply_volume (:191-195) */
+static void alpha_volume(const pdgo_problem *p, const tables *T, long e,
+                         const double *x, double *r, const coef_override *co) {
+  int d = T->d, nb = T->nb;
+  int ix[MAXD];
+  cell_index(p, e, ix);
+  double h[MAXD], detJ = 1.0;
+  for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); detJ *= h[j]; }
+  /* A at the cell centre (:124-127); scalar K -> A = K I */
+  double A = co && co->active ? co->Ks : Kof(p, e);
+  double cc = (co && co->active) ? 0.0 : (p->c ? p->c[e] : 0.0);
+  double gradphi[MAXNB][MAXD];
+  for (int q = 0; q < T->nqv; q++) {
+    const double *phi = &T->vphi[q * nb];
+    const double *js = &T->vjs[q * nb * d];
+    double u = 0.0;
+    for (int i = 0; i < nb; i++) u += x[i] * phi[i];
+    /* jac = J^{-T} = diag(1/h) on axis-parallel cells */
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < d; j++) gradphi[i][j] = js[i * d + j] / h[j];
+    double gradu[MAXD] = {0, 0, 0}, Agradu[MAXD];
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < d; j++) gradu[j] += x[i] * gradphi[i][j];
+    for (int j = 0; j < d; j++) Agradu[j] = A * gradu[j];
+    double b[MAXD] = {0, 0, 0};
+    if (!(co && co->active) && p->nmodes > 0) {
+      double xg[MAXD];
+      for (int j = 0; j < d; j++) xg[j] = (ix[j] + T->vloc[q * d + j]) * h[j];
+      velocity(p, xg, b);
+    }
+    double factor = T->vw[q] * detJ;
+    for (int i = 0; i < nb; i++) {
+      double ag = 0.0, bg = 0.0;
+      for (int j = 0; j < d; j++) { ag += Agradu[j] * gradphi[i][j]; bg += b[j] * gradphi[i][j]; }
+      r[i] += (ag - u * bg + cc * u * phi[i]) * factor;
+    }
+  }
+}
+
+/* lambda_volume (convectiondiffusiondg.hh:1047-1075) */
+static void lambda_volume(const pdgo_problem *p, const tables *T, long e, double *r) {
+  int d = T->d, nb = T->nb;
+  double detJ = 1.0;
+  for (int j = 0; j < d; j++) detJ *= cell_h(p, j);
+  for (int q = 0; q < T->nqv; q++) {
+    const double *phi = &T->vphi[q * nb];
+    double f = 0.0;
+    if (p->fq) f += p->fq[e * T->nqv + q];
+    if (p->fc) f += p->fc[e];
+    double factor = T->vw[q] * detJ;
+    for (int i = 0; i < nb; i++) r[i] += -f * phi[i] * factor;
+  }
+}
+
+/* skeleton weights (convectiondiffusiondg.hh:308-346) */
+static void face_weights(const pdgo_problem *p, double Ks, double Kn, double hF,
+                         double *omega_s, double *omega_n, double *penalty) {
+  double harmonic_average;
+  if (p->weights == PDGO_WEIGHTS_ON) {
+    double delta_s = Ks, delta_n = Kn;   /* (A n).n with A = K I, |n| = 1 */
+    *omega_s = delta_n / (delta_s + delta_n + 1e-20);
+    *omega_n = delta_s / (delta_s + delta_n + 1e-20);
+    harmonic_average = 2.0 * delta_s * delta_n / (delta_s + delta_n + 1e-20);
+  } else {
+    *omega_s = *omega_n = 0.5;
+    harmonic_average = 1.0;
+  }
+  int degree = p->k;
+  *penalty = (p->alpha / hF) * harmonic_average * degree * (degree + p->dim - 1);
+}
+
+/* alpha_skeleton (convectiondiffusiondg.hh:270-471) for the interior face
+   between inside cell s and outside cell n; the face is normal to `dir`,
+   and n lies on side `hi_s` of s (0 = lower, 1 = upper). */
+static void alpha_skeleton(const pdgo_problem *p, const tables *T, long s, long n,
+                           int dir, int hi_s, const double *x_s, const double *x_n,
+                           double *r_s, double *r_n, const coef_override *co) {
+  int d = T->d, nb = T->nb, nqf = T->nqf;
+  double h[MAXD], vol = 1.0;
+  for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); vol *= h[j]; }
+  double area = vol / h[dir];
+  double Ks = co && co->active ? co->Ks : Kof(p, s);
+  double Kn = co && co->active ? co->Kn : Kof(p, n);
+  double vol_s = vol, vol_n = vol;                   /* uniform grid */
+  double hF = (vol_s < vol_n ? vol_s : vol_n) / area; /* min(|T_s|,|T_n|)/|F| (:313) */
+  double nF[MAXD] = {0, 0, 0};
+  nF[dir] = hi_s ? 1.0 : -1.0;
+  double omega_s, omega_n, penalty;
+  face_weights(p, Ks, Kn, hF, &omega_s, &omega_n, &penalty);
+  double An_F_s[MAXD], An_F_n[MAXD];
+  for (int j = 0; j < d; j++) { An_F_s[j] = Ks * nF[j]; An_F_n[j] = Kn * nF[j]; }
+  int fs = 2 * dir + hi_s, fn = 2 * dir + (1 - hi_s);
+  int ixs[MAXD];
+  cell_index(p, s, ixs);
+  double tgs[MAXNB][MAXD], tgn[MAXNB][MAXD];
+  for (int q = 0; q < nqf; q++) {
+    const double *phi_s = &T->fphi[(fs * nqf + q) * nb];
+    const double *phi_n = &T->fphi[(fn * nqf + q) * nb];
+    const double *js_s = &T->fjs[(fs * nqf + q) * nb * d];
+    const double *js_n = &T->fjs[(fn * nqf + q) * nb * d];
+    double u_s = 0.0, u_n = 0.0;
+    for (int i = 0; i < nb; i++) u_s += x_s[i] * phi_s[i];
+    for (int i = 0; i < nb; i++) u_n += x_n[i] * phi_n[i];
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < d; j++) { tgs[i][j] = js_s[i * d + j] / h[j]; tgn[i][j] = js_n[i * d + j] / h[j]; }
+    double gus[MAXD] = {0, 0, 0}, gun[MAXD] = {0, 0, 0};
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < d; j++) { gus[j] += x_s[i] * tgs[i][j]; gun[j] += x_n[i] * tgn[i][j]; }
+    double b[MAXD] = {0, 0, 0};
+    if (!(co && co->active) && p->nmodes > 0) {
+      double xg[MAXD];
+      for (int j = 0; j < d; j++) xg[j] = (ixs[j] + T->floc[(fs * nqf + q) * d + j]) * h[j];
+      velocity(p, xg, b);
+    }
+    double normalflux = 0.0;
+    for (int j = 0; j < d; j++) normalflux += b[j] * nF[j];
+    double omegaup_s, omegaup_n;
+    if (normalflux >= 0.0) { omegaup_s = 1.0; omegaup_n = 0.0; }
+    else { omegaup_s = 0.0; omegaup_n = 1.0; }
+    double factor = T->fw[fs * nqf + q] * area;
+    double term1 = (omegaup_s * u_s + omegaup_n * u_n) * normalflux * factor;
+    double Ags = 0.0, Agn = 0.0;
+    for (int j = 0; j < d; j++) { Ags += An_F_s[j] * gus[j]; Agn += An_F_n[j] * gun[j]; }
+    double term2 = -(omega_s * Ags + omega_n * Agn) * factor;
+    double term3 = (u_s - u_n) * factor;
+    double term4 = penalty * (u_s - u_n) * factor;
+    for (int i = 0; i < nb; i++) {
+      double ans = 0.0, ann = 0.0;
+      for (int j = 0; j < d; j++) { ans += An_F_s[j] * tgs[i][j]; ann += An_F_n[j] * tgn[i][j]; }
+      r_s[i] += term1 * phi_s[i];
+      r_n[i] += -term1 * phi_n[i];
+      r_s[i] += term2 * phi_s[i];
+      r_n[i] += -term2 * phi_n[i];
+      r_s[i] += term3 * T->theta * omega_s * ans;
+      r_n[i] += term3 * T->theta * omega_n * ann;
+      r_s[i] += term4 * phi_s[i];
+      r_n[i] += -term4 * phi_n[i];
+    }
+  }
+}
+
+/* residual_boundary_integral (convectiondiffusiondg.hh:683-879), called by
+   alpha_boundary (:883-889, jacobian_apply=false) and
+   jacobian_apply_boundary (:892-899, jacobian_apply=true). */
+static int boundary_integral(const pdgo_problem *p, const tables *T, long e, int side,
+                             const double *x_s, double *r_s, int jacobian_apply,
+                             const coef_override *co) {
+  int d = T->d, nb = T->nb, nqf = T->nqf;
+  int dir = side / 2, hi = side % 2;
+  double h[MAXD], vol = 1.0;
+  for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); vol *= h[j]; }
+  double area = vol / h[dir];
+  double Ks = co && co->active ? co->Ks : Kof(p, e);
+  double hF = vol / area;
+  double nF[MAXD] = {0, 0, 0};
+  nF[dir] = hi ? 1.0 : -1.0;
+  double An_F_s[MAXD];
+  for (int j = 0; j < d; j++) An_F_s[j] = Ks * nF[j];
+  double harmonic_average = (p->weights == PDGO_WEIGHTS_ON) ? Ks : 1.0;
+  int degree = p->k;
+  double penalty_factor = (p->alpha / hF) * harmonic_average * degree * (degree + d - 1);
+  int ix[MAXD];
+  cell_index(p, e, ix);
+  long base = pdgo_bpts_offset(p, side) + boundary_face_index(p, ix, side) * nqf;
+  int bctype = p->bctype[side];
+  double tg[MAXNB][MAXD];
+  for (int q = 0; q < nqf; q++) {
+    if (bctype == PDGO_BC_NONE) continue;
+    const double *phi = &T->fphi[(side * nqf + q) * nb];
+    const double *js = &T->fjs[(side * nqf + q) * nb * d];
+    double factor = T->fw[side * nqf + q] * area;
+    if (bctype == PDGO_BC_NEUMANN) {
+      if (!jacobian_apply) {
+        double jv = p->jq ? p->jq[base + q] : 0.0;
+        for (int i = 0; i < nb; i++) r_s[i] += jv * phi[i] * factor;
+      }
+      continue;
+    }
+    double u_s = 0.0;
+    for (int i = 0; i < nb; i++) u_s += x_s[i] * phi[i];
+    double b[MAXD] = {0, 0, 0};
+    if (!(co && co->active) && p->nmodes > 0) {
+      double xg[MAXD];
+      for (int j = 0; j < d; j++) xg[j] = (ix[j] + T->floc[(side * nqf + q) * d + j]) * h[j];
+      velocity(p, xg, b);
+    }
+    double normalflux = 0.0;
+    for (int j = 0; j < d; j++) normalflux += b[j] * nF[j];
+    if (bctype == PDGO_BC_OUTFLOW) {
+      if (normalflux < -1e-30) return PDGO_EOUTFLOW_ON_INFLOW;
+      double term1 = u_s * normalflux * factor;
+      for (int i = 0; i < nb; i++) r_s[i] += term1 * phi[i];
+      if (!jacobian_apply) {
+        double ov = p->oq ? p->oq[base + q] : 0.0;
+        for (int i = 0; i < nb; i++) r_s[i] += ov * phi[i] * factor;
+      }
+      continue;
+    }
+    /* Dirichlet */
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < d; j++) tg[i][j] = js[i * d + j] / h[j];
+    double gu[MAXD] = {0, 0, 0};
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < d; j++) gu[j] += x_s[i] * tg[i][j];
+    double g = p->gq ? p->gq[base + q] : 0.0;
+    if (jacobian_apply) g = 0.0;
+    double omegaup_s, omegaup_n;
+    if (normalflux >= 0.0) { omegaup_s = 1.0; omegaup_n = 0.0; }
+    else { omegaup_s = 0.0; omegaup_n = 1.0; }
+    double term1 = (omegaup_s * u_s + omegaup_n * g) * normalflux * factor;
+    double Ag = 0.0;
+    for (int j = 0; j < d; j++) Ag += An_F_s[j] * gu[j];
+    double term2 = Ag * factor;
+    double term3 = (u_s - g) * factor;
+    double term4 = penalty_factor * (u_s - g) * factor;
+    for (int i = 0; i < nb; i++) {
+      double an = 0.0;
+      for (int j = 0; j < d; j++) an += An_F_s[j] * tg[i][j];
+      r_s[i] += term1 * phi[i];
+      r_s[i] += -term2 * phi[i];
+      r_s[i] += term3 * T->theta * an;
+      r_s[i] += term4 * phi[i];
+    }
+  }
+  return PDGO_OK;
+}
+
+/* DefaultAssembler::assemble (gridoperator/default/assembler.hh:85-279):
+   element loop, volume terms, then intersections; an interior face is
+   visited once, from the cell with the larger index (:181). */
+static int assemble_vector(const pdgo_problem *p, const double *x, double *r, int jacobian_apply) {
+  tables T;
+  if (tables_init(p, &T)) return PDGO_EARG;
+  int d = T.d, nb = T.nb;
+  long nc = pdgo_ncell(p);
+  int st = PDGO_OK;
+  for (long e = 0; e < nc && !st; e++) {
+    int ix[MAXD];
+    cell_index(p, e, ix);
+    if (!jacobian_apply) lambda_volume(p, &T, e, &r[e * nb]);
+    alpha_volume(p, &T, e, &x[e * nb], &r[e * nb], NULL);
+    for (int f = 0; f < 2 * d && !st; f++) {
+      int dir = f / 2, hi = f % 2;
+      int jx[MAXD];
+      memcpy(jx, ix, sizeof(jx));
+      jx[dir] += hi ? 1 : -1;
+      if (jx[dir] < 0 || jx[dir] >= p->nc[dir]) {
+        st = boundary_integral(p, &T, e, f, &x[e * nb], &r[e * nb], jacobian_apply, NULL);
+        continue;
+      }
+      long n = cell_of(p, jx);
+      if (!(e > n)) continue;
+      alpha_skeleton(p, &T, e, n, dir, hi, &x[e * nb], &x[n * nb], &r[e * nb], &r[n * nb], NULL);
+    }
+  }
+  tables_free(&T);
+  return st;
+}
+
+int pdgo_jacobian_apply(const pdgo_problem *p, const double *z, double *y) {
+  return assemble_vector(p, z, y, 1);
+}
+int pdgo_residual(const pdgo_problem *p, const double *x, double *r) {
+  return assemble_vector(p, x, r, 0);
+}
+
+/* ------------------------------------------------------------------ */
+/* assembled local blocks (jacobian_volume / _skeleton / _boundary)    */
+/* mat[i*nb + j]: test i, trial j                                     */
+/* ------------------------------------------------------------------ */
+
+/* jacobian_volume (convectiondiffusiondg.hh:198-266) */
+static void jacobian_volume(const pdgo_problem *p, const tables *T, long e,
+                            double *mat, const coef_override *co) {
+  int d = T->d, nb = T->nb;
+  int ix[MAXD];
+  cell_index(p, e, ix);
+  double h[MAXD], detJ = 1.0;
+  for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); detJ *= h[j]; }
+  double A = co && co->active ? co->Ks : Kof(p, e);
+  double cc = (co && co->active) ? 0.0 : (p->c ? p->c[e] : 0.0);
+  double gradphi[MAXNB][MAXD], Agradphi[MAXNB][MAXD];
+  for (int q = 0; q < T->nqv; q++) {
+    const double *phi = &T->vphi[q * nb];
+    const double *js = &T->vjs[q * nb * d];
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < d; j++) { gradphi[i][j] = js[i * d + j] / h[j]; Agradphi[i][j] = A * gradphi[i][j]; }
+    double b[MAXD] = {0, 0, 0};
+    if (!(co && co->active) && p->nmodes > 0) {
+      double xg[MAXD];
+      for (int j = 0; j < d; j++) xg[j] = (ix[j] + T->vloc[q * d + j]) * h[j];
+      velocity(p, xg, b);
+    }
+    double factor = T->vw[q] * detJ;
+    for (int jj = 0; jj < nb; jj++)
+      for (int i = 0; i < nb; i++) {
+        double ag = 0.0, bg = 0.0;
+        for (int j = 0; j < d; j++) { ag += Agradphi[jj][j] * gradphi[i][j]; bg += b[j] * gradphi[i][j]; }
+        mat[i * nb + jj] += (ag - phi[jj] * bg + cc * phi[jj] * phi[i]) * factor;
+      }
+  }
+}
+
+/* jacobian_skeleton (convectiondiffusiondg.hh:483-669); any of the output
+   blocks may be NULL (the block-diagonal wrapper keeps only mat_ss,
+   blockdiagonalwrapper.hh:141-153). */
+static void jacobian_skeleton(const pdgo_problem *p, const tables *T, long s, long n,
+                              int dir, int hi_s, double *mat_ss, double *mat_sn,
+                              double *mat_ns, double *mat_nn, const coef_override *co) {
+  int d = T->d, nb = T->nb, nqf = T->nqf;
+  double h[MAXD], vol = 1.0;
+  for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); vol *= h[j]; }
+  double area = vol / h[dir];
+  double Ks = co && co->active ? co->Ks : Kof(p, s);
+  double Kn = co && co->active ? co->Kn : Kof(p, n);
+  double hF = vol / area;
+  double nF[MAXD] = {0, 0, 0};
+  nF[dir] = hi_s ? 1.0 : -1.0;
+  double omega_s, omega_n, penalty;
+  face_weights(p, Ks, Kn, hF, &omega_s, &omega_n, &penalty);
+  double An_F_s[MAXD], An_F_n[MAXD];
+  for (int j = 0; j < d; j++) { An_F_s[j] = Ks * nF[j]; An_F_n[j] = Kn * nF[j]; }
+  int fs = 2 * dir + hi_s, fn = 2 * dir + (1 - hi_s);
+  int ixs[MAXD];
+  cell_index(p, s, ixs);
+  double tgs[MAXNB][MAXD], tgn[MAXNB][MAXD];
+  double theta = T->theta;
+  for (int q = 0; q < nqf; q++) {
+    const double *phi_s = &T->fphi[(fs * nqf + q) * nb];
+    const double *phi_n = &T->fphi[(fn * nqf + q) * nb];
+    const double *js_s = &T->fjs[(fs * nqf + q) * nb * d];
+    const double *js_n = &T->fjs[(fn * nqf + q) * nb * d];
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < d; j++) { tgs[i][j] = js_s[i * d + j] / h[j]; tgn[i][j] = js_n[i * d + j] / h[j]; }
+    double b[MAXD] = {0, 0, 0};
+    if (!(co && co->active) && p->nmodes > 0) {
+      double xg[MAXD];
+      for (int j = 0; j < d; j++) xg[j] = (ixs[j] + T->floc[(fs * nqf + q) * d + j]) * h[j];
+      velocity(p, xg, b);
+    }
+    double normalflux = 0.0;
+    for (int j = 0; j < d; j++) normalflux += b[j] * nF[j];
+    double omegaup_s, omegaup_n;
+    if (normalflux >= 0.0) { omegaup_s = 1.0; omegaup_n = 0.0; }
+    else { omegaup_s = 0.0; omegaup_n = 1.0; }
+    double factor = T->fw[fs * nqf + q] * area;
+    double ipfactor = penalty * factor;
+    double ans[MAXNB], ann[MAXNB];
+    for (int i = 0; i < nb; i++) {
+      ans[i] = 0.0; ann[i] = 0.0;
+      for (int j = 0; j < d; j++) { ans[i] += An_F_s[j] * tgs[i][j]; ann[i] += An_F_n[j] * tgn[i][j]; }
+    }
+    if (mat_ss)
+      for (int jj = 0; jj < nb; jj++) {
+        double temp1 = -ans[jj] * omega_s * factor;
+        for (int i = 0; i < nb; i++) {
+          double *m = &mat_ss[i * nb + jj];
+          *m += omegaup_s * phi_s[jj] * normalflux * factor * phi_s[i];
+          *m += temp1 * phi_s[i];
+          *m += phi_s[jj] * factor * theta * omega_s * ans[i];
+          *m += phi_s[jj] * ipfactor * phi_s[i];
+        }
+      }
+    if (mat_sn)
+      for (int jj = 0; jj < nb; jj++) {
+        double temp1 = -ann[jj] * omega_n * factor;
+        for (int i = 0; i < nb; i++) {
+          double *m = &mat_sn[i * nb + jj];
+          *m += omegaup_n * phi_n[jj] * normalflux * factor * phi_s[i];
+          *m += temp1 * phi_s[i];
+          *m += -phi_n[jj] * factor * theta * omega_s * ans[i];
+          *m += -phi_n[jj] * ipfactor * phi_s[i];
+        }
+      }
+    if (mat_ns)
+      for (int jj = 0; jj < nb; jj++) {
+        double temp1 = -ans[jj] * omega_s * factor;
+        for (int i = 0; i < nb; i++) {
+          double *m = &mat_ns[i * nb + jj];
+          *m += -omegaup_s * phi_s[jj] * normalflux * factor * phi_n[i];
+          *m += -temp1 * phi_n[i];
+          *m += phi_s[jj] * factor * theta * omega_n * ann[i];
+          *m += -phi_s[jj] * ipfactor * phi_n[i];
+        }
+      }
+    if (mat_nn)
+      for (int jj = 0; jj < nb; jj++) {
+        double temp1 = -ann[jj] * omega_n * factor;
+        for (int i = 0; i < nb; i++) {
+          double *m = &mat_nn[i * nb + jj];
+          *m += -omegaup_n * phi_n[jj] * normalflux * factor * phi_n[i];
+          *m += -temp1 * phi_n[i];
+          *m += -phi_n[jj] * factor * theta * omega_n * ann[i];
+          *m += phi_n[jj] * ipfactor * phi_n[i];
+        }
+      }
+  }
+}
+
+/* jacobian_boundary (convectiondiffusiondg.hh:901-1044) */
+static int jacobian_boundary(const pdgo_problem *p, const tables *T, long e, int side,
+                             double *mat_ss, const coef_override *co) {
+  int d = T->d, nb = T->nb, nqf = T->nqf;
+  int dir = side / 2, hi = side % 2;
+  double h[MAXD], vol = 1.0;
+  for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); vol *= h[j]; }
+  double area = vol / h[dir];
+  double Ks = co && co->active ? co->Ks : Kof(p, e);
+  double hF = vol / area;
+  double nF[MAXD] = {0, 0, 0};
+  nF[dir] = hi ? 1.0 : -1.0;
+  double An_F_s[MAXD];
+  for (int j = 0; j < d; j++) An_F_s[j] = Ks * nF[j];
+  double harmonic_average = (p->weights == PDGO_WEIGHTS_ON) ? Ks : 1.0;
+  int degree = p->k;
+  double penalty_factor = (p->alpha / hF) * harmonic_average * degree * (degree + d - 1);
+  int ix[MAXD];
+  cell_index(p, e, ix);
+  int bctype = p->bctype[side];
+  double tg[MAXNB][MAXD], an[MAXNB];
+  for (int q = 0; q < nqf; q++) {
+    if (bctype == PDGO_BC_NONE || bctype == PDGO_BC_NEUMANN) continue;
+    const double *phi = &T->fphi[(side * nqf + q) * nb];
+    const double *js = &T->fjs[(side * nqf + q) * nb * d];
+    double factor = T->fw[side * nqf + q] * area;
+    double b[MAXD] = {0, 0, 0};
+    if (!(co && co->active) && p->nmodes > 0) {
+      double xg[MAXD];
+      for (int j = 0; j < d; j++) xg[j] = (ix[j] + T->floc[(side * nqf + q) * d + j]) * h[j];
+      velocity(p, xg, b);
+    }
+    double normalflux = 0.0;
+    for (int j = 0; j < d; j++) normalflux += b[j] * nF[j];
+    if (bctype == PDGO_BC_OUTFLOW) {
+      if (normalflux < -1e-30) return PDGO_EOUTFLOW_ON_INFLOW;
+      for (int jj = 0; jj < nb; jj++)
+        for (int i = 0; i < nb; i++)
+          mat_ss[i * nb + jj] += phi[jj] * normalflux * factor * phi[i];
+      continue;
+    }
+    for (int i = 0; i < nb; i++) {
+      an[i] = 0.0;
+      for (int j = 0; j < d; j++) { tg[i][j] = js[i * d + j] / h[j]; an[i] += An_F_s[j] * tg[i][j]; }
+    }
+    double omegaup_s = normalflux >= 0.0 ? 1.0 : 0.0;
+    for (int jj = 0; jj < nb; jj++)
+      for (int i = 0; i < nb; i++)
+        mat_ss[i * nb + jj] += omegaup_s * phi[jj] * normalflux * factor * phi[i];
+    for (int jj = 0; jj < nb; jj++)
+      for (int i = 0; i < nb; i++)
+        mat_ss[i * nb + jj] += -an[jj] * factor * phi[i];
+    for (int jj = 0; jj < nb; jj++)
+      for (int i = 0; i < nb; i++)
+        mat_ss[i * nb + jj] += phi[jj] * factor * T->theta * an[i];
+    for (int jj = 0; jj < nb; jj++)
+      for (int i = 0; i < nb; i++)
+        mat_ss[i * nb + jj] += penalty_factor * phi[jj] * phi[i] * factor;
+  }
+  return PDGO_OK;
+}
+
+int pdgo_assemble_jacobian(const pdgo_problem *p, double *blocks) {
+  tables T;
+  if (tables_init(p, &T)) return PDGO_EARG;
+  int d = T.d, nb = T.nb, ns = 2 * d + 1;
+  long nc = pdgo_ncell(p);
+  long bs = (long)nb * nb;
+  memset(blocks, 0, sizeof(double) * nc * ns * bs);
+  int st = PDGO_OK;
+  /* jacobian engine over the same one-sided traversal
+     (gridoperator/default/jacobianengine.hh:247-294) */
+  for (long e = 0; e < nc && !st; e++) {
+    int ix[MAXD];
+    cell_index(p, e, ix);
+    jacobian_volume(p, &T, e, &blocks[(e * ns) * bs], NULL);
+    for (int f = 0; f < 2 * d && !st; f++) {
+      int dir = f / 2, hi = f % 2;
+      int jx[MAXD];
+      memcpy(jx, ix, sizeof(jx));
+      jx[dir] += hi ? 1 : -1;
+      if (jx[dir] < 0 || jx[dir] >= p->nc[dir]) {
+        st = jacobian_boundary(p, &T, e, f, &blocks[(e * ns) * bs], NULL);
+        continue;
+      }
+      long n = cell_of(p, jx);
+      if (!(e > n)) continue;
+      int fn = 2 * dir + (1 - hi);
+      jacobian_skeleton(p, &T, e, n, dir, hi,
+                        &blocks[(e * ns) * bs], &blocks[(e * ns + 1 + f) * bs],
+                        &blocks[(n * ns + 1 + fn) * bs], &blocks[(n * ns) * bs], NULL);
+    }
+  }
+  tables_free(&T);
+  return st;
+}
+
+static long neighbor(const pdgo_problem *p, long e, int f) {
+  int ix[MAXD];
+  cell_index(p, e, ix);
+  int dir = f / 2, hi = f % 2;
+  ix[dir] += hi ? 1 : -1;
+  if (ix[dir] < 0 || ix[dir] >= p->nc[dir]) return -1;
+  return cell_of(p, ix);
+}
+
+int pdgo_blocks_apply(const pdgo_problem *p, const double *blocks, const double *x, double *y) {
+  int d = p->dim, nb = pdgo_nbasis(p), ns = 2 * d + 1;
+  long nc = pdgo_ncell(p), bs = (long)nb * nb;
+  for (long e = 0; e < nc; e++) {
+    double *ye = &y[e * nb];
+    for (int i = 0; i < nb; i++) ye[i] = 0.0;
+    for (int sl = 0; sl < ns; sl++) {
+      long n = sl == 0 ? e : neighbor(p, e, sl - 1);
+      if (n < 0) continue;
+      const double *B = &blocks[(e * ns + sl) * bs];
+      const double *xn = &x[n * nb];
+      for (int i = 0; i < nb; i++) {
+        double s = 0.0;
+        for (int j = 0; j < nb; j++) s += B[i * nb + j] * xn[j];
+        ye[i] += s;
+      }
+    }
+  }
+  return PDGO_OK;
+}
+
+int pdgo_blocks_apply_transpose(const pdgo_problem *p, const double *blocks, const double *x, double *y) {
+  int d = p->dim, nb = pdgo_nbasis(p), ns = 2 * d + 1;
+  long nc = pdgo_ncell(p), bs = (long)nb * nb;
+  memset(y, 0, sizeof(double) * nc * nb);
+  for (long e = 0; e < nc; e++) {
+    const double *xe = &x[e * nb];
+    for (int sl = 0; sl < ns; sl++) {
+      long n = sl == 0 ? e : neighbor(p, e, sl - 1);
+      if (n < 0) continue;
+      const double *B = &blocks[(e * ns + sl) * bs];
+      double *yn = &y[n * nb];
+      for (int j = 0; j < nb; j++) {
+        double s = 0.0;
+        for (int i = 0; i < nb; i++) s += B[i * nb + j] * xe[i];
+        yn[j] += s;
+      }
+    }
+  }
+  return PDGO_OK;
+}
+
+/* assembleLocalDiagonalBlock (localoperator/blockdiagonalwrapper.hh:225-257):
+   volume + self-self part of every interior face visited from this cell
+   (two-sided) + boundary faces. */
+int pdgo_block_diagonal(const pdgo_problem *p, double *diag) {
+  tables T;
+  if (tables_init(p, &T)) return PDGO_EARG;
+  int d = T.d, nb = T.nb;
+  long nc = pdgo_ncell(p), bs = (long)nb * nb;
+  memset(diag, 0, sizeof(double) * nc * bs);
+  int st = PDGO_OK;
+  for (long e = 0; e < nc && !st; e++) {
+    jacobian_volume(p, &T, e, &diag[e * bs], NULL);
+    for (int f = 0; f < 2 * d && !st; f++) {
+      long n = neighbor(p, e, f);
+      if (n < 0) { st = jacobian_boundary(p, &T, e, f, &diag[e * bs], NULL); continue; }
+      jacobian_skeleton(p, &T, e, n, f / 2, f % 2, &diag[e * bs], NULL, NULL, NULL, NULL);
+    }
+  }
+  tables_free(&T);
+  return st;
+}
+
+/* Eigen::PartialPivLU restated: in-place LU with row pivoting.  piv[i] is
+   the original row now stored at row i. */
+int pdgo_lu_factor(int nb, long nblocks, double *a, int *piv) {
+  int st = PDGO_OK;
+  for (long b = 0; b < nblocks; b++) {
+    double *A = &a[b * (long)nb * nb];
+    int *P = &piv[b * nb];
+    for (int i = 0; i < nb; i++) P[i] = i;
+    for (int c = 0; c < nb; c++) {
+      int pr = c;
+      double best = fabs(A[c * nb + c]);
+      for (int r = c + 1; r < nb; r++)
+        if (fabs(A[r * nb + c]) > best) { best = fabs(A[r * nb + c]); pr = r; }
+      if (best == 0.0) { st = PDGO_ESINGULAR; continue; }
+      if (pr != c) {
+        for (int j = 0; j < nb; j++) { double t = A[c * nb + j]; A[c * nb + j] = A[pr * nb + j]; A[pr * nb + j] = t; }
+        int t = P[c]; P[c] = P[pr]; P[pr] = t;
+      }
+      for (int r = c + 1; r < nb; r++) {
+        double l = A[r * nb + c] / A[c * nb + c];
+        A[r * nb + c] = l;
+        for (int j = c + 1; j < nb; j++) A[r * nb + j] -= l * A[c * nb + j];
+      }
+    }
+  }
+  return st;
+}
+
+/* AssembledBlockJacobiPreconditionerLocalOperator::jacobian_apply_volume
+   (backend/istl/matrixfree/assembledblockjacobipreconditioner.hh:202-233):
+   forward solve with unit-lower L, backward solve with U. */
+void pdgo_lu_apply(int nb, long nblocks, const double *lu, const int *piv,
+                   const double *dvec, double *v) {
+  double tmp[MAXNB];
+  for (long b = 0; b < nblocks; b++) {
+    const double *A = &lu[b * (long)nb * nb];
+    const int *P = &piv[b * nb];
+    const double *z = &dvec[b * nb];
+    double *y = &v[b * nb];
+    for (int i = 0; i < nb; i++) {
+      double rhs = z[P[i]];
+      for (int j = 0; j < i; j++) rhs -= A[i * nb + j] * tmp[j];
+      tmp[i] = rhs;
+    }
+    for (int i = nb - 1; i >= 0; i--) {
+      double rhs = tmp[i];
+      for (int j = nb - 1; j > i; j--) rhs -= A[i * nb + j] * y[j];
+      y[i] = rhs / A[i * nb + i];
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Krylov solvers                                                      */
+/* ------------------------------------------------------------------ */
+
+typedef struct opctx {
+  const pdgo_problem *p;
+  int op;
+  const double *blocks;
+  const double *lu;
+  const int *piv;
+  long n;
+  int nb;
+} opctx;
+
+/* OnTheFlyOperator::apply (backend/istl/seqistlsolverbackend.hh:66-76):
+   y = 0; jacobian_apply(x, y). */
+static int op_apply(const opctx *o, const double *x, double *y) {
+  if (o->op == 0) {
+    memset(y, 0, sizeof(double) * o->n);
+    return pdgo_jacobian_apply(o->p, x, y);
+  } else if (o->op == 1) {
+    return pdgo_blocks_apply(o->p, o->blocks, x, y);
+  }
+  return pdgo_blocks_apply_transpose(o->p, o->blocks, x, y);
+}
+/* OnTheFlyOperator::applyscaleadd (:78-90): temp = J x; y += alpha temp */
+static int op_applyscaleadd(const opctx *o, double alpha, const double *x, double *y) {
+  double *t = malloc(sizeof(double) * o->n);
+  int st = op_apply(o, x, t);
+  for (long i = 0; i < o->n; i++) y[i] += alpha * t[i];
+  free(t);
+  return st;
+}
+/* GridOperatorPreconditioner::apply (gridoperatorpreconditioner.hh:78-84) */
+static void prec_apply(const opctx *o, double *v, const double *dvec) {
+  if (o->lu) pdgo_lu_apply(o->nb, o->n / o->nb, o->lu, o->piv, dvec, v);
+  else memcpy(v, dvec, sizeof(double) * o->n);
+}
+static double dot(long n, const double *a, const double *b) {
+  double s = 0.0;
+  for (long i = 0; i < n; i++) s += a[i] * b[i];
+  return s;
+}
+
+/* IterativeSolver::Iteration::step (dune-istl): converged when
+   def < def0 * reduction or def < 1e-30; non-finite defects abort. */
+typedef struct iteration { double def0, def; double i; int converged, valid; } iteration;
+static int iter_step(iteration *it, double i, double def, double reduction) {
+  if (!isfinite(def)) { it->valid = 0; it->i = i; it->def = def; return 1; }
+  if (i == 0) it->def0 = def;
+  it->def = def;
+  it->i = i;
+  it->converged = (def < it->def0 * reduction) || (def < 1e-30);
+  return it->converged;
+}
+static void iter_finalize(const iteration *it, pdgo_result *res) {
+  res->converged = it->converged && it->valid;
+  res->iterations = (int)ceil(it->i);
+  res->reduction = it->def0 > 0 ? it->def / it->def0 : 0.0;
+  res->conv_rate = res->iterations > 0 ? pow(res->reduction, 1.0 / res->iterations) : 0.0;
+  res->defect = it->def;
+  res->first_defect = it->def0;
+}
+
+/* dune-istl CGSolver::apply restated */
+int pdgo_cg(const pdgo_problem *p, int op, const double *blocks, const double *lu,
+            const int *piv, double *x, double *b, double reduction, int maxit, pdgo_result *res) {
+  opctx o = {p, op, blocks, lu, piv, pdgo_ndof(p), pdgo_nbasis(p)};
+  long n = o.n;
+  memset(res, 0, sizeof(*res));
+  iteration it = {0, 0, 0, 0, 1};
+  int st = op_applyscaleadd(&o, -1.0, x, b);       /* b = b - A x */
+  if (st) return st;
+  double *pv = malloc(sizeof(double) * n), *q = malloc(sizeof(double) * n);
+  double def = sqrt(dot(n, b, b));
+  if (iter_step(&it, 0, def, reduction)) { iter_finalize(&it, res); free(pv); free(q); return PDGO_OK; }
+  prec_apply(&o, pv, b);
+  double rholast = dot(n, pv, b);
+  int i = 1;
+  for (; i <= maxit; i++) {
+    op_apply(&o, pv, q);
+    double alpha = dot(n, pv, q);
+    double lambda = rholast / alpha;
+    for (long j = 0; j < n; j++) x[j] += lambda * pv[j];
+    for (long j = 0; j < n; j++) b[j] -= lambda * q[j];
+    def = sqrt(dot(n, b, b));
+    if (iter_step(&it, i, def, reduction)) break;
+    prec_apply(&o, q, b);
+    double rho = dot(n, q, b);
+    double beta = rho / rholast;
+    for (long j = 0; j < n; j++) pv[j] = beta * pv[j] + q[j];
+    rholast = rho;
+  }
+  if (i > maxit) it.i = maxit;
+  iter_finalize(&it, res);
+  free(pv); free(q);
+  return PDGO_OK;
+}
+
+/* dune-istl BiCGSTABSolver::apply restated */
+int pdgo_bicgstab(const pdgo_problem *p, int op, const double *blocks, const double *lu,
+                  const int *piv, double *x, double *b, double reduction, int maxit, pdgo_result *res) {
+  opctx o = {p, op, blocks, lu, piv, pdgo_ndof(p), pdgo_nbasis(p)};
+  long n = o.n;
+  const double EPSILON = 1e-80;
+  memset(res, 0, sizeof(*res));
+  iteration iter = {0, 0, 0, 0, 1};
+  double *r = b;
+  double *pv = calloc(n, sizeof(double)), *v = calloc(n, sizeof(double));
+  double *t = calloc(n, sizeof(double)), *y = calloc(n, sizeof(double));
+  double *rt = calloc(n, sizeof(double));
+  int st = op_applyscaleadd(&o, -1.0, x, r);
+  if (st) goto done;
+  memcpy(rt, r, sizeof(double) * n);
+  double norm = sqrt(dot(n, r, r));
+  if (iter_step(&iter, 0, norm, reduction)) goto fin;
+  double rho = 1, alpha = 1, omega = 1, rho_new, beta, h;
+  double it;
+  for (it = 0.5; it < maxit; it += .5) {
+    rho_new = dot(n, rt, r);
+    if (fabs(rho) <= EPSILON || fabs(omega) <= EPSILON) { st = PDGO_EBREAKDOWN; goto fin; }
+    if (it < 1) memcpy(pv, r, sizeof(double) * n);
+    else {
+      beta = (rho_new / rho) * (alpha / omega);
+      for (long j = 0; j < n; j++) pv[j] = beta * (pv[j] - omega * v[j]) + r[j];
+    }
+    prec_apply(&o, y, pv);
+    op_apply(&o, y, v);
+    h = dot(n, rt, v);
+    if (fabs(h) < EPSILON) { st = PDGO_EBREAKDOWN; goto fin; }
+    alpha = rho_new / h;
+    for (long j = 0; j < n; j++) x[j] += alpha * y[j];
+    for (long j = 0; j < n; j++) r[j] -= alpha * v[j];
+    norm = sqrt(dot(n, r, r));
+    if (iter_step(&iter, it, norm, reduction)) break;
+    it += .5;
+    prec_apply(&o, y, r);
+    op_apply(&o, y, t);
+    omega = dot(n, t, r) / dot(n, t, t);
+    for (long j = 0; j < n; j++) x[j] += omega * y[j];
+    for (long j = 0; j < n; j++) r[j] -= omega * t[j];
+    rho = rho_new;
+    norm = sqrt(dot(n, r, r));
+    if (iter_step(&iter, it, norm, reduction)) break;
+  }
+fin:
+  iter_finalize(&iter, res);
+done:
+  free(pv); free(v); free(t); free(y); free(rt);
+  res->status = st;
+  return st;
+}
+
+int pdgo_solve_linear_problem(const pdgo_problem *p, int solver, int op, double *x,
+                              double reduction, double min_defect, int maxit, pdgo_result *res) {
+  long n = pdgo_ndof(p);
+  int nb = pdgo_nbasis(p);
+  long nc = pdgo_ncell(p);
+  double *r = calloc(n, sizeof(double));
+  double *z = calloc(n, sizeof(double));
+  double *blocks = NULL, *lu = NULL;
+  int *piv = NULL;
+  int st = pdgo_residual(p, x, r);
+  if (st) goto out;
+  double defect = sqrt(dot(n, r, r));
+  double red = reduction;
+  if (defect > 0 && min_defect / defect > red) red = min_defect / defect;
+  if (op != 0) {
+    blocks = malloc(sizeof(double) * nc * (2 * p->dim + 1) * nb * nb);
+    st = pdgo_assemble_jacobian(p, blocks);
+    if (st) goto out;
+  }
+  /* GridOperatorPreconditioner::pre -> block-diagonal setup + LU
+     (assembledblockjacobipreconditioner.hh:162-186) */
+  lu = malloc(sizeof(double) * nc * nb * nb);
+  piv = malloc(sizeof(int) * nc * nb);
+  st = pdgo_block_diagonal(p, lu);
+  if (st) goto out;
+  if (op == 2) {
+    /* transpose each diagonal block for the A^T solve */
+    for (long e = 0; e < nc; e++) {
+      double *B = &lu[e * nb * nb];
+      for (int i = 0; i < nb; i++)
+        for (int j = i + 1; j < nb; j++) { double t = B[i * nb + j]; B[i * nb + j] = B[j * nb + i]; B[j * nb + i] = t; }
+    }
+  }
+  st = pdgo_lu_factor(nb, nc, lu, piv);
+  if (st) goto out;
+  if (solver == 0) st = pdgo_cg(p, op, blocks, lu, piv, z, r, red, maxit, res);
+  else st = pdgo_bicgstab(p, op, blocks, lu, piv, z, r, red, maxit, res);
+  res->first_defect = defect;
+  res->defect = defect * res->reduction;
+  for (long i = 0; i < n; i++) x[i] -= z[i];
+out:
+  free(r); free(z); free(blocks); free(lu); free(piv);
+  res->status = st;
+  return st;
+}
+
+int pdgo_eval_points(const pdgo_problem *p, const double *u, int m, double *xyz, double *w, double *val) {
+  int d = p->dim, k = p->k, nb = pdgo_nbasis(p);
+  if (m < 1 || m > 32) return PDGO_EARG;
+  double gx[32], gw[32];
+  pdgo_gauss_legendre(m, gx, gw);
+  long nc = pdgo_ncell(p);
+  int mq = 1;
+  for (int j = 0; j < d; j++) mq *= m;
+  double phi[MAXNB], js[MAXNB * MAXD];
+  double h[MAXD], detJ = 1.0;
+  for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); detJ *= h[j]; }
+  for (long e = 0; e < nc; e++) {
+    int ix[MAXD];
+    cell_index(p, e, ix);
+    for (int q = 0; q < mq; q++) {
+      double loc[MAXD];
+      double wt = 1.0;
+      int t = q;
+      for (int j = 0; j < d; j++) { int a = t % m; t /= m; loc[j] = gx[a]; wt *= gw[a]; }
+      eval_basis(d, k, loc, phi, js);
+      double s = 0.0;
+      for (int i = 0; i < nb; i++) s += u[e * nb + i] * phi[i];
+      val[e * mq + q] = s;
+      w[e * mq + q] = wt * detJ;
+      for (int j = 0; j < d; j++) xyz[(e * mq + q) * d + j] = (ix[j] + loc[j]) * h[j];
+    }
+  }
+  return PDGO_OK;
+}
+
+/* Gradient of J w.r.t. log K from assembled local blocks at unit
+   coefficient.  With weightsOn every diffusion term of a face is
+   proportional to H = 2 Ks Kn / (Ks + Kn + 1e-20) (:326-346), the volume
+   term to K_e (:124-127) and the Dirichlet face terms to K_s (:720-734). */
+int pdgo_grad_logK(const pdgo_problem *p, const double *u, const double *lam, double *g) {
+  if (p->weights != PDGO_WEIGHTS_ON) return PDGO_EARG;
+  tables T;
+  if (tables_init(p, &T)) return PDGO_EARG;
+  int d = T.d, nb = T.nb;
+  long nc = pdgo_ncell(p), bs = (long)nb * nb;
+  double *m1 = malloc(sizeof(double) * bs), *m2 = malloc(sizeof(double) * bs);
+  double *m3 = malloc(sizeof(double) * bs), *m4 = malloc(sizeof(double) * bs);
+  double *rb = malloc(sizeof(double) * nb);
+  coef_override unit = {1, 1.0, 1.0};
+  int st = PDGO_OK;
+  for (long e = 0; e < nc; e++) g[e] = 0.0;
+  for (long e = 0; e < nc && !st; e++) {
+    const double *ue = &u[e * nb], *le = &lam[e * nb];
+    double Ke = Kof(p, e);
+    /* volume */
+    memset(m1, 0, sizeof(double) * bs);
+    jacobian_volume(p, &T, e, m1, &unit);
+    double s = 0.0;
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < nb; j++) s += le[i] * m1[i * nb + j] * ue[j];
+    g[e] -= Ke * s;
+    for (int f = 0; f < 2 * d; f++) {
+      long n = neighbor(p, e, f);
+      if (n < 0) {
+        /* Dirichlet boundary: residual form incl. g, unit K, no convection */
+        for (int i = 0; i < nb; i++) rb[i] = 0.0;
+        st = boundary_integral(p, &T, e, f, ue, rb, 0, &unit);
+        double sb = 0.0;
+        for (int i = 0; i < nb; i++) sb += le[i] * rb[i];
+        g[e] -= Ke * sb;
+        continue;
+      }
+      if (!(e > n)) continue;
+      memset(m1, 0, sizeof(double) * bs); memset(m2, 0, sizeof(double) * bs);
+      memset(m3, 0, sizeof(double) * bs); memset(m4, 0, sizeof(double) * bs);
+      jacobian_skeleton(p, &T, e, n, f / 2, f % 2, m1, m2, m3, m4, &unit);
+      const double *un = &u[n * nb], *ln = &lam[n * nb];
+      double a = 0.0;
+      for (int i = 0; i < nb; i++)
+        for (int j = 0; j < nb; j++)
+          a += le[i] * (m1[i * nb + j] * ue[j] + m2[i * nb + j] * un[j]) +
+               ln[i] * (m3[i * nb + j] * ue[j] + m4[i * nb + j] * un[j]);
+      double Ks = Ke, Kn = Kof(p, n);
+      double S = Ks + Kn + 1e-20;
+      double dH_dKs = 2.0 * Kn * (Kn + 1e-20) / (S * S);
+      double dH_dKn = 2.0 * Ks * (Ks + 1e-20) / (S * S);
+      g[e] -= Ks * dH_dKs * a;
+      g[n] -= Kn * dH_dKn * a;
+    }
+  }
+  free(m1); free(m2); free(m3); free(m4); free(rb);
+  tables_free(&T);
+  return st;
+}
+
+/* dR/dfc_e = -int_e psi_i (lambda_volume, :1047-1075) */
+int pdgo_grad_fc(const pdgo_problem *p, const double *lam, double *g) {
+  tables T;
+  if (tables_init(p, &T)) return PDGO_EARG;
+  int nb = T.nb;
+  long nc = pdgo_ncell(p);
+  double detJ = 1.0;
+  for (int j = 0; j < T.d; j++) detJ *= cell_h(p, j);
+  for (long e = 0; e < nc; e++) {
+    double s = 0.0;
+    for (int q = 0; q < T.nqv; q++) {
+      const double *phi = &T.vphi[q * nb];
+      double factor = T.vw[q] * detJ;
+      for (int i = 0; i < nb; i++) s += lam[e * nb + i] * phi[i] * factor;
+    }
+    g[e] = s;
+  }
+  tables_free(&T);
+  return PDGO_OK;
+}

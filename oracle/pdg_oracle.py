@@ -1,0 +1,277 @@
+"""ctypes binding of the CPU oracle (oracle/pdg_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py`` as the checker.  The product library
+never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libpdg_oracle.so")
+
+BC_DIRICHLET, BC_NEUMANN, BC_OUTFLOW, BC_NONE = 1, -1, -2, -3
+NIPG, SIPG, IIPG = 0, 1, 2
+WEIGHTS_ON, WEIGHTS_OFF = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class _Problem(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int), ("k", C.c_int), ("nc", C.c_int * 3),
+        ("L", C.c_double * 3), ("method", C.c_int), ("weights", C.c_int),
+        ("alpha", C.c_double), ("bctype", C.c_int * 6),
+        ("K", _dp), ("c", _dp), ("nmodes", C.c_int), ("modes", _dp),
+        ("fq", _dp), ("fc", _dp), ("gq", _dp), ("jq", _dp), ("oq", _dp),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("converged", C.c_int), ("iterations", C.c_int),
+        ("reduction", C.c_double), ("conv_rate", C.c_double),
+        ("first_defect", C.c_double), ("defect", C.c_double),
+        ("status", C.c_int),
+    ]
+
+
+def build():
+    """Compile the oracle with its Makefile (plain gcc)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        P = C.POINTER(_Problem)
+        sigs = {
+            "pdgo_ncell": (C.c_long, [P]),
+            "pdgo_nbasis": (C.c_int, [P]),
+            "pdgo_ndof": (C.c_long, [P]),
+            "pdgo_nbpts_side": (C.c_long, [P, C.c_int]),
+            "pdgo_bpts_offset": (C.c_long, [P, C.c_int]),
+            "pdgo_nbpts_total": (C.c_long, [P]),
+            "pdgo_gauss_legendre": (C.c_int, [C.c_int, _dp, _dp]),
+            "pdgo_lagrange": (C.c_double, [C.c_int, C.c_int, C.c_double]),
+            "pdgo_dlagrange": (C.c_double, [C.c_int, C.c_int, C.c_double]),
+            "pdgo_volume_points": (C.c_int, [P, _dp]),
+            "pdgo_boundary_points": (C.c_int, [P, _dp]),
+            "pdgo_jacobian_apply": (C.c_int, [P, _dp, _dp]),
+            "pdgo_residual": (C.c_int, [P, _dp, _dp]),
+            "pdgo_assemble_jacobian": (C.c_int, [P, _dp]),
+            "pdgo_blocks_apply": (C.c_int, [P, _dp, _dp, _dp]),
+            "pdgo_blocks_apply_transpose": (C.c_int, [P, _dp, _dp, _dp]),
+            "pdgo_block_diagonal": (C.c_int, [P, _dp]),
+            "pdgo_lu_factor": (C.c_int, [C.c_int, C.c_long, _dp, _ip]),
+            "pdgo_lu_apply": (None, [C.c_int, C.c_long, _dp, _ip, _dp, _dp]),
+            "pdgo_cg": (C.c_int, [P, C.c_int, _dp, _dp, _ip, _dp, _dp, C.c_double, C.c_int, C.POINTER(Result)]),
+            "pdgo_bicgstab": (C.c_int, [P, C.c_int, _dp, _dp, _ip, _dp, _dp, C.c_double, C.c_int, C.POINTER(Result)]),
+            "pdgo_solve_linear_problem": (C.c_int, [P, C.c_int, C.c_int, _dp, C.c_double, C.c_double, C.c_int, C.POINTER(Result)]),
+            "pdgo_eval_points": (C.c_int, [P, _dp, C.c_int, _dp, _dp, _dp]),
+            "pdgo_grad_logK": (C.c_int, [P, _dp, _dp, _dp]),
+            "pdgo_grad_fc": (C.c_int, [P, _dp, _dp]),
+        }
+        for name, (res, args) in sigs.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_dp)
+
+
+def gauss_legendre(m):
+    x = np.zeros(m)
+    w = np.zeros(m)
+    lib().pdgo_gauss_legendre(m, _ptr(x), _ptr(w))
+    return x, w
+
+
+class Problem:
+    """SIPG/NIPG/IIPG ConvectionDiffusionDG problem on a structured grid.
+
+    Arrays given here are kept alive by this object; all are float64.
+    """
+
+    def __init__(self, dim, k, nc, L=None, method=SIPG, weights=WEIGHTS_ON,
+                 alpha=1.0, bctype=None, K=None, c=None, modes=None,
+                 fq=None, fc=None, gq=None, jq=None, oq=None):
+        self.dim, self.k = dim, k
+        self.nc = tuple(nc) + (1,) * (3 - len(nc))
+        self.L = tuple(L) if L is not None else (1.0,) * dim
+        self.L = self.L + (1.0,) * (3 - len(self.L))
+        self.method, self.weights, self.alpha = method, weights, float(alpha)
+        self.bctype = list(bctype) if bctype is not None else [BC_DIRICHLET] * 6
+        self._arrays = {}
+        self.s = _Problem()
+        s = self.s
+        s.dim, s.k = dim, k
+        for j in range(3):
+            s.nc[j] = self.nc[j]
+            s.L[j] = self.L[j]
+        s.method, s.weights, s.alpha = method, weights, self.alpha
+        for j in range(6):
+            s.bctype[j] = self.bctype[j] if j < len(self.bctype) else BC_DIRICHLET
+        self.set(K=K, c=c, fq=fq, fc=fc, gq=gq, jq=jq, oq=oq)
+        self.set_modes(modes)
+
+    def set(self, **arrays):
+        for name, a in arrays.items():
+            if a is None:
+                self._arrays.pop(name, None)
+                setattr(self.s, name, None)
+                continue
+            a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+            self._arrays[name] = a
+            setattr(self.s, name, _ptr(a))
+
+    def set_modes(self, modes):
+        if modes is None or len(modes) == 0:
+            self.s.nmodes = 0
+            self.s.modes = None
+            self._arrays.pop("modes", None)
+            return
+        m = np.ascontiguousarray(modes, dtype=np.float64).reshape(-1, 7)
+        self._arrays["modes"] = m
+        self.s.nmodes = m.shape[0]
+        self.s.modes = _ptr(m)
+
+    @property
+    def ref(self):
+        return C.byref(self.s)
+
+    @property
+    def ncell(self):
+        return lib().pdgo_ncell(self.ref)
+
+    @property
+    def nb(self):
+        return lib().pdgo_nbasis(self.ref)
+
+    @property
+    def ndof(self):
+        return lib().pdgo_ndof(self.ref)
+
+    @property
+    def nq_volume(self):
+        return (self.k + 1) ** self.dim
+
+    def nbpts_total(self):
+        return lib().pdgo_nbpts_total(self.ref)
+
+    def volume_points(self):
+        out = np.zeros((self.ncell, self.nq_volume, self.dim))
+        _check(lib().pdgo_volume_points(self.ref, _ptr(out)))
+        return out
+
+    def boundary_points(self):
+        out = np.zeros((self.nbpts_total(), self.dim))
+        _check(lib().pdgo_boundary_points(self.ref, _ptr(out)))
+        return out
+
+    def jacobian_apply(self, z, y=None):
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        y = np.zeros(self.ndof) if y is None else y
+        _check(lib().pdgo_jacobian_apply(self.ref, _ptr(z), _ptr(y)))
+        return y
+
+    def residual(self, x, r=None):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        r = np.zeros(self.ndof) if r is None else r
+        _check(lib().pdgo_residual(self.ref, _ptr(x), _ptr(r)))
+        return r
+
+    def assemble_jacobian(self):
+        nb = self.nb
+        out = np.zeros((self.ncell, 2 * self.dim + 1, nb, nb))
+        _check(lib().pdgo_assemble_jacobian(self.ref, _ptr(out)))
+        return out
+
+    def blocks_apply(self, blocks, x, transpose=False):
+        y = np.zeros(self.ndof)
+        fn = lib().pdgo_blocks_apply_transpose if transpose else lib().pdgo_blocks_apply
+        _check(fn(self.ref, _ptr(blocks), _ptr(np.ascontiguousarray(x)), _ptr(y)))
+        return y
+
+    def block_diagonal(self):
+        nb = self.nb
+        out = np.zeros((self.ncell, nb, nb))
+        _check(lib().pdgo_block_diagonal(self.ref, _ptr(out)))
+        return out
+
+    def lu(self, diag):
+        a = np.ascontiguousarray(diag.copy())
+        piv = np.zeros(a.shape[:-1], dtype=np.int32)
+        _check(lib().pdgo_lu_factor(self.nb, self.ncell, _ptr(a), piv.ctypes.data_as(_ip)))
+        return a, piv
+
+    def lu_apply(self, lu, piv, d):
+        v = np.zeros(self.ndof)
+        lib().pdgo_lu_apply(self.nb, self.ncell, _ptr(lu), piv.ctypes.data_as(_ip),
+                            _ptr(np.ascontiguousarray(d)), _ptr(v))
+        return v
+
+    def krylov(self, solver, x, b, reduction, maxit=5000, op=0, blocks=None,
+               lu=None, piv=None):
+        res = Result()
+        fn = lib().pdgo_cg if solver == "cg" else lib().pdgo_bicgstab
+        st = fn(self.ref, op, _ptr(blocks), _ptr(lu),
+                None if piv is None else piv.ctypes.data_as(_ip),
+                _ptr(x), _ptr(b), reduction, maxit, C.byref(res))
+        return st, res
+
+    def solve(self, x=None, solver="cg", op=0, reduction=1e-12, min_defect=1e-99,
+              maxit=5000):
+        x = np.zeros(self.ndof) if x is None else x
+        res = Result()
+        st = lib().pdgo_solve_linear_problem(self.ref, 0 if solver == "cg" else 1, op,
+                                             _ptr(x), reduction, min_defect, maxit,
+                                             C.byref(res))
+        return x, res, st
+
+    def eval_points(self, u, m):
+        mq = m ** self.dim
+        xyz = np.zeros((self.ncell, mq, self.dim))
+        w = np.zeros((self.ncell, mq))
+        val = np.zeros((self.ncell, mq))
+        _check(lib().pdgo_eval_points(self.ref, _ptr(np.ascontiguousarray(u)), m,
+                                      _ptr(xyz), _ptr(w), _ptr(val)))
+        return xyz, w, val
+
+    def grad_logK(self, u, lam):
+        g = np.zeros(self.ncell)
+        _check(lib().pdgo_grad_logK(self.ref, _ptr(np.ascontiguousarray(u)),
+                                    _ptr(np.ascontiguousarray(lam)), _ptr(g)))
+        return g
+
+    def grad_fc(self, lam):
+        g = np.zeros(self.ncell)
+        _check(lib().pdgo_grad_fc(self.ref, _ptr(np.ascontiguousarray(lam)), _ptr(g)))
+        return g
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def _check(st):
+    if st != 0:
+        raise OracleError(f"oracle status {st}")

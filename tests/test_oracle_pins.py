@@ -1,0 +1,117 @@
+"""The oracle reproduces the reference tests' own assertions.
+
+The reference ships no golden vectors; these assertions are the pins:
+  * dune/pdelab/test/matrixfree/matrix_free_linear.cc:387-393
+  * dune/pdelab/test/testfastdgassembler.cc:160-175
+  * dune/pdelab/test/testblocklocaloperatorwrapper.cc:200-276
+"""
+import numpy as np
+import pytest
+
+
+def _mfl_problem(O, n=16, k=1):
+    # PoissonProblem of matrix_free_linear.cc:28-60: g = exp(-|x-1/2|^2),
+    # f = 4 (1 - c) g, SIPG, weightsOn, alpha = 3 (:104-108)
+    P = O.Problem(2, k, (n, n), alpha=3.0)
+    vp = P.volume_points()
+    c = (0.5 - vp[..., 0]) ** 2 + (0.5 - vp[..., 1]) ** 2
+    P.set(fq=4 * (1 - c) * np.exp(-c))
+    bp = P.boundary_points()
+    cb = (0.5 - bp[:, 0]) ** 2 + (0.5 - bp[:, 1]) ** 2
+    P.set(gq=np.exp(-cb))
+    return P
+
+
+def _l2err2(P, u, exact, m=6):
+    xyz, w, val = P.eval_points(u, m)
+    return float(np.sum(w * (val - exact(xyz)) ** 2))
+
+
+def test_gauss_legendre(oracle):
+    for m in range(1, 9):
+        x, w = oracle.gauss_legendre(m)
+        assert abs(w.sum() - 1) < 1e-15
+        # exact for polynomials of degree 2m-1 on [0,1]
+        for p in range(2 * m):
+            assert abs(np.dot(w, x ** p) - 1.0 / (p + 1)) < 1e-14
+
+
+def test_lagrange_nodes(oracle):
+    L = oracle.lib()
+    for k in range(1, 6):
+        for i in range(k + 1):
+            for j in range(k + 1):
+                assert abs(L.pdgo_lagrange(k, i, j / k) - (i == j)) < 1e-14
+
+
+@pytest.mark.parametrize("solver", ["bicgstab", "cg"])
+def test_matrix_free_linear(oracle, solver):
+    P = _mfl_problem(oracle)
+    u_mb, res_mb, st = P.solve(solver=solver, op=1, reduction=1e-12)
+    assert st == 0
+    u_mf, res_mf, st = P.solve(solver=solver, op=0, reduction=1e-12)
+    assert st == 0
+    assert res_mb.converged and res_mf.converged
+    # equal Krylov iteration counts, matrix-based vs matrix-free (:392-393)
+    assert res_mb.iterations == res_mf.iterations
+    exact = lambda x: np.exp(-((0.5 - x[..., 0]) ** 2 + (0.5 - x[..., 1]) ** 2))
+    err = _l2err2(P, u_mf, exact, 6)     # integrateGridFunction order 10
+    assert err < 1e-6                    # (:387-391)
+
+
+def test_fastdg_assembler(oracle):
+    # ParameterA of testfastdgassembler.cc: g = exp(-|x|^2), f = (2d - 4|x|^2) g,
+    # SIPG alpha = 2, 32x32 (refine 5), CG, reduction 1e-12
+    P = oracle.Problem(2, 1, (32, 32), alpha=2.0)
+    vp = P.volume_points()
+    nrm = (vp ** 2).sum(-1)
+    P.set(fq=(4 - 4 * nrm) * np.exp(-nrm))
+    bp = P.boundary_points()
+    P.set(gq=np.exp(-(bp ** 2).sum(-1)))
+    u, res, st = P.solve(solver="cg", op=0, reduction=1e-12)
+    assert st == 0 and res.converged
+    err = _l2err2(P, u, lambda x: np.exp(-(x ** 2).sum(-1)), 7)   # order 12
+    assert err < 1e-8
+
+
+@pytest.mark.parametrize("dim,k,n", [(2, 1, 16), (2, 2, 6), (3, 1, 4), (3, 2, 3)])
+def test_block_diagonal_identity(oracle, dim, k, n):
+    # testblocklocaloperatorwrapper.cc:200-276: the wrapper's diagonal blocks
+    # equal the assembled Jacobian's diagonal blocks to 1e-14
+    rng = np.random.default_rng(1)
+    P = oracle.Problem(dim, k, (n,) * dim, alpha=3.0)
+    P.set(K=np.exp(rng.standard_normal(P.ncell)))
+    A = P.assemble_jacobian()
+    D = P.block_diagonal()
+    assert np.max(np.abs(A[:, 0] - D)) <= 1e-14 * np.max(np.abs(D))
+
+
+@pytest.mark.parametrize("dim,k,n", [(2, 1, 8), (2, 3, 4), (3, 2, 3)])
+def test_matrix_free_equals_assembled(oracle, dim, k, n):
+    rng = np.random.default_rng(2)
+    P = oracle.Problem(dim, k, (n,) * dim, alpha=3.0)
+    P.set(K=np.exp(rng.standard_normal(P.ncell)))
+    x = rng.uniform(-1, 1, P.ndof)
+    y = P.jacobian_apply(x)
+    A = P.assemble_jacobian()
+    y2 = P.blocks_apply(A, x)
+    assert np.max(np.abs(y - y2)) <= 1e-13 * np.max(np.abs(y))
+    # SIPG pure diffusion is symmetric: A^T x == A x
+    y3 = P.blocks_apply(A, x, transpose=True)
+    assert np.max(np.abs(y3 - y)) <= 1e-12 * np.max(np.abs(y))
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+def test_convergence_order(oracle, k):
+    # manufactured u = sin(pi x) sin(pi y) sin(pi z), K = 1: O(h^{k+1}) in L2
+    errs = []
+    for n in (2, 4):
+        P = oracle.Problem(3, k, (n, n, n), alpha=3.0)
+        vp = P.volume_points()
+        s = np.prod(np.sin(np.pi * vp), axis=-1)
+        P.set(fq=3 * np.pi ** 2 * s)
+        u, res, st = P.solve(solver="cg", op=0, reduction=1e-12)
+        assert st == 0 and res.converged
+        errs.append(_l2err2(P, u, lambda x: np.prod(np.sin(np.pi * x), axis=-1), k + 3) ** 0.5)
+    rate = np.log2(errs[0] / errs[1])
+    assert rate > k + 1 - 0.6, (errs, rate)
