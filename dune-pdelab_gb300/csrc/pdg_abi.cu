@@ -1,0 +1,962 @@
+// pdg_abi.cu -- the C ABI (include/pdg.h): context, 1D tables, parameter
+// uploads, operator entry points, and the device-resident Krylov drivers.
+//
+// Solver semantics follow the reference's call chain:
+//   StationaryLinearProblemSolver::apply   (stationary/linearproblem.hh:188-302)
+//   ISTLBackend_SEQ_MatrixFree_Base::apply (backend/istl/matrixfree/backends.hh:116-126)
+//   OnTheFlyOperator / GridOperatorPreconditioner (seqistlsolverbackend.hh:45-100,
+//     matrixfree/gridoperatorpreconditioner.hh:45-84)
+// with dune-istl's CGSolver / BiCGSTABSolver recurrences (external to the
+// reference; restated from the published algorithms).
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pdg_internal.cuh"
+#include "pdg_vec.cuh"
+
+namespace pdg {
+
+static thread_local std::string g_err;
+
+int set_error(int status, const std::string &msg) {
+  g_err = msg;
+  return status;
+}
+
+
+// Lagrange basis at equidistant nodes j/k, as QkStuff::p / dp
+// (finiteelement/qkdglagrange.hh:55-79).
+static double lag(int k, int i, double x) {
+  double r = 1.0;
+  for (int j = 0; j <= k; j++)
+    if (j != i) r *= (k * x - j) / (i - j);
+  return r;
+}
+static double dlag(int k, int i, double x) {
+  double r = 0.0;
+  for (int j = 0; j <= k; j++)
+    if (j != i) {
+      double prod = (k * 1.0) / (i - j);
+      for (int l = 0; l <= k; l++)
+        if (l != i && l != j) prod *= (k * x - l) / (i - l);
+      r += prod;
+    }
+  return r;
+}
+// Gauss-Legendre points/weights on [0,1] (Newton on P_m, long double).
+static void gauss_legendre(int m, double *x, double *w) {
+  for (int i = 0; i < m; i++) {
+    long double z = cosl(3.14159265358979323846264338327950288L * (i + 0.75L) / (m + 0.5L));
+    long double dp = 0;
+    for (int it = 0; it < 100; it++) {
+      long double p0 = 1.0L, p1 = 0.0L;
+      for (int j = 1; j <= m; j++) {
+        long double p2 = p1;
+        p1 = p0;
+        p0 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * p2) / j;
+      }
+      dp = m * (z * p0 - p1) / (z * z - 1.0L);
+      long double dz = p0 / dp;
+      z -= dz;
+      if (fabsl(dz) < 1e-19L) break;
+    }
+    long double p0 = 1.0L, p1 = 0.0L;
+    for (int j = 1; j <= m; j++) {
+      long double p2 = p1;
+      p1 = p0;
+      p0 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * p2) / j;
+    }
+    dp = m * (z * p0 - p1) / (z * z - 1.0L);
+    x[i] = (double)((1.0L - z) * 0.5L);
+    w[i] = (double)(1.0L / ((1.0L - z * z) * dp * dp));
+  }
+}
+
+RhsTables make_rhs_tables(const pdg_context *ctx) {
+  RhsTables t;
+  std::memset(&t, 0, sizeof(t));
+  const int N = ctx->N, k = ctx->k;
+  gauss_legendre(N, t.x, t.w);
+  for (int q = 0; q < N; q++)
+    for (int a = 0; a < N; a++) t.B[q * N + a] = lag(k, a, t.x[q]);
+  for (int a = 0; a < N; a++) {
+    t.d0[a] = dlag(k, a, 0.0);
+    t.d1[a] = dlag(k, a, 1.0);
+  }
+  return t;
+}
+
+double *rhs_r0K(pdg_context *ctx, bool alloc) {
+  if (!ctx->r0K && alloc) {
+    if (cudaMalloc(&ctx->r0K, sizeof(double) * ctx->ndof) != cudaSuccess) {
+      ctx->r0K = nullptr;
+      return nullptr;
+    }
+  }
+  return ctx->r0K;
+}
+
+template <typename T> static const T *Kp(const pdg_context *c);
+template <> const double *Kp<double>(const pdg_context *c) { return c->K64; }
+template <> const float *Kp<float>(const pdg_context *c) { return c->K32; }
+template <typename T> static const T *Cp(const pdg_context *c);
+template <> const double *Cp<double>(const pdg_context *c) { return c->c64; }
+template <> const float *Cp<float>(const pdg_context *c) { return c->c32; }
+template <typename T> static const T *Tp(const pdg_context *c);
+template <> const double *Tp<double>(const pdg_context *c) { return c->tab64; }
+template <> const float *Tp<float>(const pdg_context *c) { return c->tab32; }
+
+template <typename T>
+static int op_launch(pdg_context *ctx, const T *x, T *y, const T *add, T alpha, int acc,
+                     int transpose, const int *skip) {
+  ApplyArgs<T> a{x, y, add, alpha, acc, transpose, 0, skip};
+  return launch_apply<T>(ctx, a, Kp<T>(ctx), Cp<T>(ctx), Tp<T>(ctx));
+}
+
+static int ensure_r0(pdg_context *ctx) {
+  if (!ctx->r0_valid) {
+    PDG_TRY(launch_rhs(ctx));
+    ctx->r0_valid = 1;
+  }
+  return PDG_OK;
+}
+
+static int ensure_work(pdg_context *ctx, bool f32) {
+  for (int i = 0; i < 8; i++)
+    if (!ctx->w64[i]) PDG_CUDA_TRY(cudaMalloc(&ctx->w64[i], sizeof(double) * ctx->ndof));
+  if (f32)
+    for (int i = 0; i < 8; i++)
+      if (!ctx->w32[i]) PDG_CUDA_TRY(cudaMalloc(&ctx->w32[i], sizeof(float) * ctx->ndof));
+  return PDG_OK;
+}
+
+static RedCtx red_ctx(pdg_context *ctx) {
+  return RedCtx{ctx->red_partials, ctx->red_out, ctx->d_flag};
+}
+
+// pinned host mirror: h_red[0..S_COUNT) scalars, then F_COUNT ints
+static int fetch_state(pdg_context *ctx, double *scal, int *flags) {
+  PDG_CUDA_TRY(cudaMemcpyAsync(ctx->h_red, ctx->red_out, sizeof(double) * S_COUNT,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  int *hf = reinterpret_cast<int *>(ctx->h_red + S_COUNT);
+  PDG_CUDA_TRY(cudaMemcpyAsync(hf, ctx->d_flag, sizeof(int) * F_COUNT, cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (scal) std::memcpy(scal, ctx->h_red, sizeof(double) * S_COUNT);
+  if (flags) std::memcpy(flags, hf, sizeof(int) * F_COUNT);
+  return PDG_OK;
+}
+
+__global__ void k_set_scal(double *scal, int slot, double v) { scal[slot] = v; }
+__global__ void k_init_solve(double *scal, int *flags, double red) {
+  for (int i = 0; i < S_COUNT; i++) scal[i] = 0.0;
+  scal[S_RED] = red;
+  scal[S_RHO] = 1.0;
+  scal[S_ALPHA] = 1.0;
+  scal[S_OMEGA] = 1.0;
+  flags[F_STATE] = 0;
+  flags[F_COUNTER] = 0;
+}
+
+template <typename T>
+static int dot(pdg_context *ctx, const RedCtx &rc, const T *a, const T *b, const T *c,
+               const T *d, int fin, int s0, int s1, bool respect) {
+  if (std::is_same<T, double>::value)
+    return red_dot(ctx, rc, ctx->ndof, (const double *)a, (const double *)b, (const double *)c,
+                   (const double *)d, fin, s0, s1, respect);
+  return red_dot_f32(ctx, rc, ctx->ndof, (const float *)a, (const float *)b, (const float *)c,
+                     (const float *)d, fin, s0, s1, respect);
+}
+
+struct KrylovOut {
+  int state;       // 0 running/maxit, 1 converged, 2 non-finite, 3 breakdown
+  int iterations;
+  double def0, def;
+};
+
+// dune-istl CGSolver::apply restated on the device.  x: initial guess and
+// result; b: right-hand side, overwritten by the defect.  w0, w1: work.
+template <typename T>
+static int cg_device(pdg_context *ctx, T *x, T *b, T *p, T *q, double reduction, int maxit,
+                     int transpose, KrylovOut *out) {
+  const RedCtx rc = red_ctx(ctx);
+  const int *skip = ctx->d_flag + F_STATE;
+  k_init_solve<<<1, 1, 0, ctx->stream>>>(rc.scal, rc.flags, reduction);
+  // b -= A x   (applyscaleadd(-1, x, b))
+  PDG_TRY(op_launch<T>(ctx, x, b, nullptr, T(-1), 1, transpose, nullptr));
+  PDG_TRY(dot<T>(ctx, rc, b, b, nullptr, nullptr, FIN_DEF0, -1, -1, false));
+  // p = M^{-1} b ; rholast = <p, b>
+  PDG_TRY(prec_apply_skip<T>(ctx, b, p, transpose, skip));
+  PDG_TRY(dot<T>(ctx, rc, p, b, nullptr, nullptr, FIN_STORE, S_RHO, -1, true));
+  double scal[S_COUNT];
+  int flags[F_COUNT];
+  int i = 1;
+  const int batch = 8;
+  bool done = false;
+  for (; i <= maxit && !done; i++) {
+    PDG_TRY(set_iter(ctx, rc, (double)i));
+    PDG_TRY(op_launch<T>(ctx, p, q, nullptr, T(1), 0, transpose, skip));          // q = A p
+    PDG_TRY(dot<T>(ctx, rc, p, q, nullptr, nullptr, FIN_CG_LAMBDA, -1, -1, true)); // lambda
+    PDG_TRY(cg_update_xr<T>(ctx, rc, ctx->ndof, x, b, p, q));                     // x, b, def
+    PDG_TRY(prec_apply_skip<T>(ctx, b, q, transpose, skip));                        // q = M^-1 b
+    PDG_TRY(dot<T>(ctx, rc, q, b, nullptr, nullptr, FIN_CG_BETA, -1, -1, true));   // beta
+    PDG_TRY(cg_update_p<T>(ctx, rc, ctx->ndof, p, q));                             // p = q + beta p
+    if (i % batch == 0 || i == maxit || i == 1) {
+      PDG_TRY(fetch_state(ctx, scal, flags));
+      if (flags[F_STATE]) done = true;
+    }
+  }
+  PDG_TRY(fetch_state(ctx, scal, flags));
+  out->state = flags[F_STATE];
+  out->def0 = scal[S_DEF0];
+  out->def = scal[S_DEF];
+  out->iterations = (int)scal[S_ITER];
+  return PDG_OK;
+}
+
+// dune-istl BiCGSTABSolver::apply restated on the device.
+template <typename T>
+static int bicgstab_device(pdg_context *ctx, T *x, T *b, T *w[5], double reduction, int maxit,
+                           int transpose, KrylovOut *out) {
+  const RedCtx rc = red_ctx(ctx);
+  const int *skip = ctx->d_flag + F_STATE;
+  T *r = b, *p = w[0], *v = w[1], *t = w[2], *y = w[3], *rt = w[4];
+  k_init_solve<<<1, 1, 0, ctx->stream>>>(rc.scal, rc.flags, reduction);
+  PDG_TRY(op_launch<T>(ctx, x, r, nullptr, T(-1), 1, transpose, nullptr));
+  PDG_TRY(vec_copy<T>(ctx, ctx->ndof, r, rt));
+  PDG_TRY(dot<T>(ctx, rc, r, r, nullptr, nullptr, FIN_DEF0, -1, -1, false));
+  PDG_TRY(vec_fill<T>(ctx, ctx->ndof, p, T(0)));
+  PDG_TRY(vec_fill<T>(ctx, ctx->ndof, v, T(0)));
+  double scal[S_COUNT];
+  int flags[F_COUNT];
+  bool done = false;
+  int loop = 0;
+  for (double it = 0.5; it < maxit && !done; it += 0.5, loop++) {
+    PDG_TRY(set_iter(ctx, rc, it));
+    PDG_TRY(dot<T>(ctx, rc, rt, r, nullptr, nullptr, FIN_BI_RHONEW, -1, -1, true));
+    PDG_TRY(bi_update_p<T>(ctx, rc, ctx->ndof, p, r, v, it < 1));
+    PDG_TRY(prec_apply_skip<T>(ctx, p, y, transpose, skip));
+    PDG_TRY(op_launch<T>(ctx, y, v, nullptr, T(1), 0, transpose, skip));
+    PDG_TRY(dot<T>(ctx, rc, rt, v, nullptr, nullptr, FIN_BI_ALPHA, -1, -1, true));
+    PDG_TRY(bi_update_half<T>(ctx, rc, ctx->ndof, x, r, y, v));
+    it += 0.5;
+    PDG_TRY(set_iter(ctx, rc, it));
+    PDG_TRY(prec_apply_skip<T>(ctx, r, y, transpose, skip));
+    PDG_TRY(op_launch<T>(ctx, y, t, nullptr, T(1), 0, transpose, skip));
+    PDG_TRY(dot<T>(ctx, rc, t, r, t, t, FIN_BI_OMEGA, -1, -1, true));
+    PDG_TRY(bi_update_full<T>(ctx, rc, ctx->ndof, x, r, y, t));
+    if (loop % 4 == 3 || it + 0.5 >= maxit || loop == 0) {
+      PDG_TRY(fetch_state(ctx, scal, flags));
+      if (flags[F_STATE]) done = true;
+    }
+  }
+  PDG_TRY(fetch_state(ctx, scal, flags));
+  out->state = flags[F_STATE];
+  out->def0 = scal[S_DEF0];
+  out->def = scal[S_DEF];
+  out->iterations = (int)std::ceil(scal[S_ITER]);
+  return PDG_OK;
+}
+
+template <typename T>
+static int krylov_device(pdg_context *ctx, int method, T *x, T *b, T **w, double reduction,
+                         int maxit, int transpose, KrylovOut *out) {
+  if (method == PDG_CG) return cg_device<T>(ctx, x, b, w[0], w[1], reduction, maxit, transpose, out);
+  if (method == PDG_BICGSTAB)
+    return bicgstab_device<T>(ctx, x, b, w, reduction, maxit, transpose, out);
+  return set_error(PDG_EINVAL, "unknown Krylov method");
+}
+
+static int state_status(int state) {
+  if (state == 2) return set_error(PDG_ENONFINITE, "non-finite defect");
+  if (state == 3) return set_error(PDG_EBREAKDOWN, "breakdown in BiCGStab");
+  return PDG_OK;
+}
+
+static void fill_result(pdg_solver_result *res, const KrylovOut &o, double elapsed) {
+  res->converged = o.state == 1;
+  res->iterations = o.iterations;
+  res->elapsed = elapsed;
+  res->reduction = o.def0 > 0 ? o.def / o.def0 : 0.0;
+  res->conv_rate = o.iterations > 0 ? std::pow(res->reduction, 1.0 / o.iterations) : 0.0;
+  res->first_defect = o.def0;
+  res->defect = o.def;
+  res->outer_iterations = 0;
+}
+
+static int ensure_prec(pdg_context *ctx, int kind, int precision) {
+  PrecData &pd = ctx->prec[precision];
+  if (pd.ready && pd.kind == kind) return PDG_OK;
+  return prec_setup_impl(ctx, kind, precision);
+}
+
+// Solve J z = r (transposed when `transpose`) from z = 0 or the given z.
+// FP64 Krylov, or FP32 Krylov inside FP64 defect correction when opt->mixed.
+// r is overwritten by the final defect.
+static int solve_correction(pdg_context *ctx, const pdg_solver_options *opt, double *z,
+                            double *r, int transpose, pdg_solver_result *res) {
+  PDG_TRY(ensure_work(ctx, opt->mixed != 0));
+  cudaEventRecord(ctx->ev0, ctx->stream);
+  if (!opt->mixed) {
+    PDG_TRY(ensure_prec(ctx, opt->preconditioner, PDG_F64));
+    KrylovOut o{};
+    PDG_TRY(krylov_device<double>(ctx, opt->method, z, r, ctx->w64, opt->reduction, opt->maxit,
+                                  transpose, &o));
+    cudaEventRecord(ctx->ev1, ctx->stream);
+    cudaEventSynchronize(ctx->ev1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    fill_result(res, o, ms * 1e-3);
+    res->status = state_status(o.state);
+    if (res->status) return res->status;
+    return res->converged ? PDG_OK : set_error(PDG_ENOTCONVERGED, "Krylov solver did not converge");
+  }
+  // ---- mixed precision: FP64 defect correction around FP32 Krylov ----
+  PDG_TRY(ensure_prec(ctx, opt->preconditioner, PDG_F32));
+  const long n = ctx->ndof;
+  double *rhs = ctx->w64[5], *d = ctx->w64[6];
+  float *d32 = ctx->w32[5], *c32 = ctx->w32[6];
+  const RedCtx rc = red_ctx(ctx);
+  PDG_TRY(vec_copy<double>(ctx, n, r, rhs));
+  // d = rhs - J z
+  PDG_TRY(op_launch<double>(ctx, z, d, rhs, -1.0, 0, transpose, nullptr));
+  double scal[S_COUNT];
+  k_init_solve<<<1, 1, 0, ctx->stream>>>(rc.scal, rc.flags, opt->reduction);
+  PDG_TRY(red_dot(ctx, rc, n, d, d, nullptr, nullptr, FIN_NORM, S_DOT, -1, false));
+  PDG_TRY(fetch_state(ctx, scal, nullptr));
+  const double def0 = scal[S_DOT];
+  double def = def0;
+  const double target = opt->reduction * def0;
+  int total_inner = 0, outer = 0;
+  int st = PDG_OK;
+  while (def >= target && def >= 1e-30 && outer < opt->max_outer) {
+    if (!std::isfinite(def)) { st = set_error(PDG_ENONFINITE, "non-finite defect"); break; }
+    // d32 = d / |d|
+    k_set_scal<<<1, 1, 0, ctx->stream>>>(rc.scal, S_SCALE, def);
+    PDG_TRY(vec_to_f32_scaled(ctx, n, d, d32, rc.scal));
+    PDG_TRY(vec_fill<float>(ctx, n, c32, 0.f));
+    KrylovOut o{};
+    PDG_TRY(krylov_device<float>(ctx, opt->method, c32, d32, ctx->w32, opt->inner_reduction,
+                                 opt->inner_maxit, transpose, &o));
+    total_inner += o.iterations;
+    if (o.state == 2 || o.state == 3) { st = state_status(o.state); break; }
+    // z += |d| c32 ; d = rhs - J z
+    k_set_scal<<<1, 1, 0, ctx->stream>>>(rc.scal, S_SCALE, def);
+    PDG_TRY(vec_add_f32_scaled(ctx, n, c32, z, rc.scal, 1.0));
+    PDG_TRY(op_launch<double>(ctx, z, d, rhs, -1.0, 0, transpose, nullptr));
+    PDG_TRY(red_dot(ctx, rc, n, d, d, nullptr, nullptr, FIN_NORM, S_DOT, -1, false));
+    PDG_TRY(fetch_state(ctx, scal, nullptr));
+    def = scal[S_DOT];
+    outer++;
+    if (opt->verbose)
+      std::fprintf(stderr, "pdg mixed: outer %d inner %d defect %.3e (reduction %.3e)\n", outer,
+                   o.iterations, def, def / def0);
+  }
+  PDG_TRY(vec_copy<double>(ctx, n, d, r));
+  cudaEventRecord(ctx->ev1, ctx->stream);
+  cudaEventSynchronize(ctx->ev1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  res->converged = st == PDG_OK && (def < target || def < 1e-30);
+  res->iterations = total_inner;
+  res->outer_iterations = outer;
+  res->elapsed = ms * 1e-3;
+  res->first_defect = def0;
+  res->defect = def;
+  res->reduction = def0 > 0 ? def / def0 : 0.0;
+  res->conv_rate = total_inner > 0 ? std::pow(res->reduction, 1.0 / total_inner) : 0.0;
+  res->status = st;
+  if (st) return st;
+  return res->converged ? PDG_OK
+                        : set_error(PDG_ENOTCONVERGED, "defect correction did not converge");
+}
+
+// ---- host-pointer staging --------------------------------------------------
+static bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+template <typename T>
+struct Staged {
+  T *dev;
+  T *host;
+  size_t n;
+  bool staged;
+};
+
+template <typename T>
+static int stage_in(pdg_context *ctx, const T *p, size_t n, T *buf, bool copy, Staged<T> *s) {
+  s->n = n;
+  if (is_device_ptr(p)) {
+    s->dev = const_cast<T *>(p);
+    s->host = nullptr;
+    s->staged = false;
+    return PDG_OK;
+  }
+  s->dev = buf;
+  s->host = const_cast<T *>(p);
+  s->staged = true;
+  if (copy)
+    PDG_CUDA_TRY(cudaMemcpyAsync(buf, p, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+  return PDG_OK;
+}
+template <typename T>
+static int stage_out(pdg_context *ctx, const Staged<T> &s) {
+  if (!s.staged) return PDG_OK;
+  PDG_CUDA_TRY(cudaMemcpyAsync(s.host, s.dev, s.n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return PDG_OK;
+}
+
+static int upload(pdg_context *ctx, double **dst, const double *src, size_t n) {
+  if (!src) {
+    if (*dst) cudaFree(*dst);
+    *dst = nullptr;
+    return PDG_OK;
+  }
+  if (!*dst) PDG_CUDA_TRY(cudaMalloc(dst, n * sizeof(double)));
+  PDG_CUDA_TRY(cudaMemcpyAsync(*dst, src, n * sizeof(double),
+                               is_device_ptr(src) ? cudaMemcpyDeviceToDevice
+                                                  : cudaMemcpyHostToDevice,
+                               ctx->stream));
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return PDG_OK;
+}
+
+__global__ void k_perm(long n, const double *__restrict__ src, int is_log,
+                       double *__restrict__ K64, float *__restrict__ K32) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = is_log ? exp(src[i]) : src[i];
+  K64[i] = v;
+  K32[i] = (float)v;
+}
+
+static void invalidate(pdg_context *ctx, bool operator_changed) {
+  ctx->r0_valid = 0;
+  if (operator_changed) {
+    ctx->prec[0].ready = 0;
+    ctx->prec[1].ready = 0;
+  }
+}
+
+}  // namespace pdg
+
+using namespace pdg;
+
+#define PDG_CHECK_CTX(ctx)                                                     \
+  do {                                                                         \
+    if (!(ctx)) return set_error(PDG_EINVAL, "null context");                 \
+    PDG_CUDA_TRY(cudaSetDevice((ctx)->device));                                \
+  } while (0)
+
+extern "C" {
+
+const char *pdg_last_error(void) { return g_err.c_str(); }
+
+void pdg_default_solver_options(pdg_solver_options *o) {
+  if (!o) return;
+  o->method = PDG_CG;
+  o->preconditioner = PDG_PREC_BJ_FDM;
+  o->reduction = 1e-10;
+  o->min_defect = 1e-99;
+  o->maxit = 5000;
+  o->mixed = 0;
+  o->inner_reduction = 1e-4;
+  o->inner_maxit = 5000;
+  o->max_outer = 30;
+  o->verbose = 0;
+}
+
+int pdg_create(const pdg_config *cfg, pdg_context **out) {
+  if (!cfg || !out) return set_error(PDG_EINVAL, "null argument");
+  *out = nullptr;
+  if (cfg->dim < 2 || cfg->dim > 3) return set_error(PDG_EINVAL, "dim must be 2 or 3");
+  if (cfg->degree < 1 || cfg->degree > kMaxDeg)
+    return set_error(PDG_EUNSUPPORTED, "degree must be 1..4");
+  for (int j = 0; j < cfg->dim; j++) {
+    if (cfg->cells[j] < 1) return set_error(PDG_EINVAL, "cells must be >= 1");
+    if (!(cfg->extent[j] > 0)) return set_error(PDG_EINVAL, "extent must be > 0");
+  }
+  if (cfg->method < PDG_NIPG || cfg->method > PDG_IIPG)
+    return set_error(PDG_EINVAL, "bad method");
+  if (cfg->weights != PDG_WEIGHTS_ON && cfg->weights != PDG_WEIGHTS_OFF)
+    return set_error(PDG_EINVAL, "bad weights");
+  for (int s = 0; s < 2 * cfg->dim; s++) {
+    const int b = cfg->bctype[s];
+    if (b != PDG_BC_DIRICHLET && b != PDG_BC_NEUMANN && b != PDG_BC_OUTFLOW && b != PDG_BC_NONE)
+      return set_error(PDG_EINVAL, "bad boundary type");
+  }
+  PDG_CUDA_TRY(cudaSetDevice(cfg->device));
+  pdg_context *c = new pdg_context;
+  std::memset(c, 0, sizeof(*c));
+  c->cfg = *cfg;
+  c->device = cfg->device;
+  c->dim = cfg->dim;
+  c->k = cfg->degree;
+  c->N = c->k + 1;
+  c->nb = 1;
+  c->nqv = 1;
+  c->nqf = 1;
+  c->ncell = 1;
+  for (int j = 0; j < c->dim; j++) {
+    c->nb *= c->N;
+    c->ncell *= cfg->cells[j];
+    c->h[j] = cfg->extent[j] / cfg->cells[j];
+  }
+  for (int j = c->dim; j < 3; j++) c->h[j] = 1.0;
+  c->nqv = c->nb;
+  for (int j = 0; j < c->dim - 1; j++) c->nqf *= c->N;
+  c->ndof = c->ncell * c->nb;
+  c->nbpts = 0;
+  for (int s = 0; s < 2 * c->dim; s++) {
+    long cnt = 1;
+    for (int j = 0; j < c->dim; j++)
+      if (j != s / 2) cnt *= cfg->cells[j];
+    c->nbpts += cnt * c->nqf;
+  }
+  c->theta = cfg->method == PDG_SIPG ? -1.0 : (cfg->method == PDG_NIPG ? 1.0 : 0.0);
+  c->pen_fac = cfg->alpha * c->k * (c->k + c->dim - 1);
+  auto fail = [&](int st) {
+    pdg_destroy(c);
+    return st;
+  };
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(set_error(PDG_ECUDA, "cudaStreamCreate failed"));
+  c->stream = c->own_stream;
+  cudaEventCreate(&c->ev0);
+  cudaEventCreate(&c->ev1);
+  // 1D tables
+  RhsTables t = make_rhs_tables(c);
+  const int N = c->N;
+  std::vector<double> tab(2 * N * N + 2 * N);
+  for (int i = 0; i < N; i++)
+    for (int a = 0; a < N; a++) {
+      double m = 0.0, s = 0.0;
+      for (int q = 0; q < N; q++) {
+        m += t.w[q] * lag(c->k, i, t.x[q]) * lag(c->k, a, t.x[q]);
+        s += t.w[q] * dlag(c->k, i, t.x[q]) * dlag(c->k, a, t.x[q]);
+      }
+      tab[i * N + a] = m;
+      tab[N * N + i * N + a] = s;
+    }
+  for (int a = 0; a < N; a++) {
+    tab[2 * N * N + a] = t.d0[a];
+    tab[2 * N * N + N + a] = t.d1[a];
+  }
+  std::vector<float> tab32(tab.begin(), tab.end());
+  std::vector<double> ones(c->ncell, 1.0);
+  std::vector<float> ones32(c->ncell, 1.0f);
+  if (cudaMalloc(&c->tab64, sizeof(double) * tab.size()) != cudaSuccess ||
+      cudaMalloc(&c->tab32, sizeof(float) * tab.size()) != cudaSuccess ||
+      cudaMalloc(&c->K64, sizeof(double) * c->ncell) != cudaSuccess ||
+      cudaMalloc(&c->K32, sizeof(float) * c->ncell) != cudaSuccess ||
+      cudaMalloc(&c->r0, sizeof(double) * c->ndof) != cudaSuccess ||
+      cudaMalloc(&c->red_partials, sizeof(double) * 2 * kRedBlocks) != cudaSuccess ||
+      cudaMalloc(&c->red_out, sizeof(double) * S_COUNT) != cudaSuccess ||
+      cudaMalloc(&c->d_flag, sizeof(int) * F_COUNT) != cudaSuccess ||
+      cudaMallocHost(&c->h_red, sizeof(double) * S_COUNT + sizeof(int) * F_COUNT) != cudaSuccess)
+    return fail(set_error(PDG_ECUDA, "device allocation failed"));
+  cudaMemcpy(c->tab64, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(c->tab32, tab32.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(c->K64, ones.data(), sizeof(double) * c->ncell, cudaMemcpyHostToDevice);
+  cudaMemcpy(c->K32, ones32.data(), sizeof(float) * c->ncell, cudaMemcpyHostToDevice);
+  cudaMemset(c->d_flag, 0, sizeof(int) * F_COUNT);
+  cudaMemset(c->red_out, 0, sizeof(double) * S_COUNT);
+  if (cudaDeviceSynchronize() != cudaSuccess) return fail(set_error(PDG_ECUDA, "init failed"));
+  c->r0_valid = 0;
+  *out = c;
+  return PDG_OK;
+}
+
+int pdg_destroy(pdg_context *c) {
+  if (!c) return PDG_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  prec_free(c, 0);
+  prec_free(c, 1);
+  void *bufs[] = {c->K64, c->K32, c->c64, c->c32, c->tab64, c->tab32, c->fq, c->fc, c->gq,
+                  c->jq, c->oq, c->r0, c->r0K, c->red_partials, c->red_out, c->d_flag,
+                  c->stage_a, c->stage_b};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  for (int i = 0; i < 8; i++) {
+    if (c->w64[i]) cudaFree(c->w64[i]);
+    if (c->w32[i]) cudaFree(c->w32[i]);
+  }
+  if (c->h_red) cudaFreeHost(c->h_red);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+  return PDG_OK;
+}
+
+int pdg_set_stream(pdg_context *ctx, void *stream) {
+  PDG_CHECK_CTX(ctx);
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  return PDG_OK;
+}
+
+int pdg_sizes(const pdg_context *ctx, long *ncell, int *nbasis, long *ndof, int *nqv,
+              long *nbp) {
+  if (!ctx) return set_error(PDG_EINVAL, "null context");
+  if (ncell) *ncell = ctx->ncell;
+  if (nbasis) *nbasis = ctx->nb;
+  if (ndof) *ndof = ctx->ndof;
+  if (nqv) *nqv = ctx->nqv;
+  if (nbp) *nbp = ctx->nbpts;
+  return PDG_OK;
+}
+
+int pdg_volume_points(const pdg_context *ctx, double *xyz) {
+  if (!ctx || !xyz) return set_error(PDG_EINVAL, "null argument");
+  double gx[kMaxN1], gw[kMaxN1];
+  gauss_legendre(ctx->N, gx, gw);
+  const int N = ctx->N, d = ctx->dim;
+  const int *nc = ctx->cfg.cells;
+  for (long e = 0; e < ctx->ncell; e++) {
+    int ix[3] = {(int)(e % nc[0]), (int)((e / nc[0]) % nc[1]), (int)(e / ((long)nc[0] * nc[1]))};
+    for (int q = 0; q < ctx->nqv; q++) {
+      int qa[3] = {q % N, (q / N) % N, q / (N * N)};
+      for (int j = 0; j < d; j++) xyz[(e * ctx->nqv + q) * d + j] = (ix[j] + gx[qa[j]]) * ctx->h[j];
+    }
+  }
+  return PDG_OK;
+}
+
+int pdg_boundary_points(const pdg_context *ctx, double *xyz) {
+  if (!ctx || !xyz) return set_error(PDG_EINVAL, "null argument");
+  double gx[kMaxN1], gw[kMaxN1];
+  gauss_legendre(ctx->N, gx, gw);
+  const int N = ctx->N, d = ctx->dim;
+  const int *nc = ctx->cfg.cells;
+  long base = 0;
+  for (int s = 0; s < 2 * d; s++) {
+    const int dir = s / 2, hi = s % 2;
+    int od[2], no = 0;
+    for (int j = 0; j < d; j++)
+      if (j != dir) od[no++] = j;
+    const long nf0 = nc[od[0]], nf1 = no > 1 ? nc[od[1]] : 1;
+    for (long f1 = 0; f1 < nf1; f1++)
+      for (long f0 = 0; f0 < nf0; f0++) {
+        const long fidx = f0 + nf0 * f1;
+        for (int q = 0; q < ctx->nqf; q++) {
+          const int qt[2] = {q % N, q / N};
+          double *pt = xyz + (base + fidx * ctx->nqf + q) * d;
+          pt[dir] = hi ? ctx->cfg.extent[dir] : 0.0;
+          pt[od[0]] = (f0 + gx[qt[0]]) * ctx->h[od[0]];
+          if (no > 1) pt[od[1]] = (f1 + gx[qt[1]]) * ctx->h[od[1]];
+        }
+      }
+    base += nf0 * nf1 * ctx->nqf;
+  }
+  return PDG_OK;
+}
+
+int pdg_set_permeability(pdg_context *ctx, const double *K, int is_log) {
+  PDG_CHECK_CTX(ctx);
+  if (!K) return set_error(PDG_EINVAL, "null permeability");
+  double *tmp = nullptr;
+  PDG_TRY(upload(ctx, &tmp, K, ctx->ncell));
+  k_perm<<<(unsigned)((ctx->ncell + 255) / 256), 256, 0, ctx->stream>>>(ctx->ncell, tmp, is_log,
+                                                                        ctx->K64, ctx->K32);
+  PDG_CUDA_TRY(cudaGetLastError());
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  cudaFree(tmp);
+  invalidate(ctx, true);
+  return PDG_OK;
+}
+
+int pdg_set_reaction(pdg_context *ctx, const double *c) {
+  PDG_CHECK_CTX(ctx);
+  PDG_TRY(upload(ctx, &ctx->c64, c, ctx->ncell));
+  if (!c) {
+    if (ctx->c32) cudaFree(ctx->c32);
+    ctx->c32 = nullptr;
+  } else {
+    if (!ctx->c32) PDG_CUDA_TRY(cudaMalloc(&ctx->c32, sizeof(float) * ctx->ncell));
+    PDG_TRY(vec_to_f32(ctx, ctx->ncell, ctx->c64, ctx->c32));
+    PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  }
+  invalidate(ctx, true);
+  return PDG_OK;
+}
+
+int pdg_set_velocity_modes(pdg_context *ctx, int nmodes, const double *modes) {
+  PDG_CHECK_CTX(ctx);
+  if (nmodes < 0 || nmodes > kMaxModes) return set_error(PDG_EINVAL, "nmodes must be 0..16");
+  if (nmodes > 0 && !modes) return set_error(PDG_EINVAL, "null modes");
+  if (nmodes > 0)
+    return set_error(PDG_EUNSUPPORTED, "convection is not implemented in this build");
+  ctx->vel.nmodes = 0;
+  invalidate(ctx, true);
+  return PDG_OK;
+}
+
+int pdg_set_source(pdg_context *ctx, const double *fq, const double *fc) {
+  PDG_CHECK_CTX(ctx);
+  PDG_TRY(upload(ctx, &ctx->fq, fq, (size_t)ctx->ncell * ctx->nqv));
+  PDG_TRY(upload(ctx, &ctx->fc, fc, ctx->ncell));
+  invalidate(ctx, false);
+  return PDG_OK;
+}
+
+int pdg_set_boundary_data(pdg_context *ctx, const double *g, const double *j, const double *o) {
+  PDG_CHECK_CTX(ctx);
+  PDG_TRY(upload(ctx, &ctx->gq, g, ctx->nbpts));
+  PDG_TRY(upload(ctx, &ctx->jq, j, ctx->nbpts));
+  PDG_TRY(upload(ctx, &ctx->oq, o, ctx->nbpts));
+  if (!g && ctx->r0K) {
+    cudaFree(ctx->r0K);
+    ctx->r0K = nullptr;
+  }
+  invalidate(ctx, false);
+  return PDG_OK;
+}
+
+static int ensure_stage(pdg_context *ctx) {
+  if (!ctx->stage_a) PDG_CUDA_TRY(cudaMalloc(&ctx->stage_a, sizeof(double) * ctx->ndof));
+  if (!ctx->stage_b) PDG_CUDA_TRY(cudaMalloc(&ctx->stage_b, sizeof(double) * ctx->ndof));
+  return PDG_OK;
+}
+
+// y = (acc ? y : 0) + alpha J x + (with_r0 ? R(0) : 0), host or device vectors
+static int apply_entry(pdg_context *ctx, const double *x, double *y, double alpha, int acc,
+                       int transpose, bool with_r0) {
+  PDG_CHECK_CTX(ctx);
+  if (!x || !y) return set_error(PDG_EINVAL, "null vector");
+  if (with_r0) PDG_TRY(ensure_r0(ctx));
+  const bool hx = !is_device_ptr(x), hy = !is_device_ptr(y);
+  if (hx || hy) PDG_TRY(ensure_stage(ctx));
+  Staged<double> sx, sy;
+  PDG_TRY(stage_in<double>(ctx, x, ctx->ndof, ctx->stage_a, true, &sx));
+  PDG_TRY(stage_in<double>(ctx, y, ctx->ndof, ctx->stage_b, acc != 0, &sy));
+  PDG_TRY(op_launch<double>(ctx, sx.dev, sy.dev, with_r0 ? ctx->r0 : nullptr, alpha, acc,
+                            transpose, nullptr));
+  PDG_TRY(stage_out<double>(ctx, sy));
+  return PDG_OK;
+}
+
+int pdg_residual(pdg_context *ctx, const double *x, double *r) {
+  return apply_entry(ctx, x, r, 1.0, 1, 0, true);
+}
+int pdg_jacobian_apply(pdg_context *ctx, const double *z, double *y) {
+  return apply_entry(ctx, z, y, 1.0, 1, 0, false);
+}
+int pdg_jacobian_apply_transpose(pdg_context *ctx, const double *z, double *y) {
+  return apply_entry(ctx, z, y, 1.0, 1, 1, false);
+}
+int pdg_apply(pdg_context *ctx, const double *x, double *y) {
+  return apply_entry(ctx, x, y, 1.0, 0, 0, false);
+}
+int pdg_applyscaleadd(pdg_context *ctx, double alpha, const double *x, double *y) {
+  return apply_entry(ctx, x, y, alpha, 1, 0, false);
+}
+
+int pdg_jacobian_apply_f32(pdg_context *ctx, const float *z, float *y) {
+  PDG_CHECK_CTX(ctx);
+  if (!z || !y) return set_error(PDG_EINVAL, "null vector");
+  if (!is_device_ptr(z) || !is_device_ptr(y))
+    return set_error(PDG_EINVAL, "pdg_jacobian_apply_f32 takes device pointers");
+  return op_launch<float>(ctx, z, y, nullptr, 1.f, 1, 0, nullptr);
+}
+
+int pdg_prec_setup(pdg_context *ctx, int kind, int precision) {
+  PDG_CHECK_CTX(ctx);
+  return prec_setup_impl(ctx, kind, precision);
+}
+
+static int prec_entry(pdg_context *ctx, const double *d, double *v, int transpose) {
+  PDG_CHECK_CTX(ctx);
+  if (!d || !v) return set_error(PDG_EINVAL, "null vector");
+  const bool hd = !is_device_ptr(d), hv = !is_device_ptr(v);
+  if (hd || hv) PDG_TRY(ensure_stage(ctx));
+  Staged<double> sd, sv;
+  PDG_TRY(stage_in<double>(ctx, d, ctx->ndof, ctx->stage_a, true, &sd));
+  PDG_TRY(stage_in<double>(ctx, v, ctx->ndof, ctx->stage_b, false, &sv));
+  PDG_TRY(prec_apply_impl<double>(ctx, sd.dev, sv.dev, transpose));
+  PDG_TRY(stage_out<double>(ctx, sv));
+  return PDG_OK;
+}
+int pdg_prec_apply(pdg_context *ctx, const double *d, double *v) {
+  return prec_entry(ctx, d, v, 0);
+}
+int pdg_prec_apply_transpose(pdg_context *ctx, const double *d, double *v) {
+  return prec_entry(ctx, d, v, 1);
+}
+int pdg_prec_apply_f32(pdg_context *ctx, const float *d, float *v) {
+  PDG_CHECK_CTX(ctx);
+  if (!d || !v) return set_error(PDG_EINVAL, "null vector");
+  if (!is_device_ptr(d) || !is_device_ptr(v))
+    return set_error(PDG_EINVAL, "pdg_prec_apply_f32 takes device pointers");
+  return prec_apply_impl<float>(ctx, d, v, 0);
+}
+
+static int dot_entry(pdg_context *ctx, const double *a, const double *b, double *out, bool norm) {
+  PDG_CHECK_CTX(ctx);
+  if (!a || !b || !out) return set_error(PDG_EINVAL, "null argument");
+  const bool ha = !is_device_ptr(a), hb = !is_device_ptr(b);
+  if (ha || hb) PDG_TRY(ensure_stage(ctx));
+  Staged<double> sa, sb;
+  PDG_TRY(stage_in<double>(ctx, a, ctx->ndof, ctx->stage_a, true, &sa));
+  PDG_TRY(stage_in<double>(ctx, b, ctx->ndof, ctx->stage_b, true, &sb));
+  const RedCtx rc = red_ctx(ctx);
+  PDG_TRY(red_dot(ctx, rc, ctx->ndof, sa.dev, sb.dev, nullptr, nullptr,
+                  norm ? FIN_NORM : FIN_STORE, S_DOT, -1, false));
+  double scal[S_COUNT];
+  PDG_TRY(fetch_state(ctx, scal, nullptr));
+  *out = scal[S_DOT];
+  return PDG_OK;
+}
+int pdg_norm(pdg_context *ctx, const double *v, double *out) {
+  return dot_entry(ctx, v, v, out, true);
+}
+int pdg_dot(pdg_context *ctx, const double *a, const double *b, double *out) {
+  return dot_entry(ctx, a, b, out, false);
+}
+
+static int check_opts(const pdg_solver_options *o) {
+  if (!o) return set_error(PDG_EINVAL, "null options");
+  if (o->method != PDG_CG && o->method != PDG_BICGSTAB) return set_error(PDG_EINVAL, "bad method");
+  if (o->maxit < 1 || (o->mixed && (o->inner_maxit < 1 || o->max_outer < 1)))
+    return set_error(PDG_EINVAL, "iteration caps must be >= 1");
+  if (!(o->reduction > 0)) return set_error(PDG_EINVAL, "reduction must be > 0");
+  return PDG_OK;
+}
+
+int pdg_krylov_solve(pdg_context *ctx, const pdg_solver_options *opt, double *z, double *r,
+                     pdg_solver_result *res) {
+  PDG_CHECK_CTX(ctx);
+  PDG_TRY(check_opts(opt));
+  if (!z || !r || !res) return set_error(PDG_EINVAL, "null argument");
+  std::memset(res, 0, sizeof(*res));
+  PDG_TRY(ensure_stage(ctx));
+  Staged<double> sz, sr;
+  PDG_TRY(stage_in<double>(ctx, z, ctx->ndof, ctx->stage_a, true, &sz));
+  PDG_TRY(stage_in<double>(ctx, r, ctx->ndof, ctx->stage_b, true, &sr));
+  const int st = solve_correction(ctx, opt, sz.dev, sr.dev, 0, res);
+  PDG_TRY(stage_out<double>(ctx, sz));
+  PDG_TRY(stage_out<double>(ctx, sr));
+  return st;
+}
+
+int pdg_solve_linear_problem(pdg_context *ctx, const pdg_solver_options *opt, double *x,
+                             pdg_solver_result *res) {
+  PDG_CHECK_CTX(ctx);
+  PDG_TRY(check_opts(opt));
+  if (!x || !res) return set_error(PDG_EINVAL, "null argument");
+  std::memset(res, 0, sizeof(*res));
+  PDG_TRY(ensure_stage(ctx));
+  PDG_TRY(ensure_work(ctx, opt->mixed != 0));
+  PDG_TRY(ensure_r0(ctx));
+  Staged<double> sx;
+  PDG_TRY(stage_in<double>(ctx, x, ctx->ndof, ctx->stage_a, true, &sx));
+  double *r = ctx->stage_b, *z = ctx->w64[7];
+  const long n = ctx->ndof;
+  // r = R(x)   (linearproblem.hh:245-246)
+  PDG_TRY(op_launch<double>(ctx, sx.dev, r, ctx->r0, 1.0, 0, 0, nullptr));
+  double defect = 0.0;
+  {
+    const RedCtx rc = red_ctx(ctx);
+    PDG_TRY(red_dot(ctx, rc, n, r, r, nullptr, nullptr, FIN_NORM, S_DOT, -1, false));
+    double scal[S_COUNT];
+    PDG_TRY(fetch_state(ctx, scal, nullptr));
+    defect = scal[S_DOT];
+  }
+  // red = max(reduction, min_defect / defect)   (:260)
+  pdg_solver_options o = *opt;
+  if (defect > 0 && opt->min_defect / defect > o.reduction) o.reduction = opt->min_defect / defect;
+  PDG_TRY(vec_fill<double>(ctx, n, z, 0.0));
+  const int st = solve_correction(ctx, &o, z, r, 0, res);
+  res->first_defect = defect;
+  // x -= z   (:294)
+  if (st == PDG_OK || st == PDG_ENOTCONVERGED) PDG_TRY(vec_axpy(ctx, n, -1.0, z, sx.dev));
+  PDG_TRY(stage_out<double>(ctx, sx));
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return st;
+}
+
+int pdg_adjoint_solve(pdg_context *ctx, const pdg_solver_options *opt, const double *rhs,
+                      double *lambda, pdg_solver_result *res) {
+  PDG_CHECK_CTX(ctx);
+  PDG_TRY(check_opts(opt));
+  if (!rhs || !lambda || !res) return set_error(PDG_EINVAL, "null argument");
+  std::memset(res, 0, sizeof(*res));
+  PDG_TRY(ensure_stage(ctx));
+  PDG_TRY(ensure_work(ctx, opt->mixed != 0));
+  Staged<double> sl;
+  PDG_TRY(stage_in<double>(ctx, lambda, ctx->ndof, ctx->stage_a, true, &sl));
+  double *r = ctx->stage_b;
+  if (is_device_ptr(rhs))
+    PDG_CUDA_TRY(cudaMemcpyAsync(r, rhs, sizeof(double) * ctx->ndof, cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
+  else
+    PDG_CUDA_TRY(cudaMemcpyAsync(r, rhs, sizeof(double) * ctx->ndof, cudaMemcpyHostToDevice,
+                                 ctx->stream));
+  const int transpose = ctx->cfg.method == PDG_SIPG ? 0 : 1;   // SIPG diffusion: J^T = J
+  pdg_solver_options o = *opt;
+  if (transpose && o.preconditioner == PDG_PREC_BJ_FDM) o.preconditioner = PDG_PREC_BJ_DENSE;
+  const int st = solve_correction(ctx, &o, sl.dev, r, transpose, res);
+  PDG_TRY(stage_out<double>(ctx, sl));
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return st;
+}
+
+int pdg_grad_logK(pdg_context *ctx, const double *u, const double *lambda, double *g) {
+  PDG_CHECK_CTX(ctx);
+  if (!u || !lambda || !g) return set_error(PDG_EINVAL, "null argument");
+  if (ctx->cfg.weights != PDG_WEIGHTS_ON)
+    return set_error(PDG_EUNSUPPORTED, "log-K gradient needs weightsOn");
+  PDG_TRY(ensure_r0(ctx));
+  PDG_TRY(ensure_stage(ctx));
+  Staged<double> su, sl;
+  PDG_TRY(stage_in<double>(ctx, u, ctx->ndof, ctx->stage_a, true, &su));
+  PDG_TRY(stage_in<double>(ctx, lambda, ctx->ndof, ctx->stage_b, true, &sl));
+  double *gd = nullptr;
+  const bool hg = !is_device_ptr(g);
+  if (hg) {
+    PDG_TRY(ensure_work(ctx, false));
+    gd = ctx->w64[0];
+  } else {
+    gd = g;
+  }
+  PDG_TRY(launch_grad_logK(ctx, su.dev, sl.dev, gd));
+  if (hg)
+    PDG_CUDA_TRY(cudaMemcpyAsync(g, gd, sizeof(double) * ctx->ncell, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return PDG_OK;
+}
+
+int pdg_grad_source(pdg_context *ctx, const double *lambda, double *g) {
+  PDG_CHECK_CTX(ctx);
+  if (!lambda || !g) return set_error(PDG_EINVAL, "null argument");
+  PDG_TRY(ensure_stage(ctx));
+  Staged<double> sl;
+  PDG_TRY(stage_in<double>(ctx, lambda, ctx->ndof, ctx->stage_b, true, &sl));
+  double *gd = nullptr;
+  const bool hg = !is_device_ptr(g);
+  if (hg) {
+    PDG_TRY(ensure_work(ctx, false));
+    gd = ctx->w64[0];
+  } else {
+    gd = g;
+  }
+  PDG_TRY(launch_grad_source(ctx, sl.dev, gd));
+  if (hg)
+    PDG_CUDA_TRY(cudaMemcpyAsync(g, gd, sizeof(double) * ctx->ncell, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return PDG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,158 @@
+// pdg_internal.cuh -- shared definitions of the GB300 matrix-free SIPG DG
+// library (context, kernel parameter blocks, launch helpers).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <type_traits>
+
+#include "../../include/pdg.h"
+
+namespace pdg {
+
+constexpr int kMaxDim = 3;
+constexpr int kMaxDeg = 4;
+constexpr int kMaxN1 = kMaxDeg + 1;
+constexpr int kMaxModes = 16;
+
+// Records a message for pdg_last_error() and returns the status code.
+int set_error(int status, const std::string &msg);
+
+#define PDG_CUDA_TRY(call)                                                      \
+  do {                                                                          \
+    cudaError_t _e = (call);                                                    \
+    if (_e != cudaSuccess)                                                      \
+      return ::pdg::set_error(PDG_ECUDA, std::string(#call) + ": " +            \
+                                             cudaGetErrorString(_e));           \
+  } while (0)
+
+#define PDG_TRY(call)                                                           \
+  do {                                                                          \
+    int _s = (call);                                                            \
+    if (_s != PDG_OK) return _s;                                                \
+  } while (0)
+
+// Velocity b(x) = sum_m coef_m sin(2 pi kv_m . x + phase_m).
+struct Velocity {
+  int nmodes;
+  double m[kMaxModes][7];
+};
+
+// Everything an operator kernel needs besides the vectors.  Passed by value.
+template <typename T>
+struct OpParams {
+  int nc[3];
+  long ncell;
+  T h[3];
+  T theta;        // SIPG -1, NIPG +1, IIPG 0
+  T pen_fac;      // alpha * k * (k + d - 1)
+  int weights;    // PDG_WEIGHTS_ON / OFF
+  int bc[6];
+  const T *K;     // per cell
+  const T *c;     // per cell or nullptr
+  const T *tab;   // 1D tables: Mhat[N*N], Shat[N*N], d0[N], d1[N]
+};
+
+// One launch of the cell operator:
+//   y = (accumulate ? y : 0) + alpha * J x + (add ? add : 0)
+template <typename T>
+struct ApplyArgs {
+  const T *x;
+  T *y;
+  const T *add;
+  T alpha;
+  int accumulate;
+  int transpose;   // J^T instead of J
+  int diag_only;   // drop the neighbour coupling (cell-block diagonal)
+  const int *skip; // if non-null and *skip != 0 the launch does nothing
+};
+
+// One cell-block Jacobi preconditioner instance (per precision).
+struct PrecData {
+  int kind, ready;
+  void *Q, *L;     // FDM factors [ncell][d][N*N], [ncell][d][N]
+  void *inv;       // dense inverses, column-major per block [ncell][nb*nb]
+};
+
+}  // namespace pdg
+
+struct pdg_context {
+  pdg_config cfg;
+  int dim, k, N, nb, nqv, nqf;
+  long ncell, ndof, nbpts;
+  double h[3];
+  double theta, pen_fac;
+  cudaStream_t stream;
+  cudaStream_t own_stream;
+  int device;
+
+  // coefficients on the device
+  double *K64;
+  float *K32;
+  double *c64;
+  float *c32;
+  double *tab64;
+  float *tab32;
+  pdg::Velocity vel;
+
+  // source and boundary data on the device
+  double *fq, *fc, *gq, *jq, *oq;
+  double *r0;          // R(0): source and boundary-data part of the residual
+  int r0_valid;
+
+  // preconditioner, one instance per precision (index PDG_F64 / PDG_F32)
+  pdg::PrecData prec[2];
+  double *r0K;             // K-proportional Dirichlet-data part of R(0)
+
+  // reduction scratch (deterministic two-stage reductions)
+  double *red_partials;    // [kRedBlocks * 4]
+  double *red_out;         // [16] device results
+  double *h_red;           // pinned host mirror [16]
+
+  // staging buffers for host pointers
+  double *stage_a, *stage_b;
+
+  // solver work vectors (lazily allocated)
+  double *w64[8];
+  float *w32[8];
+  int *d_flag;             // device-side convergence flag / counters
+  cudaEvent_t ev0, ev1;
+};
+
+namespace pdg {
+
+constexpr int kRedBlocks = 1024;   // partials per reduction (grid size cap)
+
+// kernels / launchers implemented in the .cu files
+template <typename T>
+int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c,
+                 const T *tab);
+int launch_rhs(pdg_context *ctx);
+int launch_grad_logK(pdg_context *ctx, const double *u, const double *lam, double *g);
+int launch_grad_source(pdg_context *ctx, const double *lam, double *g);
+
+template <typename T>
+OpParams<T> make_params(const pdg_context *ctx, const T *K, const T *c, const T *tab);
+
+// preconditioner
+int prec_setup_impl(pdg_context *ctx, int kind, int precision);
+template <typename T>
+int prec_apply_impl(pdg_context *ctx, const T *d, T *v, int transpose);
+template <typename T>
+int prec_apply_skip(pdg_context *ctx, const T *d, T *v, int transpose, const int *skip);
+void prec_free(pdg_context *ctx, int precision);
+
+// 1D tables on the Gauss points (host-built, passed by value to kernels)
+struct RhsTables {
+  double B[kMaxN1 * kMaxN1];   // B[q][a] = phi_a(xi_q)
+  double w[kMaxN1];            // Gauss weights on [0,1]
+  double x[kMaxN1];            // Gauss points on [0,1]
+  double d0[kMaxN1], d1[kMaxN1];
+};
+RhsTables make_rhs_tables(const pdg_context *ctx);
+double *rhs_r0K(pdg_context *ctx, bool alloc);
+
+}  // namespace pdg

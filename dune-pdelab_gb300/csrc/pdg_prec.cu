@@ -1,0 +1,572 @@
+// pdg_prec.cu -- cell-block Jacobi preconditioner.
+//
+// Reference: AssembledBlockJacobiPreconditionerLocalOperator
+// (backend/istl/matrixfree/assembledblockjacobipreconditioner.hh:162-233):
+// per cell, assemble the diagonal block D_e (volume + self part of every
+// face + boundary faces, localoperator/blockdiagonalwrapper.hh:225-257),
+// factor it (Eigen PartialPivLU) and apply D_e^{-1} per Krylov iteration.
+//
+// Two GPU forms:
+//  * FDM (fast diagonalisation).  With A = K I, no convection and
+//    axis-parallel cells, D_e is the Kronecker sum
+//      D_e = A_x (x) M_y (x) M_z + M_x (x) A_y (x) M_z + M_x (x) M_y (x) A_z
+//    (M_dir = h_dir Mhat; A_dir as in the operator kernel).  For symmetric
+//    A_dir (SIPG) the generalised eigenproblems A_dir q = lambda M_dir q give
+//    D_e^{-1} = (Qx (x) Qy (x) Qz) diag(1/(lx+ly+lz)) (Qx (x) Qy (x) Qz)^T,
+//    exactly the inverse of the reference's block, at d(N^2+N) values per
+//    cell instead of N^{2d}.
+//  * DENSE.  The block D_e is built column by column with the operator
+//    kernel restricted to the cell (neighbour coupling dropped, as
+//    BlockDiagonalLocalOperatorWrapper::jacobian_apply_skeleton does with a
+//    zero neighbour vector, blockdiagonalwrapper.hh:179-192) and inverted
+//    with partial pivoting; the apply is a dense per-cell matvec.  Exact for
+//    every block (non-symmetric methods, reaction, convection).
+#include <cmath>
+#include <vector>
+
+#include "pdg_ops.cuh"
+#include "pdg_vec.cuh"
+
+namespace pdg {
+
+// ---------------------------------------------------------------------------
+// FDM setup: one thread per (cell, direction), FP64.
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void k_fdm_setup(const OpParams<double> p, int dim, const double *__restrict__ Lhinv,
+                            double *__restrict__ Qout, double *__restrict__ Lout,
+                            float *__restrict__ Qout32, float *__restrict__ Lout32) {
+  const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= p.ncell * dim) return;
+  const long e = gid / dim;
+  const int dir = (int)(gid - e * dim);
+  const double *tM = p.tab, *tS = p.tab + N * N, *td0 = tS + N * N, *td1 = td0 + N;
+  int ix[3];
+  {
+    long r = e;
+    ix[0] = (int)(r % p.nc[0]); r /= p.nc[0];
+    ix[1] = (int)(r % p.nc[1]); r /= p.nc[1];
+    ix[2] = (int)r;
+  }
+  const long stride[3] = {1, (long)p.nc[0], (long)p.nc[0] * p.nc[1]};
+  const double Ke = p.K[e];
+  const double cc = p.c ? p.c[e] : 0.0;
+  double cf[18];
+  for (int f = 2 * dir; f < 2 * dir + 2; f++) {
+    const int d = f >> 1;
+    long nb;
+    if (f & 1) nb = ix[d] + 1 < p.nc[d] ? e + stride[d] : -1;
+    else nb = ix[d] > 0 ? e - stride[d] : -1;
+    face_coefficients(p, f, Ke, nb, cf + 3 * f);
+  }
+  double A[N][N];
+  for (int i = 0; i < N; i++)
+    for (int a = 0; a < N; a++) A[i][a] = a_entry<double, N>(p, dir, i, a, Ke, cc, cf, tM, tS, td0, td1);
+  // C = (1/h) Lhinv A Lhinv^T
+  const double h = p.h[dir];
+  double Tm[N][N], C[N][N];
+  for (int i = 0; i < N; i++)
+    for (int a = 0; a < N; a++) {
+      double s = 0.0;
+      for (int q = 0; q < N; q++) s += Lhinv[i * N + q] * A[q][a];
+      Tm[i][a] = s;
+    }
+  for (int i = 0; i < N; i++)
+    for (int a = 0; a < N; a++) {
+      double s = 0.0;
+      for (int q = 0; q < N; q++) s += Tm[i][q] * Lhinv[a * N + q];
+      C[i][a] = s / h;
+    }
+  // symmetrise (A is symmetric for SIPG; rounding only)
+  for (int i = 0; i < N; i++)
+    for (int a = i + 1; a < N; a++) {
+      const double m = 0.5 * (C[i][a] + C[a][i]);
+      C[i][a] = C[a][i] = m;
+    }
+  // cyclic Jacobi eigenvalue iteration: C = V diag V^T
+  double V[N][N];
+  for (int i = 0; i < N; i++)
+    for (int a = 0; a < N; a++) V[i][a] = i == a ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 50; sweep++) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < N; i++)
+      for (int a = 0; a < N; a++) {
+        tot += C[i][a] * C[i][a];
+        if (i != a) off += C[i][a] * C[i][a];
+      }
+    if (off <= 1e-32 * tot) break;
+    for (int pp = 0; pp < N - 1; pp++)
+      for (int qq = pp + 1; qq < N; qq++) {
+        const double apq = C[pp][qq];
+        if (fabs(apq) < 1e-300) continue;
+        const double theta = (C[qq][qq] - C[pp][pp]) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < N; k++) {
+          const double ckp = C[k][pp], ckq = C[k][qq];
+          C[k][pp] = c * ckp - s * ckq;
+          C[k][qq] = s * ckp + c * ckq;
+        }
+        for (int k = 0; k < N; k++) {
+          const double cpk = C[pp][k], cqk = C[qq][k];
+          C[pp][k] = c * cpk - s * cqk;
+          C[qq][k] = s * cpk + c * cqk;
+        }
+        for (int k = 0; k < N; k++) {
+          const double vkp = V[k][pp], vkq = V[k][qq];
+          V[k][pp] = c * vkp - s * vkq;
+          V[k][qq] = s * vkp + c * vkq;
+        }
+      }
+  }
+  // Q = (1/sqrt(h)) Lhinv^T V  (columns = M-orthonormal eigenvectors)
+  const double rs = 1.0 / sqrt(h);
+  const long qo = (e * dim + dir) * N * N, lo = (e * dim + dir) * N;
+  for (int i = 0; i < N; i++)
+    for (int a = 0; a < N; a++) {
+      double s = 0.0;
+      for (int q = 0; q < N; q++) s += Lhinv[q * N + i] * V[q][a];
+      s *= rs;
+      if (Qout) Qout[qo + i * N + a] = s;
+      if (Qout32) Qout32[qo + i * N + a] = (float)s;
+    }
+  for (int a = 0; a < N; a++) {
+    if (Lout) Lout[lo + a] = C[a][a];
+    if (Lout32) Lout32[lo + a] = (float)C[a][a];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FDM apply: v = (Qx (x) Qy (x) Qz) diag(1/(lx+ly+lz)) (Qx (x) Qy (x) Qz)^T d
+// ---------------------------------------------------------------------------
+template <int D, int N>
+struct PCfg {
+  static constexpr int N2 = N * N;
+  static constexpr int NB = D == 3 ? N * N * N : N * N;
+  static constexpr int TPC = D == 3 ? N * N : N;
+  static constexpr int CPB = (128 / TPC) > 0 ? (128 / TPC) : 1;
+  static constexpr int THREADS = CPB * TPC;
+  static constexpr int PER_CELL = 2 * NB + D * N2 + D * N;
+};
+
+template <typename T, int D, int N>
+__global__ void __launch_bounds__(PCfg<D, N>::THREADS)
+    k_fdm_apply(long ncell, const T *__restrict__ Q, const T *__restrict__ L,
+                const T *__restrict__ d, T *__restrict__ v, const int *__restrict__ skip) {
+  using C = PCfg<D, N>;
+  constexpr int N2 = C::N2, NB = C::NB, TPC = C::TPC, CPB = C::CPB;
+  if (skip && *skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int t = threadIdx.x, cs = t / TPC, l = t - cs * TPC;
+  T *S0 = reinterpret_cast<T *>(smem_raw) + cs * C::PER_CELL;
+  T *S1 = S0 + NB;
+  T *Qs = S1 + NB;       // [D][N2]
+  T *Ls = Qs + D * N2;   // [D][N]
+  const long e = (long)blockIdx.x * CPB + cs;
+  const bool active = e < ncell;
+  const long ee = active ? e : 0;
+  for (int i = l; i < D * N2; i += TPC) Qs[i] = Q[ee * D * N2 + i];
+  for (int i = l; i < D * N; i += TPC) Ls[i] = L[ee * D * N + i];
+  T col[N];
+#pragma unroll
+  for (int z = 0; z < N; z++) col[z] = d[ee * NB + z * TPC + l];
+  __syncthreads();
+  if constexpr (D == 3) {
+    const int tx = l % N, ty = l / N;
+    const T *Qx = Qs, *Qy = Qs + N2, *Qz = Qs + 2 * N2;
+    // z (registers): a[z'] = sum_z Qz[z][z'] col[z]
+    T a[N];
+#pragma unroll
+    for (int zp = 0; zp < N; zp++) {
+      T s = T(0);
+#pragma unroll
+      for (int z = 0; z < N; z++) s += Qz[z * N + zp] * col[z];
+      a[zp] = s;
+    }
+#pragma unroll
+    for (int z = 0; z < N; z++) S0[z * N2 + l] = a[z];
+    __syncthreads();
+    // y: b[z][ty'] = sum_y Qy[y][ty'] a[z][y][tx]
+#pragma unroll
+    for (int z = 0; z < N; z++) {
+      T s = T(0);
+#pragma unroll
+      for (int y = 0; y < N; y++) s += Qy[y * N + ty] * S0[z * N2 + y * N + tx];
+      S1[z * N2 + l] = s;
+    }
+    __syncthreads();
+    // x + scaling: c[z][ty][tx'] = sum_x Qx[x][tx'] b[z][ty][x] / (lx+ly+lz)
+#pragma unroll
+    for (int z = 0; z < N; z++) {
+      T s = T(0);
+#pragma unroll
+      for (int x = 0; x < N; x++) s += Qx[x * N + tx] * S1[z * N2 + ty * N + x];
+      a[z] = s / (Ls[tx] + Ls[N + ty] + Ls[2 * N + z]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int z = 0; z < N; z++) S0[z * N2 + l] = a[z];
+    __syncthreads();
+    // back x: e[z][ty][tx] = sum_x' Qx[tx][x'] c[z][ty][x']
+#pragma unroll
+    for (int z = 0; z < N; z++) {
+      T s = T(0);
+#pragma unroll
+      for (int x = 0; x < N; x++) s += Qx[tx * N + x] * S0[z * N2 + ty * N + x];
+      S1[z * N2 + l] = s;
+    }
+    __syncthreads();
+    // back y
+#pragma unroll
+    for (int z = 0; z < N; z++) {
+      T s = T(0);
+#pragma unroll
+      for (int y = 0; y < N; y++) s += Qy[ty * N + y] * S1[z * N2 + y * N + tx];
+      a[z] = s;
+    }
+    // back z (registers)
+    if (active) {
+#pragma unroll
+      for (int z = 0; z < N; z++) {
+        T s = T(0);
+#pragma unroll
+        for (int zp = 0; zp < N; zp++) s += Qz[z * N + zp] * a[zp];
+        v[e * NB + z * N2 + l] = s;
+      }
+    }
+  } else {
+    const int tx = l;
+    const T *Qx = Qs, *Qy = Qs + N2;
+    T a[N];
+#pragma unroll
+    for (int yp = 0; yp < N; yp++) {
+      T s = T(0);
+#pragma unroll
+      for (int y = 0; y < N; y++) s += Qy[y * N + yp] * col[y];
+      a[yp] = s;
+    }
+#pragma unroll
+    for (int y = 0; y < N; y++) S0[y * N + tx] = a[y];
+    __syncthreads();
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      T s = T(0);
+#pragma unroll
+      for (int x = 0; x < N; x++) s += Qx[x * N + tx] * S0[y * N + x];
+      a[y] = s / (Ls[tx] + Ls[N + y]);
+    }
+#pragma unroll
+    for (int y = 0; y < N; y++) S1[y * N + tx] = a[y];
+    __syncthreads();
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      T s = T(0);
+#pragma unroll
+      for (int x = 0; x < N; x++) s += Qx[tx * N + x] * S1[y * N + x];
+      a[y] = s;
+    }
+    if (active) {
+#pragma unroll
+      for (int y = 0; y < N; y++) {
+        T s = T(0);
+#pragma unroll
+        for (int yp = 0; yp < N; yp++) s += Qy[y * N + yp] * a[yp];
+        v[e * NB + y * N + tx] = s;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// DENSE: block columns, Gauss-Jordan inversion, matvec apply
+// ---------------------------------------------------------------------------
+__global__ void k_unit_field(long ncell, int nb, int j, double *__restrict__ x) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ncell * nb) x[i] = (i % nb) == j ? 1.0 : 0.0;
+}
+// D[e][i][j] = y[e][i]   (row-major blocks)
+__global__ void k_scatter_col(long ncell, int nb, int j, const double *__restrict__ y,
+                              double *__restrict__ D) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ncell * nb) return;
+  const long e = i / nb;
+  const int r = (int)(i - e * nb);
+  D[(e * nb + r) * nb + j] = y[i];
+}
+
+// In-place Gauss-Jordan inversion with row partial pivoting of one nb x nb
+// block per CTA (FP64 in shared memory, nb*nb + 2 nb values).  The column
+// permutation is undone at the end.  Writes the inverse transposed
+// (column-major) in precision T so that the apply reads it coalesced.
+// Singular blocks leave a zero inverse and raise *bad.
+template <typename T>
+__global__ void k_invert(int nb, const double *__restrict__ D, T *__restrict__ invT,
+                         int *__restrict__ bad) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double *A = reinterpret_cast<double *>(smem_raw);   // [nb][nb]
+  double *fcol = A + nb * nb;                         // [nb]
+  int *perm = reinterpret_cast<int *>(fcol + nb);     // [nb]
+  __shared__ int piv;
+  __shared__ double pval;
+  const long e = blockIdx.x;
+  const int t = threadIdx.x, nt = blockDim.x;
+  for (int i = t; i < nb * nb; i += nt) A[i] = D[e * nb * nb + i];
+  __syncthreads();
+  bool singular = false;
+  for (int c = 0; c < nb; c++) {
+    if (t == 0) {
+      int pr = c;
+      double best = fabs(A[c * nb + c]);
+      for (int r = c + 1; r < nb; r++) {
+        const double v = fabs(A[r * nb + c]);
+        if (v > best) { best = v; pr = r; }
+      }
+      piv = pr;
+      pval = A[pr * nb + c];
+      perm[c] = pr;
+    }
+    __syncthreads();
+    if (pval == 0.0) { singular = true; break; }
+    const int pr = piv;
+    if (pr != c)
+      for (int j = t; j < nb; j += nt) {
+        const double tmp = A[c * nb + j];
+        A[c * nb + j] = A[pr * nb + j];
+        A[pr * nb + j] = tmp;
+      }
+    __syncthreads();
+    const double inv = 1.0 / pval;
+    for (int j = t; j < nb; j += nt) A[c * nb + j] = j == c ? inv : A[c * nb + j] * inv;
+    for (int r = t; r < nb; r += nt) fcol[r] = r == c ? 0.0 : A[r * nb + c];
+    __syncthreads();
+    for (int i = t; i < nb * nb; i += nt) {
+      const int r = i / nb, j = i - r * nb;
+      if (r == c) continue;
+      const double base = j == c ? 0.0 : A[i];
+      A[i] = base - fcol[r] * A[c * nb + j];
+    }
+    __syncthreads();
+  }
+  if (singular) {
+    if (t == 0) atomicExch(bad, 1);
+    for (int i = t; i < nb * nb; i += nt) invT[e * nb * nb + i] = T(0);
+    return;
+  }
+  // undo the row interchanges as column interchanges, last first
+  for (int c = nb - 1; c >= 0; c--) {
+    const int pc = perm[c];
+    if (pc != c)
+      for (int r = t; r < nb; r += nt) {
+        const double tmp = A[r * nb + c];
+        A[r * nb + c] = A[r * nb + pc];
+        A[r * nb + pc] = tmp;
+      }
+    __syncthreads();
+  }
+  // invT[e][j][i] = Inv[i][j]
+  for (int i = t; i < nb * nb; i += nt) {
+    const int j = i / nb, r = i % nb;
+    invT[e * nb * nb + i] = (T)A[r * nb + j];
+  }
+}
+
+// v_e = Inv_e d_e (transpose: v_e = Inv_e^T d_e), one warp-multiple of
+// threads per cell, d_e staged in shared memory.
+template <typename T>
+__global__ void k_dense_apply(long ncell, int nb, const T *__restrict__ invT,
+                              const T *__restrict__ d, T *__restrict__ v, int transpose,
+                              const int *__restrict__ skip) {
+  if (skip && *skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *ds = reinterpret_cast<T *>(smem_raw);
+  const long e = blockIdx.x;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) ds[i] = d[e * nb + i];
+  __syncthreads();
+  const T *B = invT + e * (long)nb * nb;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    T s = T(0);
+    if (!transpose)
+      for (int j = 0; j < nb; j++) s += B[j * nb + i] * ds[j];
+    else
+      for (int j = 0; j < nb; j++) s += B[i * nb + j] * ds[j];
+    v[e * nb + i] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static int fdm_setup(pdg_context *ctx, int precision) {
+  const int N = ctx->N, dim = ctx->dim;
+  // Cholesky of Mhat (host, from the FP64 table) and its inverse
+  std::vector<double> tab(2 * N * N + 2 * N);
+  PDG_CUDA_TRY(cudaMemcpy(tab.data(), ctx->tab64, sizeof(double) * tab.size(),
+                          cudaMemcpyDeviceToHost));
+  std::vector<double> Lc(N * N, 0.0), Li(N * N, 0.0);
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j <= i; j++) {
+      double s = tab[i * N + j];
+      for (int q = 0; q < j; q++) s -= Lc[i * N + q] * Lc[j * N + q];
+      if (i == j) {
+        if (s <= 0) return set_error(PDG_EINVAL, "mass matrix not SPD");
+        Lc[i * N + i] = std::sqrt(s);
+      } else {
+        Lc[i * N + j] = s / Lc[j * N + j];
+      }
+    }
+  for (int c = 0; c < N; c++)
+    for (int i = 0; i < N; i++) {
+      double s = i == c ? 1.0 : 0.0;
+      for (int q = 0; q < i; q++) s -= Lc[i * N + q] * Li[q * N + c];
+      Li[i * N + c] = s / Lc[i * N + i];
+    }
+  double *dLi = nullptr;
+  PDG_CUDA_TRY(cudaMalloc(&dLi, sizeof(double) * N * N));
+  PDG_CUDA_TRY(cudaMemcpyAsync(dLi, Li.data(), sizeof(double) * N * N, cudaMemcpyHostToDevice,
+                               ctx->stream));
+  const size_t nq = (size_t)ctx->ncell * dim * N * N, nl = (size_t)ctx->ncell * dim * N;
+  const size_t es = precision == PDG_F64 ? sizeof(double) : sizeof(float);
+  PrecData &pd = ctx->prec[precision];
+  PDG_CUDA_TRY(cudaMalloc(&pd.Q, nq * es));
+  PDG_CUDA_TRY(cudaMalloc(&pd.L, nl * es));
+  OpParams<double> p = make_params<double>(ctx, ctx->K64, ctx->c64, ctx->tab64);
+  const long work = ctx->ncell * dim;
+  const unsigned blocks = (unsigned)((work + 127) / 128);
+  double *Q64 = precision == PDG_F64 ? (double *)pd.Q : nullptr;
+  double *L64 = precision == PDG_F64 ? (double *)pd.L : nullptr;
+  float *Q32 = precision == PDG_F32 ? (float *)pd.Q : nullptr;
+  float *L32 = precision == PDG_F32 ? (float *)pd.L : nullptr;
+  switch (N) {
+    case 2: k_fdm_setup<2><<<blocks, 128, 0, ctx->stream>>>(p, dim, dLi, Q64, L64, Q32, L32); break;
+    case 3: k_fdm_setup<3><<<blocks, 128, 0, ctx->stream>>>(p, dim, dLi, Q64, L64, Q32, L32); break;
+    case 4: k_fdm_setup<4><<<blocks, 128, 0, ctx->stream>>>(p, dim, dLi, Q64, L64, Q32, L32); break;
+    case 5: k_fdm_setup<5><<<blocks, 128, 0, ctx->stream>>>(p, dim, dLi, Q64, L64, Q32, L32); break;
+    default: cudaFree(dLi); return set_error(PDG_EUNSUPPORTED, "degree not compiled in");
+  }
+  PDG_CUDA_TRY(cudaGetLastError());
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  cudaFree(dLi);
+  return PDG_OK;
+}
+
+static int dense_setup(pdg_context *ctx, int precision) {
+  const long nc = ctx->ncell;
+  const int nb = ctx->nb;
+  const size_t blk = (size_t)nc * nb * nb;
+  double *D = nullptr, *x = nullptr, *y = nullptr;
+  int *bad = nullptr;
+  PDG_CUDA_TRY(cudaMalloc(&D, blk * sizeof(double)));
+  PDG_CUDA_TRY(cudaMalloc(&x, sizeof(double) * ctx->ndof));
+  PDG_CUDA_TRY(cudaMalloc(&y, sizeof(double) * ctx->ndof));
+  PDG_CUDA_TRY(cudaMalloc(&bad, sizeof(int)));
+  PDG_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
+  const unsigned g = (unsigned)((ctx->ndof + 255) / 256);
+  for (int j = 0; j < nb; j++) {
+    k_unit_field<<<g, 256, 0, ctx->stream>>>(nc, nb, j, x);
+    ApplyArgs<double> a{x, y, nullptr, 1.0, 0, 0, 1, nullptr};
+    PDG_TRY(launch_apply<double>(ctx, a, ctx->K64, ctx->c64, ctx->tab64));
+    k_scatter_col<<<g, 256, 0, ctx->stream>>>(nc, nb, j, y, D);
+  }
+  const size_t es = precision == PDG_F64 ? sizeof(double) : sizeof(float);
+  PrecData &pd = ctx->prec[precision];
+  PDG_CUDA_TRY(cudaMalloc(&pd.inv, blk * es));
+  const size_t smem = sizeof(double) * (nb * nb + nb) + sizeof(int) * nb;
+  if (precision == PDG_F64) {
+    PDG_CUDA_TRY(cudaFuncSetAttribute(k_invert<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_invert<double><<<(unsigned)nc, 128, smem, ctx->stream>>>(nb, D, (double *)pd.inv, bad);
+  } else {
+    PDG_CUDA_TRY(cudaFuncSetAttribute(k_invert<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_invert<float><<<(unsigned)nc, 128, smem, ctx->stream>>>(nb, D, (float *)pd.inv, bad);
+  }
+  PDG_CUDA_TRY(cudaGetLastError());
+  int hbad = 0;
+  PDG_CUDA_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  cudaFree(D); cudaFree(x); cudaFree(y); cudaFree(bad);
+  if (hbad) return set_error(PDG_EINVAL, "singular diagonal block");
+  return PDG_OK;
+}
+
+void prec_free(pdg_context *ctx, int precision) {
+  PrecData &pd = ctx->prec[precision];
+  if (pd.Q) cudaFree(pd.Q);
+  if (pd.L) cudaFree(pd.L);
+  if (pd.inv) cudaFree(pd.inv);
+  pd = PrecData{0, 0, nullptr, nullptr, nullptr};
+}
+
+int prec_setup_impl(pdg_context *ctx, int kind, int precision) {
+  if (precision != PDG_F64 && precision != PDG_F32)
+    return set_error(PDG_EINVAL, "precision must be PDG_F64 or PDG_F32");
+  prec_free(ctx, precision);
+  if (kind == PDG_PREC_NONE) {
+    ctx->prec[precision].kind = kind;
+    ctx->prec[precision].ready = 1;
+    return PDG_OK;
+  }
+  if (kind == PDG_PREC_BJ_FDM) {
+    if (ctx->cfg.method != PDG_SIPG)
+      return set_error(PDG_EUNSUPPORTED,
+                       "FDM block Jacobi needs symmetric blocks (SIPG); use PDG_PREC_BJ_DENSE");
+    PDG_TRY(fdm_setup(ctx, precision));
+  } else if (kind == PDG_PREC_BJ_DENSE) {
+    PDG_TRY(dense_setup(ctx, precision));
+  } else {
+    return set_error(PDG_EINVAL, "unknown preconditioner kind");
+  }
+  ctx->prec[precision].kind = kind;
+  ctx->prec[precision].ready = 1;
+  return PDG_OK;
+}
+
+template <typename T, int D, int N>
+static int fdm_apply_dn(pdg_context *ctx, const T *d, T *v, const int *skip) {
+  using C = PCfg<D, N>;
+  const size_t smem = sizeof(T) * C::CPB * C::PER_CELL;
+  const unsigned blocks = (unsigned)((ctx->ncell + C::CPB - 1) / C::CPB);
+  k_fdm_apply<T, D, N><<<blocks, C::THREADS, smem, ctx->stream>>>(
+      ctx->ncell, (const T *)ctx->prec[std::is_same<T, double>::value ? 0 : 1].Q,
+      (const T *)ctx->prec[std::is_same<T, double>::value ? 0 : 1].L, d, v, skip);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+
+template <typename T>
+int prec_apply_skip(pdg_context *ctx, const T *d, T *v, int transpose, const int *skip) {
+  const int pi = std::is_same<T, double>::value ? PDG_F64 : PDG_F32;
+  const PrecData &pd = ctx->prec[pi];
+  if (!pd.ready) return set_error(PDG_ESTATE, "preconditioner not set up in this precision");
+  if (pd.kind == PDG_PREC_NONE) return vec_copy<T>(ctx, ctx->ndof, d, v);
+  if (pd.kind == PDG_PREC_BJ_DENSE) {
+    const int nb = ctx->nb;
+    const int threads = ((nb + 31) / 32) * 32;
+    k_dense_apply<T><<<(unsigned)ctx->ncell, threads, sizeof(T) * nb, ctx->stream>>>(
+        ctx->ncell, nb, (const T *)pd.inv, d, v, transpose, skip);
+    PDG_CUDA_TRY(cudaGetLastError());
+    return PDG_OK;
+  }
+  // FDM blocks are symmetric: D^{-T} = D^{-1}
+  switch (ctx->dim * 10 + ctx->k) {
+    case 21: return fdm_apply_dn<T, 2, 2>(ctx, d, v, skip);
+    case 22: return fdm_apply_dn<T, 2, 3>(ctx, d, v, skip);
+    case 23: return fdm_apply_dn<T, 2, 4>(ctx, d, v, skip);
+    case 24: return fdm_apply_dn<T, 2, 5>(ctx, d, v, skip);
+    case 31: return fdm_apply_dn<T, 3, 2>(ctx, d, v, skip);
+    case 32: return fdm_apply_dn<T, 3, 3>(ctx, d, v, skip);
+    case 33: return fdm_apply_dn<T, 3, 4>(ctx, d, v, skip);
+    case 34: return fdm_apply_dn<T, 3, 5>(ctx, d, v, skip);
+    default: return set_error(PDG_EUNSUPPORTED, "dim/degree not compiled in");
+  }
+}
+
+template <typename T>
+int prec_apply_impl(pdg_context *ctx, const T *d, T *v, int transpose) {
+  return prec_apply_skip<T>(ctx, d, v, transpose, nullptr);
+}
+
+template int prec_apply_impl<double>(pdg_context *, const double *, double *, int);
+template int prec_apply_impl<float>(pdg_context *, const float *, float *, int);
+template int prec_apply_skip<double>(pdg_context *, const double *, double *, int, const int *);
+template int prec_apply_skip<float>(pdg_context *, const float *, float *, int, const int *);
+
+}  // namespace pdg

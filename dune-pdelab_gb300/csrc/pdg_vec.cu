@@ -1,0 +1,355 @@
+// pdg_vec.cu -- deterministic reductions with device-side Krylov scalars,
+// fused Krylov vector updates (dune-istl CGSolver / BiCGSTABSolver
+// recurrences), and precision conversions for defect correction.
+#include <cmath>
+
+#include "pdg_vec.cuh"
+
+namespace pdg {
+
+constexpr int kRedThreads = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of two values, result valid in thread 0.
+__device__ __forceinline__ void block_sum2(double &a, double &b) {
+  __shared__ double sa[kRedThreads / 32], sb[kRedThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  a = warp_sum(a);
+  b = warp_sum(b);
+  if (lane == 0) { sa[w] = a; sb[w] = b; }
+  __syncthreads();
+  if (w == 0) {
+    a = lane < (int)(blockDim.x >> 5) ? sa[lane] : 0.0;
+    b = lane < (int)(blockDim.x >> 5) ? sb[lane] : 0.0;
+    a = warp_sum(a);
+    b = warp_sum(b);
+  }
+}
+
+__device__ void run_finisher(const RedCtx &rc, int fin, int slot0, int slot1, double d0,
+                             double d1) {
+  double *s = rc.scal;
+  int *fl = rc.flags;
+  switch (fin) {
+    case FIN_STORE:
+      if (slot0 >= 0) s[slot0] = d0;
+      if (slot1 >= 0) s[slot1] = d1;
+      break;
+    case FIN_NORM:
+      s[slot0] = sqrt(d0);
+      break;
+    case FIN_DEF0: {
+      const double def = sqrt(d0);
+      s[S_DEF0] = def;
+      s[S_DEF] = def;
+      if (!isfinite(def)) fl[F_STATE] = 2;
+      else if (def < def * s[S_RED] || def < 1e-30) fl[F_STATE] = 1;
+      break;
+    }
+    case FIN_DEF: {
+      const double def = sqrt(d0);
+      s[S_DEF] = def;
+      if (!isfinite(def)) fl[F_STATE] = 2;
+      else if (def < s[S_DEF0] * s[S_RED] || def < 1e-30) fl[F_STATE] = 1;
+      if (slot0 == S_RHO) s[S_RHO] = s[S_RHONEW];   // BiCGStab: rho = rho_new
+      break;
+    }
+    case FIN_CG_LAMBDA:
+      s[S_ALPHA] = s[S_RHO] / d0;
+      break;
+    case FIN_CG_BETA:
+      s[S_BETA] = d0 / s[S_RHO];
+      s[S_RHO] = d0;
+      break;
+    case FIN_BI_RHONEW:
+      s[S_RHONEW] = d0;
+      if (fabs(s[S_RHO]) <= 1e-80 || fabs(s[S_OMEGA]) <= 1e-80) fl[F_STATE] = 3;
+      else s[S_BETA] = (d0 / s[S_RHO]) * (s[S_ALPHA] / s[S_OMEGA]);
+      break;
+    case FIN_BI_ALPHA:
+      s[S_H] = d0;
+      if (fabs(d0) < 1e-80) fl[F_STATE] = 3;
+      else s[S_ALPHA] = s[S_RHONEW] / d0;
+      break;
+    case FIN_BI_OMEGA:
+      s[S_TR] = d0;
+      s[S_TT] = d1;
+      s[S_OMEGA] = d0 / d1;
+      break;
+    default:
+      break;
+  }
+}
+
+// Shared tail of every reducing kernel: publish the block partial, let the
+// last block add all partials in block order and run the finisher.
+__device__ __forceinline__ void reduce_tail(const RedCtx &rc, double s0, double s1, int fin,
+                                            int slot0, int slot1) {
+  __shared__ bool is_last;
+  block_sum2(s0, s1);
+  if (threadIdx.x == 0) {
+    rc.partials[2 * blockIdx.x] = s0;
+    rc.partials[2 * blockIdx.x + 1] = s1;
+    __threadfence();
+    const int ticket = atomicAdd(&rc.flags[F_COUNTER], 1);
+    is_last = ticket == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  // fixed-order final sum: thread t adds partials t, t+blockDim, ... then tree
+  double a = 0.0, b = 0.0;
+  for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+    a += ((volatile double *)rc.partials)[2 * i];
+    b += ((volatile double *)rc.partials)[2 * i + 1];
+  }
+  block_sum2(a, b);
+  if (threadIdx.x == 0) {
+    run_finisher(rc, fin, slot0, slot1, a, b);
+    rc.flags[F_COUNTER] = 0;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_dot(long n, const T *__restrict__ a, const T *__restrict__ b, const T *__restrict__ c,
+          const T *__restrict__ d, RedCtx rc, int fin, int slot0, int slot1, int respect) {
+  if (respect && rc.flags[F_STATE]) return;
+  T s0 = T(0), s1 = T(0);
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    s0 += a[i] * b[i];
+    if (c) s1 += c[i] * d[i];
+  }
+  reduce_tail(rc, (double)s0, (double)s1, fin, slot0, slot1);
+}
+
+static unsigned red_grid(long n) {
+  long g = (n + kRedThreads * 8 - 1) / (kRedThreads * 8);
+  if (g < 1) g = 1;
+  if (g > kRedBlocks) g = kRedBlocks;
+  return (unsigned)g;
+}
+
+int red_dot(pdg_context *ctx, const RedCtx &rc, long n, const double *a, const double *b,
+            const double *c, const double *d, int fin, int slot0, int slot1,
+            bool respect_flag) {
+  k_dot<double><<<red_grid(n), kRedThreads, 0, ctx->stream>>>(n, a, b, c, d, rc, fin, slot0,
+                                                               slot1, respect_flag);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+
+int red_dot_f32(pdg_context *ctx, const RedCtx &rc, long n, const float *a, const float *b,
+                const float *c, const float *d, int fin, int slot0, int slot1,
+                bool respect_flag) {
+  k_dot<float><<<red_grid(n), kRedThreads, 0, ctx->stream>>>(n, a, b, c, d, rc, fin, slot0,
+                                                              slot1, respect_flag);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+
+// ---- fused Krylov updates ------------------------------------------------
+
+// x += lambda p ; r -= lambda q ; |r|^2 -> defect check   (CGSolver)
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_cg_xr(long n, T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
+            const T *__restrict__ q, RedCtx rc) {
+  if (rc.flags[F_STATE]) return;
+  const T lambda = (T)rc.scal[S_ALPHA];
+  T s = T(0);
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    x[i] += lambda * p[i];
+    const T ri = r[i] - lambda * q[i];
+    r[i] = ri;
+    s += ri * ri;
+  }
+  reduce_tail(rc, (double)s, 0.0, FIN_DEF, -1, -1);
+}
+
+// p = z + beta p   (CGSolver: p *= beta; p += q)
+template <typename T>
+__global__ void k_cg_p(long n, T *__restrict__ p, const T *__restrict__ z, RedCtx rc) {
+  if (rc.flags[F_STATE]) return;
+  const T beta = (T)rc.scal[S_BETA];
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    p[i] = beta * p[i] + z[i];
+}
+
+// BiCGSTABSolver: p = r (first half step) or p = beta (p - omega v) + r
+template <typename T>
+__global__ void k_bi_p(long n, T *__restrict__ p, const T *__restrict__ r,
+                       const T *__restrict__ v, RedCtx rc, int first) {
+  if (rc.flags[F_STATE]) return;
+  const T beta = (T)rc.scal[S_BETA], omega = (T)rc.scal[S_OMEGA];
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    p[i] = first ? r[i] : beta * (p[i] - omega * v[i]) + r[i];
+}
+
+// x += a y ; r -= a v ; defect check   (a = alpha or omega)
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+    k_bi_xr(long n, T *__restrict__ x, T *__restrict__ r, const T *__restrict__ y,
+            const T *__restrict__ v, RedCtx rc, int slot, int rho_update) {
+  if (rc.flags[F_STATE]) return;
+  const T aa = (T)rc.scal[slot];
+  T s = T(0);
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    x[i] += aa * y[i];
+    const T ri = r[i] - aa * v[i];
+    r[i] = ri;
+    s += ri * ri;
+  }
+  reduce_tail(rc, (double)s, 0.0, FIN_DEF, rho_update ? S_RHO : -1, -1);
+}
+
+__global__ void k_set_iter(RedCtx rc, double it) {
+  if (rc.flags[F_STATE]) return;
+  rc.scal[S_ITER] = it;
+}
+
+static unsigned ew_grid(long n) {
+  long g = (n + 255) / 256;
+  if (g > 152 * 64) g = 152 * 64;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+template <typename T>
+int cg_update_xr(pdg_context *ctx, const RedCtx &rc, long n, T *x, T *r, const T *p,
+                 const T *q) {
+  k_cg_xr<T><<<red_grid(n), kRedThreads, 0, ctx->stream>>>(n, x, r, p, q, rc);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+template <typename T>
+int cg_update_p(pdg_context *ctx, const RedCtx &rc, long n, T *p, const T *z) {
+  k_cg_p<T><<<ew_grid(n), 256, 0, ctx->stream>>>(n, p, z, rc);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+template <typename T>
+int bi_update_p(pdg_context *ctx, const RedCtx &rc, long n, T *p, const T *r, const T *v,
+                int first) {
+  k_bi_p<T><<<ew_grid(n), 256, 0, ctx->stream>>>(n, p, r, v, rc, first);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+template <typename T>
+int bi_update_half(pdg_context *ctx, const RedCtx &rc, long n, T *x, T *r, const T *y,
+                   const T *v) {
+  k_bi_xr<T><<<red_grid(n), kRedThreads, 0, ctx->stream>>>(n, x, r, y, v, rc, S_ALPHA, 0);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+template <typename T>
+int bi_update_full(pdg_context *ctx, const RedCtx &rc, long n, T *x, T *r, const T *y,
+                   const T *t) {
+  k_bi_xr<T><<<red_grid(n), kRedThreads, 0, ctx->stream>>>(n, x, r, y, t, rc, S_OMEGA, 1);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+int set_iter(pdg_context *ctx, const RedCtx &rc, double it) {
+  k_set_iter<<<1, 1, 0, ctx->stream>>>(rc, it);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+
+#define PDG_INST_UPD(T)                                                                     \
+  template int cg_update_xr<T>(pdg_context *, const RedCtx &, long, T *, T *, const T *,    \
+                               const T *);                                                  \
+  template int cg_update_p<T>(pdg_context *, const RedCtx &, long, T *, const T *);         \
+  template int bi_update_p<T>(pdg_context *, const RedCtx &, long, T *, const T *,          \
+                              const T *, int);                                              \
+  template int bi_update_half<T>(pdg_context *, const RedCtx &, long, T *, T *, const T *,  \
+                                 const T *);                                                \
+  template int bi_update_full<T>(pdg_context *, const RedCtx &, long, T *, T *, const T *,  \
+                                 const T *);
+PDG_INST_UPD(double)
+PDG_INST_UPD(float)
+
+// ---- plain vector kernels -------------------------------------------------
+
+template <typename T>
+__global__ void k_copy(long n, const T *__restrict__ s, T *__restrict__ d) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) d[i] = s[i];
+}
+template <typename T>
+__global__ void k_fill(long n, T *__restrict__ d, T v) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) d[i] = v;
+}
+__global__ void k_axpy(long n, double a, const double *__restrict__ x, double *__restrict__ y) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) y[i] += a * x[i];
+}
+__global__ void k_to_f32_scaled(long n, const double *__restrict__ x, float *__restrict__ y,
+                                const double *__restrict__ scal) {
+  const double s = 1.0 / scal[S_SCALE];
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    y[i] = (float)(x[i] * s);
+}
+__global__ void k_add_f32_scaled(long n, const float *__restrict__ x, double *__restrict__ y,
+                                 const double *__restrict__ scal, double sign) {
+  const double s = sign * scal[S_SCALE];
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    y[i] += s * (double)x[i];
+}
+__global__ void k_to_f32(long n, const double *__restrict__ x, float *__restrict__ y) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    y[i] = (float)x[i];
+}
+
+template <typename T>
+int vec_copy(pdg_context *ctx, long n, const T *src, T *dst) {
+  k_copy<T><<<ew_grid(n), 256, 0, ctx->stream>>>(n, src, dst);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+template <typename T>
+int vec_fill(pdg_context *ctx, long n, T *dst, T v) {
+  k_fill<T><<<ew_grid(n), 256, 0, ctx->stream>>>(n, dst, v);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+template int vec_copy<double>(pdg_context *, long, const double *, double *);
+template int vec_copy<float>(pdg_context *, long, const float *, float *);
+template int vec_fill<double>(pdg_context *, long, double *, double);
+template int vec_fill<float>(pdg_context *, long, float *, float);
+
+int vec_axpy(pdg_context *ctx, long n, double alpha, const double *x, double *y) {
+  k_axpy<<<ew_grid(n), 256, 0, ctx->stream>>>(n, alpha, x, y);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+int vec_to_f32_scaled(pdg_context *ctx, long n, const double *x, float *y, const double *scal) {
+  k_to_f32_scaled<<<ew_grid(n), 256, 0, ctx->stream>>>(n, x, y, scal);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+int vec_add_f32_scaled(pdg_context *ctx, long n, const float *x, double *y, const double *scal,
+                       double sign) {
+  k_add_f32_scaled<<<ew_grid(n), 256, 0, ctx->stream>>>(n, x, y, scal, sign);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+int vec_to_f32(pdg_context *ctx, long n, const double *x, float *y) {
+  k_to_f32<<<ew_grid(n), 256, 0, ctx->stream>>>(n, x, y);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+
+}  // namespace pdg

@@ -1,0 +1,376 @@
+"""Python binding of libpdg.so (include/pdg.h) over ctypes.
+
+The classes mirror the reference's interfaces for this path so that driver
+code keeps its shape:
+
+* ``GridOperator``      -- GridOperator::residual / jacobian_apply
+  (dune/pdelab/gridoperator/gridoperator.hh:176-205) on one GPU context;
+* ``OnTheFlyOperator``  -- ISTL LinearOperator apply / applyscaleadd
+  (dune/pdelab/backend/istl/seqistlsolverbackend.hh:45-100);
+* ``GridOperatorPreconditioner`` -- pre / apply
+  (dune/pdelab/backend/istl/matrixfree/gridoperatorpreconditioner.hh:45-84);
+* ``ISTLBackend_SEQ_MatrixFree_Base`` -- apply(z, r, reduction), norm, result
+  (dune/pdelab/backend/istl/matrixfree/backends.hh:62-143);
+* ``StationaryLinearProblemSolver`` -- apply / result
+  (dune/pdelab/stationary/linearproblem.hh:59-338).
+
+Vectors are numpy float64 arrays (host) or torch tensors on the GPU (device
+pointers are passed straight through).  Every failure raises ``PDGError``
+with the library's message, as the reference raises Dune exceptions.
+There is no CPU fallback: without the CUDA library nothing here works.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libpdg.so")
+
+PDG_OK, PDG_EINVAL, PDG_ECUDA, PDG_ENOTCONVERGED, PDG_EBREAKDOWN = 0, 1, 2, 3, 4
+PDG_ESTATE, PDG_EUNSUPPORTED, PDG_EOUTFLOW, PDG_ENONFINITE, PDG_ETIMEOUT = 5, 6, 7, 8, 9
+NIPG, SIPG, IIPG = 0, 1, 2
+WEIGHTS_ON, WEIGHTS_OFF = 0, 1
+BC_DIRICHLET, BC_NEUMANN, BC_OUTFLOW, BC_NONE = 1, -1, -2, -3
+CG, BICGSTAB = 0, 1
+PREC_NONE, PREC_BJ_FDM, PREC_BJ_DENSE = 0, 1, 2
+F64, F32 = 0, 1
+
+
+class PDGError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"pdg status {status}: {msg}")
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [("dim", C.c_int), ("degree", C.c_int), ("cells", C.c_int * 3),
+                ("extent", C.c_double * 3), ("method", C.c_int), ("weights", C.c_int),
+                ("alpha", C.c_double), ("bctype", C.c_int * 6), ("device", C.c_int)]
+
+
+class SolverOptions(C.Structure):
+    _fields_ = [("method", C.c_int), ("preconditioner", C.c_int),
+                ("reduction", C.c_double), ("min_defect", C.c_double), ("maxit", C.c_int),
+                ("mixed", C.c_int), ("inner_reduction", C.c_double),
+                ("inner_maxit", C.c_int), ("max_outer", C.c_int), ("verbose", C.c_int)]
+
+
+class SolverResult(C.Structure):
+    _fields_ = [("converged", C.c_int), ("iterations", C.c_int), ("elapsed", C.c_double),
+                ("reduction", C.c_double), ("conv_rate", C.c_double),
+                ("first_defect", C.c_double), ("defect", C.c_double),
+                ("outer_iterations", C.c_int), ("status", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# exported symbols and their signatures (every declaration of include/pdg.h)
+_vp = C.c_void_p
+_SIGS = {
+    "pdg_create": (C.c_int, [C.POINTER(Config), C.POINTER(_vp)]),
+    "pdg_destroy": (C.c_int, [_vp]),
+    "pdg_last_error": (C.c_char_p, []),
+    "pdg_default_solver_options": (None, [C.POINTER(SolverOptions)]),
+    "pdg_set_stream": (C.c_int, [_vp, _vp]),
+    "pdg_sizes": (C.c_int, [_vp, C.POINTER(C.c_long), C.POINTER(C.c_int), C.POINTER(C.c_long),
+                            C.POINTER(C.c_int), C.POINTER(C.c_long)]),
+    "pdg_volume_points": (C.c_int, [_vp, _vp]),
+    "pdg_boundary_points": (C.c_int, [_vp, _vp]),
+    "pdg_set_permeability": (C.c_int, [_vp, _vp, C.c_int]),
+    "pdg_set_reaction": (C.c_int, [_vp, _vp]),
+    "pdg_set_velocity_modes": (C.c_int, [_vp, C.c_int, _vp]),
+    "pdg_set_source": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_set_boundary_data": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "pdg_residual": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_jacobian_apply": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_jacobian_apply_f32": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_jacobian_apply_transpose": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_apply": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_applyscaleadd": (C.c_int, [_vp, C.c_double, _vp, _vp]),
+    "pdg_prec_setup": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "pdg_prec_apply": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_prec_apply_f32": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_prec_apply_transpose": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_norm": (C.c_int, [_vp, _vp, C.POINTER(C.c_double)]),
+    "pdg_dot": (C.c_int, [_vp, _vp, _vp, C.POINTER(C.c_double)]),
+    "pdg_krylov_solve": (C.c_int, [_vp, C.POINTER(SolverOptions), _vp, _vp,
+                                   C.POINTER(SolverResult)]),
+    "pdg_solve_linear_problem": (C.c_int, [_vp, C.POINTER(SolverOptions), _vp,
+                                           C.POINTER(SolverResult)]),
+    "pdg_adjoint_solve": (C.c_int, [_vp, C.POINTER(SolverOptions), _vp, _vp,
+                                    C.POINTER(SolverResult)]),
+    "pdg_grad_logK": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "pdg_grad_source": (C.c_int, [_vp, _vp, _vp]),
+}
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load libpdg.so; raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise PDGError(PDG_EUNSUPPORTED,
+                           f"{path} missing: build it with __graft_entry__.build()")
+        lib = C.CDLL(path)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _check(st, allow=()):
+    if st != PDG_OK and st not in allow:
+        msg = load().pdg_last_error()
+        raise PDGError(st, msg.decode() if msg else "")
+    return st
+
+
+def _ptr(v, dtype=np.float64):
+    """Raw address of a numpy array or torch tensor (contiguous, right dtype)."""
+    if v is None:
+        return None
+    if isinstance(v, np.ndarray):
+        if v.dtype != dtype or not v.flags["C_CONTIGUOUS"]:
+            raise TypeError(f"expected contiguous {dtype} array")
+        return v.ctypes.data
+    if hasattr(v, "data_ptr"):
+        if not v.is_contiguous():
+            raise TypeError("expected a contiguous tensor")
+        return v.data_ptr()
+    raise TypeError(f"unsupported vector type {type(v)}")
+
+
+def default_options(**kw):
+    o = SolverOptions()
+    load().pdg_default_solver_options(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class GridOperator:
+    """One DG problem on the GPU: YaspGrid + QkDG space + ConvectionDiffusionDG
+    + GridOperator of the reference, as a single context."""
+
+    def __init__(self, dim, degree, cells, extent=None, method=SIPG, weights=WEIGHTS_ON,
+                 alpha=1.0, bctype=None, device=0):
+        cfg = Config()
+        cfg.dim, cfg.degree = dim, degree
+        cells = list(cells) + [1] * (3 - len(cells))
+        extent = list(extent) if extent is not None else [1.0] * dim
+        extent = extent + [1.0] * (3 - len(extent))
+        for j in range(3):
+            cfg.cells[j] = cells[j]
+            cfg.extent[j] = extent[j]
+        cfg.method, cfg.weights, cfg.alpha = method, weights, alpha
+        bct = list(bctype) if bctype is not None else [BC_DIRICHLET] * 6
+        for j in range(6):
+            cfg.bctype[j] = bct[j] if j < len(bct) else BC_DIRICHLET
+        cfg.device = device
+        self.cfg = cfg
+        self.dim, self.degree = dim, degree
+        self._h = _vp()
+        _check(load().pdg_create(C.byref(cfg), C.byref(self._h)))
+        nc, nb, nd, nq, nbp = C.c_long(), C.c_int(), C.c_long(), C.c_int(), C.c_long()
+        _check(load().pdg_sizes(self._h, C.byref(nc), C.byref(nb), C.byref(nd),
+                                C.byref(nq), C.byref(nbp)))
+        self.ncell, self.nbasis, self.ndof = nc.value, nb.value, nd.value
+        self.nq_volume, self.nq_boundary = nq.value, nbp.value
+
+    def close(self):
+        if self._h:
+            load().pdg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- geometry ---------------------------------------------------------
+    def volume_points(self):
+        out = np.zeros((self.ncell, self.nq_volume, self.dim))
+        _check(load().pdg_volume_points(self._h, out.ctypes.data))
+        return out
+
+    def boundary_points(self):
+        out = np.zeros((self.nq_boundary, self.dim))
+        _check(load().pdg_boundary_points(self._h, out.ctypes.data))
+        return out
+
+    # -- parameters -------------------------------------------------------
+    def set_permeability(self, K, is_log=False):
+        K = np.ascontiguousarray(K, dtype=np.float64) if isinstance(K, (list, np.ndarray)) else K
+        _check(load().pdg_set_permeability(self._h, _ptr(K), int(is_log)))
+
+    def set_reaction(self, c):
+        c = None if c is None else np.ascontiguousarray(c, dtype=np.float64)
+        _check(load().pdg_set_reaction(self._h, _ptr(c)))
+
+    def set_velocity_modes(self, modes):
+        m = None if modes is None else np.ascontiguousarray(modes, dtype=np.float64).reshape(-1, 7)
+        n = 0 if m is None else m.shape[0]
+        _check(load().pdg_set_velocity_modes(self._h, n, _ptr(m)))
+
+    def set_source(self, fq=None, fc=None):
+        fq = None if fq is None else np.ascontiguousarray(fq, dtype=np.float64)
+        fc = None if fc is None else np.ascontiguousarray(fc, dtype=np.float64)
+        _check(load().pdg_set_source(self._h, _ptr(fq), _ptr(fc)))
+
+    def set_boundary_data(self, g=None, j=None, o=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+                for a in (g, j, o)]
+        _check(load().pdg_set_boundary_data(self._h, *[_ptr(a) for a in arrs]))
+
+    # -- GridOperator -----------------------------------------------------
+    def residual(self, x, r):
+        """r += R(x)"""
+        _check(load().pdg_residual(self._h, _ptr(x), _ptr(r)))
+        return r
+
+    def jacobian_apply(self, z, y):
+        """y += J z"""
+        _check(load().pdg_jacobian_apply(self._h, _ptr(z), _ptr(y)))
+        return y
+
+    def jacobian_apply_f32(self, z, y):
+        """y += J z in FP32 (device tensors)"""
+        _check(load().pdg_jacobian_apply_f32(self._h, _ptr(z, np.float32), _ptr(y, np.float32)))
+        return y
+
+    def jacobian_apply_transpose(self, z, y):
+        """y += J^T z"""
+        _check(load().pdg_jacobian_apply_transpose(self._h, _ptr(z), _ptr(y)))
+        return y
+
+    def norm(self, v):
+        out = C.c_double()
+        _check(load().pdg_norm(self._h, _ptr(v), C.byref(out)))
+        return out.value
+
+    def dot(self, a, b):
+        out = C.c_double()
+        _check(load().pdg_dot(self._h, _ptr(a), _ptr(b), C.byref(out)))
+        return out.value
+
+    def grad_logK(self, u, lam, g):
+        _check(load().pdg_grad_logK(self._h, _ptr(u), _ptr(lam), _ptr(g)))
+        return g
+
+    def grad_source(self, lam, g):
+        _check(load().pdg_grad_source(self._h, _ptr(lam), _ptr(g)))
+        return g
+
+    def adjoint_solve(self, rhs, lam, options=None):
+        o = options or default_options()
+        res = SolverResult()
+        _check(load().pdg_adjoint_solve(self._h, C.byref(o), _ptr(rhs), _ptr(lam),
+                                        C.byref(res)), allow=(PDG_ENOTCONVERGED,))
+        return res
+
+    def zeros(self):
+        return np.zeros(self.ndof)
+
+
+class OnTheFlyOperator:
+    """ISTL LinearOperator over GridOperator::jacobian_apply."""
+
+    def __init__(self, go: GridOperator):
+        self.go = go
+
+    def apply(self, x, y):
+        """y = J x"""
+        _check(load().pdg_apply(self.go.handle, _ptr(x), _ptr(y)))
+
+    def applyscaleadd(self, alpha, x, y):
+        """y += alpha J x"""
+        _check(load().pdg_applyscaleadd(self.go.handle, float(alpha), _ptr(x), _ptr(y)))
+
+    def category(self):
+        return "sequential"
+
+
+class GridOperatorPreconditioner:
+    """ISTL Preconditioner: pre() sets up the cell-block Jacobi, apply(v, d)
+    computes v = D^{-1} d."""
+
+    def __init__(self, go: GridOperator, kind=PREC_BJ_FDM, precision=F64):
+        self.go, self.kind, self.precision = go, kind, precision
+        self._ready = False
+
+    def pre(self, v=None, d=None):
+        if not self._ready:
+            _check(load().pdg_prec_setup(self.go.handle, self.kind, self.precision))
+            self._ready = True
+
+    def apply(self, v, d):
+        if self.precision == F64:
+            _check(load().pdg_prec_apply(self.go.handle, _ptr(d), _ptr(v)))
+        else:
+            _check(load().pdg_prec_apply_f32(self.go.handle, _ptr(d, np.float32),
+                                             _ptr(v, np.float32)))
+
+    def post(self, v=None):
+        pass
+
+
+class ISTLBackend_SEQ_MatrixFree_Base:
+    """Matrix-free Krylov backend: apply(z, r, reduction) solves J z = r."""
+
+    isMatrixFree = True
+
+    def __init__(self, go: GridOperator, method=CG, preconditioner=PREC_BJ_FDM,
+                 maxiter=5000, verbose=0, mixed=False, inner_reduction=1e-4):
+        self.go = go
+        self.opts = default_options(method=method, preconditioner=preconditioner,
+                                    maxit=maxiter, verbose=verbose, mixed=int(mixed),
+                                    inner_reduction=inner_reduction)
+        self.res = SolverResult()
+
+    def apply(self, z, r, reduction):
+        self.opts.reduction = reduction
+        _check(load().pdg_krylov_solve(self.go.handle, C.byref(self.opts), _ptr(z), _ptr(r),
+                                       C.byref(self.res)), allow=(PDG_ENOTCONVERGED,))
+
+    def norm(self, v):
+        return self.go.norm(v)
+
+    def result(self):
+        return self.res
+
+
+class StationaryLinearProblemSolver:
+    """r = R(x); J z = r; x -= z   (linearproblem.hh:188-302)."""
+
+    def __init__(self, go: GridOperator, ls: ISTLBackend_SEQ_MatrixFree_Base, x, reduction,
+                 min_defect=1e-99, verbose=0):
+        self.go, self.ls, self.x = go, ls, x
+        self.reduction, self.min_defect = reduction, min_defect
+        self.res = SolverResult()
+
+    def apply(self, x=None):
+        if x is not None:
+            self.x = x
+        o = SolverOptions()
+        C.memmove(C.byref(o), C.byref(self.ls.opts), C.sizeof(SolverOptions))
+        o.reduction, o.min_defect = self.reduction, self.min_defect
+        _check(load().pdg_solve_linear_problem(self.go.handle, C.byref(o), _ptr(self.x),
+                                               C.byref(self.res)), allow=(PDG_ENOTCONVERGED,))
+        self.ls.res = self.res
+        return self.x
+
+    def result(self):
+        return self.res

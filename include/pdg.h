@@ -1,0 +1,244 @@
+/*
+ * pdg.h -- C ABI of the GB300-native matrix-free SIPG DG operator.
+ *
+ * One context holds one structured grid, one Q_k DG space and one
+ * ConvectionDiffusionDG operator (SIPG/NIPG/IIPG), all resident on one
+ * GPU.  Every entry point returns an int status (PDG_OK = 0); no C++
+ * exception crosses this boundary.  pdg_last_error() returns a message for
+ * the last failure on the calling thread.
+ *
+ * Vectors are Blocking::fixed DG vectors: DOF index = cell * (k+1)^d +
+ * local basis index, cells numbered lexicographically with x fastest
+ * (YaspGrid leaf order), local index x fastest (QkDG multiindex).
+ *
+ * Pointer convention: vector arguments may be device pointers (the fast
+ * path) or host pointers; host pointers are detected and staged through
+ * device buffers on the context's stream.  Nothing is allocated or freed
+ * on behalf of the caller: ownership of every buffer stays with the caller.
+ *
+ * Streams: every call is ordered on the context's stream (pdg_set_stream);
+ * calls that return host values (solves, norms, dots) synchronise it.
+ */
+#ifndef PDG_H
+#define PDG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- */
+/* status codes                                                      */
+/* ---------------------------------------------------------------- */
+enum {
+  PDG_OK = 0,
+  PDG_EINVAL = 1,          /* bad argument (null pointer, bad size, bad enum) */
+  PDG_ECUDA = 2,           /* a CUDA runtime call failed */
+  PDG_ENOTCONVERGED = 3,   /* solver reached maxit without the reduction */
+  PDG_EBREAKDOWN = 4,      /* Krylov breakdown (BiCGStab rho/omega/h tiny) */
+  PDG_ESTATE = 5,          /* call order violated (e.g. prec not set up) */
+  PDG_EUNSUPPORTED = 6,    /* configuration not compiled in / not supported */
+  PDG_EOUTFLOW = 7,        /* outflow boundary on inflow (convectiondiffusiondg.hh:802-806) */
+  PDG_ENONFINITE = 8,      /* NaN/Inf defect */
+  PDG_ETIMEOUT = 9         /* a bounded device wait ran out */
+};
+
+/* ConvectionDiffusionDGMethod::Type  (convectiondiffusiondg.hh:29-32) */
+enum { PDG_NIPG = 0, PDG_SIPG = 1, PDG_IIPG = 2 };
+/* ConvectionDiffusionDGWeights::Type (convectiondiffusiondg.hh:34-37) */
+enum { PDG_WEIGHTS_ON = 0, PDG_WEIGHTS_OFF = 1 };
+/* ConvectionDiffusionBoundaryConditions::Type
+   (convectiondiffusionparameter.hh:111-115) */
+enum { PDG_BC_DIRICHLET = 1, PDG_BC_NEUMANN = -1, PDG_BC_OUTFLOW = -2,
+       PDG_BC_NONE = -3 };
+
+/* Krylov methods (dune-istl CGSolver / BiCGSTABSolver as used by
+   ISTLBackend_SEQ_MatrixFree_Base, backend/istl/matrixfree/backends.hh:62-143) */
+enum { PDG_CG = 0, PDG_BICGSTAB = 1 };
+/* preconditioners */
+enum {
+  PDG_PREC_NONE = 0,
+  PDG_PREC_BJ_FDM = 1,     /* cell-block Jacobi, inverse applied by fast
+                              diagonalisation of the Kronecker-sum block
+                              (exact for symmetric separable blocks) */
+  PDG_PREC_BJ_DENSE = 2    /* cell-block Jacobi, explicit per-cell inverse
+                              (exact for every block, n^2 values per cell) */
+};
+/* precisions */
+enum { PDG_F64 = 0, PDG_F32 = 1 };
+
+typedef struct pdg_context pdg_context;
+
+/* Grid, space and operator configuration.  Mirrors the constructor
+   arguments of YaspGrid (unit-cube extent), QkDGLocalFiniteElementMap
+   (degree, dim) and ConvectionDiffusionDG (convectiondiffusiondg.hh:87-101:
+   method, weights, alpha; intorderadd = 0). */
+typedef struct pdg_config {
+  int dim;                 /* 2 or 3 */
+  int degree;              /* 1..4 */
+  int cells[3];            /* cells per direction (cells[2] ignored in 2D) */
+  double extent[3];        /* domain [0,extent[0]] x ... */
+  int method;              /* PDG_SIPG, PDG_NIPG, PDG_IIPG */
+  int weights;             /* PDG_WEIGHTS_ON / PDG_WEIGHTS_OFF */
+  double alpha;            /* penalty factor */
+  int bctype[6];           /* boundary type per side -x,+x,-y,+y,-z,+z */
+  int device;              /* CUDA device ordinal */
+} pdg_config;
+
+/* Solver options: ISTLBackend_SEQ_MatrixFree_Base(go, precgo, maxiter,
+   verbose) (backends.hh:71-72) plus StationaryLinearProblemSolver's
+   reduction / min_defect (stationary/linearproblem.hh:111-120). */
+typedef struct pdg_solver_options {
+  int method;              /* PDG_CG / PDG_BICGSTAB */
+  int preconditioner;      /* PDG_PREC_* */
+  double reduction;        /* defect reduction relative to the first defect */
+  double min_defect;       /* StationaryLinearProblemSolver min_defect */
+  int maxit;
+  int mixed;               /* 0: FP64 Krylov; 1: FP32 apply + FP32 block
+                              Jacobi inside an FP64 defect-correction loop */
+  double inner_reduction;  /* mixed: reduction of each FP32 inner solve */
+  int inner_maxit;         /* mixed: iteration cap of each inner solve */
+  int max_outer;           /* mixed: cap on defect-correction steps */
+  int verbose;
+} pdg_solver_options;
+
+/* LinearSolverResult (backend/solver.hh:29-51) +
+   StationaryLinearProblemSolverResult (stationary/linearproblem.hh:27-44) */
+typedef struct pdg_solver_result {
+  int converged;
+  int iterations;          /* Krylov iterations (sum of inner ones if mixed) */
+  double elapsed;          /* seconds, device clock */
+  double reduction;
+  double conv_rate;
+  double first_defect;
+  double defect;
+  int outer_iterations;    /* mixed: defect-correction steps */
+  int status;
+} pdg_solver_result;
+
+/* ---------------------------------------------------------------- */
+/* context                                                           */
+/* ---------------------------------------------------------------- */
+
+/* Replaces building YaspGrid + GridFunctionSpace + ConvectionDiffusionDG +
+   GridOperator (test/matrixfree/matrix_free_linear.cc:73-151). */
+int pdg_create(const pdg_config *cfg, pdg_context **out);
+int pdg_destroy(pdg_context *ctx);
+const char *pdg_last_error(void);
+void pdg_default_solver_options(pdg_solver_options *opt);
+
+/* Stream for all subsequent work (cudaStream_t passed as void*; NULL =
+   the context's own non-blocking stream). */
+int pdg_set_stream(pdg_context *ctx, void *stream);
+
+/* sizes: cells, basis functions per cell, DOFs, volume quadrature points
+   per cell ((k+1)^d) and boundary quadrature points in total */
+int pdg_sizes(const pdg_context *ctx, long *ncell, int *nbasis, long *ndof,
+              int *nq_volume, long *nq_boundary);
+
+/* Quadrature-point coordinates (host output) so that callers evaluate
+   their parameter functions where the operator integrates them:
+   volume [ncell][(k+1)^d][dim]; boundary points grouped by side, faces
+   lexicographic over the remaining directions, (k+1)^(d-1) points each. */
+int pdg_volume_points(const pdg_context *ctx, double *xyz);
+int pdg_boundary_points(const pdg_context *ctx, double *xyz);
+
+/* ---------------------------------------------------------------- */
+/* parameters (ConvectionDiffusionModelProblem, convectiondiffusion-   */
+/* parameter.hh:134-209; permeabilityIsConstantPerCell() == true)     */
+/* ---------------------------------------------------------------- */
+
+/* A(cell) = K_e I per cell; is_log != 0 means the array holds log K. */
+int pdg_set_permeability(pdg_context *ctx, const double *K, int is_log);
+/* c(cell) per cell (NULL = 0) */
+int pdg_set_reaction(pdg_context *ctx, const double *c);
+/* b(x) = sum_m coef_m sin(2 pi kv_m . x + phase_m); modes [n][7] =
+   kx ky kz phase cx cy cz (n = 0 clears the velocity). */
+int pdg_set_velocity_modes(pdg_context *ctx, int nmodes, const double *modes);
+/* f at volume quadrature points [ncell][(k+1)^d] (NULL = 0) plus a per-cell
+   constant fc [ncell] (NULL = 0).  Used by lambda_volume
+   (convectiondiffusiondg.hh:1047-1075). */
+int pdg_set_source(pdg_context *ctx, const double *fq, const double *fc);
+/* Boundary data at boundary quadrature points (NULL = 0): Dirichlet g,
+   Neumann j, outflow o (convectiondiffusiondg.hh:770-879). */
+int pdg_set_boundary_data(pdg_context *ctx, const double *g, const double *j,
+                          const double *o);
+
+/* ---------------------------------------------------------------- */
+/* operator (GridOperator, gridoperator/gridoperator.hh:176-205)      */
+/* ---------------------------------------------------------------- */
+
+/* GridOperator::residual(x, r): r += R(x)  (gridoperator.hh:176-181) */
+int pdg_residual(pdg_context *ctx, const double *x, double *r);
+/* GridOperator::jacobian_apply(z, y): y += J z  (gridoperator.hh:192-197) */
+int pdg_jacobian_apply(pdg_context *ctx, const double *z, double *y);
+/* Same in FP32 (the inner operator of the mixed-precision solve). */
+int pdg_jacobian_apply_f32(pdg_context *ctx, const float *z, float *y);
+/* Transposed apply y += J^T z (adjoint; no reference counterpart, derived
+   from jacobian_skeleton's sn/ns blocks, convectiondiffusiondg.hh:483-669) */
+int pdg_jacobian_apply_transpose(pdg_context *ctx, const double *z, double *y);
+/* OnTheFlyOperator::apply(x, y): y = J x
+   (backend/istl/seqistlsolverbackend.hh:66-76) */
+int pdg_apply(pdg_context *ctx, const double *x, double *y);
+/* OnTheFlyOperator::applyscaleadd(alpha, x, y): y += alpha J x
+   (seqistlsolverbackend.hh:78-90), without the full-vector temporary */
+int pdg_applyscaleadd(pdg_context *ctx, double alpha, const double *x, double *y);
+
+/* ---------------------------------------------------------------- */
+/* preconditioner (GridOperatorPreconditioner over                    */
+/* AssembledBlockJacobiPreconditionerLocalOperator,                   */
+/* backend/istl/matrixfree/gridoperatorpreconditioner.hh:45-84,       */
+/* assembledblockjacobipreconditioner.hh:162-233)                     */
+/* ---------------------------------------------------------------- */
+
+/* GridOperatorPreconditioner::pre: set up cell-block Jacobi of the given
+   kind in the given precision (PDG_F64 or PDG_F32). */
+int pdg_prec_setup(pdg_context *ctx, int kind, int precision);
+/* GridOperatorPreconditioner::apply(v, d): v = D^{-1} d */
+int pdg_prec_apply(pdg_context *ctx, const double *d, double *v);
+int pdg_prec_apply_f32(pdg_context *ctx, const float *d, float *v);
+/* v = D^{-T} d (adjoint solve preconditioner) */
+int pdg_prec_apply_transpose(pdg_context *ctx, const double *d, double *v);
+
+/* ---------------------------------------------------------------- */
+/* vector helpers (SequentialNorm, backend/solver.hh:16-25)           */
+/* ---------------------------------------------------------------- */
+int pdg_norm(pdg_context *ctx, const double *v, double *out);
+int pdg_dot(pdg_context *ctx, const double *a, const double *b, double *out);
+
+/* ---------------------------------------------------------------- */
+/* solvers                                                           */
+/* ---------------------------------------------------------------- */
+
+/* ISTLBackend_SEQ_MatrixFree_Base::apply(z, r, reduction)
+   (backends.hh:116-126): Krylov solve J z = r from the initial guess in z;
+   r is overwritten with the final defect. */
+int pdg_krylov_solve(pdg_context *ctx, const pdg_solver_options *opt,
+                     double *z, double *r, pdg_solver_result *res);
+
+/* StationaryLinearProblemSolver::apply (stationary/linearproblem.hh:
+   188-302): r = R(x); solve J z = r to max(reduction, min_defect/|r|);
+   x -= z.  With opt->mixed the correction is computed by FP32 Krylov
+   solves inside an FP64 defect-correction loop that stops on the true
+   FP64 defect. */
+int pdg_solve_linear_problem(pdg_context *ctx, const pdg_solver_options *opt,
+                             double *x, pdg_solver_result *res);
+
+/* ---------------------------------------------------------------- */
+/* adjoint (no reference counterpart)                                */
+/* ---------------------------------------------------------------- */
+
+/* Solve J^T lambda = rhs (lambda: initial guess in, solution out). */
+int pdg_adjoint_solve(pdg_context *ctx, const pdg_solver_options *opt,
+                      const double *rhs, double *lambda,
+                      pdg_solver_result *res);
+/* Fused per-cell gradient g_e = -lambda^T dR(u)/d(log K_e), the sum of the
+   volume, interior-face and Dirichlet-face contributions. */
+int pdg_grad_logK(pdg_context *ctx, const double *u, const double *lambda,
+                  double *g);
+/* g_e = -lambda^T dR/d(fc_e) = sum_i lambda_{e,i} int_e psi_i */
+int pdg_grad_source(pdg_context *ctx, const double *lambda, double *g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

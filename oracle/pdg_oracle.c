@@ -538,13 +538,15 @@ static int boundary_integral(const pdgo_problem *p, const tables *T, long e, int
 /* DefaultAssembler::assemble (gridoperator/default/assembler.hh:85-279):
    element loop, volume terms, then intersections; an interior face is
    visited once, from the cell with the larger index (:181). */
-static int assemble_vector(const pdgo_problem *p, const double *x, double *r, int jacobian_apply) {
+static int assemble_vector(const pdgo_problem *p, const double *x, double *r, int jacobian_apply,
+                           long e_begin, long e_end) {
   tables T;
   if (tables_init(p, &T)) return PDGO_EARG;
   int d = T.d, nb = T.nb;
   long nc = pdgo_ncell(p);
+  if (e_end > nc) e_end = nc;
   int st = PDGO_OK;
-  for (long e = 0; e < nc && !st; e++) {
+  for (long e = e_begin; e < e_end && !st; e++) {
     int ix[MAXD];
     cell_index(p, e, ix);
     if (!jacobian_apply) lambda_volume(p, &T, e, &r[e * nb]);
@@ -568,10 +570,14 @@ static int assemble_vector(const pdgo_problem *p, const double *x, double *r, in
 }
 
 int pdgo_jacobian_apply(const pdgo_problem *p, const double *z, double *y) {
-  return assemble_vector(p, z, y, 1);
+  return assemble_vector(p, z, y, 1, 0, pdgo_ncell(p));
+}
+int pdgo_jacobian_apply_range(const pdgo_problem *p, const double *z, double *y,
+                              long e_begin, long e_end) {
+  return assemble_vector(p, z, y, 1, e_begin, e_end);
 }
 int pdgo_residual(const pdgo_problem *p, const double *x, double *r) {
-  return assemble_vector(p, x, r, 0);
+  return assemble_vector(p, x, r, 0, 0, pdgo_ncell(p));
 }
 
 /* ------------------------------------------------------------------ */

@@ -102,6 +102,11 @@ int pdgo_boundary_points(const pdgo_problem *p, double *xyz);
 
 /* GridOperator::jacobian_apply(z, y): y += J z  (gridoperator.hh:192-197) */
 int pdgo_jacobian_apply(const pdgo_problem *p, const double *z, double *y);
+/* Same, restricted to the element loop over cells [e_begin, e_end) (the
+   faces those cells visit included); partial results over a partition of
+   the cells sum to the full apply. */
+int pdgo_jacobian_apply_range(const pdgo_problem *p, const double *z, double *y,
+                              long e_begin, long e_end);
 /* GridOperator::residual(x, r): r += R(x)  (gridoperator.hh:176-181) */
 int pdgo_residual(const pdgo_problem *p, const double *x, double *r);
 

@@ -71,6 +71,7 @@ def lib():
             "pdgo_boundary_points": (C.c_int, [P, _dp]),
             "pdgo_jacobian_apply": (C.c_int, [P, _dp, _dp]),
             "pdgo_residual": (C.c_int, [P, _dp, _dp]),
+            "pdgo_jacobian_apply_range": (C.c_int, [P, _dp, _dp, C.c_long, C.c_long]),
             "pdgo_assemble_jacobian": (C.c_int, [P, _dp]),
             "pdgo_blocks_apply": (C.c_int, [P, _dp, _dp, _dp]),
             "pdgo_blocks_apply_transpose": (C.c_int, [P, _dp, _dp, _dp]),
@@ -191,6 +192,10 @@ class Problem:
         z = np.ascontiguousarray(z, dtype=np.float64)
         y = np.zeros(self.ndof) if y is None else y
         _check(lib().pdgo_jacobian_apply(self.ref, _ptr(z), _ptr(y)))
+        return y
+
+    def jacobian_apply_range(self, z, y, e_begin, e_end):
+        _check(lib().pdgo_jacobian_apply_range(self.ref, _ptr(z), _ptr(y), e_begin, e_end))
         return y
 
     def residual(self, x, r=None):
