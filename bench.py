@@ -1,0 +1,547 @@
+#!/usr/bin/env python3
+"""Benchmark of the matrix-free SIPG DG operator on GB300.
+
+Headline workload (one "step" = one FP64 jacobian_apply over the whole
+grid): 3D SIPG diffusion, QkDG degree 2 (27 DoF/cell) on a 64^3 structured
+grid (7,077,888 DoF), cellwise log-normal K = exp(g), g ~ N(0,1) seeded,
+Dirichlet boundary, alpha = 3 (sigma = 3 k (k+d-1)).  Metric: GDoF/s.
+
+Also reported on the same line: the end-to-end number through the C ABI
+with host buffers (H2D input, D2H result every step), the roofline of the
+operator kernel (FP64 pipe; measured DFMA peak), the CPU baseline (the
+oracle restating the reference's loop structure, one core), and the solve
+metrics of the same problem: time to 1e-10 relative residual for the FP64
+CG + cell-block-Jacobi solve and for the FP32-apply / FP64-defect-correction
+solve, and the adjoint gradient cost relative to one forward solve.
+
+``--impl reference`` times the reference's CPU algorithm (the oracle port:
+PDELab itself cannot be built here) on all host cores for the same
+workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "dune-pdelab_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "GDoF/s matrix-free SIPG apply; time-to-1e-10 solve, mixed vs FP64 on GB300; grad/solve"
+WORKLOAD = dict(dim=3, degree=2, cells=64, alpha=3.0, seed=2)
+
+
+def flops_per_cell(dim, N):
+    """FP64/FP32 arithmetic of one cell in the operator kernel as written:
+    d-direction 1D operators + tangential mass contractions (8 N^4 MAC in
+    3D, 4 N^3 in 2D) plus neighbour traces and face expansions
+    (4 d N^d MAC); one MAC = 2 flops."""
+    mac = (8 * N ** 4 + 12 * N ** 3) if dim == 3 else (4 * N ** 3 + 8 * N ** 2)
+    return 2 * mac
+
+
+def survey_flops_per_dof(dim, N):
+    """Sum-factorised count of the reference algorithm (volume at quadrature
+    points + both-sided face quadrature): 8 d N^{d+1} + 16 d^2 N^d per cell."""
+    return (8 * dim * N ** (dim + 1) + 16 * dim * dim * N ** dim) / N ** dim
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index, period_ms=50):
+        self.index, self.period_ms = index, period_ms
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.1)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        self.f.close()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.f.name):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        finally:
+            os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows),
+                "power_w_max": max((float(r[3]) for r in rows
+                                    if r[3].replace(".", "").isdigit()), default=None)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_problem(pdg, np, device, wl=WORKLOAD):
+    n = wl["cells"]
+    go = pdg.GridOperator(wl["dim"], wl["degree"], (n,) * wl["dim"], alpha=wl["alpha"],
+                          device=device)
+    rng = np.random.default_rng(wl["seed"])
+    logK = rng.standard_normal(go.ncell)
+    go.set_permeability(logK, is_log=True)
+    return go, logK
+
+
+def fma_peaks(pdg):
+    import build_lib
+    lib = ctypes.CDLL(build_lib.PROBE_LIB)
+    lib.pdg_probe_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    out = {}
+    for prec, name, iters in ((0, "fp64", 2000), (1, "fp32", 20000)):
+        best = 0.0
+        for _ in range(3):
+            v = ctypes.c_double()
+            if lib.pdg_probe_fma_peak(prec, iters, ctypes.byref(v)) == 0:
+                best = max(best, v.value)
+        out[name] = best
+    return out
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def profile_traffic(key):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(key)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline_port(np, wl=WORKLOAD, applies=2):
+    import pdg_oracle as O
+    n = wl["cells"]
+    rng = np.random.default_rng(wl["seed"])
+    P = O.Problem(wl["dim"], wl["degree"], (n,) * wl["dim"], alpha=wl["alpha"])
+    P.set(K=np.exp(rng.standard_normal(P.ncell)))
+    x = np.random.default_rng(1).uniform(-1, 1, P.ndof)
+    y = np.zeros(P.ndof)
+    t0 = time.perf_counter()
+    for _ in range(applies):
+        P.jacobian_apply(x, y)
+    dt = time.perf_counter() - t0
+    return {"value": P.ndof * applies / dt / 1e9, "unit": "GDoF/s", "cores": 1, "kind": "port",
+            "sample": f"{applies} full FP64 jacobian_apply of the {n}^3 Q{wl['degree']} grid "
+                      f"({P.ndof} DoF) by the oracle's reference-faithful loops, "
+                      f"{dt:.1f} s on one core"}
+
+
+# --------------------------------------------------------------------------
+# reference arm: the oracle port on all host cores
+# --------------------------------------------------------------------------
+_W = {}
+
+
+def _ref_worker_init(wl, shm_x, ndof):
+    import numpy as np
+    from multiprocessing import shared_memory
+    import pdg_oracle as O
+    n = wl["cells"]
+    rng = np.random.default_rng(wl["seed"])
+    P = O.Problem(wl["dim"], wl["degree"], (n,) * wl["dim"], alpha=wl["alpha"])
+    P.set(K=np.exp(rng.standard_normal(P.ncell)))
+    sx = shared_memory.SharedMemory(name=shm_x)
+    _W.update(P=P, sx=sx, x=np.ndarray((ndof,), dtype=np.float64, buffer=sx.buf))
+
+
+def _ref_worker_apply(args):
+    import numpy as np
+    from multiprocessing import shared_memory
+    b, e, shm_y, ndof = args
+    sy = shared_memory.SharedMemory(name=shm_y)
+    y = np.ndarray((ndof,), dtype=np.float64, buffer=sy.buf)
+    y[:] = 0.0
+    _W["P"].jacobian_apply_range(_W["x"], y, b, e)
+    del y
+    sy.close()
+    return 0
+
+
+def run_reference(args, world, rank):
+    import multiprocessing as mp
+    from multiprocessing import shared_memory
+    import numpy as np
+    import pdg_oracle as O
+    if rank != 0:
+        return
+    O.build()
+    wl = WORKLOAD
+    n = wl["cells"]
+    ncell = n ** wl["dim"]
+    ndof = ncell * (wl["degree"] + 1) ** wl["dim"]
+    cores = os.cpu_count() or 1
+    sx = shared_memory.SharedMemory(create=True, size=ndof * 8)
+    x = np.ndarray((ndof,), dtype=np.float64, buffer=sx.buf)
+    x[:] = np.random.default_rng(1).uniform(-1, 1, ndof)
+    sys_ = [shared_memory.SharedMemory(create=True, size=ndof * 8) for _ in range(cores)]
+    ys = [np.ndarray((ndof,), dtype=np.float64, buffer=s.buf) for s in sys_]
+    bounds = np.linspace(0, ncell, cores + 1).astype(int)
+    jobs = [(int(bounds[i]), int(bounds[i + 1]), sys_[i].name, ndof) for i in range(cores)]
+    ctx = mp.get_context("spawn")
+    y = np.zeros(ndof)
+    with ctx.Pool(cores, initializer=_ref_worker_init, initargs=(wl, sx.name, ndof)) as pool:
+        def step():
+            pool.map(_ref_worker_apply, jobs, chunksize=1)
+            np.sum(ys, axis=0, out=y)
+        for _ in range(args.warmup):
+            step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        dt = time.perf_counter() - t0
+    del x, ys
+    sx.close(); sx.unlink()
+    for s in sys_:
+        s.close(); s.unlink()
+    value = ndof * args.steps / dt / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "GDoF/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded log-normal K, x ~ U(-1,1))",
+        "config": {"workload": f"sipg3d_q{wl['degree']}_{n}^3_fp64_apply", "ndof": ndof,
+                   "l2": "n/a (CPU)"},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "GDoF/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full FP64 jacobian_apply of the {n}^3 grid, "
+                                   f"cells split over {cores} processes, partial results "
+                                   f"summed (oracle restating the reference's loops; PDELab "
+                                   f"itself needs the DUNE core modules, absent here)"},
+        "e2e": {"value": value, "unit": "GDoF/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+# GB300 arm
+# --------------------------------------------------------------------------
+def run_gb300(args, world, rank, local):
+    import numpy as np
+    import torch
+    import __graft_entry__
+    if rank == 0:
+        __graft_entry__.build()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        dist.barrier()
+        __graft_entry__.build()
+    import pdg
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    go, logK = make_problem(pdg, np, local)
+    pdg.load().pdg_set_stream(go.handle, ctypes.c_void_p(stream.cuda_stream))
+    if args.solves_only:
+        if rank == 0:
+            print(json.dumps(solve_metrics(pdg, np, torch, go, stream, logK)), flush=True)
+        go.close()
+        return
+    op = pdg.OnTheFlyOperator(go)
+    ndof, ncell = go.ndof, go.ncell
+    N = WORKLOAD["degree"] + 1
+    f32 = args.precision == "f32"
+    dt_ = torch.float32 if f32 else torch.float64
+    esz = 4 if f32 else 8
+    # rotating input/output pairs so that every step streams from HBM
+    npairs = max(2, min(16, int(4 * 129e6 / (2 * esz * ndof)) + 1))
+    gen = torch.Generator(device=dev).manual_seed(1)
+    xs = [(torch.rand(ndof, dtype=torch.float64, device=dev, generator=gen) * 2 - 1).to(dt_)
+          for _ in range(npairs)]
+    ys = [torch.zeros(ndof, dtype=dt_, device=dev) for _ in range(npairs)]
+    torch.cuda.synchronize()
+    step_fn = (lambda x, y: go.jacobian_apply_f32(x, y)) if f32 else op.apply
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            step_fn(xs[i % npairs], ys[i % npairs])
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            barrier()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for i in range(args.steps):
+                step_fn(xs[i % npairs], ys[i % npairs])
+            e1.record(stream)
+            torch.cuda.synchronize()
+            barrier()
+        ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * ndof / (ms * 1e-3) / 1e9
+    clocks = clk.summary()
+
+    # end to end through the public API with host (pinned) buffers
+    xh = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
+    yh = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
+    xh.copy_(xs[0].double().cpu())
+    for _ in range(max(1, args.warmup)):
+        op.apply(xh, yh)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        op.apply(xh, yh)       # H2D x, kernel, D2H y, synchronise
+    t_e2e = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([t_e2e], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = {"value": world * ndof * args.steps / t_e2e / 1e9, "unit": "GDoF/s",
+           "h2d_bytes_per_step": ndof * 8, "d2h_bytes_per_step": ndof * 8}
+
+    if rank != 0:
+        go.close()
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    peaks = fma_peaks(pdg) if not args.no_probe else {"fp64": None, "fp32": None}
+    mp_ = measured_peaks()
+    fl = flops_per_cell(3, N) * ncell
+    achieved = fl / (ms * 1e-3) / 1e12
+    alg_bytes = 2 * esz * ndof + esz * ncell
+    pk = peaks["fp32" if f32 else "fp64"]
+    wname = f"sipg3d_q{WORKLOAD['degree']}_{WORKLOAD['cells']}^3_{args.precision}_apply"
+    roofline = {
+        "bound": "fp32" if f32 else "fp64", "achieved": achieved, "peak": pk,
+        "unit": "TFLOP/s", "frac": achieved / pk if pk else None,
+        "traffic": profile_traffic(wname),
+        "peak_source": "measured in this run: FMA throughput microbenchmark of the CUDA "
+                       "cores (libpdg_probe.so); MEASURED_PEAKS.json has no FP64/FP32 "
+                       "CUDA-core figure",
+        "flops_per_launch": fl, "flops_per_dof": fl / ndof,
+        "reference_algorithm_flops_per_dof": survey_flops_per_dof(3, N),
+        "algorithmic_bytes_per_launch": alg_bytes,
+        "hbm_achieved_gbs": alg_bytes / (ms * 1e-3) / 1e9,
+        "hbm_peak_gbs": mp_.get("hbm_gbs"),
+        "hbm_frac": (alg_bytes / (ms * 1e-3) / 1e9) / mp_["hbm_gbs"] if mp_.get("hbm_gbs") else None,
+        "fp32_fma_peak_tflops": peaks["fp32"],
+    }
+
+    extras = {}
+    if not args.no_solves:
+        extras = solve_metrics(pdg, np, torch, go, stream, logK)
+    if args.extended:
+        extras["solve_q3_96"] = c3_metrics(pdg, np, torch, stream)
+    cpu = cpu_baseline_port(np, WORKLOAD) if not args.no_cpu else None
+    go.close()
+    line = {
+        "metric": METRIC, "value": value, "unit": "GDoF/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": args.precision,
+        "data": "synthetic (seeded log-normal K per cell, x ~ U(-1,1))",
+        "config": {"workload": wname, "ndof": ndof, "cells": ncell,
+                   "degree": WORKLOAD["degree"], "alpha": 3.0,
+                   "l2": f"{npairs} rotating x/y pairs ({npairs * 2 * esz * ndof / 1e6:.0f} MB "
+                         f"> 129 MB L2)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": e2e, "gpu_launches": args.steps, "clocks": clocks, "roofline": roofline,
+        "cpu_baseline": cpu,
+    }
+    line.update(extras)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def smoothed_logK(np, n, seed=3, sigma=1.5):
+    """Log-permeability of the 96^3 Q3 workload: i.i.d. N(0,1) per cell,
+    3x3x3-cell box filter (zero-flux edges: the window is clipped at the
+    boundary), rescaled to standard deviation sigma."""
+    g = np.random.default_rng(seed).standard_normal((n, n, n))   # [z][y][x]
+    pad = np.pad(g, 1, mode="edge")
+    s = np.zeros_like(g)
+    for dz in range(3):
+        for dy in range(3):
+            for dx in range(3):
+                s += pad[dz:dz + n, dy:dy + n, dx:dx + n]
+    s /= 27.0
+    s = (s - s.mean()) / s.std() * sigma
+    return np.ascontiguousarray(s.ravel())
+
+
+def c3_metrics(pdg, np, torch, stream, inner_reduction=1e-4):
+    """96^3 Q3 (56.6M DoF): FP64 CG + block Jacobi vs FP32-apply / FP64
+    defect correction, both to 1e-10, f = 1; errors of the mixed solution
+    against the FP64 one."""
+    n = 96
+    go = pdg.GridOperator(3, 3, (n, n, n), alpha=3.0, device=stream.device.index or 0)
+    pdg.load().pdg_set_stream(go.handle, ctypes.c_void_p(stream.cuda_stream))
+    go.set_permeability(smoothed_logK(np, n), is_log=True)
+    go.set_source(fc=np.ones(go.ncell))
+    out = {"workload": "sipg3d_q3_96^3 (56.6M DoF), log-normal K box-filtered, sigma_g=1.5, "
+                       "f=1, CG + cell-block Jacobi (FDM), reduction 1e-10"}
+    sols = {}
+    for mixed in (True, False):
+        ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG, mixed=mixed, maxiter=20000,
+                                                 inner_reduction=inner_reduction)
+        u = torch.zeros(go.ndof, dtype=torch.float64, device=stream.device)
+        pdg.GridOperatorPreconditioner(go, precision=pdg.F32 if mixed else pdg.F64).pre()
+        slp = pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        slp.apply()
+        dt = time.perf_counter() - t0
+        r = slp.result()
+        key = "mixed" if mixed else "fp64"
+        sols[key] = u
+        out[f"{key}_s"] = dt
+        out[f"{key}_iterations"] = r.iterations
+        out[f"{key}_converged"] = bool(r.converged)
+        if mixed:
+            out["mixed_outer_iterations"] = r.outer_iterations
+    e = sols["mixed"] - sols["fp64"]
+    out["speedup_mixed_vs_fp64"] = out["fp64_s"] / out["mixed_s"]
+    out["mixed_vs_fp64_rel_l2"] = float(torch.linalg.norm(e) / torch.linalg.norm(sols["fp64"]))
+    out["mixed_vs_fp64_rel_max"] = float(e.abs().max() / sols["fp64"].abs().max())
+    go.close()
+    return out
+
+
+def solve_metrics(pdg, np, torch, go, stream, logK):
+    """Time-to-1e-10 of the FP64 and the mixed-precision solve (f = 1), and
+    the adjoint gradient cost relative to one forward solve."""
+    out = {}
+    go.set_source(fc=np.ones(go.ncell))
+    res = {}
+    for mixed in (False, True):
+        ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG, mixed=mixed)
+        for rep in range(2):      # first run includes one-time set-up (preconditioner, r0)
+            u = torch.zeros(go.ndof, dtype=torch.float64, device=stream.device)
+            slp = pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            slp.apply()
+            dt = time.perf_counter() - t0
+        r = slp.result()
+        res["mixed" if mixed else "fp64"] = (dt, r, u)
+    (t64, r64, u64), (tmx, rmx, umx) = res["fp64"], res["mixed"]
+    err = (umx - u64)
+    out["solve"] = {
+        "workload": "same grid and K, f = 1, CG + cell-block Jacobi (FDM), reduction 1e-10",
+        "fp64_s": t64, "fp64_iterations": r64.iterations, "fp64_converged": bool(r64.converged),
+        "mixed_s": tmx, "mixed_inner_iterations": rmx.iterations,
+        "mixed_outer_iterations": rmx.outer_iterations, "mixed_converged": bool(rmx.converged),
+        "speedup_mixed_vs_fp64": t64 / tmx,
+        "mixed_vs_fp64_rel_l2": float(torch.linalg.norm(err) / torch.linalg.norm(u64)),
+        "mixed_vs_fp64_rel_max": float(err.abs().max() / u64.abs().max()),
+    }
+    # adjoint: J = 1/2 |u - u_obs|^2, gradient w.r.t. log K
+    rng = np.random.default_rng(5)
+    u_obs = u64 * (1 + 0.01 * torch.tensor(rng.standard_normal(go.ndof), device=u64.device))
+    opts = pdg.default_options(mixed=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    u = torch.zeros_like(u64)
+    ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG, mixed=True)
+    pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10).apply()
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    lam = torch.zeros_like(u)
+    go.adjoint_solve(u - u_obs, lam, opts)
+    g = torch.zeros(go.ncell, dtype=torch.float64, device=u.device)
+    go.grad_logK(u, lam, g)
+    torch.cuda.synchronize()
+    t_adj = time.perf_counter() - t0
+    out["adjoint"] = {"forward_solve_s": t_fwd, "adjoint_solve_plus_grad_s": t_adj,
+                      "grad_over_solve": t_adj / t_fwd,
+                      "total_over_solve": (t_fwd + t_adj) / t_fwd}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--no-solves", action="store_true", help="skip solve/adjoint metrics")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--extended", action="store_true",
+                    help="also time the 96^3 Q3 FP64 and mixed-precision solves")
+    ap.add_argument("--no-probe", action="store_true",
+                    help="skip the FMA peak probe (profiling runs); roofline frac is then null")
+    ap.add_argument("--solves-only", action="store_true",
+                    help="run only the solve/adjoint metrics (profiling runs)")
+    ap.add_argument("--cells", type=int, default=None, help="override cells per direction")
+    ap.add_argument("--degree", type=int, default=None, help="override polynomial degree")
+    ap.add_argument("--precision", choices=["f64", "f32"], default="f64",
+                    help="operator precision of the timed steps")
+    args = ap.parse_args()
+    if args.cells:
+        WORKLOAD["cells"] = args.cells
+    if args.degree:
+        WORKLOAD["degree"] = args.degree
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gb300(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -443,6 +443,7 @@ __global__ void k_perm(long n, const double *__restrict__ src, int is_log,
 static void invalidate(pdg_context *ctx, bool operator_changed) {
   ctx->r0_valid = 0;
   if (operator_changed) {
+    ctx->rec_valid = 0;
     ctx->prec[0].ready = 0;
     ctx->prec[1].ready = 0;
   }
@@ -585,7 +586,7 @@ int pdg_destroy(pdg_context *c) {
   prec_free(c, 1);
   void *bufs[] = {c->K64, c->K32, c->c64, c->c32, c->tab64, c->tab32, c->fq, c->fc, c->gq,
                   c->jq, c->oq, c->r0, c->r0K, c->red_partials, c->red_out, c->d_flag,
-                  c->stage_a, c->stage_b};
+                  c->stage_a, c->stage_b, c->rec64};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 8; i++) {

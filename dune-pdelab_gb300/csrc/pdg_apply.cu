@@ -12,20 +12,28 @@
 // matrices (the Gauss rule with k+1 points integrates all 1D products of
 // degree <= 2k exactly).  The block row of cell e is
 //
-//   y_e = sum_dir  hperp_dir (A_dir (x) M (x) M)_dir u_e
-//       + sum_faces hperp_dir (B_face (x) M (x) M)_dir u_neighbour
+//   y_e = sum_dir  (A'_dir (x) M (x) M)_dir u_e
+//       + sum_faces (B'_face (x) M (x) M)_dir u_neighbour
 //
-// with Mhat the 1D mass matrix, A_dir = (K_e/h) Shat + (c h Mhat if dir=x)
-// + the self terms of the two faces normal to dir, and B_face the rank-2
+// with Mhat the 1D mass matrix, A'_dir = hperp_dir [ (K_e/h) Shat
+// + (c h Mhat if dir = x) + the self terms of the two faces normal to dir ]
+// (hperp = product of the tangential cell sizes) and B'_face the rank-2
 // coupling through the neighbour's face value and normal derivative.
 // Face coefficients reproduce the reference exactly: kappa_e = omega_e K_e
 // (omega_e = K_o/(K_e+K_o+1e-20), :326-332), penalty =
 // alpha/h_F * harmonic_average * k(k+d-1) (:346, :734), Dirichlet faces
 // with K_e and h_F = |T|/|F| (:717-727), theta = -1/+1/0 (:99-101).
 //
+// Per-cell data (A'_dir and five scaled coefficients per face) is either
+// read from a record precomputed once per coefficient field (FP64: its FP64
+// pipe is the bottleneck, the record removes all divisions and matrix
+// assembly from the apply) or formed on the fly (FP32: memory traffic is
+// the scarcer resource).
+//
 // Thread mapping (d = 3): N*N threads per cell, thread (tx,ty) holds the
 // z-column u[.,ty,tx] in registers; x/y contractions go through shared
-// memory.  d = 2: N threads per cell holding y-columns.
+// memory.  d = 2: N threads per cell holding y-columns.  All neighbour
+// lines are loaded before any arithmetic so that 2dN loads are in flight.
 #include "pdg_ops.cuh"
 
 namespace pdg {
@@ -37,16 +45,89 @@ struct Cfg {
   static constexpr int TPC = D == 3 ? N * N : N;          // threads per cell
   static constexpr int CPB = (128 / TPC) > 0 ? (128 / TPC) : 1;  // cells per block
   static constexpr int THREADS = CPB * TPC;
-  // shared memory per cell (elements): ue, Xs, Ys, Zs, face data, A_dir
-  static constexpr int PER_CELL = (D == 3 ? 4 * NB : 2 * NB) + 4 * D * TPC + D * N2 + 6 * D;
+  static constexpr int NF = 2 * D;
+  static constexpr int REC = D * N2 + 5 * NF;             // per-cell record
+  // shared memory per cell (elements): ue, Xs, Ys, Zs, face data, record, raw coefs
+  static constexpr int PER_CELL = (D == 3 ? 4 * NB : 2 * NB) + 4 * D * TPC + REC + 3 * NF;
   static constexpr int TAB = 2 * N2 + 2 * N;
 };
 
+// tangential face scale of direction dir (product of the other cell sizes)
+template <typename T, int D>
+__device__ __forceinline__ T hperp(const OpParams<T> &p, int dir) {
+  T s = T(1);
+#pragma unroll
+  for (int j = 0; j < D; j++)
+    if (j != dir) s *= p.h[j];
+  return s;
+}
+
+// Scaled face coefficients of face f from the raw {kappa_e/h, kappa_o/h, pen}:
+// {hp ke, hp ko, hp pen, theta hp ke, theta hp ko}
+template <typename T, int D>
+__device__ __forceinline__ void scale_face(const OpParams<T> &p, int f, const T *raw, T *c5) {
+  const T hp = hperp<T, D>(p, f >> 1);
+  c5[0] = hp * raw[0];
+  c5[1] = hp * raw[1];
+  c5[2] = hp * raw[2];
+  c5[3] = p.theta * c5[0];
+  c5[4] = p.theta * c5[1];
+}
+
+// lexicographic cell coordinates (x fastest) by multiply-high division
+template <typename T>
+__device__ __forceinline__ void cell_coords(const OpParams<T> &p, unsigned e, int *ix) {
+  const unsigned q0 = p.div0.div(e);
+  const unsigned q1 = p.div1.div(q0);
+  ix[0] = (int)(e - q0 * (unsigned)p.nc[0]);
+  ix[1] = (int)(q0 - q1 * (unsigned)p.nc[1]);
+  ix[2] = (int)q1;
+}
+
+// Record of one cell (computed in FP64, stored in T): A'_dir row-major, then
+// five scaled coefficients per face.
+template <typename T, int D, int N>
+__global__ void k_cell_record(const OpParams<double> p, T *__restrict__ rec) {
+  using C = Cfg<D, N>;
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.ncell) return;
+  const double *tM = p.tab, *tS = p.tab + N * N, *td0 = tS + N * N, *td1 = td0 + N;
+  int ix[3];
+  cell_coords(p, (unsigned)e, ix);
+  const long stride[3] = {1, (long)p.nc[0], (long)p.nc[0] * p.nc[1]};
+  const double Ke = p.K[e];
+  const double cc = p.c ? p.c[e] : 0.0;
+  double raw[3 * 2 * D];
+#pragma unroll
+  for (int f = 0; f < 2 * D; f++) {
+    const int dir = f >> 1;
+    long nb;
+    if (f & 1) nb = ix[dir] + 1 < p.nc[dir] ? e + stride[dir] : -1;
+    else nb = ix[dir] > 0 ? e - stride[dir] : -1;
+    face_coefficients(p, f, Ke, nb, raw + 3 * f);
+  }
+  T *r = rec + e * C::REC;
+#pragma unroll
+  for (int dir = 0; dir < D; dir++) {
+    const double hp = hperp<double, D>(p, dir);
+    for (int i = 0; i < N; i++)
+      for (int a = 0; a < N; a++)
+        r[dir * N * N + i * N + a] =
+            (T)(hp * a_entry<double, N>(p, dir, i, a, Ke, cc, raw, tM, tS, td0, td1));
+  }
+#pragma unroll
+  for (int f = 0; f < 2 * D; f++) {
+    double c5[5];
+    scale_face<double, D>(p, f, raw + 3 * f, c5);
+    for (int j = 0; j < 5; j++) r[D * N * N + 5 * f + j] = (T)c5[j];
+  }
+}
+
 template <typename T, int D, int N>
 __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
-    k_apply(const OpParams<T> p, const ApplyArgs<T> a) {
+    k_apply(const OpParams<T> p, const ApplyArgs<T> a, const T *__restrict__ rec) {
   using C = Cfg<D, N>;
-  constexpr int N2 = C::N2, NB = C::NB, TPC = C::TPC, CPB = C::CPB;
+  constexpr int N2 = C::N2, NB = C::NB, TPC = C::TPC, CPB = C::CPB, NF = C::NF;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *tM = reinterpret_cast<T *>(smem_raw);
   T *tS = tM + N2;
@@ -61,113 +142,111 @@ __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
   T *Ys = Xs + (D == 3 ? NB : 0);
   T *Zs = Ys + NB;
   T *fa = (D == 3 ? Zs + NB : Ys + NB);     // [2D][2][TPC]
-  T *Am = fa + 4 * D * TPC;                 // [D][N2]
-  T *cf = Am + D * N2;                      // [2D][3]
+  T *Am = fa + 4 * D * TPC;                 // record: [D][N2] then [2D][5]
+  T *c5 = Am + D * N2;
+  T *raw = c5 + 5 * NF;                     // [2D][3] (on-the-fly path)
 
   if (a.skip && *a.skip) return;
   for (int i = t; i < C::TAB; i += blockDim.x) tM[i] = p.tab[i];
 
-  const long e = (long)blockIdx.x * CPB + cs;
+  const int e = blockIdx.x * CPB + cs;          // cell counts fit 31 bits
   const bool active = e < p.ncell;
-  const long ee = active ? e : 0;
+  const int ee = active ? e : 0;
   int ix[3];
-  {
-    long r = ee;
-    ix[0] = (int)(r % p.nc[0]); r /= p.nc[0];
-    ix[1] = (int)(r % p.nc[1]); r /= p.nc[1];
-    ix[2] = (int)r;
-  }
-  const long stride[3] = {1, (long)p.nc[0], (long)p.nc[0] * p.nc[1]};
-  auto neighbour = [&](int f) -> long {
-    const int dir = f >> 1;
-    if (f & 1) return ix[dir] + 1 < p.nc[dir] ? ee + stride[dir] : -1;
-    return ix[dir] > 0 ? ee - stride[dir] : -1;
-  };
-  const T Ke = p.K[ee];
-
-  // own values: z-column (3D) / y-column (2D) in registers, copy in smem
-  T col[N];
-  const T *xe = a.x + ee * NB;
+  cell_coords(p, (unsigned)ee, ix);
+  const int stride[3] = {1, p.nc[0], p.nc[0] * p.nc[1]};
+  int nbr[NF];
 #pragma unroll
-  for (int z = 0; z < N; z++) {
-    col[z] = xe[z * TPC + l];
-    ue[z * TPC + l] = col[z];
+  for (int f = 0; f < NF; f++) {
+    const int dir = f >> 1;
+    if (f & 1) nbr[f] = ix[dir] + 1 < p.nc[dir] ? ee + stride[dir] : -1;
+    else nbr[f] = ix[dir] > 0 ? ee - stride[dir] : -1;
   }
-  for (int f = l; f < 2 * D; f += TPC) face_coefficients(p, f, Ke, neighbour(f), cf + 3 * f);
-  __syncthreads();
 
-  // ---- per-cell 1D operators A_dir (self terms of volume and faces) ----
-  {
+  // ---- all global loads first: own column, neighbour lines, record ----
+  T col[N];
+  const T *xe = a.x + (size_t)ee * NB;
+#pragma unroll
+  for (int z = 0; z < N; z++) col[z] = xe[z * TPC + l];
+  T v[NF][N];
+#pragma unroll
+  for (int f = 0; f < NF; f++) {
+    const int dir = f >> 1;
+    const int nb = (nbr[f] >= 0 && !a.diag_only) ? nbr[f] : ee;
+    const T *xn = a.x + (size_t)nb * NB;
+#pragma unroll
+    for (int q = 0; q < N; q++) {
+      int off;
+      if (D == 3)
+        off = dir == 0 ? l * N + q : (dir == 1 ? (l / N) * N2 + q * N + (l % N) : q * N2 + l);
+      else
+        off = dir == 0 ? l * N + q : q * N + l;
+      v[f][q] = xn[off];
+    }
+  }
+  if (rec) {
+    const T *r = rec + (size_t)ee * C::REC;
+    for (int i = l; i < C::REC; i += TPC) Am[i] = r[i];
+  }
+#pragma unroll
+  for (int z = 0; z < N; z++) ue[z * TPC + l] = col[z];
+  if (!rec) {
+    const T Ke = p.K[ee];
+#pragma unroll
+    for (int f = 0; f < NF; f++)
+      if (f % TPC == l) {
+        face_coefficients(p, f, Ke, nbr[f], raw + 3 * f);
+        scale_face<T, D>(p, f, raw + 3 * f, c5 + 5 * f);
+      }
+    __syncthreads();
     const T cc = p.c ? p.c[ee] : T(0);
-    auto Aentry = [&](int dir, int i, int aa) -> T {
-      return a_entry<T, N>(p, dir, a.transpose ? aa : i, a.transpose ? i : aa, Ke, cc, cf, tM, tS, td0, td1);
-    };
     if (D == 3) {
       const int i = l / N, aa = l % N;
 #pragma unroll
-      for (int dir = 0; dir < D; dir++) Am[dir * N2 + l] = Aentry(dir, i, aa);
+      for (int dir = 0; dir < D; dir++)
+        Am[dir * N2 + l] =
+            hperp<T, D>(p, dir) * a_entry<T, N>(p, dir, i, aa, Ke, cc, raw, tM, tS, td0, td1);
     } else {
 #pragma unroll
       for (int dir = 0; dir < D; dir++)
 #pragma unroll
-        for (int aa = 0; aa < N; aa++) Am[dir * N2 + l * N + aa] = Aentry(dir, l, aa);
+        for (int aa = 0; aa < N; aa++)
+          Am[dir * N2 + l * N + aa] =
+              hperp<T, D>(p, dir) * a_entry<T, N>(p, dir, l, aa, Ke, cc, raw, tM, tS, td0, td1);
     }
   }
+  __syncthreads();
 
   // ---- neighbour face data: one line per thread per face ----
 #pragma unroll
-  for (int f = 0; f < 2 * D; f++) {
-    const int dir = f >> 1, hi = f & 1;
-    const long nb = a.diag_only ? -1 : neighbour(f);
+  for (int f = 0; f < NF; f++) {
+    const int hi = f & 1;
     T s1 = T(0), s2 = T(0);
-    if (nb >= 0) {
-      const T *xn = a.x + nb * NB;
-      T v[N];
-      if (D == 3) {
-        if (dir == 0) {
-#pragma unroll
-          for (int q = 0; q < N; q++) v[q] = xn[l * N + q];
-        } else if (dir == 1) {
-#pragma unroll
-          for (int q = 0; q < N; q++) v[q] = xn[(l / N) * N2 + q * N + (l % N)];
-        } else {
-#pragma unroll
-          for (int q = 0; q < N; q++) v[q] = xn[q * N2 + l];
-        }
-      } else {
-        if (dir == 0) {
-#pragma unroll
-          for (int q = 0; q < N; q++) v[q] = xn[l * N + q];
-        } else {
-#pragma unroll
-          for (int q = 0; q < N; q++) v[q] = xn[q * N + l];
-        }
-      }
-      const T *c3 = cf + 3 * f;   // kappa_e/h, kappa_o/h, pen
+    if (nbr[f] >= 0 && !a.diag_only) {
+      const T *cf = c5 + 5 * f;   // hp ke, hp ko, hp pen, th hp ke, th hp ko
       T dv = T(0);
-      T val;
       if (!hi) {
         // neighbour below: its upper face touches this cell's lower face
 #pragma unroll
-        for (int q = 0; q < N; q++) dv += td1[q] * v[q];
-        val = v[N - 1];
+        for (int q = 0; q < N; q++) dv += td1[q] * v[f][q];
+        const T val = v[f][N - 1];
         if (!a.transpose) {
-          s1 = c3[1] * dv - c3[2] * val;
-          s2 = p.theta * c3[0] * val;
+          s1 = cf[1] * dv - cf[2] * val;
+          s2 = cf[3] * val;
         } else {
-          s1 = -c3[2] * val - p.theta * c3[1] * dv;
-          s2 = -c3[0] * val;
+          s1 = -cf[2] * val - cf[4] * dv;
+          s2 = -cf[0] * val;
         }
       } else {
 #pragma unroll
-        for (int q = 0; q < N; q++) dv += td0[q] * v[q];
-        val = v[0];
+        for (int q = 0; q < N; q++) dv += td0[q] * v[f][q];
+        const T val = v[f][0];
         if (!a.transpose) {
-          s1 = -c3[1] * dv - c3[2] * val;
-          s2 = -p.theta * c3[0] * val;
+          s1 = -cf[1] * dv - cf[2] * val;
+          s2 = -cf[3] * val;
         } else {
-          s1 = -c3[2] * val + p.theta * c3[1] * dv;
-          s2 = c3[0] * val;
+          s1 = -cf[2] * val + cf[4] * dv;
+          s2 = cf[0] * val;
         }
       }
     }
@@ -176,33 +255,50 @@ __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
   }
   __syncthreads();
 
+  // A'_dir rows (transposed operator: columns) needed by this thread, and
+  // the tangential mass rows, in registers
+  const int tr = a.transpose;
+  auto Aat = [&](int dir, int i, int q) -> T {
+    return Am[dir * N2 + (tr ? q * N + i : i * N + q)];
+  };
+
   T out[N];
   if constexpr (D == 3) {
     const int tx = l % N, ty = l / N;
-    const T *Ax = Am, *Ay = Am + N2, *Az = Am + 2 * N2;
+    T Arx[N], Ary[N], Mtx[N], Mty[N];
+#pragma unroll
+    for (int q = 0; q < N; q++) {
+      Arx[q] = Aat(0, tx, q);
+      Ary[q] = Aat(1, ty, q);
+      Mtx[q] = tM[tx * N + q];
+      Mty[q] = tM[ty * N + q];
+    }
+    const T d0x = td0[tx], d1x = td1[tx], d0y = td0[ty], d1y = td1[ty];
+    const T zf0 = fa[8 * TPC + l], zf1 = fa[9 * TPC + l];
+    const T zf2 = fa[10 * TPC + l], zf3 = fa[11 * TPC + l];
     T X[N], Y[N], Z[N];
 #pragma unroll
     for (int z = 0; z < N; z++) {
       T sx = T(0), sy = T(0), sz = T(0);
 #pragma unroll
       for (int q = 0; q < N; q++) {
-        sx += Ax[tx * N + q] * ue[z * N2 + ty * N + q];
-        sy += Ay[ty * N + q] * ue[z * N2 + q * N + tx];
-        sz += Az[z * N + q] * col[q];
+        sx += Arx[q] * ue[z * N2 + ty * N + q];
+        sy += Ary[q] * ue[z * N2 + q * N + tx];
+        sz += Aat(2, z, q) * col[q];
       }
       const int lx = z * N + ty, ly = z * N + tx;
       if (tx == 0) sx += fa[0 * TPC + lx];
-      sx += td0[tx] * fa[1 * TPC + lx];
+      sx += d0x * fa[1 * TPC + lx];
       if (tx == N - 1) sx += fa[2 * TPC + lx];
-      sx += td1[tx] * fa[3 * TPC + lx];
+      sx += d1x * fa[3 * TPC + lx];
       if (ty == 0) sy += fa[4 * TPC + ly];
-      sy += td0[ty] * fa[5 * TPC + ly];
+      sy += d0y * fa[5 * TPC + ly];
       if (ty == N - 1) sy += fa[6 * TPC + ly];
-      sy += td1[ty] * fa[7 * TPC + ly];
-      if (z == 0) sz += fa[8 * TPC + l];
-      sz += td0[z] * fa[9 * TPC + l];
-      if (z == N - 1) sz += fa[10 * TPC + l];
-      sz += td1[z] * fa[11 * TPC + l];
+      sy += d1y * fa[7 * TPC + ly];
+      if (z == 0) sz += zf0;
+      sz += td0[z] * zf1;
+      if (z == N - 1) sz += zf2;
+      sz += td1[z] * zf3;
       X[z] = sx;
       Y[z] = sy;
       Z[z] = sz;
@@ -214,77 +310,88 @@ __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
       Zs[z * N2 + l] = Z[z];
     }
     __syncthreads();
-    const T hyz = p.h[1] * p.h[2], hxz = p.h[0] * p.h[2], hxy = p.h[0] * p.h[1];
+    // W = M_y X + M_x Y ; T1 = M_x Z   (tangential masses; scales are in A')
     T W[N];
 #pragma unroll
     for (int z = 0; z < N; z++) {
-      T w1 = T(0), w2 = T(0), t1 = T(0);
+      T w = T(0), t1 = T(0);
 #pragma unroll
       for (int q = 0; q < N; q++) {
-        w1 += tM[ty * N + q] * Xs[z * N2 + q * N + tx];
-        w2 += tM[tx * N + q] * Ys[z * N2 + ty * N + q];
-        t1 += tM[tx * N + q] * Zs[z * N2 + ty * N + q];
+        w += Mty[q] * Xs[z * N2 + q * N + tx];
+        w += Mtx[q] * Ys[z * N2 + ty * N + q];
+        t1 += Mtx[q] * Zs[z * N2 + ty * N + q];
       }
-      W[z] = hyz * w1 + hxz * w2;
+      W[z] = w;
       ue[z * N2 + l] = t1;   // ue is free: all reads finished before the sync
     }
     __syncthreads();
+    // out = M_z W + M_y T1
 #pragma unroll
     for (int z = 0; z < N; z++) {
-      T s = T(0), s2 = T(0);
+      T s = T(0);
 #pragma unroll
       for (int q = 0; q < N; q++) {
         s += tM[z * N + q] * W[q];
-        s2 += tM[ty * N + q] * ue[z * N2 + q * N + tx];
+        s += Mty[q] * ue[z * N2 + q * N + tx];
       }
-      out[z] = s + hxy * s2;
+      out[z] = s;
     }
   } else {
     const int tx = l;
-    const T *Ax = Am, *Ay = Am + N2;
+    T Arx[N], Mtx[N];
+#pragma unroll
+    for (int q = 0; q < N; q++) {
+      Arx[q] = Aat(0, tx, q);
+      Mtx[q] = tM[tx * N + q];
+    }
+    const T d0x = td0[tx], d1x = td1[tx];
+    const T yf0 = fa[4 * TPC + tx], yf1 = fa[5 * TPC + tx];
+    const T yf2 = fa[6 * TPC + tx], yf3 = fa[7 * TPC + tx];
     T X[N];
 #pragma unroll
     for (int y = 0; y < N; y++) {
       T sx = T(0), sy = T(0);
 #pragma unroll
       for (int q = 0; q < N; q++) {
-        sx += Ax[tx * N + q] * ue[y * N + q];
-        sy += Ay[y * N + q] * col[q];
+        sx += Arx[q] * ue[y * N + q];
+        sy += Aat(1, y, q) * col[q];
       }
       if (tx == 0) sx += fa[0 * TPC + y];
-      sx += td0[tx] * fa[1 * TPC + y];
+      sx += d0x * fa[1 * TPC + y];
       if (tx == N - 1) sx += fa[2 * TPC + y];
-      sx += td1[tx] * fa[3 * TPC + y];
-      if (y == 0) sy += fa[4 * TPC + tx];
-      sy += td0[y] * fa[5 * TPC + tx];
-      if (y == N - 1) sy += fa[6 * TPC + tx];
-      sy += td1[y] * fa[7 * TPC + tx];
+      sx += d1x * fa[3 * TPC + y];
+      if (y == 0) sy += yf0;
+      sy += td0[y] * yf1;
+      if (y == N - 1) sy += yf2;
+      sy += td1[y] * yf3;
       X[y] = sx;
       Ys[y * N + tx] = sy;
     }
     __syncthreads();
+    // out = M_y X + M_x Y
 #pragma unroll
     for (int y = 0; y < N; y++) {
-      T s = T(0), s2 = T(0);
+      T s = T(0);
 #pragma unroll
       for (int q = 0; q < N; q++) {
         s += tM[y * N + q] * X[q];
-        s2 += tM[tx * N + q] * Ys[y * N + q];
+        s += Mtx[q] * Ys[y * N + q];
       }
-      out[y] = p.h[1] * s + p.h[0] * s2;
+      out[y] = s;
     }
   }
 
   if (active) {
-    T *ye = a.y + e * NB;
-    const T *ad = a.add ? a.add + e * NB : nullptr;
+    T *ye = a.y + (size_t)e * NB;
+    const T *ad = a.add ? a.add + (size_t)e * NB : nullptr;
+    const bool scale = a.alpha != T(1);
 #pragma unroll
     for (int z = 0; z < N; z++) {
       const int idx = z * TPC + l;
-      T v = a.alpha * out[z];
-      if (a.accumulate) v += ye[idx];
-      if (ad) v += ad[idx];
-      ye[idx] = v;
+      T r = scale ? a.alpha * out[z] : out[z];
+      if (a.accumulate) r += ye[idx];
+      if (ad) r += ad[idx];
+      ye[idx] = r;
     }
   }
 }
@@ -295,7 +402,10 @@ OpParams<T> make_params(const pdg_context *ctx, const T *K, const T *c, const T 
   for (int j = 0; j < 3; j++) {
     p.nc[j] = j < ctx->dim ? ctx->cfg.cells[j] : 1;
     p.h[j] = (T)ctx->h[j];
+    p.inv_h[j] = (T)(1.0 / ctx->h[j]);
   }
+  p.div0.init((unsigned)p.nc[0]);
+  p.div1.init((unsigned)p.nc[1]);
   p.ncell = ctx->ncell;
   p.theta = (T)ctx->theta;
   p.pen_fac = (T)ctx->pen_fac;
@@ -312,36 +422,73 @@ template OpParams<float> make_params<float>(const pdg_context *, const float *,
                                             const float *, const float *);
 
 template <typename T, int D, int N>
-static int launch_apply_dn(pdg_context *ctx, const ApplyArgs<T> &a, const OpParams<T> &p) {
+static int launch_apply_dn(pdg_context *ctx, const ApplyArgs<T> &a, const OpParams<T> &p,
+                           const T *rec) {
   using C = Cfg<D, N>;
   const size_t smem = sizeof(T) * (C::TAB + C::CPB * C::PER_CELL);
-  static bool attr_done = false;
-  if (!attr_done) {
+  static int attr_done = -1;
+  if (attr_done != ctx->device) {
     PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply<T, D, N>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-    attr_done = true;
+    attr_done = ctx->device;
   }
   const long blocks = (ctx->ncell + C::CPB - 1) / C::CPB;
-  k_apply<T, D, N><<<(unsigned)blocks, C::THREADS, smem, ctx->stream>>>(p, a);
+  k_apply<T, D, N><<<(unsigned)blocks, C::THREADS, smem, ctx->stream>>>(p, a, rec);
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
+}
+
+template <int D, int N>
+static int record_dn(pdg_context *ctx) {
+  using C = Cfg<D, N>;
+  if (!ctx->rec64)
+    PDG_CUDA_TRY(cudaMalloc(&ctx->rec64, sizeof(double) * C::REC * ctx->ncell));
+  OpParams<double> p = make_params<double>(ctx, ctx->K64, ctx->c64, ctx->tab64);
+  const unsigned blocks = (unsigned)((ctx->ncell + 127) / 128);
+  k_cell_record<double, D, N><<<blocks, 128, 0, ctx->stream>>>(p, ctx->rec64);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+
+// FP64 cell records (rebuilt after the coefficients change)
+static int ensure_record(pdg_context *ctx) {
+  if (ctx->rec_valid) return PDG_OK;
+  int st;
+  switch (ctx->dim * 10 + ctx->k) {
+    case 21: st = record_dn<2, 2>(ctx); break;
+    case 22: st = record_dn<2, 3>(ctx); break;
+    case 23: st = record_dn<2, 4>(ctx); break;
+    case 24: st = record_dn<2, 5>(ctx); break;
+    case 31: st = record_dn<3, 2>(ctx); break;
+    case 32: st = record_dn<3, 3>(ctx); break;
+    case 33: st = record_dn<3, 4>(ctx); break;
+    case 34: st = record_dn<3, 5>(ctx); break;
+    default: return set_error(PDG_EUNSUPPORTED, "dim/degree not compiled in");
+  }
+  if (st == PDG_OK) ctx->rec_valid = 1;
+  return st;
 }
 
 template <typename T>
 int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c,
                  const T *tab) {
   OpParams<T> p = make_params<T>(ctx, K, c, tab);
+  const T *rec = nullptr;
+  if (std::is_same<T, double>::value && K == (const T *)ctx->K64) {
+    PDG_TRY(ensure_record(ctx));
+    rec = (const T *)ctx->rec64;
+  }
   const int key = ctx->dim * 10 + ctx->k;
   switch (key) {
-    case 21: return launch_apply_dn<T, 2, 2>(ctx, a, p);
-    case 22: return launch_apply_dn<T, 2, 3>(ctx, a, p);
-    case 23: return launch_apply_dn<T, 2, 4>(ctx, a, p);
-    case 24: return launch_apply_dn<T, 2, 5>(ctx, a, p);
-    case 31: return launch_apply_dn<T, 3, 2>(ctx, a, p);
-    case 32: return launch_apply_dn<T, 3, 3>(ctx, a, p);
-    case 33: return launch_apply_dn<T, 3, 4>(ctx, a, p);
-    case 34: return launch_apply_dn<T, 3, 5>(ctx, a, p);
+    case 21: return launch_apply_dn<T, 2, 2>(ctx, a, p, rec);
+    case 22: return launch_apply_dn<T, 2, 3>(ctx, a, p, rec);
+    case 23: return launch_apply_dn<T, 2, 4>(ctx, a, p, rec);
+    case 24: return launch_apply_dn<T, 2, 5>(ctx, a, p, rec);
+    case 31: return launch_apply_dn<T, 3, 2>(ctx, a, p, rec);
+    case 32: return launch_apply_dn<T, 3, 3>(ctx, a, p, rec);
+    case 33: return launch_apply_dn<T, 3, 4>(ctx, a, p, rec);
+    case 34: return launch_apply_dn<T, 3, 5>(ctx, a, p, rec);
     default: return set_error(PDG_EUNSUPPORTED, "dim/degree not compiled in");
   }
 }

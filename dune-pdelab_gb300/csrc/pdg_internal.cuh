@@ -41,12 +41,38 @@ struct Velocity {
   double m[kMaxModes][7];
 };
 
+// Unsigned division by a runtime constant d >= 1 via a 32x32 high multiply
+// (round-up method): q = (umulhi(n, m) + n) >> s ... computed as
+// t = umulhi(n, m); q = (t + ((n - t) >> 1)) >> (s - 1) for s >= 1.
+struct FastDiv {
+  unsigned d, m, s;
+  void init(unsigned dd) {
+    d = dd;
+    if (dd == 1) { m = 0; s = 0; return; }
+    unsigned l = 0;
+    while ((1ull << l) < dd) l++;
+    m = (unsigned)(((1ull << 32) * ((1ull << l) - dd)) / dd + 1);
+    s = l;
+  }
+  __host__ __device__ __forceinline__ unsigned div(unsigned n) const {
+    if (d == 1) return n;
+#ifdef __CUDA_ARCH__
+    const unsigned t = __umulhi(n, m);
+#else
+    const unsigned t = (unsigned)(((unsigned long long)n * m) >> 32);
+#endif
+    return (t + ((n - t) >> 1)) >> (s - 1);
+  }
+};
+
 // Everything an operator kernel needs besides the vectors.  Passed by value.
 template <typename T>
 struct OpParams {
   int nc[3];
+  FastDiv div0, div1;   // division by nc[0], nc[1]
   long ncell;
   T h[3];
+  T inv_h[3];
   T theta;        // SIPG -1, NIPG +1, IIPG 0
   T pen_fac;      // alpha * k * (k + d - 1)
   int weights;    // PDG_WEIGHTS_ON / OFF
@@ -102,6 +128,8 @@ struct pdg_context {
   double *fq, *fc, *gq, *jq, *oq;
   double *r0;          // R(0): source and boundary-data part of the residual
   int r0_valid;
+  double *rec64;       // FP64 per-cell operator records (scaled A'_dir + face coefficients)
+  int rec_valid;
 
   // preconditioner, one instance per precision (index PDG_F64 / PDG_F32)
   pdg::PrecData prec[2];

@@ -7,37 +7,47 @@
 
 namespace pdg {
 
+// Division helpers: exact IEEE division in FP64 (the reference's
+// arithmetic); fast reciprocal-based forms in FP32, whose apply only feeds
+// the inner solve of the defect-correction loop.
+__device__ __forceinline__ double qdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float qdiv(float a, float b) { return __fdividef(a, b); }
+template <typename T>
+__device__ __forceinline__ T over_h(const OpParams<T> &p, int dir, T x) {
+  if (sizeof(T) == 8) return x / p.h[dir];
+  return x * p.inv_h[dir];
+}
+
 template <typename T>
 __device__ __forceinline__ void face_coefficients(const OpParams<T> &p, int f, T Ke,
                                                   long nb, T *coef) {
   // coef = {kappa_e/h, kappa_o/h, penalty}
   const int dir = f >> 1;
-  const T h = p.h[dir];
   T kap_e = T(0), kap_o = T(0), pen = T(0);
   if (nb >= 0) {
     const T Ko = p.K[nb];
     if (p.weights == PDG_WEIGHTS_ON) {
       // convectiondiffusiondg.hh:326-332: delta = (A n).n = K
       const T S = Ke + Ko + T(1e-20);
-      const T omega_e = Ko / S;
-      const T omega_o = Ke / S;
+      const T omega_e = qdiv(Ko, S);
+      const T omega_o = qdiv(Ke, S);
       kap_e = omega_e * Ke;
       kap_o = omega_o * Ko;
-      const T harm = T(2) * Ke * Ko / S;
-      pen = (p.pen_fac / h) * harm;          // h_F = min(|T_s|,|T_n|)/|F| = h
+      const T harm = qdiv(T(2) * Ke * Ko, S);
+      pen = over_h(p, dir, p.pen_fac) * harm;   // h_F = min(|T_s|,|T_n|)/|F| = h
     } else {
       kap_e = T(0.5) * Ke;
       kap_o = T(0.5) * Ko;
-      pen = p.pen_fac / h;
+      pen = over_h(p, dir, p.pen_fac);
     }
   } else if (p.bc[f] == PDG_BC_DIRICHLET) {
     // residual_boundary_integral: A_s n uses K_s; harmonic_average = K_s
     // (weightsOn) or 1 (:720-734)
     kap_e = Ke;
-    pen = (p.pen_fac / h) * (p.weights == PDG_WEIGHTS_ON ? Ke : T(1));
+    pen = over_h(p, dir, p.pen_fac) * (p.weights == PDG_WEIGHTS_ON ? Ke : T(1));
   }
-  coef[0] = kap_e / h;
-  coef[1] = kap_o / h;
+  coef[0] = over_h(p, dir, kap_e);
+  coef[1] = over_h(p, dir, kap_o);
   coef[2] = pen;
 }
 
@@ -55,7 +65,7 @@ __device__ __forceinline__ T a_entry(const OpParams<T> &p, int dir, int i, int a
                                      const T *cf, const T *tM, const T *tS, const T *td0,
                                      const T *td1) {
   const T h = p.h[dir];
-  T v = (Ke / h) * tS[i * N + aa];
+  T v = over_h(p, dir, Ke) * tS[i * N + aa];
   if (dir == 0) v += cc * h * tM[i * N + aa];
   const T *cl = cf + 3 * (2 * dir);
   const T *ch = cf + 3 * (2 * dir + 1);

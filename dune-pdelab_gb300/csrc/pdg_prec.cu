@@ -162,14 +162,14 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
   T *S1 = S0 + NB;
   T *Qs = S1 + NB;       // [D][N2]
   T *Ls = Qs + D * N2;   // [D][N]
-  const long e = (long)blockIdx.x * CPB + cs;
+  const int e = blockIdx.x * CPB + cs;
   const bool active = e < ncell;
-  const long ee = active ? e : 0;
-  for (int i = l; i < D * N2; i += TPC) Qs[i] = Q[ee * D * N2 + i];
-  for (int i = l; i < D * N; i += TPC) Ls[i] = L[ee * D * N + i];
+  const int ee = active ? e : 0;
+  for (int i = l; i < D * N2; i += TPC) Qs[i] = Q[(size_t)ee * D * N2 + i];
+  for (int i = l; i < D * N; i += TPC) Ls[i] = L[(size_t)ee * D * N + i];
   T col[N];
 #pragma unroll
-  for (int z = 0; z < N; z++) col[z] = d[ee * NB + z * TPC + l];
+  for (int z = 0; z < N; z++) col[z] = d[(size_t)ee * NB + z * TPC + l];
   __syncthreads();
   if constexpr (D == 3) {
     const int tx = l % N, ty = l / N;
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
       T s = T(0);
 #pragma unroll
       for (int x = 0; x < N; x++) s += Qx[x * N + tx] * S1[z * N2 + ty * N + x];
-      a[z] = s / (Ls[tx] + Ls[N + ty] + Ls[2 * N + z]);
+      a[z] = qdiv(s, Ls[tx] + Ls[N + ty] + Ls[2 * N + z]);
     }
     __syncthreads();
 #pragma unroll
@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
         T s = T(0);
 #pragma unroll
         for (int zp = 0; zp < N; zp++) s += Qz[z * N + zp] * a[zp];
-        v[e * NB + z * N2 + l] = s;
+        v[(size_t)e * NB + z * N2 + l] = s;
       }
     }
   } else {
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
       T s = T(0);
 #pragma unroll
       for (int x = 0; x < N; x++) s += Qx[x * N + tx] * S0[y * N + x];
-      a[y] = s / (Ls[tx] + Ls[N + y]);
+      a[y] = qdiv(s, Ls[tx] + Ls[N + y]);
     }
 #pragma unroll
     for (int y = 0; y < N; y++) S1[y * N + tx] = a[y];
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
         T s = T(0);
 #pragma unroll
         for (int yp = 0; yp < N; yp++) s += Qy[y * N + yp] * a[yp];
-        v[e * NB + y * N + tx] = s;
+        v[(size_t)e * NB + y * N + tx] = s;
       }
     }
   }
