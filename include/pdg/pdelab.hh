@@ -1,0 +1,202 @@
+// pdg/pdelab.hh -- C++ adapters over the C ABI (include/pdg.h) with the
+// names and method signatures of the PDELab / dune-istl interfaces they
+// replace, so driver code written against PDELab keeps its shape.
+//
+//   pdg::GridOperator                    GridOperator::residual / jacobian_apply
+//                                        (dune/pdelab/gridoperator/gridoperator.hh:176-205)
+//   pdg::OnTheFlyOperator                LinearOperator::apply / applyscaleadd
+//                                        (dune/pdelab/backend/istl/seqistlsolverbackend.hh:45-100)
+//   pdg::GridOperatorPreconditioner      Preconditioner::pre / apply / post
+//                                        (dune/pdelab/backend/istl/matrixfree/gridoperatorpreconditioner.hh:18-91)
+//   pdg::ISTLBackend_SEQ_MatrixFree_Base apply(z, r, reduction), norm, result
+//                                        (dune/pdelab/backend/istl/matrixfree/backends.hh:62-143)
+//   pdg::StationaryLinearProblemSolver   apply, result
+//                                        (dune/pdelab/stationary/linearproblem.hh:59-338)
+//
+// Vectors are any contiguous double container with data()/size() (for a
+// PDELab ISTL BlockVector of FieldVector<double,n>, pass
+// Dune::PDELab::Backend::native(v) through pdg::span(&v[0][0], v.dim())).
+// Failures throw pdg::Error (the reference throws Dune::Exception); solver
+// non-convergence is reported through result(), as LinearSolverResult does.
+// Header-only; link with libpdg.so.
+#pragma once
+
+#include <cstddef>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../pdg.h"
+
+namespace pdg {
+
+struct Error : std::runtime_error {
+  int status;
+  Error(int st, const std::string &m) : std::runtime_error(m), status(st) {}
+};
+
+inline void check(int st, bool allow_not_converged = false) {
+  if (st == PDG_OK) return;
+  if (allow_not_converged && st == PDG_ENOTCONVERGED) return;
+  throw Error(st, std::string("pdg: ") + pdg_last_error());
+}
+
+// non-owning view of contiguous doubles (host or device memory)
+struct span {
+  double *p;
+  std::size_t n;
+  span(double *ptr, std::size_t size) : p(ptr), n(size) {}
+  template <class V>
+  span(V &v) : p(v.data()), n(v.size()) {}
+  double *data() const { return p; }
+  std::size_t size() const { return n; }
+};
+
+struct Config : pdg_config {
+  Config(int dim, int degree, int nx, int ny, int nz = 1) : pdg_config() {
+    this->dim = dim;
+    this->degree = degree;
+    cells[0] = nx;
+    cells[1] = ny;
+    cells[2] = nz;
+    extent[0] = extent[1] = extent[2] = 1.0;
+    method = PDG_SIPG;
+    weights = PDG_WEIGHTS_ON;
+    alpha = 1.0;   // ConvectionDiffusionDG default (convectiondiffusiondg.hh:87-91)
+    for (int &b : bctype) b = PDG_BC_DIRICHLET;
+    device = 0;
+  }
+};
+
+// GridFunctionSpace + ConvectionDiffusionDG + GridOperator on one GPU.
+class GridOperator {
+ public:
+  explicit GridOperator(const pdg_config &cfg) { check(pdg_create(&cfg, &ctx_)); }
+  ~GridOperator() { pdg_destroy(ctx_); }
+  GridOperator(const GridOperator &) = delete;
+  GridOperator &operator=(const GridOperator &) = delete;
+
+  pdg_context *handle() const { return ctx_; }
+  long size() const {
+    long nd = 0;
+    check(pdg_sizes(ctx_, nullptr, nullptr, &nd, nullptr, nullptr));
+    return nd;
+  }
+  long cells() const {
+    long nc = 0;
+    check(pdg_sizes(ctx_, &nc, nullptr, nullptr, nullptr, nullptr));
+    return nc;
+  }
+
+  // r += R(x)
+  void residual(span x, span r) const { check(pdg_residual(ctx_, x.data(), r.data())); }
+  // y += J z  (linear problem: the linearization point is not needed)
+  void jacobian_apply(span z, span y) const {
+    check(pdg_jacobian_apply(ctx_, z.data(), y.data()));
+  }
+
+  void setPermeability(const std::vector<double> &K, bool is_log = false) {
+    check(pdg_set_permeability(ctx_, K.data(), is_log ? 1 : 0));
+  }
+  void setSource(const double *fq, const double *fc) { check(pdg_set_source(ctx_, fq, fc)); }
+  void setBoundaryData(const double *g, const double *j = nullptr, const double *o = nullptr) {
+    check(pdg_set_boundary_data(ctx_, g, j, o));
+  }
+
+ private:
+  pdg_context *ctx_ = nullptr;
+};
+
+// Dune::LinearOperator over GridOperator::jacobian_apply
+class OnTheFlyOperator {
+ public:
+  explicit OnTheFlyOperator(const GridOperator &go) : go_(go) {}
+  void apply(span x, span y) const { check(pdg_apply(go_.handle(), x.data(), y.data())); }
+  void applyscaleadd(double alpha, span x, span y) const {
+    check(pdg_applyscaleadd(go_.handle(), alpha, x.data(), y.data()));
+  }
+
+ private:
+  const GridOperator &go_;
+};
+
+// Dune::Preconditioner over the cell-block Jacobi of the operator
+class GridOperatorPreconditioner {
+ public:
+  explicit GridOperatorPreconditioner(const GridOperator &go, int kind = PDG_PREC_BJ_FDM,
+                                      int precision = PDG_F64)
+      : go_(go), kind_(kind), precision_(precision) {}
+  void pre(span, span) {
+    if (!ready_) {
+      check(pdg_prec_setup(go_.handle(), kind_, precision_));
+      ready_ = true;
+    }
+  }
+  void apply(span v, span d) { check(pdg_prec_apply(go_.handle(), d.data(), v.data())); }
+  void post(span) {}
+
+ private:
+  const GridOperator &go_;
+  int kind_, precision_;
+  bool ready_ = false;
+};
+
+// Sequential matrix-free Krylov backend: apply(z, r, reduction) solves J z = r
+class ISTLBackend_SEQ_MatrixFree_Base {
+ public:
+  static constexpr bool isMatrixFree = true;
+  ISTLBackend_SEQ_MatrixFree_Base(const GridOperator &go, int method = PDG_CG,
+                                  int preconditioner = PDG_PREC_BJ_FDM, unsigned maxiter = 5000,
+                                  int verbose = 0)
+      : go_(go) {
+    pdg_default_solver_options(&opt_);
+    opt_.method = method;
+    opt_.preconditioner = preconditioner;
+    opt_.maxit = (int)maxiter;
+    opt_.verbose = verbose;
+  }
+  void setMixedPrecision(bool on, double inner_reduction = 1e-3) {
+    opt_.mixed = on ? 1 : 0;
+    opt_.inner_reduction = inner_reduction;
+  }
+  void apply(span z, span r, double reduction) {
+    opt_.reduction = reduction;
+    check(pdg_krylov_solve(go_.handle(), &opt_, z.data(), r.data(), &res_), true);
+  }
+  double norm(span v) const {
+    double out = 0.0;
+    check(pdg_norm(go_.handle(), v.data(), &out));
+    return out;
+  }
+  const pdg_solver_result &result() const { return res_; }
+  pdg_solver_options &options() { return opt_; }
+
+ private:
+  const GridOperator &go_;
+  pdg_solver_options opt_;
+  pdg_solver_result res_{};
+};
+
+// r = R(x); J z = r; x -= z
+class StationaryLinearProblemSolver {
+ public:
+  StationaryLinearProblemSolver(const GridOperator &go, ISTLBackend_SEQ_MatrixFree_Base &ls,
+                                span x, double reduction, double min_defect = 1e-99)
+      : go_(go), ls_(ls), x_(x), reduction_(reduction), min_defect_(min_defect) {}
+  void apply() {
+    pdg_solver_options o = ls_.options();
+    o.reduction = reduction_;
+    o.min_defect = min_defect_;
+    check(pdg_solve_linear_problem(go_.handle(), &o, x_.data(), &res_), true);
+  }
+  const pdg_solver_result &result() const { return res_; }
+
+ private:
+  const GridOperator &go_;
+  ISTLBackend_SEQ_MatrixFree_Base &ls_;
+  span x_;
+  double reduction_, min_defect_;
+  pdg_solver_result res_{};
+};
+
+}  // namespace pdg
