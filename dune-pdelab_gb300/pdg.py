@@ -97,6 +97,7 @@ _SIGS = {
     "pdg_prec_apply_transpose": (C.c_int, [_vp, _vp, _vp]),
     "pdg_norm": (C.c_int, [_vp, _vp, C.POINTER(C.c_double)]),
     "pdg_dot": (C.c_int, [_vp, _vp, _vp, C.POINTER(C.c_double)]),
+    "pdg_dot_noalloc": (C.c_int, [C.c_long, _vp, _vp, _vp, _vp]),
     "pdg_krylov_solve": (C.c_int, [_vp, C.POINTER(SolverOptions), _vp, _vp,
                                    C.POINTER(SolverResult)]),
     "pdg_solve_linear_problem": (C.c_int, [_vp, C.POINTER(SolverOptions), _vp,
