@@ -1,0 +1,90 @@
+"""Adjoint gradient through torch.autograd (config C4 at test size).
+
+J(logK, f) = 1/2 |u - u_obs|^2, u_obs = u(target logK) + 1% noise.  The
+hand-written adjoint (pdg_adjoint_solve + pdg_grad_logK / pdg_grad_source)
+is checked against central finite differences (h = 1e-6) along seeded random
+directions and against the gradient built by the oracle from the assembled
+CPU Jacobian transpose (the oracle's own A^T solve and local blocks).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mods():
+    import __graft_entry__
+    __graft_entry__.build()
+    import pdg
+    import pdg_torch
+    return pdg, pdg_torch
+
+
+def _setup(pdg, pdg_torch, torch, n=6, k=2, seed=0):
+    rng = np.random.default_rng(seed)
+    go = pdg.GridOperator(3, k, (n, n, n), alpha=3.0)
+    go.set_source(fc=np.ones(go.ncell))
+    prob = pdg_torch.DGProblem(go, reduction=1e-13)
+    logK_t = torch.tensor(rng.standard_normal(go.ncell), device="cuda")
+    u_t = pdg_torch.solve_dg(logK_t, None, prob).detach()
+    noise = torch.tensor(rng.standard_normal(go.ndof), device="cuda")
+    u_obs = u_t * (1 + 0.01 * noise)
+    logK = torch.tensor(rng.standard_normal(go.ncell), device="cuda")
+    fc = torch.ones(go.ncell, dtype=torch.float64, device="cuda")
+    return go, prob, logK, fc, u_obs, rng
+
+
+def _loss(pdg_torch, prob, logK, fc, u_obs):
+    u = pdg_torch.solve_dg(logK, fc, prob)
+    return 0.5 * ((u - u_obs) ** 2).sum(), u
+
+
+def test_grad_logK_and_source_vs_finite_differences(mods):
+    import torch
+    pdg, pdg_torch = mods
+    go, prob, logK, fc, u_obs, rng = _setup(pdg, pdg_torch, torch)
+    logK.requires_grad_(True)
+    fc.requires_grad_(True)
+    J, u = _loss(pdg_torch, prob, logK, fc, u_obs)
+    J.backward()
+    g, gf = logK.grad.clone(), fc.grad.clone()
+    h = 1e-6
+    with torch.no_grad():
+        for i in range(4):
+            d = torch.tensor(rng.standard_normal(go.ncell), device="cuda")
+            Jp, _ = _loss(pdg_torch, prob, logK + h * d, fc, u_obs)
+            Jm, _ = _loss(pdg_torch, prob, logK - h * d, fc, u_obs)
+            fd = float((Jp - Jm) / (2 * h))
+            ad = float((g * d).sum())
+            assert abs(fd - ad) <= 1e-5 * abs(ad) + 1e-12 * float(J), (i, fd, ad)
+        for i in range(2):
+            d = torch.tensor(rng.standard_normal(go.ncell), device="cuda")
+            Jp, _ = _loss(pdg_torch, prob, logK, fc + h * d, u_obs)
+            Jm, _ = _loss(pdg_torch, prob, logK, fc - h * d, u_obs)
+            fd = float((Jp - Jm) / (2 * h))
+            ad = float((gf * d).sum())
+            assert abs(fd - ad) <= 1e-5 * abs(ad) + 1e-12 * float(J), (i, fd, ad)
+
+
+def test_grad_logK_vs_assembled_transpose(mods, oracle):
+    import torch
+    pdg, pdg_torch = mods
+    go, prob, logK, fc, u_obs, rng = _setup(pdg, pdg_torch, torch, n=5, seed=3)
+    logK.requires_grad_(True)
+    J, u = _loss(pdg_torch, prob, logK, fc, u_obs)
+    J.backward()
+    g = logK.grad.detach().cpu().numpy()
+    # oracle: A^T lambda = u - u_obs with the assembled Jacobian, then the
+    # gradient from unit-coefficient local blocks
+    K = np.exp(logK.detach().cpu().numpy())
+    P = oracle.Problem(3, 2, (5, 5, 5), alpha=3.0, K=K, fc=np.ones(go.ncell))
+    A = P.assemble_jacobian()
+    un = u.detach().cpu().numpy()
+    rhs = un - u_obs.cpu().numpy()
+    lam = np.zeros(go.ndof)
+    st, res = P.krylov("cg", lam, rhs.copy(), 1e-14, maxit=20000, op=2, blocks=A)
+    assert st == 0 and res.converged
+    gref = P.grad_logK(un, lam)
+    rel = np.max(np.abs(g - gref)) / np.max(np.abs(gref))
+    assert rel <= 1e-8, rel
