@@ -74,6 +74,8 @@ static void gauss_legendre(int m, double *x, double *w) {
   }
 }
 
+double lagrange_derivative(int k, int i, double x) { return dlag(k, i, x); }
+
 RhsTables make_rhs_tables(const pdg_context *ctx) {
   RhsTables t;
   std::memset(&t, 0, sizeof(t));
@@ -586,7 +588,8 @@ int pdg_destroy(pdg_context *c) {
   prec_free(c, 1);
   void *bufs[] = {c->K64, c->K32, c->c64, c->c32, c->tab64, c->tab32, c->fq, c->fc, c->gq,
                   c->jq, c->oq, c->r0, c->r0K, c->red_partials, c->red_out, c->d_flag,
-                  c->stage_a, c->stage_b, c->rec64};
+                  c->stage_a, c->stage_b, c->rec64, c->conv64, c->conv32, c->convtab64,
+                  c->convtab32};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 8; i++) {
@@ -696,10 +699,19 @@ int pdg_set_velocity_modes(pdg_context *ctx, int nmodes, const double *modes) {
   PDG_CHECK_CTX(ctx);
   if (nmodes < 0 || nmodes > kMaxModes) return set_error(PDG_EINVAL, "nmodes must be 0..16");
   if (nmodes > 0 && !modes) return set_error(PDG_EINVAL, "null modes");
-  if (nmodes > 0)
-    return set_error(PDG_EUNSUPPORTED, "convection is not implemented in this build");
-  ctx->vel.nmodes = 0;
+  if (nmodes > 0 && ctx->dim != 3)
+    return set_error(PDG_EUNSUPPORTED, "convection is implemented for 3D grids");
+  ctx->vel.nmodes = nmodes;
+  for (int m = 0; m < nmodes; m++)
+    for (int j = 0; j < 7; j++) ctx->vel.m[m][j] = modes[7 * m + j];
   invalidate(ctx, true);
+  if (nmodes > 0) {
+    const int st = conv_setup(ctx);
+    if (st != PDG_OK) {
+      ctx->vel.nmodes = 0;
+      return st;
+    }
+  }
   return PDG_OK;
 }
 

@@ -480,17 +480,20 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
     rec = (const T *)ctx->rec64;
   }
   const int key = ctx->dim * 10 + ctx->k;
+  int st;
   switch (key) {
-    case 21: return launch_apply_dn<T, 2, 2>(ctx, a, p, rec);
-    case 22: return launch_apply_dn<T, 2, 3>(ctx, a, p, rec);
-    case 23: return launch_apply_dn<T, 2, 4>(ctx, a, p, rec);
-    case 24: return launch_apply_dn<T, 2, 5>(ctx, a, p, rec);
-    case 31: return launch_apply_dn<T, 3, 2>(ctx, a, p, rec);
-    case 32: return launch_apply_dn<T, 3, 3>(ctx, a, p, rec);
-    case 33: return launch_apply_dn<T, 3, 4>(ctx, a, p, rec);
-    case 34: return launch_apply_dn<T, 3, 5>(ctx, a, p, rec);
+    case 21: st = launch_apply_dn<T, 2, 2>(ctx, a, p, rec); break;
+    case 22: st = launch_apply_dn<T, 2, 3>(ctx, a, p, rec); break;
+    case 23: st = launch_apply_dn<T, 2, 4>(ctx, a, p, rec); break;
+    case 24: st = launch_apply_dn<T, 2, 5>(ctx, a, p, rec); break;
+    case 31: st = launch_apply_dn<T, 3, 2>(ctx, a, p, rec); break;
+    case 32: st = launch_apply_dn<T, 3, 3>(ctx, a, p, rec); break;
+    case 33: st = launch_apply_dn<T, 3, 4>(ctx, a, p, rec); break;
+    case 34: st = launch_apply_dn<T, 3, 5>(ctx, a, p, rec); break;
     default: return set_error(PDG_EUNSUPPORTED, "dim/degree not compiled in");
   }
+  if (st == PDG_OK && ctx->vel.nmodes > 0) st = launch_convection<T>(ctx, a);
+  return st;
 }
 
 template int launch_apply<double>(pdg_context *, const ApplyArgs<double> &, const double *,

@@ -130,6 +130,10 @@ struct pdg_context {
   int r0_valid;
   double *rec64;       // FP64 per-cell operator records (scaled A'_dir + face coefficients)
   int rec_valid;
+  double *conv64;      // per-cell weighted velocity at volume and face points (FP64)
+  float *conv32;       // the same in FP32
+  double *convtab64;   // B and D (basis values / derivatives at Gauss points)
+  float *convtab32;
 
   // preconditioner, one instance per precision (index PDG_F64 / PDG_F32)
   pdg::PrecData prec[2];
@@ -182,5 +186,12 @@ struct RhsTables {
 };
 RhsTables make_rhs_tables(const pdg_context *ctx);
 double *rhs_r0K(pdg_context *ctx, bool alloc);
+double lagrange_derivative(int k, int i, double x);
+
+// convection (3D): set-up of the per-cell velocity records, and the launch
+// that adds alpha * C x (or C^T x) to y after the diffusion operator
+int conv_setup(pdg_context *ctx);
+template <typename T>
+int launch_convection(pdg_context *ctx, const ApplyArgs<T> &a);
 
 }  // namespace pdg

@@ -149,6 +149,27 @@ def _ptr(v, dtype=np.float64):
     raise TypeError(f"unsupported vector type {type(v)}")
 
 
+def fourier_velocity_modes(seed, nmodes=8, bmax=10.0, kmax=2):
+    """Divergence-free velocity b = curl A of a seeded Fourier vector potential
+    A(x) = sum_m a_m cos(2 pi k_m.x + phi_m):
+    b(x) = sum_m c_m sin(2 pi k_m.x + phi_m) with c_m = -2 pi k_m x a_m
+    (so k_m . c_m = 0 and div b = 0), scaled so that sum_m |c_m| = bmax,
+    which bounds |b| <= bmax everywhere.  Rows: kx ky kz phase cx cy cz."""
+    rng = np.random.default_rng(seed)
+    modes = np.zeros((nmodes, 7))
+    for m in range(nmodes):
+        k = np.zeros(3)
+        while not k.any():
+            k = rng.integers(-kmax, kmax + 1, 3).astype(float)
+        a = rng.standard_normal(3)
+        modes[m, :3] = k
+        modes[m, 3] = rng.uniform(0, 2 * np.pi)
+        modes[m, 4:] = -2 * np.pi * np.cross(k, a)
+    s = np.linalg.norm(modes[:, 4:], axis=1).sum()
+    modes[:, 4:] *= bmax / s
+    return modes
+
+
 def default_options(**kw):
     o = SolverOptions()
     load().pdg_default_solver_options(C.byref(o))

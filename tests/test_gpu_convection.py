@@ -1,0 +1,125 @@
+"""Convection-diffusion-reaction (upwind DG, config C5 at test size):
+the CUDA operator with a divergence-free Fourier velocity against the oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def pdg():
+    import __graft_entry__
+    __graft_entry__.build()
+    import pdg as m
+    return m
+
+
+def _pair(pdg, oracle, k, n, seed, method=1, bct=None, react=True):
+    rng = np.random.default_rng(seed)
+    nc = (n,) * 3 if np.isscalar(n) else tuple(n)
+    ncell = int(np.prod(nc))
+    K = np.exp(rng.standard_normal(ncell))
+    c = np.ones(ncell) if react else None
+    modes = pdg.fourier_velocity_modes(seed)
+    go = pdg.GridOperator(3, k, nc, alpha=3.0, method=method, bctype=bct)
+    go.set_permeability(K)
+    if react:
+        go.set_reaction(c)
+    go.set_velocity_modes(modes)
+    P = oracle.Problem(3, k, nc, alpha=3.0, method=method, bctype=bct, K=K, c=c, modes=modes)
+    return go, P, rng
+
+
+def test_velocity_is_divergence_free_and_bounded(pdg):
+    m = pdg.fourier_velocity_modes(5)
+    assert np.allclose((m[:, :3] * m[:, 4:]).sum(1), 0)
+    assert np.linalg.norm(m[:, 4:], axis=1).sum() <= 10 + 1e-12
+
+
+@pytest.mark.parametrize("k,n", [(1, 4), (2, 3), (3, 3), (4, 2), (2, (4, 3, 2))])
+def test_convection_apply_f64(pdg, oracle, k, n):
+    go, P, rng = _pair(pdg, oracle, k, n, seed=40 + k)
+    x = rng.uniform(-1, 1, go.ndof)
+    y0 = rng.uniform(-1, 1, go.ndof)
+    y = y0.copy()
+    go.jacobian_apply(x, y)
+    assert _rel(y, P.jacobian_apply(x, y0.copy())) <= 1e-12
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_convection_transpose(pdg, oracle, method):
+    go, P, rng = _pair(pdg, oracle, 2, 3, seed=50 + method, method=method)
+    A = P.assemble_jacobian()
+    x = rng.uniform(-1, 1, go.ndof)
+    y = np.zeros(go.ndof)
+    go.jacobian_apply_transpose(x, y)
+    assert _rel(y, P.blocks_apply(A, x, transpose=True)) <= 1e-12
+
+
+def test_convection_f32_and_boundary_types(pdg, oracle):
+    import torch
+    bct = [1, -1, 1, -3, 1, -1]
+    go, P, rng = _pair(pdg, oracle, 3, 3, seed=61, bct=bct)
+    x = rng.uniform(-1, 1, go.ndof)
+    y = np.zeros(go.ndof)
+    go.jacobian_apply(x, y)
+    yref = P.jacobian_apply(x)
+    assert _rel(y, yref) <= 1e-12
+    xt = torch.tensor(x, dtype=torch.float32, device="cuda")
+    yt = torch.zeros_like(xt)
+    go.jacobian_apply_f32(xt, yt)
+    torch.cuda.synchronize()
+    assert _rel(yt.cpu().double().numpy(), yref) <= 2e-5
+
+
+def test_outflow_on_inflow_is_an_error(pdg):
+    # every side outflow: b.n < 0 somewhere -> PDG_EOUTFLOW (convectiondiffusiondg.hh:802-806)
+    go = pdg.GridOperator(3, 2, (3, 3, 3), bctype=[-2] * 6)
+    with pytest.raises(pdg.PDGError) as e:
+        go.set_velocity_modes(pdg.fourier_velocity_modes(1))
+    assert e.value.status == pdg.PDG_EOUTFLOW
+
+
+def test_convection_residual_with_inflow_data(pdg, oracle):
+    go, P, rng = _pair(pdg, oracle, 2, 3, seed=71)
+    g = rng.standard_normal(go.nq_boundary)
+    fc = rng.standard_normal(go.ncell)
+    go.set_boundary_data(g=g)
+    go.set_source(fc=fc)
+    P.set(gq=g, fc=fc)
+    x = rng.uniform(-1, 1, go.ndof)
+    r = np.zeros(go.ndof)
+    go.residual(x, r)
+    assert _rel(r, P.residual(x)) <= 1e-12
+
+
+def test_convection_block_jacobi_dense(pdg, oracle):
+    go, P, rng = _pair(pdg, oracle, 2, 3, seed=81)
+    lu, piv = P.lu(P.block_diagonal())
+    d = rng.uniform(-1, 1, go.ndof)
+    prec = pdg.GridOperatorPreconditioner(go, kind=pdg.PREC_BJ_DENSE)
+    prec.pre()
+    v = np.zeros(go.ndof)
+    prec.apply(v, d)
+    assert _rel(v, P.lu_apply(lu, piv, d)) <= 1e-10
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_convection_bicgstab_solve(pdg, oracle, mixed):
+    go, P, rng = _pair(pdg, oracle, 2, 4, seed=91)
+    go.set_source(fc=np.ones(go.ncell))
+    P.set(fc=np.ones(go.ncell))
+    uref, rres, st = P.solve(solver="bicgstab", op=0, reduction=1e-10)
+    assert rres.converged
+    ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.BICGSTAB,
+                                             preconditioner=pdg.PREC_BJ_DENSE, mixed=mixed)
+    u = np.zeros(go.ndof)
+    pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10).apply()
+    assert ls.result().converged
+    if not mixed:
+        assert abs(ls.result().iterations - rres.iterations) <= 1
+    assert _rel(u, uref) <= 1e-8

@@ -115,3 +115,19 @@ def test_convergence_order(oracle, k):
         errs.append(_l2err2(P, u, lambda x: np.prod(np.sin(np.pi * x), axis=-1), k + 3) ** 0.5)
     rate = np.log2(errs[0] / errs[1])
     assert rate > k + 1 - 0.6, (errs, rate)
+
+
+def test_convection_matrix_free_equals_assembled(oracle):
+    import sys
+    import os
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "..", "dune-pdelab_gb300"))
+    import pdg
+    rng = np.random.default_rng(4)
+    m = pdg.fourier_velocity_modes(3)
+    for method in (oracle.SIPG, oracle.NIPG):
+        P = oracle.Problem(3, 2, (3, 3, 3), alpha=3.0, method=method,
+                           K=np.exp(rng.standard_normal(27)), c=np.ones(27), modes=m)
+        x = rng.uniform(-1, 1, P.ndof)
+        y = P.jacobian_apply(x)
+        A = P.assemble_jacobian()
+        assert np.max(np.abs(y - P.blocks_apply(A, x))) <= 1e-13 * np.max(np.abs(y))
