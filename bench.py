@@ -382,7 +382,15 @@ def run_gb300(args, world, rank, local):
     if not args.no_solves:
         extras = solve_metrics(pdg, np, torch, go, stream, logK)
     if args.extended:
-        extras["solve_q3_96"] = c3_metrics(pdg, np, torch, stream)
+        legs = set(args.legs.split(","))
+        for leg, key, fn in (("c3", "solve_q3_96", c3_metrics), ("c4", "adjoint_q2_64", c4_metrics),
+                             ("c5", "cdr_q4_48", c5_metrics)):
+            if leg not in legs:
+                continue
+            try:
+                extras[key] = fn(pdg, np, torch, stream)
+            except Exception as exc:   # report the failing leg, keep the others
+                extras[key] = {"error": f"{type(exc).__name__}: {exc}"}
     cpu = cpu_baseline_port(np, WORKLOAD) if not args.no_cpu else None
     go.close()
     line = {
@@ -451,12 +459,180 @@ def c3_metrics(pdg, np, torch, stream, inner_reduction=1e-4):
         out[f"{key}_converged"] = bool(r.converged)
         if mixed:
             out["mixed_outer_iterations"] = r.outer_iterations
+        if mixed:
+            out["mixed_outer_iterations"] = r.outer_iterations
     e = sols["mixed"] - sols["fp64"]
     out["speedup_mixed_vs_fp64"] = out["fp64_s"] / out["mixed_s"]
     out["mixed_vs_fp64_rel_l2"] = float(torch.linalg.norm(e) / torch.linalg.norm(sols["fp64"]))
     out["mixed_vs_fp64_rel_max"] = float(e.abs().max() / sols["fp64"].abs().max())
     go.close()
     return out
+
+
+def c4_metrics(pdg, np, torch, stream, ndirs=16):
+    """Adjoint on 64^3 Q2: J = 1/2 |u - u_obs|^2, u_obs = u(target log K) + 1%
+    noise; the autograd gradient against central differences (h = 1e-6) along
+    16 seeded directions, and (on a 16^3 grid) against the oracle's gradient
+    from the assembled CPU Jacobian transpose."""
+    import pdg_torch
+    out = {}
+    for n, check in ((64, "fd"), (16, "jt")):
+        rng = np.random.default_rng(40 + n)
+        go = pdg.GridOperator(3, 2, (n, n, n), alpha=3.0, device=stream.device.index or 0)
+        pdg.load().pdg_set_stream(go.handle, ctypes.c_void_p(stream.cuda_stream))
+        go.set_source(fc=np.ones(go.ncell))
+        prob = pdg_torch.DGProblem(go, reduction=1e-11)
+        logK_t = torch.tensor(rng.standard_normal(go.ncell), device=stream.device)
+        u_obs = pdg_torch.solve_dg(logK_t, None, prob).detach()
+        u_obs = u_obs * (1 + 0.01 * torch.tensor(rng.standard_normal(go.ndof), device=u_obs.device))
+        logK = torch.tensor(rng.standard_normal(go.ncell), device=stream.device,
+                            requires_grad=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        u = pdg_torch.solve_dg(logK, None, prob)
+        torch.cuda.synchronize()
+        t_fwd = time.perf_counter() - t0
+        J = 0.5 * ((u - u_obs) ** 2).sum()
+        t0 = time.perf_counter()
+        J.backward()
+        torch.cuda.synchronize()
+        t_bwd = time.perf_counter() - t0
+        g = logK.grad.detach()
+        if check == "fd":
+            h, errs = 1e-6, []
+            with torch.no_grad():
+                for _ in range(ndirs):
+                    d = torch.tensor(rng.standard_normal(go.ncell), device=g.device)
+                    Jp = 0.5 * ((pdg_torch.solve_dg(logK + h * d, None, prob) - u_obs) ** 2).sum()
+                    Jm = 0.5 * ((pdg_torch.solve_dg(logK - h * d, None, prob) - u_obs) ** 2).sum()
+                    fd = float((Jp - Jm) / (2 * h))
+                    ad = float((g * d).sum())
+                    errs.append(abs(fd - ad) / abs(ad))
+            out["grid_64"] = {"forward_solve_s": t_fwd, "adjoint_solve_plus_grad_s": t_bwd,
+                              "grad_over_solve": t_bwd / t_fwd,
+                              "total_over_solve": (t_fwd + t_bwd) / t_fwd,
+                              "fd_directions": ndirs, "fd_h": h,
+                              "fd_rel_err_max": max(errs), "fd_rel_err_median": float(np.median(errs))}
+        else:
+            import pdg_oracle as O
+            K = np.exp(logK.detach().cpu().numpy())
+            P = O.Problem(3, 2, (n, n, n), alpha=3.0, K=K, fc=np.ones(go.ncell))
+            A = P.assemble_jacobian()
+            un = u.detach().cpu().numpy()
+            lam = np.zeros(go.ndof)
+            lu, piv = P.lu(P.block_diagonal())
+            st, res = P.krylov("cg", lam, un - u_obs.cpu().numpy(), 1e-13, maxit=50000, op=2,
+                               blocks=A, lu=lu, piv=piv)
+            gref = P.grad_logK(un, lam)
+            gg = g.cpu().numpy()
+            out["grid_16_assembled_transpose"] = {
+                "rel_err_max": float(np.max(np.abs(gg - gref)) / np.max(np.abs(gref))),
+                "oracle_cg_iterations": res.iterations}
+        go.close()
+    return out
+
+
+C5_INNER_REDUCTION = 1e-1
+C5_INNER_MAXIT = 50
+
+
+def c5_metrics(pdg, np, torch, stream):
+    """48^3 Q4 (13.8M DoF) convection-diffusion-reaction, upwind flux, b = curl
+    of a seeded 8-mode Fourier potential (|b| <= 10), c = 1, log-normal K,
+    f = 1, Dirichlet 0; BiCGStab + dense cell-block Jacobi, FP32 apply in FP64
+    refinement vs FP64, reduction 1e-9; gradients w.r.t. log K and f vs central
+    differences along 2 seeded directions each.  The mixed solve is FP64
+    flexible GMRES around FP32 BiCGStab inner solves of reduction 1e-1 (at
+    most 50 iterations each)."""
+    import pdg_torch
+    n = 48
+    dev = stream.device
+    go = pdg.GridOperator(3, 4, (n, n, n), alpha=3.0, device=dev.index or 0)
+    pdg.load().pdg_set_stream(go.handle, ctypes.c_void_p(stream.cuda_stream))
+    rng = np.random.default_rng(5)
+    logK0 = rng.standard_normal(go.ncell)
+    go.set_permeability(logK0, is_log=True)
+    go.set_reaction(np.ones(go.ncell))
+    go.set_velocity_modes(pdg.fourier_velocity_modes(5))
+    go.set_source(fc=np.ones(go.ncell))
+    out = {"workload": "sipg3d_q4_48^3 (13.8M DoF), upwind convection |b|<=10, c=1, "
+                       "BiCGStab + dense cell-block Jacobi, reduction 1e-9"}
+    sols = {}
+    for mixed in (True, False):
+        pdg.GridOperatorPreconditioner(go, kind=pdg.PREC_BJ_DENSE,
+                                       precision=pdg.F32 if mixed else pdg.F64).pre()
+        ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.BICGSTAB,
+                                                 preconditioner=pdg.PREC_BJ_DENSE,
+                                                 mixed=mixed, maxiter=20000,
+                                                 inner_reduction=C5_INNER_REDUCTION)
+        ls.opts.inner_maxit = C5_INNER_MAXIT
+        ls.opts.max_outer = 60
+        u = torch.zeros(go.ndof, dtype=torch.float64, device=dev)
+        slp = pdg.StationaryLinearProblemSolver(go, ls, u, 1e-9)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        slp.apply()
+        dt = time.perf_counter() - t0
+        r = slp.result()
+        key = "mixed" if mixed else "fp64"
+        sols[key] = u
+        out[f"{key}_s"] = dt
+        out[f"{key}_iterations"] = r.iterations
+        out[f"{key}_converged"] = bool(r.converged)
+        if mixed:
+            out["mixed_outer_iterations"] = r.outer_iterations
+    e = sols["mixed"] - sols["fp64"]
+    out["speedup_mixed_vs_fp64"] = out["fp64_s"] / out["mixed_s"]
+    out["mixed_vs_fp64_rel_l2"] = float(torch.linalg.norm(e) / torch.linalg.norm(sols["fp64"]))
+    try:
+        out["adjoint"] = _c5_gradients(pdg, pdg_torch, np, torch, go, dev, rng, logK0,
+                                       sols["fp64"])
+    except Exception as exc:
+        out["adjoint"] = {"error": f"{type(exc).__name__}: {exc}"}
+    go.close()
+    return out
+
+
+def _c5_gradients(pdg, pdg_torch, np, torch, go, dev, rng, logK0, u_ref):
+    # mixed-precision solves to the configuration's 1e-9
+    prob = pdg_torch.DGProblem(go, method=pdg.BICGSTAB, preconditioner=pdg.PREC_BJ_DENSE,
+                               reduction=1e-9, inner_reduction=C5_INNER_REDUCTION,
+                               inner_maxit=C5_INNER_MAXIT)
+    sols = {"fp64": u_ref}
+    u_obs = sols["fp64"] * (1 + 0.01 * torch.tensor(rng.standard_normal(go.ndof), device=dev))
+    logK = torch.tensor(logK0 + 0.3 * rng.standard_normal(go.ncell), device=dev,
+                        requires_grad=True)
+    fc = torch.ones(go.ncell, dtype=torch.float64, device=dev, requires_grad=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    u = pdg_torch.solve_dg(logK, fc, prob)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    J = 0.5 * ((u - u_obs) ** 2).sum()
+    t0 = time.perf_counter()
+    J.backward()
+    torch.cuda.synchronize()
+    t_bwd = time.perf_counter() - t0
+    errs = {}
+    h = 1e-6
+    with torch.no_grad():
+        for name, grad in (("logK", logK.grad), ("f", fc.grad)):
+            ee = []
+            for _ in range(2):
+                d = torch.tensor(rng.standard_normal(go.ncell), device=dev)
+                if name == "logK":
+                    Jp = 0.5 * ((pdg_torch.solve_dg(logK + h * d, fc, prob) - u_obs) ** 2).sum()
+                    Jm = 0.5 * ((pdg_torch.solve_dg(logK - h * d, fc, prob) - u_obs) ** 2).sum()
+                else:
+                    Jp = 0.5 * ((pdg_torch.solve_dg(logK, fc + h * d, prob) - u_obs) ** 2).sum()
+                    Jm = 0.5 * ((pdg_torch.solve_dg(logK, fc - h * d, prob) - u_obs) ** 2).sum()
+                fd = float((Jp - Jm) / (2 * h))
+                ad = float((grad * d).sum())
+                ee.append(abs(fd - ad) / abs(ad))
+            errs[name] = max(ee)
+    return {"forward_solve_s": t_fwd, "adjoint_solve_plus_grads_s": t_bwd,
+            "grad_over_solve": t_bwd / t_fwd, "reduction": 1e-9, "fd_h": h,
+            "fd_rel_err_max_logK": errs["logK"], "fd_rel_err_max_f": errs["f"]}
 
 
 def solve_metrics(pdg, np, torch, go, stream, logK):
@@ -520,7 +696,9 @@ def main():
     ap.add_argument("--no-solves", action="store_true", help="skip solve/adjoint metrics")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--extended", action="store_true",
-                    help="also time the 96^3 Q3 FP64 and mixed-precision solves")
+                    help="also run the 96^3 Q3 solves (c3), the 64^3 adjoint checks (c4) and "
+                         "the 48^3 Q4 convection-diffusion-reaction solves and gradients (c5)")
+    ap.add_argument("--legs", default="c3,c4,c5", help="subset of the extended legs")
     ap.add_argument("--no-probe", action="store_true",
                     help="skip the FMA peak probe (profiling runs); roofline frac is then null")
     ap.add_argument("--solves-only", action="store_true",

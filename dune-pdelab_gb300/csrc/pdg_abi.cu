@@ -8,11 +8,13 @@
 //     matrixfree/gridoperatorpreconditioner.hh:45-84)
 // with dune-istl's CGSolver / BiCGSTABSolver recurrences (external to the
 // reference; restated from the published algorithms).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
 
+#include "pdg_gmres.cuh"
 #include "pdg_internal.cuh"
 #include "pdg_vec.cuh"
 
@@ -113,8 +115,29 @@ template <> const float *Tp<float>(const pdg_context *c) { return c->tab32; }
 template <typename T>
 static int op_launch(pdg_context *ctx, const T *x, T *y, const T *add, T alpha, int acc,
                      int transpose, const int *skip) {
+  if (std::is_same<T, double>::value && ctx->ops32) {
+    // FP64 Krylov vectors, FP32 operator: convert, apply in FP32, combine in FP64
+    float *s0 = ctx->w32[0], *s1 = ctx->w32[1];
+    PDG_TRY(vec_to_f32_skip(ctx, ctx->ndof, (const double *)x, s0, skip));
+    ApplyArgs<float> a{s0, s1, nullptr, 1.f, 0, transpose, 0, skip};
+    PDG_TRY(launch_apply<float>(ctx, a, ctx->K32, ctx->c32, ctx->tab32));
+    return vec_from_f32_combine(ctx, ctx->ndof, s1, (double *)y, (const double *)add,
+                                (double)alpha, acc, skip);
+  }
   ApplyArgs<T> a{x, y, add, alpha, acc, transpose, 0, skip};
   return launch_apply<T>(ctx, a, Kp<T>(ctx), Cp<T>(ctx), Tp<T>(ctx));
+}
+
+// preconditioner inside a Krylov solve (FP32 block Jacobi under ctx->ops32)
+template <typename T>
+static int prec_op(pdg_context *ctx, const T *d, T *v, int transpose, const int *skip) {
+  if (std::is_same<T, double>::value && ctx->ops32) {
+    float *s0 = ctx->w32[0], *s1 = ctx->w32[1];
+    PDG_TRY(vec_to_f32_skip(ctx, ctx->ndof, (const double *)d, s0, skip));
+    PDG_TRY(prec_apply_skip<float>(ctx, s0, s1, transpose, skip));
+    return vec_from_f32_combine(ctx, ctx->ndof, s1, (double *)v, nullptr, 1.0, 0, skip);
+  }
+  return prec_apply_skip<T>(ctx, d, v, transpose, skip);
 }
 
 static int ensure_r0(pdg_context *ctx) {
@@ -126,7 +149,7 @@ static int ensure_r0(pdg_context *ctx) {
 }
 
 static int ensure_work(pdg_context *ctx, bool f32) {
-  for (int i = 0; i < 8; i++)
+  for (int i = 0; i < (f32 ? 10 : 8); i++)
     if (!ctx->w64[i]) PDG_CUDA_TRY(cudaMalloc(&ctx->w64[i], sizeof(double) * ctx->ndof));
   if (f32)
     for (int i = 0; i < 8; i++)
@@ -152,9 +175,10 @@ static int fetch_state(pdg_context *ctx, double *scal, int *flags) {
 }
 
 __global__ void k_set_scal(double *scal, int slot, double v) { scal[slot] = v; }
-__global__ void k_init_solve(double *scal, int *flags, double red) {
+__global__ void k_init_solve(double *scal, int *flags, double red, double guard = 0.0) {
   for (int i = 0; i < S_COUNT; i++) scal[i] = 0.0;
   scal[S_RED] = red;
+  scal[S_GUARD] = guard;
   scal[S_RHO] = 1.0;
   scal[S_ALPHA] = 1.0;
   scal[S_OMEGA] = 1.0;
@@ -190,7 +214,7 @@ static int cg_device(pdg_context *ctx, T *x, T *b, T *p, T *q, double reduction,
   PDG_TRY(op_launch<T>(ctx, x, b, nullptr, T(-1), 1, transpose, nullptr));
   PDG_TRY(dot<T>(ctx, rc, b, b, nullptr, nullptr, FIN_DEF0, -1, -1, false));
   // p = M^{-1} b ; rholast = <p, b>
-  PDG_TRY(prec_apply_skip<T>(ctx, b, p, transpose, skip));
+  PDG_TRY(prec_op<T>(ctx, b, p, transpose, skip));
   PDG_TRY(dot<T>(ctx, rc, p, b, nullptr, nullptr, FIN_STORE, S_RHO, -1, true));
   double scal[S_COUNT];
   int flags[F_COUNT];
@@ -202,7 +226,7 @@ static int cg_device(pdg_context *ctx, T *x, T *b, T *p, T *q, double reduction,
     PDG_TRY(op_launch<T>(ctx, p, q, nullptr, T(1), 0, transpose, skip));          // q = A p
     PDG_TRY(dot<T>(ctx, rc, p, q, nullptr, nullptr, FIN_CG_LAMBDA, -1, -1, true)); // lambda
     PDG_TRY(cg_update_xr<T>(ctx, rc, ctx->ndof, x, b, p, q));                     // x, b, def
-    PDG_TRY(prec_apply_skip<T>(ctx, b, q, transpose, skip));                        // q = M^-1 b
+    PDG_TRY(prec_op<T>(ctx, b, q, transpose, skip));                        // q = M^-1 b
     PDG_TRY(dot<T>(ctx, rc, q, b, nullptr, nullptr, FIN_CG_BETA, -1, -1, true));   // beta
     PDG_TRY(cg_update_p<T>(ctx, rc, ctx->ndof, p, q));                             // p = q + beta p
     if (i % batch == 0 || i == maxit || i == 1) {
@@ -220,12 +244,20 @@ static int cg_device(pdg_context *ctx, T *x, T *b, T *p, T *q, double reduction,
 
 // dune-istl BiCGSTABSolver::apply restated on the device.
 template <typename T>
-static int bicgstab_device(pdg_context *ctx, T *x, T *b, T *w[5], double reduction, int maxit,
-                           int transpose, KrylovOut *out) {
+static int bicgstab_device(pdg_context *ctx, T *x, T *b, T *w[8], double reduction, int maxit,
+                           int transpose, KrylovOut *out, double guard, int replace) {
   const RedCtx rc = red_ctx(ctx);
   const int *skip = ctx->d_flag + F_STATE;
-  T *r = b, *p = w[0], *v = w[1], *t = w[2], *y = w[3], *rt = w[4];
-  k_init_solve<<<1, 1, 0, ctx->stream>>>(rc.scal, rc.flags, reduction);
+  T *r = b, *p = w[0], *v = w[1], *t = w[2], *y = w[3], *rt = w[4], *bk = w[7];
+  // guard > 0 (FP32 inner solves) adds relative breakdown tests to dune-istl's.
+  // replace > 0 (FP32 inner solves): every `replace` iterations the
+  // recursively updated residual is replaced by the true one, r = b - A x,
+  // keeping the recurrence (p, v, rt, rho, alpha, omega) -- reliable updating
+  // (Sleijpen & van der Vorst 1996; van der Vorst & Ye 2000).  In FP32 the
+  // recursive residual of a long BiCGStab run otherwise drifts away from the
+  // true residual.
+  if (replace > 0) PDG_TRY(vec_copy<T>(ctx, ctx->ndof, b, bk));
+  k_init_solve<<<1, 1, 0, ctx->stream>>>(rc.scal, rc.flags, reduction, guard);
   PDG_TRY(op_launch<T>(ctx, x, r, nullptr, T(-1), 1, transpose, nullptr));
   PDG_TRY(vec_copy<T>(ctx, ctx->ndof, r, rt));
   PDG_TRY(dot<T>(ctx, rc, r, r, nullptr, nullptr, FIN_DEF0, -1, -1, false));
@@ -239,16 +271,18 @@ static int bicgstab_device(pdg_context *ctx, T *x, T *b, T *w[5], double reducti
     PDG_TRY(set_iter(ctx, rc, it));
     PDG_TRY(dot<T>(ctx, rc, rt, r, nullptr, nullptr, FIN_BI_RHONEW, -1, -1, true));
     PDG_TRY(bi_update_p<T>(ctx, rc, ctx->ndof, p, r, v, it < 1));
-    PDG_TRY(prec_apply_skip<T>(ctx, p, y, transpose, skip));
+    PDG_TRY(prec_op<T>(ctx, p, y, transpose, skip));
     PDG_TRY(op_launch<T>(ctx, y, v, nullptr, T(1), 0, transpose, skip));
-    PDG_TRY(dot<T>(ctx, rc, rt, v, nullptr, nullptr, FIN_BI_ALPHA, -1, -1, true));
+    PDG_TRY(dot<T>(ctx, rc, rt, v, v, v, FIN_BI_ALPHA, -1, -1, true));
     PDG_TRY(bi_update_half<T>(ctx, rc, ctx->ndof, x, r, y, v));
     it += 0.5;
     PDG_TRY(set_iter(ctx, rc, it));
-    PDG_TRY(prec_apply_skip<T>(ctx, r, y, transpose, skip));
+    PDG_TRY(prec_op<T>(ctx, r, y, transpose, skip));
     PDG_TRY(op_launch<T>(ctx, y, t, nullptr, T(1), 0, transpose, skip));
     PDG_TRY(dot<T>(ctx, rc, t, r, t, t, FIN_BI_OMEGA, -1, -1, true));
     PDG_TRY(bi_update_full<T>(ctx, rc, ctx->ndof, x, r, y, t));
+    if (replace > 0 && (loop + 1) % replace == 0)
+      PDG_TRY(op_launch<T>(ctx, x, r, bk, T(-1), 0, transpose, skip));   // r = b - A x
     if (loop % 4 == 3 || it + 0.5 >= maxit || loop == 0) {
       PDG_TRY(fetch_state(ctx, scal, flags));
       if (flags[F_STATE]) done = true;
@@ -264,10 +298,30 @@ static int bicgstab_device(pdg_context *ctx, T *x, T *b, T *w[5], double reducti
 
 template <typename T>
 static int krylov_device(pdg_context *ctx, int method, T *x, T *b, T **w, double reduction,
-                         int maxit, int transpose, KrylovOut *out) {
+                         int maxit, int transpose, KrylovOut *out, double guard = 0.0,
+                         int restart = 30, int replace = 0) {
   if (method == PDG_CG) return cg_device<T>(ctx, x, b, w[0], w[1], reduction, maxit, transpose, out);
   if (method == PDG_BICGSTAB)
-    return bicgstab_device<T>(ctx, x, b, w, reduction, maxit, transpose, out);
+    return bicgstab_device<T>(ctx, x, b, w, reduction, maxit, transpose, out, guard, replace);
+  if (method == PDG_GMRES) {
+    // b is the right-hand side; GMRES keeps the residual in place of b.
+    // Work vectors w[2], w[3] (free of the defect-correction loop's slots).
+    const bool f32 = std::is_same<T, float>::value;
+    void *&V = f32 ? ctx->gm_V32 : ctx->gm_V64;
+    int &Vm = f32 ? ctx->gm_m32 : ctx->gm_m64;
+    auto op = [&](const T *in, T *o) -> int {
+      return op_launch<T>(ctx, in, o, nullptr, T(1), 0, transpose, nullptr);
+    };
+    auto prec = [&](const T *in, T *o) -> int { return prec_op<T>(ctx, in, o, transpose, nullptr); };
+    GmresOut go;
+    PDG_TRY(gmres_core<T>(ctx, x, b, w[2], w[3], V, Vm, reduction, maxit, restart, false, false, op,
+                          prec, &go));
+    out->state = go.state;
+    out->iterations = go.iterations;
+    out->def0 = go.def0;
+    out->def = go.def;
+    return PDG_OK;
+  }
   return set_error(PDG_EINVAL, "unknown Krylov method");
 }
 
@@ -294,18 +348,96 @@ static int ensure_prec(pdg_context *ctx, int kind, int precision) {
   return prec_setup_impl(ctx, kind, precision);
 }
 
+static double elapsed_since_ev0(pdg_context *ctx) {
+  cudaEventRecord(ctx->ev1, ctx->stream);
+  cudaEventSynchronize(ctx->ev1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  return ms * 1e-3;
+}
+
+// Mixed precision for non-symmetric operators: FP64 flexible GMRES with the
+// exact FP64 operator, whose preconditioner for each new direction v is a
+// short inner Krylov solve J c = v with the FP32 operator and FP32 block
+// Jacobi (inner_reduction / inner_maxit).  Every outer step minimises the
+// true FP64 residual over all inner corrections so far, so an inaccurate
+// inner solve slows the outer iteration but cannot make it diverge.  An inner
+// solve that ends non-finite is replaced by one FP32 block-Jacobi application.
+static int solve_fgmres_ir(pdg_context *ctx, const pdg_solver_options *opt, double *z, double *r,
+                           int transpose, pdg_solver_result *res) {
+  PDG_TRY(ensure_prec(ctx, opt->preconditioner, PDG_F32));
+  const long n = ctx->ndof;
+  const int inner = opt->inner_method >= 0 ? opt->inner_method : opt->method;
+  const bool vec64 = opt->inner_vectors == PDG_F64;
+  int total_inner = 0, fallbacks = 0;
+  auto op = [&](const double *in, double *o) -> int {
+    return op_launch<double>(ctx, in, o, nullptr, 1.0, 0, transpose, nullptr);
+  };
+  auto prec = [&](const double *v, double *o) -> int {
+    KrylovOut ko{};
+    if (!vec64) {
+      float *d32 = ctx->w32[5], *c32 = ctx->w32[6];
+      PDG_TRY(vec_to_f32(ctx, n, v, d32));
+      PDG_TRY(vec_fill<float>(ctx, n, c32, 0.f));
+      PDG_TRY(krylov_device<float>(ctx, inner, c32, d32, ctx->w32, opt->inner_reduction,
+                                   opt->inner_maxit, transpose, &ko, opt->inner_breakdown,
+                                   opt->restart, opt->inner_replace));
+      total_inner += ko.iterations;
+      if (ko.state != 2) return vec_from_f32_combine(ctx, n, c32, o, nullptr, 1.0, 0, nullptr);
+    } else {
+      double *c64 = ctx->w64[8], *d64 = ctx->w64[9];
+      PDG_TRY(vec_copy<double>(ctx, n, v, d64));
+      PDG_TRY(vec_fill<double>(ctx, n, c64, 0.0));
+      ctx->ops32 = 1;
+      const int ks = krylov_device<double>(ctx, inner, c64, d64, ctx->w64, opt->inner_reduction,
+                                           opt->inner_maxit, transpose, &ko, 0.0, opt->restart, 0);
+      ctx->ops32 = 0;
+      PDG_TRY(ks);
+      total_inner += ko.iterations;
+      if (ko.state != 2) return vec_copy<double>(ctx, n, c64, o);
+    }
+    fallbacks++;
+    ctx->ops32 = 1;
+    const int s = prec_op<double>(ctx, v, o, transpose, nullptr);
+    ctx->ops32 = 0;
+    return s;
+  };
+  const int m = std::max(1, std::min(opt->restart, opt->max_outer));
+  GmresOut go;
+  PDG_TRY(gmres_core<double>(ctx, z, r, ctx->w64[5], ctx->w64[6], ctx->gm_F64, ctx->gm_mF,
+                             opt->reduction, opt->max_outer, m, true, opt->verbose != 0, op, prec,
+                             &go));
+  if (opt->verbose && fallbacks)
+    std::fprintf(stderr, "pdg fgmres: %d inner solves replaced by block Jacobi\n", fallbacks);
+  res->converged = go.state == 1;
+  res->iterations = total_inner;
+  res->outer_iterations = go.iterations;
+  res->elapsed = elapsed_since_ev0(ctx);
+  res->first_defect = go.def0;
+  res->defect = go.def;
+  res->reduction = go.def0 > 0 ? go.def / go.def0 : 0.0;
+  res->conv_rate = total_inner > 0 ? std::pow(res->reduction, 1.0 / total_inner) : 0.0;
+  res->status = state_status(go.state);
+  if (res->status) return res->status;
+  return res->converged ? PDG_OK
+                        : set_error(PDG_ENOTCONVERGED, "flexible GMRES did not converge");
+}
+
 // Solve J z = r (transposed when `transpose`) from z = 0 or the given z.
-// FP64 Krylov, or FP32 Krylov inside FP64 defect correction when opt->mixed.
-// r is overwritten by the final defect.
+// FP64 Krylov; with opt->mixed, FP32 Krylov inside FP64 defect correction
+// (CG, or mixed = 2) or inside FP64 flexible GMRES (BiCGStab / GMRES, or
+// mixed = 3).  r is overwritten by the final defect.
 static int solve_correction(pdg_context *ctx, const pdg_solver_options *opt, double *z,
                             double *r, int transpose, pdg_solver_result *res) {
   PDG_TRY(ensure_work(ctx, opt->mixed != 0));
   cudaEventRecord(ctx->ev0, ctx->stream);
+  if (opt->mixed == 3 || (opt->mixed == 1 && opt->method != PDG_CG))
+    return solve_fgmres_ir(ctx, opt, z, r, transpose, res);
   if (!opt->mixed) {
     PDG_TRY(ensure_prec(ctx, opt->preconditioner, PDG_F64));
     KrylovOut o{};
     PDG_TRY(krylov_device<double>(ctx, opt->method, z, r, ctx->w64, opt->reduction, opt->maxit,
-                                  transpose, &o));
+                                  transpose, &o, 0.0, opt->restart));
     cudaEventRecord(ctx->ev1, ctx->stream);
     cudaEventSynchronize(ctx->ev1);
     float ms = 0.f;
@@ -331,27 +463,60 @@ static int solve_correction(pdg_context *ctx, const pdg_solver_options *opt, dou
   const double def0 = scal[S_DOT];
   double def = def0;
   const double target = opt->reduction * def0;
-  int total_inner = 0, outer = 0;
+  int total_inner = 0, outer = 0, weak = 0;
   int st = PDG_OK;
   while (def >= target && def >= 1e-30 && outer < opt->max_outer) {
     if (!std::isfinite(def)) { st = set_error(PDG_ENONFINITE, "non-finite defect"); break; }
-    // d32 = d / |d|
-    k_set_scal<<<1, 1, 0, ctx->stream>>>(rc.scal, S_SCALE, def);
-    PDG_TRY(vec_to_f32_scaled(ctx, n, d, d32, rc.scal));
-    PDG_TRY(vec_fill<float>(ctx, n, c32, 0.f));
     KrylovOut o{};
-    PDG_TRY(krylov_device<float>(ctx, opt->method, c32, d32, ctx->w32, opt->inner_reduction,
-                                 opt->inner_maxit, transpose, &o));
+    const int inner = opt->inner_method >= 0 ? opt->inner_method : opt->method;
+    const int vec64 = opt->inner_vectors >= 0 ? opt->inner_vectors == PDG_F64
+                                              : inner != PDG_CG;
+    if (!vec64) {
+      // FP32 inner solve of the scaled defect: d32 = d / |d|, c32 = 0
+      k_set_scal<<<1, 1, 0, ctx->stream>>>(rc.scal, S_SCALE, def);
+      PDG_TRY(vec_to_f32_scaled(ctx, n, d, d32, rc.scal));
+      PDG_TRY(vec_fill<float>(ctx, n, c32, 0.f));
+      PDG_TRY(krylov_device<float>(ctx, inner, c32, d32, ctx->w32, opt->inner_reduction,
+                                   opt->inner_maxit, transpose, &o, opt->inner_breakdown,
+                                   opt->restart, opt->inner_replace));
+    } else {
+      // FP64 Krylov vectors, FP32 operator and block Jacobi (ctx->ops32)
+      double *c64 = ctx->w64[8], *d64 = ctx->w64[9];
+      PDG_TRY(vec_copy<double>(ctx, n, d, d64));
+      PDG_TRY(vec_fill<double>(ctx, n, c64, 0.0));
+      ctx->ops32 = 1;
+      const int ks = krylov_device<double>(ctx, inner, c64, d64, ctx->w64, opt->inner_reduction,
+                                           opt->inner_maxit, transpose, &o, 0.0, opt->restart, 0);
+      ctx->ops32 = 0;
+      PDG_TRY(ks);
+    }
     total_inner += o.iterations;
-    if (o.state == 2 || o.state == 3) { st = state_status(o.state); break; }
-    // z += |d| c32 ; d = rhs - J z
-    k_set_scal<<<1, 1, 0, ctx->stream>>>(rc.scal, S_SCALE, def);
-    PDG_TRY(vec_add_f32_scaled(ctx, n, c32, z, rc.scal, 1.0));
+    // a non-finite inner solve leaves no usable correction; after an inner
+    // breakdown (state 3) the last finite iterate is applied and the outer
+    // loop restarts the Krylov method from the new defect
+    if (o.state == 2) { st = state_status(o.state); break; }
+    // z += correction ; d = rhs - J z
+    if (!vec64) {
+      k_set_scal<<<1, 1, 0, ctx->stream>>>(rc.scal, S_SCALE, def);
+      PDG_TRY(vec_add_f32_scaled(ctx, n, c32, z, rc.scal, 1.0));
+    } else {
+      PDG_TRY(vec_axpy(ctx, n, 1.0, ctx->w64[8], z));
+    }
     PDG_TRY(op_launch<double>(ctx, z, d, rhs, -1.0, 0, transpose, nullptr));
     PDG_TRY(red_dot(ctx, rc, n, d, d, nullptr, nullptr, FIN_NORM, S_DOT, -1, false));
     PDG_TRY(fetch_state(ctx, scal, nullptr));
+    const double prev = def;
     def = scal[S_DOT];
     outer++;
+    // the FP64 defect has reached its rounding floor when corrections stop
+    // reducing it: no decrease at all, or three weak steps (< 2x) in a row
+    weak = def > 0.5 * prev ? weak + 1 : 0;
+    if ((def >= prev || weak >= 3) && def >= target) {
+      if (opt->verbose)
+        std::fprintf(stderr, "pdg mixed: stagnation at defect %.3e (reduction %.3e)\n", def,
+                     def / def0);
+      break;
+    }
     if (opt->verbose)
       std::fprintf(stderr, "pdg mixed: outer %d inner %d defect %.3e (reduction %.3e)\n", outer,
                    o.iterations, def, def / def0);
@@ -473,10 +638,15 @@ void pdg_default_solver_options(pdg_solver_options *o) {
   o->min_defect = 1e-99;
   o->maxit = 5000;
   o->mixed = 0;
-  o->inner_reduction = 1e-4;
+  o->inner_reduction = 1e-3;
   o->inner_maxit = 5000;
   o->max_outer = 30;
   o->verbose = 0;
+  o->inner_breakdown = 1e-9;
+  o->inner_method = -1;
+  o->restart = 30;
+  o->inner_replace = 25;
+  o->inner_vectors = -1;
 }
 
 int pdg_create(const pdg_config *cfg, pdg_context **out) {
@@ -589,13 +759,13 @@ int pdg_destroy(pdg_context *c) {
   void *bufs[] = {c->K64, c->K32, c->c64, c->c32, c->tab64, c->tab32, c->fq, c->fc, c->gq,
                   c->jq, c->oq, c->r0, c->r0K, c->red_partials, c->red_out, c->d_flag,
                   c->stage_a, c->stage_b, c->rec64, c->conv64, c->conv32, c->convtab64,
-                  c->convtab32};
+                  c->convtab32, c->gm_V32, c->gm_V64, c->gm_F64, c->gm_partial, c->gm_coef};
   for (void *b : bufs)
     if (b) cudaFree(b);
-  for (int i = 0; i < 8; i++) {
+  for (int i = 0; i < 10; i++)
     if (c->w64[i]) cudaFree(c->w64[i]);
+  for (int i = 0; i < 8; i++)
     if (c->w32[i]) cudaFree(c->w32[i]);
-  }
   if (c->h_red) cudaFreeHost(c->h_red);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -839,7 +1009,15 @@ int pdg_dot(pdg_context *ctx, const double *a, const double *b, double *out) {
 
 static int check_opts(const pdg_solver_options *o) {
   if (!o) return set_error(PDG_EINVAL, "null options");
-  if (o->method != PDG_CG && o->method != PDG_BICGSTAB) return set_error(PDG_EINVAL, "bad method");
+  if (o->method != PDG_CG && o->method != PDG_BICGSTAB && o->method != PDG_GMRES)
+    return set_error(PDG_EINVAL, "bad method");
+  if (o->inner_method < -1 || o->inner_method > PDG_GMRES)
+    return set_error(PDG_EINVAL, "bad inner method");
+  if ((o->method == PDG_GMRES || o->inner_method != PDG_CG) && (o->restart < 1 || o->restart > 64))
+    return set_error(PDG_EINVAL, "GMRES restart length must be 1..64");
+  if (o->mixed < 0 || o->mixed > 3) return set_error(PDG_EINVAL, "mixed must be 0..3");
+  if (o->inner_vectors < -1 || o->inner_vectors > PDG_F32)
+    return set_error(PDG_EINVAL, "bad inner vector precision");
   if (o->maxit < 1 || (o->mixed && (o->inner_maxit < 1 || o->max_outer < 1)))
     return set_error(PDG_EINVAL, "iteration caps must be >= 1");
   if (!(o->reduction > 0)) return set_error(PDG_EINVAL, "reduction must be > 0");
@@ -915,7 +1093,9 @@ int pdg_adjoint_solve(pdg_context *ctx, const pdg_solver_options *opt, const dou
   else
     PDG_CUDA_TRY(cudaMemcpyAsync(r, rhs, sizeof(double) * ctx->ndof, cudaMemcpyHostToDevice,
                                  ctx->stream));
-  const int transpose = ctx->cfg.method == PDG_SIPG ? 0 : 1;   // SIPG diffusion: J^T = J
+  // SIPG diffusion-reaction is symmetric (J^T = J); NIPG/IIPG and upwind
+  // convection are not
+  const int transpose = (ctx->cfg.method == PDG_SIPG && ctx->vel.nmodes == 0) ? 0 : 1;
   pdg_solver_options o = *opt;
   if (transpose && o.preconditioner == PDG_PREC_BJ_FDM) o.preconditioner = PDG_PREC_BJ_DENSE;
   const int st = solve_correction(ctx, &o, sl.dev, r, transpose, res);

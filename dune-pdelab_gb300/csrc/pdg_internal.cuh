@@ -134,6 +134,12 @@ struct pdg_context {
   float *conv32;       // the same in FP32
   double *convtab64;   // B and D (basis values / derivatives at Gauss points)
   float *convtab32;
+  // GMRES Krylov bases (m+1 vectors), the FP64 flexible-GMRES basis of the
+  // mixed solve (2m+1 vectors: V and the preconditioned directions Z), and
+  // coefficient scratch
+  void *gm_V32, *gm_V64, *gm_F64;
+  int gm_m32, gm_m64, gm_mF;
+  double *gm_partial, *gm_coef;
 
   // preconditioner, one instance per precision (index PDG_F64 / PDG_F32)
   pdg::PrecData prec[2];
@@ -148,8 +154,9 @@ struct pdg_context {
   double *stage_a, *stage_b;
 
   // solver work vectors (lazily allocated)
-  double *w64[8];
+  double *w64[10];
   float *w32[8];
+  int ops32;               // FP64 Krylov vectors with FP32 operator / preconditioner
   int *d_flag;             // device-side convergence flag / counters
   cudaEvent_t ev0, ev1;
 };

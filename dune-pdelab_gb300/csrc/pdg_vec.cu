@@ -66,20 +66,32 @@ __device__ void run_finisher(const RedCtx &rc, int fin, int slot0, int slot1, do
       s[S_BETA] = d0 / s[S_RHO];
       s[S_RHO] = d0;
       break;
+    // BiCGSTABSolver breakdown tests are absolute (rho, omega <= 1e-80,
+    // |h| < 1e-80).  With S_GUARD > 0 (FP32 inner solves, whose dot products
+    // carry ~1e-7 relative noise) a relative test is added:
+    // |<rt, r>| or |<rt, v>| below S_GUARD |rt| |r| (|rt| |v|) is treated as a
+    // breakdown, and the solve stops with the last finite iterate.
     case FIN_BI_RHONEW:
       s[S_RHONEW] = d0;
-      if (fabs(s[S_RHO]) <= 1e-80 || fabs(s[S_OMEGA]) <= 1e-80) fl[F_STATE] = 3;
-      else s[S_BETA] = (d0 / s[S_RHO]) * (s[S_ALPHA] / s[S_OMEGA]);
+      if (fabs(s[S_RHO]) <= 1e-80 || fabs(s[S_OMEGA]) <= 1e-80 || !isfinite(d0) ||
+          (s[S_GUARD] > 0 && fabs(d0) < s[S_GUARD] * s[S_DEF0] * s[S_DEF]))
+        fl[F_STATE] = 3;
+      else
+        s[S_BETA] = (d0 / s[S_RHO]) * (s[S_ALPHA] / s[S_OMEGA]);
       break;
     case FIN_BI_ALPHA:
       s[S_H] = d0;
-      if (fabs(d0) < 1e-80) fl[F_STATE] = 3;
-      else s[S_ALPHA] = s[S_RHONEW] / d0;
+      if (fabs(d0) < 1e-80 || !isfinite(d0) ||
+          (s[S_GUARD] > 0 && fabs(d0) < s[S_GUARD] * s[S_DEF0] * sqrt(d1)))
+        fl[F_STATE] = 3;
+      else
+        s[S_ALPHA] = s[S_RHONEW] / d0;
       break;
     case FIN_BI_OMEGA:
       s[S_TR] = d0;
       s[S_TT] = d1;
-      s[S_OMEGA] = d0 / d1;
+      if (!(d1 > 0.0) || !isfinite(d0 / d1)) fl[F_STATE] = 3;
+      else s[S_OMEGA] = d0 / d1;
       break;
     default:
       break;
@@ -346,6 +358,37 @@ int vec_add_f32_scaled(pdg_context *ctx, long n, const float *x, double *y, cons
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
 }
+__global__ void k_to_f32_skip(long n, const double *__restrict__ x, float *__restrict__ y,
+                              const int *__restrict__ skip) {
+  if (skip && *skip) return;
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    y[i] = (float)x[i];
+}
+__global__ void k_from_f32_combine(long n, const float *__restrict__ s, double *__restrict__ y,
+                                   const double *__restrict__ add, double alpha, int acc,
+                                   const int *__restrict__ skip) {
+  if (skip && *skip) return;
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    double v = alpha * (double)s[i];
+    if (acc) v += y[i];
+    if (add) v += add[i];
+    y[i] = v;
+  }
+}
+int vec_to_f32_skip(pdg_context *ctx, long n, const double *x, float *y, const int *skip) {
+  k_to_f32_skip<<<ew_grid(n), 256, 0, ctx->stream>>>(n, x, y, skip);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+int vec_from_f32_combine(pdg_context *ctx, long n, const float *s32, double *y, const double *add,
+                         double alpha, int acc, const int *skip) {
+  k_from_f32_combine<<<ew_grid(n), 256, 0, ctx->stream>>>(n, s32, y, add, alpha, acc, skip);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+
 int vec_to_f32(pdg_context *ctx, long n, const double *x, float *y) {
   k_to_f32<<<ew_grid(n), 256, 0, ctx->stream>>>(n, x, y);
   PDG_CUDA_TRY(cudaGetLastError());

@@ -34,6 +34,7 @@ enum Slot {
   S_DOT = 12,     // generic dot result
   S_DOT2 = 13,
   S_SCALE = 14,   // mixed precision: scaling of the inner right-hand side
+  S_GUARD = 15,   // relative breakdown threshold (0: dune-istl's absolute tests only)
   S_COUNT = 16
 };
 
@@ -94,5 +95,10 @@ int vec_to_f32_scaled(pdg_context *ctx, long n, const double *x, float *y, const
 int vec_add_f32_scaled(pdg_context *ctx, long n, const float *x, double *y, const double *scal,
                        double sign);
 int vec_to_f32(pdg_context *ctx, long n, const double *x, float *y);
+// skip-aware conversions around an FP32 operator inside an FP64 Krylov solve:
+// y32 = (float)x ;  y = (acc ? y : 0) + alpha (double)s32 + (add ? add : 0)
+int vec_to_f32_skip(pdg_context *ctx, long n, const double *x, float *y, const int *skip);
+int vec_from_f32_combine(pdg_context *ctx, long n, const float *s32, double *y, const double *add,
+                         double alpha, int acc, const int *skip);
 
 }  // namespace pdg

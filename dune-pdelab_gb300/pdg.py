@@ -34,7 +34,7 @@ PDG_ESTATE, PDG_EUNSUPPORTED, PDG_EOUTFLOW, PDG_ENONFINITE, PDG_ETIMEOUT = 5, 6,
 NIPG, SIPG, IIPG = 0, 1, 2
 WEIGHTS_ON, WEIGHTS_OFF = 0, 1
 BC_DIRICHLET, BC_NEUMANN, BC_OUTFLOW, BC_NONE = 1, -1, -2, -3
-CG, BICGSTAB = 0, 1
+CG, BICGSTAB, GMRES = 0, 1, 2
 PREC_NONE, PREC_BJ_FDM, PREC_BJ_DENSE = 0, 1, 2
 F64, F32 = 0, 1
 
@@ -55,7 +55,9 @@ class SolverOptions(C.Structure):
     _fields_ = [("method", C.c_int), ("preconditioner", C.c_int),
                 ("reduction", C.c_double), ("min_defect", C.c_double), ("maxit", C.c_int),
                 ("mixed", C.c_int), ("inner_reduction", C.c_double),
-                ("inner_maxit", C.c_int), ("max_outer", C.c_int), ("verbose", C.c_int)]
+                ("inner_maxit", C.c_int), ("max_outer", C.c_int), ("verbose", C.c_int),
+                ("inner_breakdown", C.c_double), ("inner_method", C.c_int),
+                ("restart", C.c_int), ("inner_replace", C.c_int), ("inner_vectors", C.c_int)]
 
 
 class SolverResult(C.Structure):
@@ -355,7 +357,7 @@ class ISTLBackend_SEQ_MatrixFree_Base:
     isMatrixFree = True
 
     def __init__(self, go: GridOperator, method=CG, preconditioner=PREC_BJ_FDM,
-                 maxiter=5000, verbose=0, mixed=False, inner_reduction=1e-4):
+                 maxiter=5000, verbose=0, mixed=False, inner_reduction=1e-3):
         self.go = go
         self.opts = default_options(method=method, preconditioner=preconditioner,
                                     maxit=maxiter, verbose=verbose, mixed=int(mixed),

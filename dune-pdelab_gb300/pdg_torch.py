@@ -21,12 +21,13 @@ class DGProblem:
     """A GridOperator plus solver options used by ``solve_dg``."""
 
     def __init__(self, go: "pdg.GridOperator", method=pdg.CG, preconditioner=pdg.PREC_BJ_FDM,
-                 reduction=1e-12, mixed=True, inner_reduction=1e-3, maxit=20000):
+                 reduction=1e-12, mixed=True, inner_reduction=1e-3, maxit=20000,
+                 inner_maxit=None):
         self.go = go
         self.opts = pdg.default_options(method=method, preconditioner=preconditioner,
                                         reduction=reduction, mixed=int(mixed),
                                         inner_reduction=inner_reduction, maxit=maxit,
-                                        inner_maxit=maxit, max_outer=60)
+                                        inner_maxit=inner_maxit or maxit, max_outer=60)
         self.last_forward = None
         self.last_adjoint = None
 

@@ -53,7 +53,10 @@ enum { PDG_BC_DIRICHLET = 1, PDG_BC_NEUMANN = -1, PDG_BC_OUTFLOW = -2,
 
 /* Krylov methods (dune-istl CGSolver / BiCGSTABSolver as used by
    ISTLBackend_SEQ_MatrixFree_Base, backend/istl/matrixfree/backends.hh:62-143) */
-enum { PDG_CG = 0, PDG_BICGSTAB = 1 };
+enum { PDG_CG = 0, PDG_BICGSTAB = 1,
+       PDG_GMRES = 2 /* restarted right-preconditioned GMRES(m); no
+                        reference counterpart, the inner solver of the
+                        mixed-precision solve for non-symmetric operators */ };
 /* preconditioners */
 enum {
   PDG_PREC_NONE = 0,
@@ -93,12 +96,30 @@ typedef struct pdg_solver_options {
   double reduction;        /* defect reduction relative to the first defect */
   double min_defect;       /* StationaryLinearProblemSolver min_defect */
   int maxit;
-  int mixed;               /* 0: FP64 Krylov; 1: FP32 apply + FP32 block
-                              Jacobi inside an FP64 defect-correction loop */
+  int mixed;               /* 0: FP64 Krylov.  1: FP32 operator + FP32 block
+                              Jacobi inside an FP64 outer loop: defect
+                              correction for CG, flexible GMRES (outer
+                              restart min(restart, max_outer)) for BiCGStab /
+                              GMRES.  2: always defect correction.  3: always
+                              flexible GMRES. */
   double inner_reduction;  /* mixed: reduction of each FP32 inner solve */
   int inner_maxit;         /* mixed: iteration cap of each inner solve */
-  int max_outer;           /* mixed: cap on defect-correction steps */
+  int max_outer;           /* mixed: cap on outer steps (defect corrections
+                              or flexible-GMRES steps) */
   int verbose;
+  double inner_breakdown;  /* mixed: relative breakdown test of the FP32
+                              BiCGStab (|<rt,v>| < tol |rt||v|, likewise rho);
+                              0 keeps only dune-istl's absolute tests */
+  int inner_method;        /* mixed: Krylov method of the FP32 inner solves;
+                              -1 = the outer method (CG or BiCGStab) */
+  int restart;             /* GMRES restart length m (1..64) */
+  int inner_replace;       /* mixed, BiCGStab: replace the recursive residual
+                              by b - A x every this many iterations (0 = never) */
+  int inner_vectors;       /* mixed: precision of the inner Krylov vectors and
+                              recurrences: PDG_F32, or PDG_F64 with the operator
+                              and the block Jacobi still applied in FP32;
+                              -1 = FP32, except FP64 for BiCGStab / GMRES
+                              under plain defect correction (mixed = 2) */
 } pdg_solver_options;
 
 /* LinearSolverResult (backend/solver.hh:29-51) +
@@ -111,7 +132,7 @@ typedef struct pdg_solver_result {
   double conv_rate;
   double first_defect;
   double defect;
-  int outer_iterations;    /* mixed: defect-correction steps */
+  int outer_iterations;    /* mixed: outer steps */
   int status;
 } pdg_solver_result;
 

@@ -156,6 +156,7 @@ class ISTLBackend_SEQ_MatrixFree_Base {
     opt_.verbose = verbose;
   }
   void setMixedPrecision(bool on, double inner_reduction = 1e-3) {
+    // inner FP32 Krylov solves inside FP64 defect correction
     opt_.mixed = on ? 1 : 0;
     opt_.inner_reduction = inner_reduction;
   }

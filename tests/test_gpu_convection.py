@@ -123,3 +123,58 @@ def test_convection_bicgstab_solve(pdg, oracle, mixed):
     if not mixed:
         assert abs(ls.result().iterations - rres.iterations) <= 1
     assert _rel(u, uref) <= 1e-8
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_gmres_solve_nonsymmetric(pdg, oracle, mixed):
+    # restarted GMRES(m) as the outer (FP64) and as the inner (FP32) method
+    go, P, rng = _pair(pdg, oracle, 2, 4, seed=93, method=0)
+    go.set_source(fc=np.ones(go.ncell))
+    P.set(fc=np.ones(go.ncell))
+    uref, rres, st = P.solve(solver="bicgstab", op=0, reduction=1e-12)
+    ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.GMRES if not mixed else pdg.BICGSTAB,
+                                             preconditioner=pdg.PREC_BJ_DENSE, mixed=mixed)
+    ls.opts.restart = 20
+    ls.opts.inner_method = pdg.GMRES
+    u = np.zeros(go.ndof)
+    pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10).apply()
+    assert ls.result().converged
+    assert _rel(u, uref) <= 1e-8
+
+
+@pytest.mark.parametrize("mode,inner", [(2, 1), (3, 1), (3, 2), (1, 1)])
+def test_mixed_outer_modes(pdg, oracle, mode, inner):
+    # mixed = 2: FP64 defect correction; 3 (and 1 for BiCGStab): FP64 flexible
+    # GMRES whose preconditioner is a short FP32 inner solve
+    go, P, rng = _pair(pdg, oracle, 2, 4, seed=95)
+    go.set_source(fc=np.ones(go.ncell))
+    P.set(fc=np.ones(go.ncell))
+    uref, rres, st = P.solve(solver="bicgstab", op=0, reduction=1e-12)
+    ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.BICGSTAB,
+                                             preconditioner=pdg.PREC_BJ_DENSE, mixed=True,
+                                             inner_reduction=1e-1)
+    ls.opts.mixed = mode
+    ls.opts.inner_method = inner
+    ls.opts.inner_maxit = 20
+    ls.opts.restart = 10
+    ls.opts.max_outer = 40
+    u = np.zeros(go.ndof)
+    pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10).apply()
+    r = ls.result()
+    assert r.converged and r.outer_iterations >= 1 and r.iterations >= r.outer_iterations
+    assert _rel(u, uref) <= 1e-8
+
+
+def test_mixed_flexible_adjoint_solve(pdg, oracle):
+    # J^T lam = rhs with the flexible outer loop (transposed FP32 operator and
+    # block Jacobi inside), checked through the FP64 transposed operator
+    go, P, rng = _pair(pdg, oracle, 2, 3, seed=97)
+    rhs = rng.uniform(-1, 1, go.ndof)
+    o = pdg.default_options(method=pdg.BICGSTAB, preconditioner=pdg.PREC_BJ_DENSE,
+                            reduction=1e-11, mixed=3, inner_reduction=1e-1, inner_maxit=20,
+                            max_outer=40, restart=20)
+    lam = np.zeros(go.ndof)
+    res = go.adjoint_solve(rhs, lam, o)
+    assert res.converged and res.outer_iterations >= 1
+    A = P.assemble_jacobian()
+    assert _rel(P.blocks_apply(A, lam, transpose=True), rhs) <= 1e-9
