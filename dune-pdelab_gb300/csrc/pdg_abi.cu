@@ -115,6 +115,9 @@ template <> const float *Tp<float>(const pdg_context *c) { return c->tab32; }
 template <typename T>
 static int op_launch(pdg_context *ctx, const T *x, T *y, const T *add, T alpha, int acc,
                      int transpose, const int *skip) {
+  if (std::is_same<T, double>::value && ctx->use_matrix)
+    return matrix_apply(ctx, (const double *)x, (double *)y, (const double *)add,
+                        (double)alpha, acc, transpose, skip);
   if (std::is_same<T, double>::value && ctx->ops32) {
     // FP64 Krylov vectors, FP32 operator: convert, apply in FP32, combine in FP64
     float *s0 = ctx->w32[0], *s1 = ctx->w32[1];
@@ -427,9 +430,21 @@ static int solve_fgmres_ir(pdg_context *ctx, const pdg_solver_options *opt, doub
 // FP64 Krylov; with opt->mixed, FP32 Krylov inside FP64 defect correction
 // (CG, or mixed = 2) or inside FP64 flexible GMRES (BiCGStab / GMRES, or
 // mixed = 3).  r is overwritten by the final defect.
+struct UseMatrixScope {
+  pdg_context *ctx;
+  int saved;
+  UseMatrixScope(pdg_context *c, int on) : ctx(c), saved(c->use_matrix) { c->use_matrix = on; }
+  ~UseMatrixScope() { ctx->use_matrix = saved; }
+};
+
 static int solve_correction(pdg_context *ctx, const pdg_solver_options *opt, double *z,
                             double *r, int transpose, pdg_solver_result *res) {
   PDG_TRY(ensure_work(ctx, opt->mixed != 0));
+  if (opt->assembled) {
+    if (opt->mixed) return set_error(PDG_EUNSUPPORTED, "the assembled operator is FP64 only");
+    if (!ctx->A_valid) PDG_TRY(assemble_jacobian(ctx));
+  }
+  UseMatrixScope use_matrix(ctx, opt->assembled != 0);
   cudaEventRecord(ctx->ev0, ctx->stream);
   if (opt->mixed == 3 || (opt->mixed == 1 && opt->method != PDG_CG))
     return solve_fgmres_ir(ctx, opt, z, r, transpose, res);
@@ -611,6 +626,7 @@ static void invalidate(pdg_context *ctx, bool operator_changed) {
   ctx->r0_valid = 0;
   if (operator_changed) {
     ctx->rec_valid = 0;
+    ctx->A_valid = 0;
     ctx->prec[0].ready = 0;
     ctx->prec[1].ready = 0;
   }
@@ -647,6 +663,41 @@ void pdg_default_solver_options(pdg_solver_options *o) {
   o->restart = 30;
   o->inner_replace = 25;
   o->inner_vectors = -1;
+  o->assembled = 0;
+}
+
+void pdg_default_prec_options(pdg_prec_options *o) {
+  if (!o) return;
+  o->omega = 1.0;
+  o->block_reduction = 1e-5;
+  o->block_maxit = 100;
+  o->block_precondition = 1;
+  o->block_weight = 1.0;
+}
+
+int pdg_set_prec_options(pdg_context *ctx, const pdg_prec_options *o) {
+  PDG_CHECK_CTX(ctx);
+  if (!o) return set_error(PDG_EINVAL, "null options");
+  if (!(o->omega > 0.0 && o->omega < 2.0)) return set_error(PDG_EINVAL, "omega must be in (0,2)");
+  if (!(o->block_reduction > 0.0) || o->block_maxit < 1)
+    return set_error(PDG_EINVAL, "bad block solver options");
+  ctx->popt = *o;
+  return PDG_OK;
+}
+
+int pdg_prec_block_iterations(pdg_context *ctx, int precision, int *iterations) {
+  PDG_CHECK_CTX(ctx);
+  if (!iterations || (precision != PDG_F64 && precision != PDG_F32))
+    return set_error(PDG_EINVAL, "bad argument");
+  const PrecData &pd = ctx->prec[precision];
+  if (!pd.ready || !pd.iters)
+    return set_error(PDG_ESTATE, "no iterative block Jacobi set up in this precision");
+  PDG_CUDA_TRY(cudaMemcpyAsync(iterations, pd.iters, sizeof(int) * ctx->ncell,
+                               is_device_ptr(iterations) ? cudaMemcpyDeviceToDevice
+                                                         : cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return PDG_OK;
 }
 
 int pdg_create(const pdg_config *cfg, pdg_context **out) {
@@ -672,6 +723,7 @@ int pdg_create(const pdg_config *cfg, pdg_context **out) {
   pdg_context *c = new pdg_context;
   std::memset(c, 0, sizeof(*c));
   c->cfg = *cfg;
+  pdg_default_prec_options(&c->popt);
   c->device = cfg->device;
   c->dim = cfg->dim;
   c->k = cfg->degree;
@@ -756,10 +808,12 @@ int pdg_destroy(pdg_context *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   prec_free(c, 0);
   prec_free(c, 1);
+  sor_free(c);
   void *bufs[] = {c->K64, c->K32, c->c64, c->c32, c->tab64, c->tab32, c->fq, c->fc, c->gq,
                   c->jq, c->oq, c->r0, c->r0K, c->red_partials, c->red_out, c->d_flag,
                   c->stage_a, c->stage_b, c->rec64, c->conv64, c->conv32, c->convtab64,
-                  c->convtab32, c->gm_V32, c->gm_V64, c->gm_F64, c->gm_partial, c->gm_coef};
+                  c->convtab32, c->gm_V32, c->gm_V64, c->gm_F64, c->gm_partial, c->gm_coef,
+                  c->A64};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 10; i++)
@@ -1016,12 +1070,71 @@ static int check_opts(const pdg_solver_options *o) {
   if ((o->method == PDG_GMRES || o->inner_method != PDG_CG) && (o->restart < 1 || o->restart > 64))
     return set_error(PDG_EINVAL, "GMRES restart length must be 1..64");
   if (o->mixed < 0 || o->mixed > 3) return set_error(PDG_EINVAL, "mixed must be 0..3");
+  if (o->assembled != 0 && o->assembled != 1) return set_error(PDG_EINVAL, "bad assembled flag");
+  if ((o->preconditioner & ~(PDG_PREC_BLOCK_MASK | PDG_PREC_SOR)) != 0 ||
+      (o->preconditioner & PDG_PREC_BLOCK_MASK) > PDG_PREC_BJ_ITERATIVE)
+    return set_error(PDG_EINVAL, "bad preconditioner kind");
   if (o->inner_vectors < -1 || o->inner_vectors > PDG_F32)
     return set_error(PDG_EINVAL, "bad inner vector precision");
   if (o->maxit < 1 || (o->mixed && (o->inner_maxit < 1 || o->max_outer < 1)))
     return set_error(PDG_EINVAL, "iteration caps must be >= 1");
   if (!(o->reduction > 0)) return set_error(PDG_EINVAL, "reduction must be > 0");
   return PDG_OK;
+}
+
+int pdg_jacobian_assemble(pdg_context *ctx) {
+  PDG_CHECK_CTX(ctx);
+  PDG_TRY(ensure_work(ctx, false));
+  PDG_TRY(assemble_jacobian(ctx));
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return PDG_OK;
+}
+
+int pdg_jacobian_pattern(const pdg_context *ctx, long *nnz_blocks) {
+  if (!ctx || !nnz_blocks) return set_error(PDG_EINVAL, "null argument");
+  *nnz_blocks = jacobian_nnz_blocks(ctx);
+  return PDG_OK;
+}
+
+int pdg_jacobian_export(pdg_context *ctx, long *rowptr, long *colind, double *values) {
+  PDG_CHECK_CTX(ctx);
+  if (!ctx->A_valid) return set_error(PDG_EINVAL, "the Jacobian has not been assembled");
+  const long nnzb = jacobian_nnz_blocks(ctx);
+  std::vector<long> rp(ctx->ncell + 1), ci(nnzb);
+  PDG_TRY(jacobian_rowptr(ctx, rp.data(), ci.data()));
+  if (rowptr) std::memcpy(rowptr, rp.data(), sizeof(long) * rp.size());
+  if (colind) std::memcpy(colind, ci.data(), sizeof(long) * ci.size());
+  if (!values) return PDG_OK;
+  const size_t nval = (size_t)nnzb * ctx->nb * ctx->nb;
+  long *rp_dev = nullptr;
+  double *vdev = nullptr;
+  const bool host = !is_device_ptr(values);
+  int st = PDG_OK;
+  if (cudaMalloc(&rp_dev, sizeof(long) * rp.size()) != cudaSuccess ||
+      (host && cudaMalloc(&vdev, sizeof(double) * nval) != cudaSuccess)) {
+    st = set_error(PDG_ECUDA, "out of device memory for the export");
+  } else {
+    cudaMemcpyAsync(rp_dev, rp.data(), sizeof(long) * rp.size(), cudaMemcpyHostToDevice,
+                    ctx->stream);
+    st = matrix_export(ctx, rp_dev, host ? vdev : values);
+    if (st == PDG_OK && host &&
+        cudaMemcpyAsync(values, vdev, sizeof(double) * nval, cudaMemcpyDeviceToHost,
+                        ctx->stream) != cudaSuccess)
+      st = set_error(PDG_ECUDA, "export copy failed");
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess && st == PDG_OK)
+      st = set_error(PDG_ECUDA, "export failed");
+  }
+  if (rp_dev) cudaFree(rp_dev);
+  if (vdev) cudaFree(vdev);
+  return st;
+}
+
+int pdg_matrix_apply(pdg_context *ctx, const double *x, double *y) {
+  PDG_CHECK_CTX(ctx);
+  if (!x || !y) return set_error(PDG_EINVAL, "null vector");
+  if (!ctx->A_valid) return set_error(PDG_EINVAL, "the Jacobian has not been assembled");
+  UseMatrixScope use_matrix(ctx, 1);
+  return apply_entry(ctx, x, y, 1.0, 0, 0, false);
 }
 
 int pdg_krylov_solve(pdg_context *ctx, const pdg_solver_options *opt, double *z, double *r,
@@ -1097,7 +1210,8 @@ int pdg_adjoint_solve(pdg_context *ctx, const pdg_solver_options *opt, const dou
   // convection are not
   const int transpose = (ctx->cfg.method == PDG_SIPG && ctx->vel.nmodes == 0) ? 0 : 1;
   pdg_solver_options o = *opt;
-  if (transpose && o.preconditioner == PDG_PREC_BJ_FDM) o.preconditioner = PDG_PREC_BJ_DENSE;
+  if (transpose && (o.preconditioner & PDG_PREC_BLOCK_MASK) == PDG_PREC_BJ_FDM)
+    o.preconditioner = (o.preconditioner & ~PDG_PREC_BLOCK_MASK) | PDG_PREC_BJ_DENSE;
   const int st = solve_correction(ctx, &o, sl.dev, r, transpose, res);
   PDG_TRY(stage_out<double>(ctx, sl));
   PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));

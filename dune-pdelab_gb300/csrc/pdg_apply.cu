@@ -149,8 +149,9 @@ __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
   if (a.skip && *a.skip) return;
   for (int i = t; i < C::TAB; i += blockDim.x) tM[i] = p.tab[i];
 
-  const int e = blockIdx.x * CPB + cs;          // cell counts fit 31 bits
-  const bool active = e < p.ncell;
+  const int li = blockIdx.x * CPB + cs;         // cell counts fit 31 bits
+  const bool active = a.cells ? li < a.ncells : li < p.ncell;
+  const int e = a.cells ? (active ? a.cells[li] : 0) : li;
   const int ee = active ? e : 0;
   int ix[3];
   cell_coords(p, (unsigned)ee, ix);
@@ -433,7 +434,9 @@ static int launch_apply_dn(pdg_context *ctx, const ApplyArgs<T> &a, const OpPara
                                       (int)smem));
     attr_done = ctx->device;
   }
-  const long blocks = (ctx->ncell + C::CPB - 1) / C::CPB;
+  const long work = a.cells ? a.ncells : ctx->ncell;
+  if (work <= 0) return PDG_OK;
+  const long blocks = (work + C::CPB - 1) / C::CPB;
   k_apply<T, D, N><<<(unsigned)blocks, C::THREADS, smem, ctx->stream>>>(p, a, rec);
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;

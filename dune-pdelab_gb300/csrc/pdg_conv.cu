@@ -118,8 +118,9 @@ __global__ void __launch_bounds__(CCfg<N>::THREADS)
   T *fl = S3 + NB;                           // [6][N2]
   if (a.skip && *a.skip) return;
   for (int i = t; i < C::TAB; i += blockDim.x) tB[i] = tabBD[i];
-  const long e = (long)blockIdx.x * CPB + cs;
-  const bool active = e < p.ncell;
+  const long li = (long)blockIdx.x * CPB + cs;
+  const bool active = a.cells ? li < a.ncells : li < p.ncell;
+  const long e = a.cells ? (active ? (long)a.cells[li] : 0) : li;
   const long ee = active ? e : 0;
   int ix[3];
   {
@@ -447,7 +448,9 @@ static int conv_launch_n(pdg_context *ctx, const ApplyArgs<T> &a) {
                                  dbl ? (const T *)ctx->tab64 : (const T *)ctx->tab32);
   const T *rec = dbl ? (const T *)ctx->conv64 : (const T *)ctx->conv32;
   const T *tab = dbl ? (const T *)ctx->convtab64 : (const T *)ctx->convtab32;
-  const unsigned blocks = (unsigned)((ctx->ncell + C::CPB - 1) / C::CPB);
+  const long work = a.cells ? a.ncells : ctx->ncell;
+  if (work <= 0) return PDG_OK;
+  const unsigned blocks = (unsigned)((work + C::CPB - 1) / C::CPB);
   k_conv<T, N><<<blocks, C::THREADS, smem, ctx->stream>>>(p, a, rec, tab);
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;

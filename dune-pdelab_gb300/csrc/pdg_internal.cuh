@@ -94,6 +94,8 @@ struct ApplyArgs {
   int transpose;   // J^T instead of J
   int diag_only;   // drop the neighbour coupling (cell-block diagonal)
   const int *skip; // if non-null and *skip != 0 the launch does nothing
+  const int *cells; // if non-null: only these cells (ncells of them) are computed
+  int ncells;
 };
 
 // One cell-block Jacobi preconditioner instance (per precision).
@@ -101,6 +103,9 @@ struct PrecData {
   int kind, ready;
   void *Q, *L;     // FDM factors [ncell][d][N*N], [ncell][d][N]
   void *inv;       // dense inverses, column-major per block [ncell][nb*nb]
+  void *blk;       // iterative block Jacobi: diagonal blocks, column-major [ncell][nb*nb]
+  void *invdiag;   // and the inverses of their diagonals [ncell][nb]
+  int *iters;      // block-solve iteration counts of the last apply [ncell]
 };
 
 }  // namespace pdg
@@ -141,8 +146,21 @@ struct pdg_context {
   int gm_m32, gm_m64, gm_mF;
   double *gm_partial, *gm_coef;
 
+  // assembled Jacobian: [ncell][2d+1][nb][nb], column-major blocks
+  double *A64;
+  int A_valid;
+  int use_matrix;          // Krylov operator = assembled Jacobian (matrix-based path)
+
   // preconditioner, one instance per precision (index PDG_F64 / PDG_F32)
   pdg::PrecData prec[2];
+  pdg_prec_options popt;
+  // block SOR: cells grouped by hyperplane ix+iy+iz = s (grid order within
+  // each), hp_off[s] .. hp_off[s+1] on the host; the sweep's scratch vectors
+  int *hp_cells;
+  long *hp_off;
+  int hp_n;
+  double *sor_a64;
+  float *sor_a32;
   double *r0K;             // K-proportional Dirichlet-data part of R(0)
 
   // reduction scratch (deterministic two-stage reductions)
@@ -183,6 +201,19 @@ int prec_apply_impl(pdg_context *ctx, const T *d, T *v, int transpose);
 template <typename T>
 int prec_apply_skip(pdg_context *ctx, const T *d, T *v, int transpose, const int *skip);
 void prec_free(pdg_context *ctx, int precision);
+// v_e = scale * D_e^{-1} d_e on a cell list (all cells if null)
+template <typename T>
+int block_solve(pdg_context *ctx, const T *d, T *v, int transpose, const int *skip,
+                const int *cells, int ncells, T scale);
+int diag_blocks(pdg_context *ctx, double **D);   // row-major FP64 diagonal blocks
+int bj_iterative_setup(pdg_context *ctx, int precision);
+template <typename T>
+int bj_iterative_apply(pdg_context *ctx, const T *d, T *v, int transpose, const int *skip,
+                       const int *cells, int ncells, T scale);
+int sor_setup(pdg_context *ctx);
+template <typename T>
+int sor_apply(pdg_context *ctx, const T *d, T *v, int transpose, const int *skip);
+void sor_free(pdg_context *ctx);
 
 // 1D tables on the Gauss points (host-built, passed by value to kernels)
 struct RhsTables {
@@ -194,6 +225,14 @@ struct RhsTables {
 RhsTables make_rhs_tables(const pdg_context *ctx);
 double *rhs_r0K(pdg_context *ctx, bool alloc);
 double lagrange_derivative(int k, int i, double x);
+
+// assembled Jacobian (probing the matrix-free operator) and its block product
+int assemble_jacobian(pdg_context *ctx);
+long jacobian_nnz_blocks(const pdg_context *ctx);
+int jacobian_rowptr(const pdg_context *ctx, long *rowptr, long *colind);
+int matrix_apply(pdg_context *ctx, const double *x, double *y, const double *add, double alpha,
+                 int accumulate, int transpose, const int *skip);
+int matrix_export(pdg_context *ctx, const long *rowptr_dev, double *values_dev);
 
 // convection (3D): set-up of the per-cell velocity records, and the launch
 // that adds alpha * C x (or C^T x) to y after the diffusion operator

@@ -152,7 +152,8 @@ struct PCfg {
 template <typename T, int D, int N>
 __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
     k_fdm_apply(long ncell, const T *__restrict__ Q, const T *__restrict__ L,
-                const T *__restrict__ d, T *__restrict__ v, const int *__restrict__ skip) {
+                const T *__restrict__ d, T *__restrict__ v, const int *__restrict__ skip,
+                const int *__restrict__ cells, int ncells, T scale) {
   using C = PCfg<D, N>;
   constexpr int N2 = C::N2, NB = C::NB, TPC = C::TPC, CPB = C::CPB;
   if (skip && *skip) return;
@@ -162,8 +163,9 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
   T *S1 = S0 + NB;
   T *Qs = S1 + NB;       // [D][N2]
   T *Ls = Qs + D * N2;   // [D][N]
-  const int e = blockIdx.x * CPB + cs;
-  const bool active = e < ncell;
+  const int li = blockIdx.x * CPB + cs;
+  const bool active = cells ? li < ncells : li < ncell;
+  const int e = cells ? (active ? cells[li] : 0) : li;
   const int ee = active ? e : 0;
   for (int i = l; i < D * N2; i += TPC) Qs[i] = Q[(size_t)ee * D * N2 + i];
   for (int i = l; i < D * N; i += TPC) Ls[i] = L[(size_t)ee * D * N + i];
@@ -231,7 +233,7 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
         T s = T(0);
 #pragma unroll
         for (int zp = 0; zp < N; zp++) s += Qz[z * N + zp] * a[zp];
-        v[(size_t)e * NB + z * N2 + l] = s;
+        v[(size_t)e * NB + z * N2 + l] = scale * s;
       }
     }
   } else {
@@ -271,7 +273,7 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
         T s = T(0);
 #pragma unroll
         for (int yp = 0; yp < N; yp++) s += Qy[y * N + yp] * a[yp];
-        v[(size_t)e * NB + y * N + tx] = s;
+        v[(size_t)e * NB + y * N + tx] = scale * s;
       }
     }
   }
@@ -375,11 +377,12 @@ __global__ void k_invert(int nb, const double *__restrict__ D, T *__restrict__ i
 template <typename T>
 __global__ void k_dense_apply(long ncell, int nb, const T *__restrict__ invT,
                               const T *__restrict__ d, T *__restrict__ v, int transpose,
-                              const int *__restrict__ skip) {
+                              const int *__restrict__ skip, const int *__restrict__ cells,
+                              T scale) {
   if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *ds = reinterpret_cast<T *>(smem_raw);
-  const long e = blockIdx.x;
+  const long e = cells ? (long)cells[blockIdx.x] : (long)blockIdx.x;
   for (int i = threadIdx.x; i < nb; i += blockDim.x) ds[i] = d[e * nb + i];
   __syncthreads();
   const T *B = invT + e * (long)nb * nb;
@@ -389,7 +392,7 @@ __global__ void k_dense_apply(long ncell, int nb, const T *__restrict__ invT,
       for (int j = 0; j < nb; j++) s += B[j * nb + i] * ds[j];
     else
       for (int j = 0; j < nb; j++) s += B[i * nb + j] * ds[j];
-    v[e * nb + i] = s;
+    v[e * nb + i] = scale * s;
   }
 }
 
@@ -449,24 +452,53 @@ static int fdm_setup(pdg_context *ctx, int precision) {
   return PDG_OK;
 }
 
-static int dense_setup(pdg_context *ctx, int precision) {
+// The diagonal blocks D_e (row-major, FP64) by probing the operator kernel
+// restricted to the cell; *D is allocated here and freed by the caller.
+int diag_blocks(pdg_context *ctx, double **Dout) {
   const long nc = ctx->ncell;
   const int nb = ctx->nb;
   const size_t blk = (size_t)nc * nb * nb;
   double *D = nullptr, *x = nullptr, *y = nullptr;
-  int *bad = nullptr;
+  *Dout = nullptr;
   PDG_CUDA_TRY(cudaMalloc(&D, blk * sizeof(double)));
-  PDG_CUDA_TRY(cudaMalloc(&x, sizeof(double) * ctx->ndof));
-  PDG_CUDA_TRY(cudaMalloc(&y, sizeof(double) * ctx->ndof));
-  PDG_CUDA_TRY(cudaMalloc(&bad, sizeof(int)));
-  PDG_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
+  if (cudaMalloc(&x, sizeof(double) * ctx->ndof) != cudaSuccess ||
+      cudaMalloc(&y, sizeof(double) * ctx->ndof) != cudaSuccess) {
+    cudaFree(D);
+    if (x) cudaFree(x);
+    return set_error(PDG_ECUDA, "out of device memory for the diagonal blocks");
+  }
   const unsigned g = (unsigned)((ctx->ndof + 255) / 256);
-  for (int j = 0; j < nb; j++) {
+  int st = PDG_OK;
+  for (int j = 0; j < nb && st == PDG_OK; j++) {
     k_unit_field<<<g, 256, 0, ctx->stream>>>(nc, nb, j, x);
     ApplyArgs<double> a{x, y, nullptr, 1.0, 0, 0, 1, nullptr};
-    PDG_TRY(launch_apply<double>(ctx, a, ctx->K64, ctx->c64, ctx->tab64));
-    k_scatter_col<<<g, 256, 0, ctx->stream>>>(nc, nb, j, y, D);
+    st = launch_apply<double>(ctx, a, ctx->K64, ctx->c64, ctx->tab64);
+    if (st == PDG_OK) k_scatter_col<<<g, 256, 0, ctx->stream>>>(nc, nb, j, y, D);
   }
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(x);
+  cudaFree(y);
+  if (st != PDG_OK) {
+    cudaFree(D);
+    return st;
+  }
+  PDG_CUDA_TRY(cudaGetLastError());
+  *Dout = D;
+  return PDG_OK;
+}
+
+static int dense_setup(pdg_context *ctx, int precision) {
+  const long nc = ctx->ncell;
+  const int nb = ctx->nb;
+  const size_t blk = (size_t)nc * nb * nb;
+  double *D = nullptr;
+  int *bad = nullptr;
+  PDG_TRY(diag_blocks(ctx, &D));
+  if (cudaMalloc(&bad, sizeof(int)) != cudaSuccess) {
+    cudaFree(D);
+    return set_error(PDG_ECUDA, "cudaMalloc failed");
+  }
+  PDG_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
   const size_t es = precision == PDG_F64 ? sizeof(double) : sizeof(float);
   PrecData &pd = ctx->prec[precision];
   PDG_CUDA_TRY(cudaMalloc(&pd.inv, blk * es));
@@ -482,7 +514,7 @@ static int dense_setup(pdg_context *ctx, int precision) {
   int hbad = 0;
   PDG_CUDA_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  cudaFree(D); cudaFree(x); cudaFree(y); cudaFree(bad);
+  cudaFree(D); cudaFree(bad);
   if (hbad) return set_error(PDG_EINVAL, "singular diagonal block");
   return PDG_OK;
 }
@@ -492,7 +524,10 @@ void prec_free(pdg_context *ctx, int precision) {
   if (pd.Q) cudaFree(pd.Q);
   if (pd.L) cudaFree(pd.L);
   if (pd.inv) cudaFree(pd.inv);
-  pd = PrecData{0, 0, nullptr, nullptr, nullptr};
+  if (pd.blk) cudaFree(pd.blk);
+  if (pd.invdiag) cudaFree(pd.invdiag);
+  if (pd.iters) cudaFree(pd.iters);
+  pd = PrecData{0, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 }
 
 int prec_setup_impl(pdg_context *ctx, int kind, int precision) {
@@ -504,31 +539,96 @@ int prec_setup_impl(pdg_context *ctx, int kind, int precision) {
     ctx->prec[precision].ready = 1;
     return PDG_OK;
   }
-  if (kind == PDG_PREC_BJ_FDM) {
+  const int base = kind & PDG_PREC_BLOCK_MASK;
+  if ((kind & ~(PDG_PREC_BLOCK_MASK | PDG_PREC_SOR)) != 0 || base > PDG_PREC_BJ_ITERATIVE)
+    return set_error(PDG_EINVAL, "unknown preconditioner kind");
+  if (base == PDG_PREC_BJ_FDM) {
     if (ctx->cfg.method != PDG_SIPG)
       return set_error(PDG_EUNSUPPORTED,
                        "FDM block Jacobi needs symmetric blocks (SIPG); use PDG_PREC_BJ_DENSE");
     PDG_TRY(fdm_setup(ctx, precision));
-  } else if (kind == PDG_PREC_BJ_DENSE) {
+  } else if (base == PDG_PREC_BJ_DENSE) {
     PDG_TRY(dense_setup(ctx, precision));
-  } else {
-    return set_error(PDG_EINVAL, "unknown preconditioner kind");
+  } else if (base == PDG_PREC_BJ_ITERATIVE) {
+    PDG_TRY(bj_iterative_setup(ctx, precision));
   }
+  if (kind & PDG_PREC_SOR) PDG_TRY(sor_setup(ctx));
   ctx->prec[precision].kind = kind;
   ctx->prec[precision].ready = 1;
   return PDG_OK;
 }
 
 template <typename T, int D, int N>
-static int fdm_apply_dn(pdg_context *ctx, const T *d, T *v, const int *skip) {
+static int fdm_apply_dn(pdg_context *ctx, const T *d, T *v, const int *skip, const int *cells,
+                        int ncells, T scale) {
   using C = PCfg<D, N>;
   const size_t smem = sizeof(T) * C::CPB * C::PER_CELL;
-  const unsigned blocks = (unsigned)((ctx->ncell + C::CPB - 1) / C::CPB);
+  const long work = cells ? ncells : ctx->ncell;
+  if (work <= 0) return PDG_OK;
+  const unsigned blocks = (unsigned)((work + C::CPB - 1) / C::CPB);
   k_fdm_apply<T, D, N><<<blocks, C::THREADS, smem, ctx->stream>>>(
       ctx->ncell, (const T *)ctx->prec[std::is_same<T, double>::value ? 0 : 1].Q,
-      (const T *)ctx->prec[std::is_same<T, double>::value ? 0 : 1].L, d, v, skip);
+      (const T *)ctx->prec[std::is_same<T, double>::value ? 0 : 1].L, d, v, skip, cells, ncells,
+      scale);
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
+}
+
+template <typename T>
+__global__ void k_scale_cells(long ncell, int nb, const T *__restrict__ d, T *__restrict__ v,
+                              const int *__restrict__ cells, int ncells, T scale,
+                              const int *__restrict__ skip) {
+  if (skip && *skip) return;
+  const long n = (cells ? (long)ncells : ncell) * nb;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long)gridDim.x * blockDim.x) {
+    const long li = t / nb;
+    const long e = cells ? (long)cells[li] : li;
+    const long idx = e * nb + (t - li * nb);
+    v[idx] = scale * d[idx];
+  }
+}
+
+// v_e = scale * D_e^{-1} d_e (D_e^{-T} with `transpose`) on the listed cells
+// (all cells if `cells` is null), with the block solver of the instance.
+template <typename T>
+int block_solve(pdg_context *ctx, const T *d, T *v, int transpose, const int *skip,
+                const int *cells, int ncells, T scale) {
+  const int pi = std::is_same<T, double>::value ? PDG_F64 : PDG_F32;
+  const PrecData &pd = ctx->prec[pi];
+  const int base = pd.kind & PDG_PREC_BLOCK_MASK;
+  const long work = cells ? ncells : ctx->ncell;
+  if (work <= 0) return PDG_OK;
+  if (base == PDG_PREC_NONE) {
+    long g = (work * ctx->nb + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    k_scale_cells<T><<<(unsigned)g, 256, 0, ctx->stream>>>(ctx->ncell, ctx->nb, d, v, cells,
+                                                           ncells, scale, skip);
+    PDG_CUDA_TRY(cudaGetLastError());
+    return PDG_OK;
+  }
+  if (base == PDG_PREC_BJ_DENSE) {
+    const int nb = ctx->nb;
+    const int threads = ((nb + 31) / 32) * 32;
+    k_dense_apply<T><<<(unsigned)work, threads, sizeof(T) * nb, ctx->stream>>>(
+        ctx->ncell, nb, (const T *)pd.inv, d, v, transpose, skip, cells, scale);
+    PDG_CUDA_TRY(cudaGetLastError());
+    return PDG_OK;
+  }
+  if (base == PDG_PREC_BJ_ITERATIVE)
+    return bj_iterative_apply<T>(ctx, d, v, transpose, skip, cells, ncells, scale);
+  // FDM blocks are symmetric: D^{-T} = D^{-1}
+  switch (ctx->dim * 10 + ctx->k) {
+    case 21: return fdm_apply_dn<T, 2, 2>(ctx, d, v, skip, cells, ncells, scale);
+    case 22: return fdm_apply_dn<T, 2, 3>(ctx, d, v, skip, cells, ncells, scale);
+    case 23: return fdm_apply_dn<T, 2, 4>(ctx, d, v, skip, cells, ncells, scale);
+    case 24: return fdm_apply_dn<T, 2, 5>(ctx, d, v, skip, cells, ncells, scale);
+    case 31: return fdm_apply_dn<T, 3, 2>(ctx, d, v, skip, cells, ncells, scale);
+    case 32: return fdm_apply_dn<T, 3, 3>(ctx, d, v, skip, cells, ncells, scale);
+    case 33: return fdm_apply_dn<T, 3, 4>(ctx, d, v, skip, cells, ncells, scale);
+    case 34: return fdm_apply_dn<T, 3, 5>(ctx, d, v, skip, cells, ncells, scale);
+    default: return set_error(PDG_EUNSUPPORTED, "dim/degree not compiled in");
+  }
 }
 
 template <typename T>
@@ -537,26 +637,8 @@ int prec_apply_skip(pdg_context *ctx, const T *d, T *v, int transpose, const int
   const PrecData &pd = ctx->prec[pi];
   if (!pd.ready) return set_error(PDG_ESTATE, "preconditioner not set up in this precision");
   if (pd.kind == PDG_PREC_NONE) return vec_copy<T>(ctx, ctx->ndof, d, v);
-  if (pd.kind == PDG_PREC_BJ_DENSE) {
-    const int nb = ctx->nb;
-    const int threads = ((nb + 31) / 32) * 32;
-    k_dense_apply<T><<<(unsigned)ctx->ncell, threads, sizeof(T) * nb, ctx->stream>>>(
-        ctx->ncell, nb, (const T *)pd.inv, d, v, transpose, skip);
-    PDG_CUDA_TRY(cudaGetLastError());
-    return PDG_OK;
-  }
-  // FDM blocks are symmetric: D^{-T} = D^{-1}
-  switch (ctx->dim * 10 + ctx->k) {
-    case 21: return fdm_apply_dn<T, 2, 2>(ctx, d, v, skip);
-    case 22: return fdm_apply_dn<T, 2, 3>(ctx, d, v, skip);
-    case 23: return fdm_apply_dn<T, 2, 4>(ctx, d, v, skip);
-    case 24: return fdm_apply_dn<T, 2, 5>(ctx, d, v, skip);
-    case 31: return fdm_apply_dn<T, 3, 2>(ctx, d, v, skip);
-    case 32: return fdm_apply_dn<T, 3, 3>(ctx, d, v, skip);
-    case 33: return fdm_apply_dn<T, 3, 4>(ctx, d, v, skip);
-    case 34: return fdm_apply_dn<T, 3, 5>(ctx, d, v, skip);
-    default: return set_error(PDG_EUNSUPPORTED, "dim/degree not compiled in");
-  }
+  if (pd.kind & PDG_PREC_SOR) return sor_apply<T>(ctx, d, v, transpose, skip);
+  return block_solve<T>(ctx, d, v, transpose, skip, nullptr, 0, T(1));
 }
 
 template <typename T>
@@ -568,5 +650,9 @@ template int prec_apply_impl<double>(pdg_context *, const double *, double *, in
 template int prec_apply_impl<float>(pdg_context *, const float *, float *, int);
 template int prec_apply_skip<double>(pdg_context *, const double *, double *, int, const int *);
 template int prec_apply_skip<float>(pdg_context *, const float *, float *, int, const int *);
+template int block_solve<double>(pdg_context *, const double *, double *, int, const int *,
+                                 const int *, int, double);
+template int block_solve<float>(pdg_context *, const float *, float *, int, const int *,
+                                const int *, int, float);
 
 }  // namespace pdg

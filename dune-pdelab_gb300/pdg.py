@@ -35,7 +35,8 @@ NIPG, SIPG, IIPG = 0, 1, 2
 WEIGHTS_ON, WEIGHTS_OFF = 0, 1
 BC_DIRICHLET, BC_NEUMANN, BC_OUTFLOW, BC_NONE = 1, -1, -2, -3
 CG, BICGSTAB, GMRES = 0, 1, 2
-PREC_NONE, PREC_BJ_FDM, PREC_BJ_DENSE = 0, 1, 2
+PREC_NONE, PREC_BJ_FDM, PREC_BJ_DENSE, PREC_BJ_ITERATIVE = 0, 1, 2, 3
+PREC_SOR = 16          # OR-ed with a block kind: one block-SOR sweep
 F64, F32 = 0, 1
 
 
@@ -57,7 +58,15 @@ class SolverOptions(C.Structure):
                 ("mixed", C.c_int), ("inner_reduction", C.c_double),
                 ("inner_maxit", C.c_int), ("max_outer", C.c_int), ("verbose", C.c_int),
                 ("inner_breakdown", C.c_double), ("inner_method", C.c_int),
-                ("restart", C.c_int), ("inner_replace", C.c_int), ("inner_vectors", C.c_int)]
+                ("restart", C.c_int), ("inner_replace", C.c_int), ("inner_vectors", C.c_int),
+                ("assembled", C.c_int)]
+
+
+class PrecOptions(C.Structure):
+    """BlockSORPreconditionerLocalOperator omega + BlockSolverOptions."""
+    _fields_ = [("omega", C.c_double), ("block_reduction", C.c_double),
+                ("block_maxit", C.c_int), ("block_precondition", C.c_int),
+                ("block_weight", C.c_double)]
 
 
 class SolverResult(C.Structure):
@@ -108,6 +117,13 @@ _SIGS = {
                                     C.POINTER(SolverResult)]),
     "pdg_grad_logK": (C.c_int, [_vp, _vp, _vp, _vp]),
     "pdg_grad_source": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_default_prec_options": (None, [C.POINTER(PrecOptions)]),
+    "pdg_set_prec_options": (C.c_int, [_vp, C.POINTER(PrecOptions)]),
+    "pdg_prec_block_iterations": (C.c_int, [_vp, C.c_int, _vp]),
+    "pdg_jacobian_assemble": (C.c_int, [_vp]),
+    "pdg_jacobian_pattern": (C.c_int, [_vp, C.POINTER(C.c_long)]),
+    "pdg_jacobian_export": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "pdg_matrix_apply": (C.c_int, [_vp, _vp, _vp]),
 }
 
 _lib = None
@@ -170,6 +186,14 @@ def fourier_velocity_modes(seed, nmodes=8, bmax=10.0, kmax=2):
     s = np.linalg.norm(modes[:, 4:], axis=1).sum()
     modes[:, 4:] *= bmax / s
     return modes
+
+
+def prec_options(**kw):
+    o = PrecOptions()
+    load().pdg_default_prec_options(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
 
 
 def default_options(**kw):
@@ -293,6 +317,42 @@ class GridOperator:
     def grad_logK(self, u, lam, g):
         _check(load().pdg_grad_logK(self._h, _ptr(u), _ptr(lam), _ptr(g)))
         return g
+
+    def set_prec_options(self, options=None, **kw):
+        """Options of the block preconditioners (SOR omega, block solver)."""
+        o = options if options is not None else prec_options(**kw)
+        _check(load().pdg_set_prec_options(self._h, C.byref(o)))
+
+    def prec_block_iterations(self, precision=F64):
+        """Iteration count of every block solve of the last iterative
+        block-Jacobi application (SolverStatistics)."""
+        out = np.zeros(self.ncell, dtype=np.int32)
+        _check(load().pdg_prec_block_iterations(self._h, precision, out.ctypes.data))
+        return out
+
+    def jacobian_assemble(self):
+        """Assemble the Jacobian on the device (GridOperator::jacobian)."""
+        _check(load().pdg_jacobian_assemble(self._h))
+
+    def jacobian_pattern(self):
+        nnz = C.c_long()
+        _check(load().pdg_jacobian_pattern(self._h, C.byref(nnz)))
+        return nnz.value
+
+    def jacobian_export(self, values=True):
+        """(rowptr, colind, blocks[nnz, n, n]) in BCRS order; blocks row-major."""
+        nnz = self.jacobian_pattern()
+        rowptr = np.zeros(self.ncell + 1, dtype=np.int64)
+        colind = np.zeros(nnz, dtype=np.int64)
+        vals = np.zeros((nnz, self.nbasis, self.nbasis)) if values else None
+        _check(load().pdg_jacobian_export(self._h, rowptr.ctypes.data, colind.ctypes.data,
+                                          _ptr(vals) if values else None))
+        return rowptr, colind, vals
+
+    def matrix_apply(self, x, y):
+        """y = A x with the assembled Jacobian"""
+        _check(load().pdg_matrix_apply(self._h, _ptr(x), _ptr(y)))
+        return y
 
     def grad_source(self, lam, g):
         _check(load().pdg_grad_source(self._h, _ptr(lam), _ptr(g)))

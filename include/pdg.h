@@ -63,9 +63,34 @@ enum {
   PDG_PREC_BJ_FDM = 1,     /* cell-block Jacobi, inverse applied by fast
                               diagonalisation of the Kronecker-sum block
                               (exact for symmetric separable blocks) */
-  PDG_PREC_BJ_DENSE = 2    /* cell-block Jacobi, explicit per-cell inverse
+  PDG_PREC_BJ_DENSE = 2,   /* cell-block Jacobi, explicit per-cell inverse
                               (exact for every block, n^2 values per cell) */
+  PDG_PREC_BJ_ITERATIVE = 3,/* fully matrix-free-style block Jacobi: each
+                              block system solved by a local BiCGStab with
+                              point-Jacobi preconditioner
+                              (IterativeBlockJacobiPreconditionerLocalOperator,
+                              matrixfree/iterativeblockjacobipreconditioner.hh:
+                              262-452); options in pdg_prec_options */
+  PDG_PREC_SOR = 16,       /* OR-ed with a block kind above: one forward
+                              block-SOR sweep over the cells in grid order,
+                              each block inverted by that kind
+                              (BlockSORPreconditionerLocalOperator,
+                              matrixfree/blocksorpreconditioner.hh:37-296);
+                              the transposed preconditioner is the backward
+                              sweep with transposed blocks */
+  PDG_PREC_BLOCK_MASK = 15
 };
+
+/* Options of the block solvers: BlockSORPreconditionerLocalOperator's omega
+   (blocksorpreconditioner.hh:59-63) and BlockSolverOptions
+   (iterativeblockjacobipreconditioner.hh:202-233). */
+typedef struct pdg_prec_options {
+  double omega;            /* SOR relaxation factor (1.0) */
+  double block_reduction;  /* residual reduction of each block solve (1e-5) */
+  int block_maxit;         /* iteration cap of each block solve (100) */
+  int block_precondition;  /* point-Jacobi inside the block solve (1) */
+  double block_weight;     /* weight of that point Jacobi (1.0) */
+} pdg_prec_options;
 /* precisions */
 enum { PDG_F64 = 0, PDG_F32 = 1 };
 
@@ -120,6 +145,10 @@ typedef struct pdg_solver_options {
                               and the block Jacobi still applied in FP32;
                               -1 = FP32, except FP64 for BiCGStab / GMRES
                               under plain defect correction (mixed = 2) */
+  int assembled;           /* 1: the Krylov operator is the assembled Jacobian
+                              (pdg_jacobian_assemble; assembled on first use),
+                              the matrix-based path of the reference's
+                              matrix-free tests; FP64 only */
 } pdg_solver_options;
 
 /* LinearSolverResult (backend/solver.hh:29-51) +
@@ -261,6 +290,37 @@ int pdg_krylov_solve(pdg_context *ctx, const pdg_solver_options *opt,
    FP64 defect. */
 int pdg_solve_linear_problem(pdg_context *ctx, const pdg_solver_options *opt,
                              double *x, pdg_solver_result *res);
+
+/* Defaults of pdg_prec_options (the reference's defaults). */
+void pdg_default_prec_options(pdg_prec_options *o);
+/* Options used by the next pdg_prec_setup (and every apply after it). */
+int pdg_set_prec_options(pdg_context *ctx, const pdg_prec_options *o);
+/* SolverStatistics (matrixfree/solverstatistics.hh:17-146): iteration count
+   of every block solve of the last application of the PDG_PREC_BJ_ITERATIVE
+   preconditioner in `precision`, one per cell (ncell ints, host array). */
+int pdg_prec_block_iterations(pdg_context *ctx, int precision, int *iterations);
+
+/* ---------------------------------------------------------------- */
+/* assembled Jacobian                                                */
+/* ---------------------------------------------------------------- */
+
+/* GridOperator::jacobian(x, A) (gridoperator/gridoperator.hh:184-189) with
+   ConvectionDiffusionDG::jacobian_volume / _skeleton / _boundary
+   (convectiondiffusiondg.hh:198-266, 483-669, 901-1044): assembles every
+   block of the Jacobian on the device (kept in the context; invalidated
+   when a coefficient changes). */
+int pdg_jacobian_assemble(pdg_context *ctx);
+/* Number of nonzero blocks of the BCRS pattern (ncell + 2 * interior faces;
+   PDELab's pattern: the cell and its face neighbours). */
+int pdg_jacobian_pattern(const pdg_context *ctx, long *nnz_blocks);
+/* Export in ISTL BCRSMatrix<FieldMatrix<double,n,n>> layout: rowptr
+   [ncell+1] and colind [nnz_blocks] (host arrays; either may be NULL),
+   values [nnz_blocks * n * n] (host or device; NULL skips), block rows in
+   cell order, column blocks ascending, each block row-major (test function
+   i, trial function j). */
+int pdg_jacobian_export(pdg_context *ctx, long *rowptr, long *colind, double *values);
+/* y = A x with the assembled Jacobian (ISTL MatrixAdapter::apply). */
+int pdg_matrix_apply(pdg_context *ctx, const double *x, double *y);
 
 /* ---------------------------------------------------------------- */
 /* adjoint (no reference counterpart)                                */

@@ -947,6 +947,11 @@ typedef struct opctx {
   const int *piv;
   long n;
   int nb;
+  /* optional: block SOR / iterative block Jacobi (pdgo_prec_apply_cfg) */
+  const pdgo_prec_config *pc;
+  const double *diag;      /* diagonal blocks, row-major */
+  const double *ablocks;   /* assembled blocks (SOR coupling) */
+  int transpose;
 } opctx;
 
 /* OnTheFlyOperator::apply (backend/istl/seqistlsolverbackend.hh:66-76):
@@ -970,6 +975,11 @@ static int op_applyscaleadd(const opctx *o, double alpha, const double *x, doubl
 }
 /* GridOperatorPreconditioner::apply (gridoperatorpreconditioner.hh:78-84) */
 static void prec_apply(const opctx *o, double *v, const double *dvec) {
+  if (o->pc) {
+    pdgo_prec_apply_cfg(o->p, o->pc, o->diag, o->lu, o->piv, o->ablocks, o->transpose, dvec, v,
+                        NULL);
+    return;
+  }
   if (o->lu) pdgo_lu_apply(o->nb, o->n / o->nb, o->lu, o->piv, dvec, v);
   else memcpy(v, dvec, sizeof(double) * o->n);
 }
@@ -1000,9 +1010,20 @@ static void iter_finalize(const iteration *it, pdgo_result *res) {
 }
 
 /* dune-istl CGSolver::apply restated */
+static int cg_run(const opctx *op_, double *x, double *b, double reduction, int maxit,
+                  pdgo_result *res);
+static int bicgstab_run(const opctx *op_, double *x, double *b, double reduction, int maxit,
+                        pdgo_result *res);
+
 int pdgo_cg(const pdgo_problem *p, int op, const double *blocks, const double *lu,
             const int *piv, double *x, double *b, double reduction, int maxit, pdgo_result *res) {
-  opctx o = {p, op, blocks, lu, piv, pdgo_ndof(p), pdgo_nbasis(p)};
+  opctx o = {p, op, blocks, lu, piv, pdgo_ndof(p), pdgo_nbasis(p), NULL, NULL, NULL, 0};
+  return cg_run(&o, x, b, reduction, maxit, res);
+}
+
+static int cg_run(const opctx *op_, double *x, double *b, double reduction, int maxit,
+                  pdgo_result *res) {
+  const opctx o = *op_;
   long n = o.n;
   memset(res, 0, sizeof(*res));
   iteration it = {0, 0, 0, 0, 1};
@@ -1037,7 +1058,13 @@ int pdgo_cg(const pdgo_problem *p, int op, const double *blocks, const double *l
 /* dune-istl BiCGSTABSolver::apply restated */
 int pdgo_bicgstab(const pdgo_problem *p, int op, const double *blocks, const double *lu,
                   const int *piv, double *x, double *b, double reduction, int maxit, pdgo_result *res) {
-  opctx o = {p, op, blocks, lu, piv, pdgo_ndof(p), pdgo_nbasis(p)};
+  opctx o = {p, op, blocks, lu, piv, pdgo_ndof(p), pdgo_nbasis(p), NULL, NULL, NULL, 0};
+  return bicgstab_run(&o, x, b, reduction, maxit, res);
+}
+
+static int bicgstab_run(const opctx *op_, double *x, double *b, double reduction, int maxit,
+                        pdgo_result *res) {
+  const opctx o = *op_;
   long n = o.n;
   const double EPSILON = 1e-80;
   memset(res, 0, sizeof(*res));
@@ -1130,6 +1157,194 @@ int pdgo_solve_linear_problem(const pdgo_problem *p, int solver, int op, double 
   for (long i = 0; i < n; i++) x[i] -= z[i];
 out:
   free(r); free(z); free(blocks); free(lu); free(piv);
+  res->status = st;
+  return st;
+}
+
+/* ------------------------------------------------------------------ */
+/* Matrix-free block preconditioners beyond block Jacobi               */
+/* ------------------------------------------------------------------ */
+
+/* dune-istl BiCGSTABSolver on one dense block system D x = d (row-major D,
+   D^T with `transpose`), x = 0 initially, preconditioned by
+   LocalPointJacobiPreconditioner (iterativeblockjacobipreconditioner.hh:
+   28-80): v = weight * d / diag(D) (copy when precond = 0).  As
+   IterativeBlockJacobiPreconditionerLocalOperator::jacobian_apply_volume
+   (:357-394) drives it; a breakdown ends the solve with the last iterate. */
+int pdgo_block_bicgstab(int nb, const double *D, int transpose, const double *d, double *x,
+                        double red, int maxit, int precond, double weight, int *iterations) {
+  double r[MAXNB], rt[MAXNB], pv[MAXNB], v[MAXNB], t[MAXNB], y[MAXNB], idg[MAXNB];
+  const double EPSILON = 1e-80;
+  for (int i = 0; i < nb; i++) {
+    x[i] = 0.0;
+    r[i] = d[i];
+    rt[i] = d[i];
+    pv[i] = v[i] = 0.0;
+    idg[i] = 1.0 / D[i * nb + i];
+  }
+#define BAPPLY(in, out)                                                         \
+  for (int i = 0; i < nb; i++) {                                                \
+    double s_ = 0.0;                                                            \
+    for (int j = 0; j < nb; j++) s_ += (transpose ? D[j * nb + i] : D[i * nb + j]) * in[j]; \
+    out[i] = s_;                                                                \
+  }
+#define BPREC(in, out)                                                          \
+  for (int i = 0; i < nb; i++) out[i] = precond ? weight * in[i] * idg[i] : in[i];
+  iteration iter = {0, 0, 0, 0, 1};
+  double norm = sqrt(dot(nb, r, r));
+  int st = PDGO_OK;
+  if (iter_step(&iter, 0, norm, red)) goto fin;
+  double rho = 1, alpha = 1, omega = 1, rho_new, beta, h;
+  for (double it = 0.5; it < maxit; it += .5) {
+    rho_new = dot(nb, rt, r);
+    if (fabs(rho) <= EPSILON || fabs(omega) <= EPSILON) { st = PDGO_EBREAKDOWN; iter.i = it; break; }
+    if (it < 1) memcpy(pv, r, sizeof(double) * nb);
+    else {
+      beta = (rho_new / rho) * (alpha / omega);
+      for (int j = 0; j < nb; j++) pv[j] = beta * (pv[j] - omega * v[j]) + r[j];
+    }
+    BPREC(pv, y);
+    BAPPLY(y, v);
+    h = dot(nb, rt, v);
+    if (fabs(h) < EPSILON) { st = PDGO_EBREAKDOWN; iter.i = it; break; }
+    alpha = rho_new / h;
+    for (int j = 0; j < nb; j++) x[j] += alpha * y[j];
+    for (int j = 0; j < nb; j++) r[j] -= alpha * v[j];
+    norm = sqrt(dot(nb, r, r));
+    if (iter_step(&iter, it, norm, red)) break;
+    it += .5;
+    BPREC(r, y);
+    BAPPLY(y, t);
+    omega = dot(nb, t, r) / dot(nb, t, t);
+    for (int j = 0; j < nb; j++) x[j] += omega * y[j];
+    for (int j = 0; j < nb; j++) r[j] -= omega * t[j];
+    rho = rho_new;
+    norm = sqrt(dot(nb, r, r));
+    if (iter_step(&iter, it, norm, red)) break;
+  }
+#undef BAPPLY
+#undef BPREC
+fin:
+  if (iterations) *iterations = (int)ceil(iter.i);
+  return st;
+}
+
+/* One block solve b = scale * D_e^{-1} a of the configured kind. */
+static void block_solve_cfg(const pdgo_problem *p, const pdgo_prec_config *pc, const double *diag,
+                            const double *lu, const int *piv, int transpose, long e,
+                            const double *a, double *b, double scale, int *iters) {
+  const int nb = pdgo_nbasis(p);
+  const int base = pc->kind & 15;
+  if (base == 3) {
+    int it = 0;
+    pdgo_block_bicgstab(nb, &diag[e * nb * nb], transpose, a, b, pc->block_reduction,
+                        pc->block_maxit, pc->block_precondition, pc->block_weight, &it);
+    if (iters) iters[e] = it;
+  } else if (base == 0 && !lu) {
+    for (int i = 0; i < nb; i++) b[i] = a[i];
+  } else {
+    /* lu / piv hold the factors of D_e (of D_e^T for transposed solves) */
+    pdgo_lu_apply(nb, 1, &lu[e * nb * nb], &piv[e * nb], a, b);
+  }
+  for (int i = 0; i < nb; i++) b[i] *= scale;
+}
+
+/* Block Jacobi of the configured block kind, or (kind & 16) one block-SOR
+   sweep from v = 0 (BlockSORPreconditionerLocalOperator,
+   blocksorpreconditioner.hh:37-296): cells in grid order,
+     a = d_e - sum_{n != e} A_en v_n;   v_e = omega D_e^{-1} a
+   (unvisited neighbours still hold 0).  The transposed preconditioner runs
+   the cells backwards with the transposed blocks. */
+int pdgo_prec_apply_cfg(const pdgo_problem *p, const pdgo_prec_config *pc, const double *diag,
+                        const double *lu, const int *piv, const double *ablocks, int transpose,
+                        const double *d, double *v, int *iters) {
+  const int nb = pdgo_nbasis(p), ns = 2 * p->dim + 1;
+  const long nc = pdgo_ncell(p), bs = (long)nb * nb;
+  double a[MAXNB];
+  if (!(pc->kind & 16)) {
+    for (long e = 0; e < nc; e++)
+      block_solve_cfg(p, pc, diag, lu, piv, transpose, e, &d[e * nb], &v[e * nb], 1.0, iters);
+    return PDGO_OK;
+  }
+  if (!ablocks) return PDGO_EARG;
+  memset(v, 0, sizeof(double) * nc * nb);
+  for (long q = 0; q < nc; q++) {
+    const long e = transpose ? nc - 1 - q : q;
+    for (int i = 0; i < nb; i++) a[i] = d[e * nb + i];
+    for (int sl = 1; sl < ns; sl++) {
+      const long n = neighbor(p, e, sl - 1);
+      if (n < 0) continue;
+      const double *vn = &v[n * nb];
+      if (!transpose) {
+        const double *B = &ablocks[(e * ns + sl) * bs];
+        for (int i = 0; i < nb; i++) {
+          double s = 0.0;
+          for (int j = 0; j < nb; j++) s += B[i * nb + j] * vn[j];
+          a[i] -= s;
+        }
+      } else {
+        /* (A^T)_(e,n) = (A_(n,e))^T; A_(n,e) sits in n's row at the opposite face */
+        const int f = sl - 1, msl = 1 + (f ^ 1);
+        const double *B = &ablocks[(n * ns + msl) * bs];
+        for (int i = 0; i < nb; i++) {
+          double s = 0.0;
+          for (int j = 0; j < nb; j++) s += B[j * nb + i] * vn[j];
+          a[i] -= s;
+        }
+      }
+    }
+    block_solve_cfg(p, pc, diag, lu, piv, transpose, e, a, &v[e * nb], pc->omega, iters);
+  }
+  return PDGO_OK;
+}
+
+/* pdgo_solve_linear_problem with a configured preconditioner (block kind
+   0 = none, 1/2 = LU block Jacobi, 3 = iterative block Jacobi; | 16 block
+   SOR).  op as for pdgo_solve_linear_problem (op = 2: A^T). */
+int pdgo_solve_linear_problem_prec(const pdgo_problem *p, int solver, int op,
+                                   const pdgo_prec_config *pc, double *x, double reduction,
+                                   double min_defect, int maxit, pdgo_result *res) {
+  long n = pdgo_ndof(p);
+  int nb = pdgo_nbasis(p);
+  long nc = pdgo_ncell(p);
+  const int transpose = op == 2;
+  double *r = calloc(n, sizeof(double));
+  double *z = calloc(n, sizeof(double));
+  double *ablocks = malloc(sizeof(double) * nc * (2 * p->dim + 1) * nb * nb);
+  double *diag = malloc(sizeof(double) * nc * nb * nb);
+  double *lu = NULL;
+  int *piv = NULL;
+  int st = pdgo_residual(p, x, r);
+  if (st) goto out;
+  double defect = sqrt(dot(n, r, r));
+  double red = reduction;
+  if (defect > 0 && min_defect / defect > red) red = min_defect / defect;
+  st = pdgo_assemble_jacobian(p, ablocks);
+  if (st) goto out;
+  st = pdgo_block_diagonal(p, diag);
+  if (st) goto out;
+  const int base = pc->kind & 15;
+  if (base == 1 || base == 2) {
+    lu = malloc(sizeof(double) * nc * nb * nb);
+    piv = malloc(sizeof(int) * nc * nb);
+    memcpy(lu, diag, sizeof(double) * nc * nb * nb);
+    if (transpose)
+      for (long e = 0; e < nc; e++) {
+        double *B = &lu[e * nb * nb];
+        for (int i = 0; i < nb; i++)
+          for (int j = i + 1; j < nb; j++) { double t = B[i * nb + j]; B[i * nb + j] = B[j * nb + i]; B[j * nb + i] = t; }
+      }
+    st = pdgo_lu_factor(nb, nc, lu, piv);
+    if (st) goto out;
+  }
+  opctx o = {p, op, op ? ablocks : NULL, lu, piv, n, nb, pc, diag, ablocks, transpose};
+  if (solver == 0) st = cg_run(&o, z, r, red, maxit, res);
+  else st = bicgstab_run(&o, z, r, red, maxit, res);
+  res->first_defect = defect;
+  res->defect = defect * res->reduction;
+  for (long i = 0; i < n; i++) x[i] -= z[i];
+out:
+  free(r); free(z); free(ablocks); free(diag); free(lu); free(piv);
   res->status = st;
   return st;
 }

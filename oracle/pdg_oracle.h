@@ -147,6 +147,32 @@ int pdgo_solve_linear_problem(const pdgo_problem *p, int solver, int op,
                               double *x, double reduction, double min_defect,
                               int maxit, pdgo_result *res);
 
+/* Matrix-free block preconditioners beyond block Jacobi:
+   BlockSORPreconditionerLocalOperator (matrixfree/blocksorpreconditioner.hh)
+   and IterativeBlockJacobiPreconditionerLocalOperator
+   (matrixfree/iterativeblockjacobipreconditioner.hh). */
+typedef struct pdgo_prec_config {
+  int kind;                /* block kind: 0 none, 1/2 LU, 3 iterative; | 16 SOR */
+  double omega;
+  double block_reduction;
+  int block_maxit;
+  int block_precondition;
+  double block_weight;
+} pdgo_prec_config;
+/* Local dune-istl BiCGStab with point Jacobi on one dense block (row-major);
+   returns PDGO_EBREAKDOWN after a breakdown (x holds the last iterate). */
+int pdgo_block_bicgstab(int nb, const double *D, int transpose, const double *d, double *x,
+                        double red, int maxit, int precond, double weight, int *iterations);
+/* v = M^{-1} d; diag: diagonal blocks (row-major), lu/piv: their LU (of the
+   transposed blocks when transpose), ablocks: assembled blocks (SOR).
+   iters (optional, ncell): block-solve iteration counts. */
+int pdgo_prec_apply_cfg(const pdgo_problem *p, const pdgo_prec_config *pc, const double *diag,
+                        const double *lu, const int *piv, const double *ablocks, int transpose,
+                        const double *d, double *v, int *iters);
+int pdgo_solve_linear_problem_prec(const pdgo_problem *p, int solver, int op,
+                                   const pdgo_prec_config *pc, double *x, double reduction,
+                                   double min_defect, int maxit, pdgo_result *res);
+
 /* Evaluate u_h at an m-point tensor Gauss rule in every cell:
    xyz [ncell][m^d][dim], w [ncell][m^d] (weights times |J|),
    val [ncell][m^d]. */

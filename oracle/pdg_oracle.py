@@ -42,6 +42,22 @@ class Result(C.Structure):
     ]
 
 
+class PrecConfig(C.Structure):
+    """Block preconditioner: kind 0 none, 1/2 LU block Jacobi, 3 iterative
+    block Jacobi; + 16 for one block-SOR sweep."""
+    _fields_ = [
+        ("kind", C.c_int), ("omega", C.c_double), ("block_reduction", C.c_double),
+        ("block_maxit", C.c_int), ("block_precondition", C.c_int),
+        ("block_weight", C.c_double),
+    ]
+
+
+def prec_config(kind, omega=1.0, block_reduction=1e-5, block_maxit=100, block_precondition=1,
+                block_weight=1.0):
+    return PrecConfig(kind, omega, block_reduction, block_maxit, block_precondition,
+                      block_weight)
+
+
 def build():
     """Compile the oracle with its Makefile (plain gcc)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
@@ -84,6 +100,14 @@ def lib():
             "pdgo_eval_points": (C.c_int, [P, _dp, C.c_int, _dp, _dp, _dp]),
             "pdgo_grad_logK": (C.c_int, [P, _dp, _dp, _dp]),
             "pdgo_grad_fc": (C.c_int, [P, _dp, _dp]),
+            "pdgo_block_bicgstab": (C.c_int, [C.c_int, _dp, C.c_int, _dp, _dp, C.c_double,
+                                              C.c_int, C.c_int, C.c_double, _ip]),
+            "pdgo_prec_apply_cfg": (C.c_int, [P, C.POINTER(PrecConfig), _dp, _dp, _ip, _dp,
+                                              C.c_int, _dp, _dp, _ip]),
+            "pdgo_solve_linear_problem_prec": (C.c_int, [P, C.c_int, C.c_int,
+                                                         C.POINTER(PrecConfig), _dp, C.c_double,
+                                                         C.c_double, C.c_int,
+                                                         C.POINTER(Result)]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -250,6 +274,33 @@ class Problem:
         st = lib().pdgo_solve_linear_problem(self.ref, 0 if solver == "cg" else 1, op,
                                              _ptr(x), reduction, min_defect, maxit,
                                              C.byref(res))
+        return x, res, st
+
+    def prec_apply_cfg(self, pc, d, transpose=False):
+        """v = M^{-1} d for a PrecConfig; returns (v, per-cell block iterations)."""
+        nb, nc = self.nb, self.ncell
+        diag = self.block_diagonal()
+        lu = piv = None
+        if pc.kind & 15 in (1, 2):
+            src = np.ascontiguousarray(np.swapaxes(diag, 1, 2)) if transpose else diag
+            lu, piv = self.lu(src)
+        ab = self.assemble_jacobian() if pc.kind & 16 else None
+        v = np.zeros(self.ndof)
+        its = np.zeros(nc, dtype=np.int32)
+        _check(lib().pdgo_prec_apply_cfg(self.ref, C.byref(pc), _ptr(diag), _ptr(lu),
+                                         None if piv is None else piv.ctypes.data_as(_ip),
+                                         _ptr(ab), int(transpose),
+                                         _ptr(np.ascontiguousarray(d)), _ptr(v),
+                                         its.ctypes.data_as(_ip)))
+        return v, its
+
+    def solve_prec(self, pc, x=None, solver="cg", op=0, reduction=1e-12, min_defect=1e-99,
+                   maxit=5000):
+        x = np.zeros(self.ndof) if x is None else x
+        res = Result()
+        st = lib().pdgo_solve_linear_problem_prec(self.ref, 0 if solver == "cg" else 1, op,
+                                                  C.byref(pc), _ptr(x), reduction, min_defect,
+                                                  maxit, C.byref(res))
         return x, res, st
 
     def eval_points(self, u, m):

@@ -131,3 +131,47 @@ def test_convection_matrix_free_equals_assembled(oracle):
         y = P.jacobian_apply(x)
         A = P.assemble_jacobian()
         assert np.max(np.abs(y - P.blocks_apply(A, x))) <= 1e-13 * np.max(np.abs(y))
+
+
+def test_block_sor_and_iterative_jacobi_oracle(oracle):
+    """The oracle's block SOR sweep equals the explicit triangular solve
+    omega (D + omega L)^{-1} d, and the iterative block Jacobi matches the
+    exact block inverse to its block-solver reduction."""
+    import numpy as np
+    rng = np.random.default_rng(3)
+    P = oracle.Problem(2, 2, (4, 3), alpha=3.0, K=np.exp(rng.standard_normal(12)))
+    nb, nc = P.nb, P.ncell
+    A = P.assemble_jacobian()
+    dense = np.zeros((P.ndof, P.ndof))
+    strides = [1, 4]
+    for e in range(nc):
+        ix = (e % 4, e // 4)
+        for s in range(5):
+            if s == 0:
+                n = e
+            else:
+                f = s - 1
+                dd, hi = f // 2, f % 2
+                j = ix[dd] + (1 if hi else -1)
+                if j < 0 or j >= (4, 3)[dd]:
+                    continue
+                n = e + (strides[dd] if hi else -strides[dd])
+            dense[e * nb:(e + 1) * nb, n * nb:(n + 1) * nb] = A[e, s]
+    d = rng.uniform(-1, 1, P.ndof)
+    omega = 1.2
+    Dm = np.zeros_like(dense)
+    Lm = np.zeros_like(dense)
+    for e in range(nc):
+        sl = slice(e * nb, (e + 1) * nb)
+        Dm[sl, sl] = dense[sl, sl]
+        Lm[sl, :e * nb] = dense[sl, :e * nb]
+    v, _ = P.prec_apply_cfg(oracle.prec_config(16 | 2, omega=omega), d)
+    vref = omega * np.linalg.solve(Dm + omega * Lm, d)
+    assert np.max(np.abs(v - vref)) <= 1e-12 * np.max(np.abs(vref))
+    vt, _ = P.prec_apply_cfg(oracle.prec_config(16 | 2, omega=omega), d, transpose=True)
+    vtref = omega * np.linalg.solve((Dm + omega * Lm).T, d)
+    assert np.max(np.abs(vt - vtref)) <= 1e-12 * np.max(np.abs(vtref))
+    vi, its = P.prec_apply_cfg(oracle.prec_config(3), d)
+    vex = np.linalg.solve(Dm, d)
+    assert np.max(np.abs(vi - vex)) <= 1e-4 * np.max(np.abs(vex))
+    assert its.min() >= 1 and its.max() <= 100
