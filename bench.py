@@ -384,7 +384,8 @@ def run_gb300(args, world, rank, local):
     if args.extended:
         legs = set(args.legs.split(","))
         for leg, key, fn in (("c3", "solve_q3_96", c3_metrics), ("c4", "adjoint_q2_64", c4_metrics),
-                             ("c5", "cdr_q4_48", c5_metrics)):
+                             ("c5", "cdr_q4_48", c5_metrics), ("prec", "block_prec_q2_64", prec_metrics),
+                             ("asm", "assembled_q2_32", assembled_metrics)):
             if leg not in legs:
                 continue
             try:
@@ -411,6 +412,114 @@ def run_gb300(args, world, rank, local):
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def _event_ms(torch, stream, fn, reps=5):
+    """Median CUDA-event time of fn() on the stream, after one warm-up call."""
+    fn()
+    times = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    times.sort()
+    return times[len(times) // 2]
+
+
+def prec_metrics(pdg, np, torch, stream):
+    """64^3 Q2 (7.08M DoF), log-normal K, f = 1: each block preconditioner's
+    set-up and apply time and the BiCGStab solve it gives (reduction 1e-10)."""
+    n = 64
+    dev = stream.device
+    go = pdg.GridOperator(3, 2, (n, n, n), alpha=3.0, device=dev.index or 0)
+    pdg.load().pdg_set_stream(go.handle, ctypes.c_void_p(stream.cuda_stream))
+    rng = np.random.default_rng(7)
+    go.set_permeability(rng.standard_normal(go.ncell), is_log=True)
+    go.set_source(fc=np.ones(go.ncell))
+    out = {"workload": "sipg3d_q2_64^3 (7.08M DoF), BiCGStab, reduction 1e-10",
+           "sor_hyperplane_steps": 3 * n - 2}
+    d = torch.rand(go.ndof, dtype=torch.float64, device=dev)
+    v = torch.zeros_like(d)
+    kinds = (("bj_fdm", pdg.PREC_BJ_FDM), ("bj_dense", pdg.PREC_BJ_DENSE),
+             ("bj_iterative", pdg.PREC_BJ_ITERATIVE),
+             ("sor_dense", pdg.PREC_SOR | pdg.PREC_BJ_DENSE),
+             ("sor_fdm", pdg.PREC_SOR | pdg.PREC_BJ_FDM),
+             ("sor_iterative", pdg.PREC_SOR | pdg.PREC_BJ_ITERATIVE))
+    for name, kind in kinds:
+        rec = {}
+        try:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            pdg._check(pdg.load().pdg_prec_setup(go.handle, kind, pdg.F64))
+            torch.cuda.synchronize()
+            rec["setup_s"] = time.perf_counter() - t0
+            rec["apply_ms"] = _event_ms(torch, stream, lambda: pdg._check(
+                pdg.load().pdg_prec_apply(go.handle, d.data_ptr(), v.data_ptr())))
+            if kind & 15 == pdg.PREC_BJ_ITERATIVE:
+                its = go.prec_block_iterations()
+                rec["block_iterations_mean"] = float(its.mean())
+                rec["block_iterations_max"] = int(its.max())
+            ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.BICGSTAB, preconditioner=kind,
+                                                     maxiter=20000)
+            u = torch.zeros(go.ndof, dtype=torch.float64, device=dev)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10).apply()
+            torch.cuda.synchronize()
+            r = ls.result()
+            rec.update({"solve_s": time.perf_counter() - t0, "iterations": r.iterations,
+                        "converged": bool(r.converged)})
+        except Exception as exc:
+            rec["error"] = f"{type(exc).__name__}: {exc}"
+        out[name] = rec
+    go.close()
+    return out
+
+
+def assembled_metrics(pdg, np, torch, stream):
+    """32^3 Q2 (884,736 DoF): the Jacobian assembled on the device by probing,
+    the BCRS block product against the matrix-free apply, and the
+    matrix-based vs matrix-free CG solve (reduction 1e-10)."""
+    n = 32
+    dev = stream.device
+    go = pdg.GridOperator(3, 2, (n, n, n), alpha=3.0, device=dev.index or 0)
+    pdg.load().pdg_set_stream(go.handle, ctypes.c_void_p(stream.cuda_stream))
+    rng = np.random.default_rng(8)
+    go.set_permeability(rng.standard_normal(go.ncell), is_log=True)
+    go.set_source(fc=np.ones(go.ncell))
+    out = {"workload": "sipg3d_q2_32^3 (884,736 DoF), CG + block Jacobi (FDM), reduction 1e-10"}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    go.jacobian_assemble()
+    torch.cuda.synchronize()
+    out["assemble_s"] = time.perf_counter() - t0
+    nnzb = go.jacobian_pattern()
+    out["nnz_blocks"] = nnzb
+    out["matrix_bytes"] = go.ncell * 7 * 27 * 27 * 8
+    x = torch.rand(go.ndof, dtype=torch.float64, device=dev)
+    y = torch.zeros_like(x)
+    out["matrix_apply_ms"] = _event_ms(torch, stream, lambda: go.matrix_apply(x, y))
+    out["matrix_apply_gbs"] = out["matrix_bytes"] / (out["matrix_apply_ms"] * 1e-3) / 1e9
+    out["matrix_free_apply_ms"] = _event_ms(torch, stream, lambda: pdg._check(
+        pdg.load().pdg_apply(go.handle, x.data_ptr(), y.data_ptr())))
+    for assembled in (0, 1):
+        ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG)
+        ls.opts.assembled = assembled
+        u = torch.zeros(go.ndof, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10).apply()
+        torch.cuda.synchronize()
+        r = ls.result()
+        key = "matrix_based" if assembled else "matrix_free"
+        out[f"{key}_solve_s"] = time.perf_counter() - t0
+        out[f"{key}_iterations"] = r.iterations
+    go.close()
+    return out
 
 
 def smoothed_logK(np, n, seed=3, sigma=1.5):
@@ -615,23 +724,28 @@ def _c5_gradients(pdg, pdg_torch, np, torch, go, dev, rng, logK0, u_ref):
     t_bwd = time.perf_counter() - t0
     errs = {}
     h = 1e-6
+    # the central differences need solves well below h * |grad|: reduction 1e-11
+    fdp = pdg_torch.DGProblem(go, method=pdg.BICGSTAB, preconditioner=pdg.PREC_BJ_DENSE,
+                              reduction=1e-11, inner_reduction=C5_INNER_REDUCTION,
+                              inner_maxit=C5_INNER_MAXIT)
     with torch.no_grad():
         for name, grad in (("logK", logK.grad), ("f", fc.grad)):
             ee = []
             for _ in range(2):
                 d = torch.tensor(rng.standard_normal(go.ncell), device=dev)
                 if name == "logK":
-                    Jp = 0.5 * ((pdg_torch.solve_dg(logK + h * d, fc, prob) - u_obs) ** 2).sum()
-                    Jm = 0.5 * ((pdg_torch.solve_dg(logK - h * d, fc, prob) - u_obs) ** 2).sum()
+                    Jp = 0.5 * ((pdg_torch.solve_dg(logK + h * d, fc, fdp) - u_obs) ** 2).sum()
+                    Jm = 0.5 * ((pdg_torch.solve_dg(logK - h * d, fc, fdp) - u_obs) ** 2).sum()
                 else:
-                    Jp = 0.5 * ((pdg_torch.solve_dg(logK, fc + h * d, prob) - u_obs) ** 2).sum()
-                    Jm = 0.5 * ((pdg_torch.solve_dg(logK, fc - h * d, prob) - u_obs) ** 2).sum()
+                    Jp = 0.5 * ((pdg_torch.solve_dg(logK, fc + h * d, fdp) - u_obs) ** 2).sum()
+                    Jm = 0.5 * ((pdg_torch.solve_dg(logK, fc - h * d, fdp) - u_obs) ** 2).sum()
                 fd = float((Jp - Jm) / (2 * h))
                 ad = float((grad * d).sum())
                 ee.append(abs(fd - ad) / abs(ad))
             errs[name] = max(ee)
     return {"forward_solve_s": t_fwd, "adjoint_solve_plus_grads_s": t_bwd,
             "grad_over_solve": t_bwd / t_fwd, "reduction": 1e-9, "fd_h": h,
+            "fd_solve_reduction": 1e-11,
             "fd_rel_err_max_logK": errs["logK"], "fd_rel_err_max_f": errs["f"]}
 
 

@@ -626,6 +626,7 @@ static void invalidate(pdg_context *ctx, bool operator_changed) {
   ctx->r0_valid = 0;
   if (operator_changed) {
     ctx->rec_valid = 0;
+    ctx->rec32_valid = 0;
     ctx->A_valid = 0;
     ctx->prec[0].ready = 0;
     ctx->prec[1].ready = 0;
@@ -813,7 +814,7 @@ int pdg_destroy(pdg_context *c) {
                   c->jq, c->oq, c->r0, c->r0K, c->red_partials, c->red_out, c->d_flag,
                   c->stage_a, c->stage_b, c->rec64, c->conv64, c->conv32, c->convtab64,
                   c->convtab32, c->gm_V32, c->gm_V64, c->gm_F64, c->gm_partial, c->gm_coef,
-                  c->A64};
+                  c->A64, c->rec32, c->nlW64, c->nlW32, c->nlB64, c->nlB32};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 10; i++)
@@ -977,9 +978,37 @@ static int apply_entry(pdg_context *ctx, const double *x, double *y, double alph
   Staged<double> sx, sy;
   PDG_TRY(stage_in<double>(ctx, x, ctx->ndof, ctx->stage_a, true, &sx));
   PDG_TRY(stage_in<double>(ctx, y, ctx->ndof, ctx->stage_b, acc != 0, &sy));
-  PDG_TRY(op_launch<double>(ctx, sx.dev, sy.dev, with_r0 ? ctx->r0 : nullptr, alpha, acc,
-                            transpose, nullptr));
+  if (with_r0 && ctx->nl_deg > 0) {
+    // R(x) = J_lin x + R(0) + int q(u) psi: the linearized term stays out
+    ctx->nl_off = 1;
+    const int st = op_launch<double>(ctx, sx.dev, sy.dev, ctx->r0, alpha, acc, transpose, nullptr);
+    ctx->nl_off = 0;
+    PDG_TRY(st);
+    PDG_TRY(nl_residual(ctx, sx.dev, sy.dev));
+  } else {
+    PDG_TRY(op_launch<double>(ctx, sx.dev, sy.dev, with_r0 ? ctx->r0 : nullptr, alpha, acc,
+                              transpose, nullptr));
+  }
   PDG_TRY(stage_out<double>(ctx, sy));
+  return PDG_OK;
+}
+
+// r = R(x) on device vectors (overwrites r)
+static int residual_dev(pdg_context *ctx, const double *x, double *r) {
+  PDG_TRY(ensure_r0(ctx));
+  ctx->nl_off = 1;
+  const int st = op_launch<double>(ctx, x, r, ctx->r0, 1.0, 0, 0, nullptr);
+  ctx->nl_off = 0;
+  PDG_TRY(st);
+  return nl_residual(ctx, x, r);
+}
+
+static int norm_dev(pdg_context *ctx, const double *v, double *out) {
+  const RedCtx rc = red_ctx(ctx);
+  PDG_TRY(red_dot(ctx, rc, ctx->ndof, v, v, nullptr, nullptr, FIN_NORM, S_DOT, -1, false));
+  double scal[S_COUNT];
+  PDG_TRY(fetch_state(ctx, scal, nullptr));
+  *out = scal[S_DOT];
   return PDG_OK;
 }
 
@@ -1080,6 +1109,180 @@ static int check_opts(const pdg_solver_options *o) {
     return set_error(PDG_EINVAL, "iteration caps must be >= 1");
   if (!(o->reduction > 0)) return set_error(PDG_EINVAL, "reduction must be > 0");
   return PDG_OK;
+}
+
+int pdg_set_nonlinearity(pdg_context *ctx, int degree, const double *coef) {
+  PDG_CHECK_CTX(ctx);
+  if (coef && (degree < 1 || degree > 4)) return set_error(PDG_EINVAL, "degree must be 1..4");
+  ctx->nl_deg = coef ? degree : 0;
+  for (int m = 0; m < 5; m++) ctx->nl_coef[m] = (coef && m <= degree) ? coef[m] : 0.0;
+  ctx->nl_point = 0;
+  invalidate(ctx, true);
+  return PDG_OK;
+}
+
+int pdg_set_linearization_point(pdg_context *ctx, const double *x) {
+  PDG_CHECK_CTX(ctx);
+  if (!x) return set_error(PDG_EINVAL, "null vector");
+  PDG_TRY(ensure_stage(ctx));
+  Staged<double> sx;
+  PDG_TRY(stage_in<double>(ctx, x, ctx->ndof, ctx->stage_a, true, &sx));
+  PDG_TRY(nl_set_point(ctx, sx.dev));
+  ctx->A_valid = 0;
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return PDG_OK;
+}
+
+int pdg_jacobian_apply_nonlinear(pdg_context *ctx, const double *x, const double *z, double *y) {
+  PDG_TRY(pdg_set_linearization_point(ctx, x));
+  return apply_entry(ctx, z, y, 1.0, 1, 0, false);
+}
+
+void pdg_default_newton_options(pdg_newton_options *o) {
+  if (!o) return;
+  o->reduction = 1e-8;
+  o->absolute_limit = 1e-12;
+  o->max_iterations = 40;
+  o->force_iteration = 0;
+  o->min_linear_reduction = 1e-3;
+  o->fixed_linear_reduction = 0;
+  o->line_search = 1;
+  o->line_search_max_iterations = 10;
+  o->line_search_damping = 0.5;
+  o->line_search_accept_best = 0;
+  o->verbose = 0;
+}
+
+// NewtonMethod::apply (solver/newton.hh:177-335) on device vectors.
+static int newton_run(pdg_context *ctx, const pdg_newton_options *opt,
+                      const pdg_solver_options *lin, double *u, pdg_newton_result *res,
+                      double *r, double *z, double *uprev) {
+  const long n = ctx->ndof;
+  double defect = 0.0;
+  // updateDefect (:341-369): r = R(u), defect = |r|
+  auto update_defect = [&]() -> int {
+    PDG_TRY(residual_dev(ctx, u, r));
+    return norm_dev(ctx, r, &defect);
+  };
+  PDG_TRY(update_defect());
+  res->first_defect = defect;
+  res->defect = defect;
+  double prev = defect;
+  int prec_ready = 0;
+  for (;;) {
+    // DefaultTerminate::terminate (terminate.hh:29-40)
+    if (!(opt->force_iteration && res->iterations == 0)) {
+      res->converged = defect < opt->absolute_limit || defect < res->first_defect * opt->reduction;
+      if (res->converged) break;
+      if (res->iterations >= opt->max_iterations)
+        return set_error(PDG_ENOTCONVERGED, "Newton: maximum iteration count reached");
+    }
+    if (!std::isfinite(defect)) return set_error(PDG_ENONFINITE, "Newton: non-finite defect");
+    // prepareStep (:99-143): linear reduction
+    double linred = opt->min_linear_reduction;
+    if (!opt->fixed_linear_reduction &&
+        !(res->iterations == 0 && res->first_defect < opt->absolute_limit)) {
+      const double stop = std::max(res->first_defect * opt->reduction, opt->absolute_limit);
+      linred = std::max(stop / (10 * defect),
+                        std::min(opt->min_linear_reduction, defect * defect / (prev * prev)));
+    }
+    prev = defect;
+    // linearSolve (:145-170) at the linearization point u
+    PDG_TRY(nl_set_point(ctx, u));
+    ctx->A_valid = 0;
+    if (!prec_ready) {
+      // GridOperatorPreconditioner::pre sets the block preconditioner up
+      // once, at the first linearization point (gridoperatorpreconditioner.hh:45-75)
+      PDG_TRY(prec_setup_impl(ctx, lin->preconditioner, lin->mixed ? PDG_F32 : PDG_F64));
+      prec_ready = 1;
+    }
+    pdg_solver_options o = *lin;
+    o.reduction = linred;
+    PDG_TRY(vec_fill<double>(ctx, n, z, 0.0));
+    pdg_solver_result lr;
+    std::memset(&lr, 0, sizeof(lr));
+    const int ls = solve_correction(ctx, &o, z, r, 0, &lr);
+    res->linear_solver_iterations += lr.iterations;
+    if (ls != PDG_OK && ls != PDG_ENOTCONVERGED) return ls;
+    // line search (linesearch.hh:81-165)
+    if (!opt->line_search || defect < opt->absolute_limit) {
+      PDG_TRY(vec_axpy(ctx, n, -1.0, z, u));
+      PDG_TRY(update_defect());
+    } else {
+      double lambda = 1.0, best_lambda = 0.0, best = defect;
+      const double previous = defect;
+      bool ok = false;
+      PDG_TRY(vec_copy<double>(ctx, n, u, uprev));
+      for (int it = 0; it < opt->line_search_max_iterations; it++) {
+        PDG_TRY(vec_axpy(ctx, n, -lambda, z, u));
+        PDG_TRY(update_defect());
+        if (defect <= (1.0 - lambda / 4) * previous) { ok = true; break; }
+        if (defect < best) { best = defect; best_lambda = lambda; }
+        lambda *= opt->line_search_damping;
+        PDG_TRY(vec_copy<double>(ctx, n, uprev, u));
+      }
+      if (!ok) {
+        if (!opt->line_search_accept_best || best_lambda == 0.0) {
+          PDG_TRY(vec_copy<double>(ctx, n, uprev, u));
+          PDG_TRY(update_defect());
+          res->defect = defect;
+          return set_error(PDG_ELINESEARCH, "Newton: line search failed");
+        }
+        if (best_lambda != lambda) {
+          PDG_TRY(vec_copy<double>(ctx, n, uprev, u));
+          PDG_TRY(vec_axpy(ctx, n, -best_lambda, z, u));
+          PDG_TRY(update_defect());
+        }
+      }
+    }
+    res->iterations++;
+    res->defect = defect;
+    res->reduction = res->first_defect > 0 ? defect / res->first_defect : 0.0;
+    res->conv_rate = std::pow(res->reduction, 1.0 / res->iterations);
+    if (opt->verbose)
+      std::fprintf(stderr, "pdg newton: iteration %d defect %.3e (linear %d its, reduction %.2e)\n",
+                   res->iterations, defect, lr.iterations, linred);
+  }
+  res->defect = defect;
+  res->reduction = res->first_defect > 0 ? defect / res->first_defect : 0.0;
+  return PDG_OK;
+}
+
+int pdg_newton_solve(pdg_context *ctx, const pdg_newton_options *opt,
+                     const pdg_solver_options *lin, double *u, pdg_newton_result *res) {
+  PDG_CHECK_CTX(ctx);
+  if (!opt || !lin || !u || !res) return set_error(PDG_EINVAL, "null argument");
+  PDG_TRY(check_opts(lin));
+  if (opt->max_iterations < 1 || !(opt->line_search_damping > 0 && opt->line_search_damping < 1))
+    return set_error(PDG_EINVAL, "bad Newton options");
+  std::memset(res, 0, sizeof(*res));
+  PDG_TRY(ensure_stage(ctx));
+  PDG_TRY(ensure_work(ctx, lin->mixed != 0));
+  Staged<double> su;
+  PDG_TRY(stage_in<double>(ctx, u, ctx->ndof, ctx->stage_a, true, &su));
+  double *buf[3] = {nullptr, nullptr, nullptr};
+  for (auto &b : buf)
+    if (cudaMalloc(&b, sizeof(double) * ctx->ndof) != cudaSuccess) {
+      for (auto &c : buf)
+        if (c) cudaFree(c);
+      return set_error(PDG_ECUDA, "out of device memory for Newton");
+    }
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, ctx->stream);
+  const int st = newton_run(ctx, opt, lin, su.dev, res, buf[0], buf[1], buf[2]);
+  cudaEventRecord(t1, ctx->stream);
+  cudaEventSynchronize(t1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  res->elapsed = ms * 1e-3;
+  res->status = st;
+  for (auto &b : buf) cudaFree(b);
+  const int so = stage_out<double>(ctx, su);
+  return st != PDG_OK ? st : so;
 }
 
 int pdg_jacobian_assemble(pdg_context *ctx) {

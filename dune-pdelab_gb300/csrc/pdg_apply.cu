@@ -454,6 +454,33 @@ static int record_dn(pdg_context *ctx) {
   return PDG_OK;
 }
 
+template <int N>
+static int record32_n(pdg_context *ctx) {
+  using C = Cfg<3, N>;
+  if (!ctx->rec32)
+    PDG_CUDA_TRY(cudaMalloc(&ctx->rec32, sizeof(float) * C::REC * ctx->ncell));
+  OpParams<double> p = make_params<double>(ctx, ctx->K64, ctx->c64, ctx->tab64);
+  const unsigned blocks = (unsigned)((ctx->ncell + 127) / 128);
+  k_cell_record<float, 3, N><<<blocks, 128, 0, ctx->stream>>>(p, ctx->rec32);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+
+// FP32 records of the 3D FP32 operator (computed in FP64, rounded)
+static int ensure_record32(pdg_context *ctx) {
+  if (ctx->rec32_valid) return PDG_OK;
+  int st;
+  switch (ctx->N) {
+    case 2: st = record32_n<2>(ctx); break;
+    case 3: st = record32_n<3>(ctx); break;
+    case 4: st = record32_n<4>(ctx); break;
+    case 5: st = record32_n<5>(ctx); break;
+    default: return set_error(PDG_EUNSUPPORTED, "degree not compiled in");
+  }
+  if (st == PDG_OK) ctx->rec32_valid = 1;
+  return st;
+}
+
 // FP64 cell records (rebuilt after the coefficients change)
 static int ensure_record(pdg_context *ctx) {
   if (ctx->rec_valid) return PDG_OK;
@@ -477,6 +504,14 @@ template <typename T>
 int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c,
                  const T *tab) {
   OpParams<T> p = make_params<T>(ctx, K, c, tab);
+  if constexpr (std::is_same<T, float>::value) {
+    if (ctx->dim == 3 && !a.cells && K == ctx->K32) {
+      PDG_TRY(ensure_record32(ctx));
+      PDG_TRY(launch_apply32_3d(ctx, a, p, ctx->rec32));
+      if (ctx->vel.nmodes > 0) PDG_TRY(launch_convection<T>(ctx, a));
+      return nl_apply<T>(ctx, a);
+    }
+  }
   const T *rec = nullptr;
   if (std::is_same<T, double>::value && K == (const T *)ctx->K64) {
     PDG_TRY(ensure_record(ctx));
@@ -496,6 +531,7 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
     default: return set_error(PDG_EUNSUPPORTED, "dim/degree not compiled in");
   }
   if (st == PDG_OK && ctx->vel.nmodes > 0) st = launch_convection<T>(ctx, a);
+  if (st == PDG_OK) st = nl_apply<T>(ctx, a);
   return st;
 }
 

@@ -135,6 +135,8 @@ struct pdg_context {
   int r0_valid;
   double *rec64;       // FP64 per-cell operator records (scaled A'_dir + face coefficients)
   int rec_valid;
+  float *rec32;        // the same records rounded to FP32 (3D FP32 operator)
+  int rec32_valid;
   double *conv64;      // per-cell weighted velocity at volume and face points (FP64)
   float *conv32;       // the same in FP32
   double *convtab64;   // B and D (basis values / derivatives at Gauss points)
@@ -145,6 +147,15 @@ struct pdg_context {
   void *gm_V32, *gm_V64, *gm_F64;
   int gm_m32, gm_m64, gm_mF;
   double *gm_partial, *gm_coef;
+
+  // nonlinear volume term q(u) = sum_m nl_coef[m] u^m (nl_deg 0 = none) and
+  // its weights w_q |J| q'(u_x) at the linearization point x
+  int nl_deg;
+  double nl_coef[5];
+  double *nlW64, *nlB64;
+  float *nlW32, *nlB32;
+  int nl_point;            // weights valid for the current linearization point
+  int nl_off;              // temporarily exclude the term (residual evaluation)
 
   // assembled Jacobian: [ncell][2d+1][nb][nb], column-major blocks
   double *A64;
@@ -188,6 +199,9 @@ template <typename T>
 int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c,
                  const T *tab);
 int launch_rhs(pdg_context *ctx);
+// 3D FP32 operator with staged neighbour runs (all cells, coupled or diag_only)
+int launch_apply32_3d(pdg_context *ctx, const ApplyArgs<float> &a, const OpParams<float> &p,
+                      const float *rec);
 int launch_grad_logK(pdg_context *ctx, const double *u, const double *lam, double *g);
 int launch_grad_source(pdg_context *ctx, const double *lam, double *g);
 
@@ -225,6 +239,12 @@ struct RhsTables {
 RhsTables make_rhs_tables(const pdg_context *ctx);
 double *rhs_r0K(pdg_context *ctx, bool alloc);
 double lagrange_derivative(int k, int i, double x);
+
+// nonlinear volume term: linearization point, residual part, Jacobian part
+int nl_set_point(pdg_context *ctx, const double *x);
+int nl_residual(pdg_context *ctx, const double *x, double *r);
+template <typename T>
+int nl_apply(pdg_context *ctx, const ApplyArgs<T> &a);
 
 // assembled Jacobian (probing the matrix-free operator) and its block product
 int assemble_jacobian(pdg_context *ctx);

@@ -31,6 +31,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libpdg.so")
 
 PDG_OK, PDG_EINVAL, PDG_ECUDA, PDG_ENOTCONVERGED, PDG_EBREAKDOWN = 0, 1, 2, 3, 4
 PDG_ESTATE, PDG_EUNSUPPORTED, PDG_EOUTFLOW, PDG_ENONFINITE, PDG_ETIMEOUT = 5, 6, 7, 8, 9
+PDG_ELINESEARCH = 10
 NIPG, SIPG, IIPG = 0, 1, 2
 WEIGHTS_ON, WEIGHTS_OFF = 0, 1
 BC_DIRICHLET, BC_NEUMANN, BC_OUTFLOW, BC_NONE = 1, -1, -2, -3
@@ -67,6 +68,27 @@ class PrecOptions(C.Structure):
     _fields_ = [("omega", C.c_double), ("block_reduction", C.c_double),
                 ("block_maxit", C.c_int), ("block_precondition", C.c_int),
                 ("block_weight", C.c_double)]
+
+
+class NewtonOptions(C.Structure):
+    """NewtonMethod parameters (solver/newton.hh), reference defaults."""
+    _fields_ = [("reduction", C.c_double), ("absolute_limit", C.c_double),
+                ("max_iterations", C.c_int), ("force_iteration", C.c_int),
+                ("min_linear_reduction", C.c_double), ("fixed_linear_reduction", C.c_int),
+                ("line_search", C.c_int), ("line_search_max_iterations", C.c_int),
+                ("line_search_damping", C.c_double), ("line_search_accept_best", C.c_int),
+                ("verbose", C.c_int)]
+
+
+class NewtonResult(C.Structure):
+    _fields_ = [("converged", C.c_int), ("iterations", C.c_int),
+                ("first_defect", C.c_double), ("defect", C.c_double),
+                ("reduction", C.c_double), ("conv_rate", C.c_double),
+                ("linear_solver_iterations", C.c_int), ("elapsed", C.c_double),
+                ("status", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class SolverResult(C.Structure):
@@ -120,6 +142,12 @@ _SIGS = {
     "pdg_default_prec_options": (None, [C.POINTER(PrecOptions)]),
     "pdg_set_prec_options": (C.c_int, [_vp, C.POINTER(PrecOptions)]),
     "pdg_prec_block_iterations": (C.c_int, [_vp, C.c_int, _vp]),
+    "pdg_set_nonlinearity": (C.c_int, [_vp, C.c_int, _vp]),
+    "pdg_set_linearization_point": (C.c_int, [_vp, _vp]),
+    "pdg_jacobian_apply_nonlinear": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "pdg_default_newton_options": (None, [C.POINTER(NewtonOptions)]),
+    "pdg_newton_solve": (C.c_int, [_vp, C.POINTER(NewtonOptions), C.POINTER(SolverOptions), _vp,
+                                   C.POINTER(NewtonResult)]),
     "pdg_jacobian_assemble": (C.c_int, [_vp]),
     "pdg_jacobian_pattern": (C.c_int, [_vp, C.POINTER(C.c_long)]),
     "pdg_jacobian_export": (C.c_int, [_vp, _vp, _vp, _vp]),
@@ -186,6 +214,14 @@ def fourier_velocity_modes(seed, nmodes=8, bmax=10.0, kmax=2):
     s = np.linalg.norm(modes[:, 4:], axis=1).sum()
     modes[:, 4:] *= bmax / s
     return modes
+
+
+def newton_options(**kw):
+    o = NewtonOptions()
+    load().pdg_default_newton_options(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
 
 
 def prec_options(**kw):
@@ -318,6 +354,22 @@ class GridOperator:
         _check(load().pdg_grad_logK(self._h, _ptr(u), _ptr(lam), _ptr(g)))
         return g
 
+    def set_nonlinearity(self, coef):
+        """Volume term int q(u) psi, q(u) = sum_m coef[m] u^m (None removes it)."""
+        if coef is None:
+            _check(load().pdg_set_nonlinearity(self._h, 0, None))
+            return
+        c = np.ascontiguousarray(coef, dtype=np.float64)
+        _check(load().pdg_set_nonlinearity(self._h, len(c) - 1, c.ctypes.data))
+
+    def set_linearization_point(self, x):
+        _check(load().pdg_set_linearization_point(self._h, _ptr(x)))
+
+    def jacobian_apply_nonlinear(self, x, z, y):
+        """y += J(x) z"""
+        _check(load().pdg_jacobian_apply_nonlinear(self._h, _ptr(x), _ptr(z), _ptr(y)))
+        return y
+
     def set_prec_options(self, options=None, **kw):
         """Options of the block preconditioners (SOR omega, block solver)."""
         o = options if options is not None else prec_options(**kw)
@@ -431,6 +483,26 @@ class ISTLBackend_SEQ_MatrixFree_Base:
 
     def norm(self, v):
         return self.go.norm(v)
+
+    def result(self):
+        return self.res
+
+
+class NewtonMethod:
+    """NewtonMethod<GridOperator, LinearSolver> (solver/newton.hh): apply(u)
+    solves R(u) = 0 from the initial guess u with the backend's Krylov
+    method and preconditioner for the linear steps."""
+
+    def __init__(self, go: GridOperator, ls: "ISTLBackend_SEQ_MatrixFree_Base", **kw):
+        self.go, self.ls = go, ls
+        self.opts = newton_options(**kw)
+        self.res = NewtonResult()
+
+    def apply(self, u):
+        st = load().pdg_newton_solve(self.go.handle, C.byref(self.opts), C.byref(self.ls.opts),
+                                     _ptr(u), C.byref(self.res))
+        _check(st)
+        return u
 
     def result(self):
         return self.res

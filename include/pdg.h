@@ -39,7 +39,9 @@ enum {
   PDG_EUNSUPPORTED = 6,    /* configuration not compiled in / not supported */
   PDG_EOUTFLOW = 7,        /* outflow boundary on inflow (convectiondiffusiondg.hh:802-806) */
   PDG_ENONFINITE = 8,      /* NaN/Inf defect */
-  PDG_ETIMEOUT = 9         /* a bounded device wait ran out */
+  PDG_ETIMEOUT = 9,        /* a bounded device wait ran out */
+  PDG_ELINESEARCH = 10     /* Newton line search failed (LineSearchError,
+                              solver/linesearch.hh:134-154) */
 };
 
 /* ConvectionDiffusionDGMethod::Type  (convectiondiffusiondg.hh:29-32) */
@@ -299,6 +301,58 @@ int pdg_set_prec_options(pdg_context *ctx, const pdg_prec_options *o);
    of every block solve of the last application of the PDG_PREC_BJ_ITERATIVE
    preconditioner in `precision`, one per cell (ncell ints, host array). */
 int pdg_prec_block_iterations(pdg_context *ctx, int precision, int *iterations);
+
+/* ---------------------------------------------------------------- */
+/* nonlinear operator and Newton                                     */
+/* ---------------------------------------------------------------- */
+
+/* NonlinearConvectionDiffusionDG (test/localoperator/
+   nonlinearconvectiondiffusiondg.hh:28-307): the operator plus the volume
+   term int q(u) psi with q(u) = sum_{m<=degree} coef[m] u^m (degree 1..4);
+   coef = NULL removes it.  The residual includes the term; Jacobian applies
+   add int q'(u(x)) z psi at the linearization point x. */
+int pdg_set_nonlinearity(pdg_context *ctx, int degree, const double *coef);
+/* OnTheFlyOperator / GridOperatorPreconditioner::setLinearizationPoint
+   (backends.hh:129-135, gridoperatorpreconditioner.hh:38-42): the point x
+   of every following Jacobian apply and Krylov solve. */
+int pdg_set_linearization_point(pdg_context *ctx, const double *x);
+/* GridOperator::jacobian_apply(x, z, y) (gridoperator.hh:200-205):
+   y += J(x) z (sets x as the linearization point). */
+int pdg_jacobian_apply_nonlinear(pdg_context *ctx, const double *x, const double *z,
+                                 double *y);
+
+/* NewtonMethod (solver/newton.hh:63-669) with DefaultTerminate
+   (solver/terminate.hh:20-76) and the Hackbusch-Reusken line search
+   (solver/linesearch.hh:71-209); defaults are the reference's. */
+typedef struct pdg_newton_options {
+  double reduction;              /* 1e-8 */
+  double absolute_limit;         /* 1e-12 */
+  int max_iterations;            /* 40 */
+  int force_iteration;           /* 0 */
+  double min_linear_reduction;   /* 1e-3 */
+  int fixed_linear_reduction;    /* 0 */
+  int line_search;               /* 1: Hackbusch-Reusken, 0: none (full steps) */
+  int line_search_max_iterations;/* 10 */
+  double line_search_damping;    /* 0.5 */
+  int line_search_accept_best;   /* 0 */
+  int verbose;
+} pdg_newton_options;
+/* NewtonResult (newton.hh) */
+typedef struct pdg_newton_result {
+  int converged;
+  int iterations;
+  double first_defect, defect, reduction, conv_rate;
+  int linear_solver_iterations;
+  double elapsed;
+  int status;
+} pdg_newton_result;
+void pdg_default_newton_options(pdg_newton_options *o);
+/* NewtonMethod::apply(u): u is the initial guess and the result; the
+   linear solves use `lin` (its reduction is replaced by Newton's linear
+   reduction; the preconditioner is set up at the first linearization point
+   and kept, as GridOperatorPreconditioner::pre does). */
+int pdg_newton_solve(pdg_context *ctx, const pdg_newton_options *opt,
+                     const pdg_solver_options *lin, double *u, pdg_newton_result *res);
 
 /* ---------------------------------------------------------------- */
 /* assembled Jacobian                                                */

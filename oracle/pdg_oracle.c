@@ -347,6 +347,38 @@ static void alpha_volume(const pdgo_problem *p, const tables *T, long e,
   }
 }
 
+/* nonlinear volume term (nonlinearconvectiondiffusiondg.hh:93-176):
+   mode 0: r += int q(u) psi (alpha_volume), u from x;
+   mode 1: r += int q'(u_lin) z psi (jacobian_apply_volume), x = z. */
+static double nl_q(const pdgo_problem *p, double u) {
+  double s = 0.0;
+  for (int m = p->nl_deg; m >= 0; m--) s = s * u + p->nl_coef[m];
+  return s;
+}
+static double nl_qprime(const pdgo_problem *p, double u) {
+  double s = 0.0;
+  for (int m = p->nl_deg; m >= 1; m--) s = s * u + m * p->nl_coef[m];
+  return s;
+}
+static void nl_volume(const pdgo_problem *p, const tables *T, long e, const double *x,
+                      double *r, int mode) {
+  if (p->nl_deg <= 0 || (mode == 1 && !p->xlin)) return;
+  int d = T->d, nb = T->nb;
+  double detJ = 1.0;
+  for (int j = 0; j < d; j++) detJ *= cell_h(p, j);
+  const double *xl = mode == 1 ? &p->xlin[e * nb] : x;
+  for (int q = 0; q < T->nqv; q++) {
+    const double *phi = &T->vphi[q * nb];
+    double u = 0.0, zq = 0.0;
+    for (int i = 0; i < nb; i++) u += xl[i] * phi[i];
+    if (mode == 1)
+      for (int i = 0; i < nb; i++) zq += x[i] * phi[i];
+    const double v = mode == 1 ? nl_qprime(p, u) * zq : nl_q(p, u);
+    const double factor = T->vw[q] * detJ;
+    for (int i = 0; i < nb; i++) r[i] += v * phi[i] * factor;
+  }
+}
+
 /* lambda_volume (convectiondiffusiondg.hh:1047-1075) */
 static void lambda_volume(const pdgo_problem *p, const tables *T, long e, double *r) {
   int d = T->d, nb = T->nb;
@@ -551,6 +583,7 @@ static int assemble_vector(const pdgo_problem *p, const double *x, double *r, in
     cell_index(p, e, ix);
     if (!jacobian_apply) lambda_volume(p, &T, e, &r[e * nb]);
     alpha_volume(p, &T, e, &x[e * nb], &r[e * nb], NULL);
+    nl_volume(p, &T, e, &x[e * nb], &r[e * nb], jacobian_apply);
     for (int f = 0; f < 2 * d && !st; f++) {
       int dir = f / 2, hi = f % 2;
       int jx[MAXD];
@@ -608,11 +641,19 @@ static void jacobian_volume(const pdgo_problem *p, const tables *T, long e,
       velocity(p, xg, b);
     }
     double factor = T->vw[q] * detJ;
+    /* nonlinear part at the linearization point (jacobian_volume of
+       nonlinearconvectiondiffusiondg.hh:178-223) */
+    double qp = 0.0;
+    if (!(co && co->active) && p->nl_deg > 0 && p->xlin) {
+      double u = 0.0;
+      for (int i = 0; i < nb; i++) u += p->xlin[e * nb + i] * phi[i];
+      qp = nl_qprime(p, u);
+    }
     for (int jj = 0; jj < nb; jj++)
       for (int i = 0; i < nb; i++) {
         double ag = 0.0, bg = 0.0;
         for (int j = 0; j < d; j++) { ag += Agradphi[jj][j] * gradphi[i][j]; bg += b[j] * gradphi[i][j]; }
-        mat[i * nb + jj] += (ag - phi[jj] * bg + cc * phi[jj] * phi[i]) * factor;
+        mat[i * nb + jj] += (ag - phi[jj] * bg + (cc + qp) * phi[jj] * phi[i]) * factor;
       }
   }
 }
@@ -1346,6 +1387,120 @@ int pdgo_solve_linear_problem_prec(const pdgo_problem *p, int solver, int op,
 out:
   free(r); free(z); free(ablocks); free(diag); free(lu); free(piv);
   res->status = st;
+  return st;
+}
+
+/* NewtonMethod::apply (solver/newton.hh:177-335) restated. */
+int pdgo_newton(pdgo_problem *p, int solver, const pdgo_prec_config *pc,
+                const pdgo_newton_opts *o, double *x, pdgo_newton_result *res) {
+  const long n = pdgo_ndof(p), nc = pdgo_ncell(p);
+  const int nb = pdgo_nbasis(p);
+  memset(res, 0, sizeof(*res));
+  double *r = calloc(n, sizeof(double)), *z = calloc(n, sizeof(double));
+  double *xprev = calloc(n, sizeof(double)), *xl = calloc(n, sizeof(double));
+  double *diag = NULL, *lu = NULL, *ablocks = NULL;
+  int *piv = NULL;
+  int st = PDGO_OK, prec_ready = 0;
+  double defect = 0.0;
+  const double *saved = p->xlin;
+#define UPDATE_DEFECT()                                   \
+  do {                                                    \
+    memset(r, 0, sizeof(double) * n);                     \
+    st = pdgo_residual(p, x, r);                          \
+    defect = sqrt(dot(n, r, r));                          \
+  } while (0)
+  UPDATE_DEFECT();
+  if (st) goto out;
+  res->first_defect = defect;
+  double prev = defect;
+  for (;;) {
+    if (!(o->force_iteration && res->iterations == 0)) {
+      res->converged = defect < o->absolute_limit || defect < res->first_defect * o->reduction;
+      if (res->converged) break;
+      if (res->iterations >= o->max_iterations) { st = PDGO_ENOTCONV; goto out; }
+    }
+    if (!isfinite(defect)) { st = PDGO_ENOTCONV; goto out; }
+    double linred = o->min_linear_reduction;
+    if (!o->fixed_linear_reduction &&
+        !(res->iterations == 0 && res->first_defect < o->absolute_limit)) {
+      double stop = fmax(res->first_defect * o->reduction, o->absolute_limit);
+      linred = fmax(stop / (10 * defect), fmin(o->min_linear_reduction, defect * defect / (prev * prev)));
+    }
+    prev = defect;
+    memcpy(xl, x, sizeof(double) * n);
+    p->xlin = xl;
+    if (!prec_ready) {
+      diag = malloc(sizeof(double) * nc * nb * nb);
+      st = pdgo_block_diagonal(p, diag);
+      if (st) goto out;
+      const int base = pc->kind & 15;
+      if (base == 1 || base == 2) {
+        lu = malloc(sizeof(double) * nc * nb * nb);
+        piv = malloc(sizeof(int) * nc * nb);
+        memcpy(lu, diag, sizeof(double) * nc * nb * nb);
+        st = pdgo_lu_factor(nb, nc, lu, piv);
+        if (st) goto out;
+      }
+      if (pc->kind & 16) {
+        ablocks = malloc(sizeof(double) * nc * (2 * p->dim + 1) * nb * nb);
+        st = pdgo_assemble_jacobian(p, ablocks);
+        if (st) goto out;
+      }
+      prec_ready = 1;
+    }
+    memset(z, 0, sizeof(double) * n);
+    {
+      opctx oc = {p, 0, NULL, lu, piv, n, nb, pc, diag, ablocks, 0};
+      pdgo_result lr;
+      int ls = solver == 0 ? cg_run(&oc, z, r, linred, o->linear_maxit, &lr)
+                           : bicgstab_run(&oc, z, r, linred, o->linear_maxit, &lr);
+      res->linear_iterations += lr.iterations;
+      if (ls != PDGO_OK) { st = ls; goto out; }
+    }
+    if (!o->line_search || defect < o->absolute_limit) {
+      for (long i = 0; i < n; i++) x[i] -= z[i];
+      UPDATE_DEFECT();
+      if (st) goto out;
+    } else {
+      double lambda = 1.0, best_lambda = 0.0, best = defect, previous = defect;
+      int ok = 0;
+      memcpy(xprev, x, sizeof(double) * n);
+      for (int it = 0; it < o->line_search_max_iterations; it++) {
+        for (long i = 0; i < n; i++) x[i] -= lambda * z[i];
+        UPDATE_DEFECT();
+        if (st) goto out;
+        if (defect <= (1.0 - lambda / 4) * previous) { ok = 1; break; }
+        if (defect < best) { best = defect; best_lambda = lambda; }
+        lambda *= o->line_search_damping;
+        memcpy(x, xprev, sizeof(double) * n);
+      }
+      if (!ok) {
+        if (!o->line_search_accept_best || best_lambda == 0.0) {
+          memcpy(x, xprev, sizeof(double) * n);
+          UPDATE_DEFECT();
+          st = PDGO_ENOTCONV;
+          goto out;
+        }
+        if (best_lambda != lambda) {
+          memcpy(x, xprev, sizeof(double) * n);
+          for (long i = 0; i < n; i++) x[i] -= best_lambda * z[i];
+          UPDATE_DEFECT();
+          if (st) goto out;
+        }
+      }
+    }
+    res->iterations++;
+    res->defect = defect;
+    res->reduction = defect / res->first_defect;
+    res->conv_rate = pow(res->reduction, 1.0 / res->iterations);
+  }
+#undef UPDATE_DEFECT
+out:
+  res->defect = defect;
+  if (res->first_defect > 0) res->reduction = defect / res->first_defect;
+  res->status = st;
+  p->xlin = saved;
+  free(r); free(z); free(xprev); free(xl); free(diag); free(lu); free(piv); free(ablocks);
   return st;
 }
 

@@ -46,7 +46,8 @@ enum { PDGO_WEIGHTS_ON = 0, PDGO_WEIGHTS_OFF = 1 };
 
 /* status codes */
 enum { PDGO_OK = 0, PDGO_EARG = 1, PDGO_EOUTFLOW_ON_INFLOW = 2,
-       PDGO_EBREAKDOWN = 3, PDGO_ESINGULAR = 4 };
+       PDGO_EBREAKDOWN = 3, PDGO_ESINGULAR = 4,
+       PDGO_ENOTCONV = 5 /* Newton: iteration cap, line search or non-finite defect */ };
 
 typedef struct pdgo_problem {
   int dim;            /* 2 or 3 */
@@ -67,6 +68,13 @@ typedef struct pdgo_problem {
   const double *gq;   /* Dirichlet g at boundary quadrature points */
   const double *jq;   /* Neumann flux j at boundary quadrature points */
   const double *oq;   /* outflow flux o at boundary quadrature points */
+  /* NonlinearConvectionDiffusionDG (test/localoperator/
+     nonlinearconvectiondiffusiondg.hh): volume term int q(u) psi,
+     q(u) = sum_m nl_coef[m] u^m (nl_deg 0 = none); Jacobian applies and
+     assembled blocks are taken at the linearization point xlin. */
+  int nl_deg;
+  double nl_coef[5];
+  const double *xlin;
 } pdgo_problem;
 
 typedef struct pdgo_result {
@@ -172,6 +180,29 @@ int pdgo_prec_apply_cfg(const pdgo_problem *p, const pdgo_prec_config *pc, const
 int pdgo_solve_linear_problem_prec(const pdgo_problem *p, int solver, int op,
                                    const pdgo_prec_config *pc, double *x, double reduction,
                                    double min_defect, int maxit, pdgo_result *res);
+
+/* NewtonMethod (solver/newton.hh) with DefaultTerminate and the
+   Hackbusch-Reusken line search; linear solves by CG (solver 0) or BiCGStab
+   (1) with the configured preconditioner, set up at the first
+   linearization point and kept.  p->xlin is set during the solve. */
+typedef struct pdgo_newton_opts {
+  double reduction, absolute_limit;
+  int max_iterations, force_iteration;
+  double min_linear_reduction;
+  int fixed_linear_reduction;
+  int line_search, line_search_max_iterations;
+  double line_search_damping;
+  int line_search_accept_best;
+  int linear_maxit;
+} pdgo_newton_opts;
+typedef struct pdgo_newton_result {
+  int converged, iterations;
+  double first_defect, defect, reduction, conv_rate;
+  int linear_iterations;
+  int status;
+} pdgo_newton_result;
+int pdgo_newton(pdgo_problem *p, int solver, const pdgo_prec_config *pc,
+                const pdgo_newton_opts *o, double *x, pdgo_newton_result *res);
 
 /* Evaluate u_h at an m-point tensor Gauss rule in every cell:
    xyz [ncell][m^d][dim], w [ncell][m^d] (weights times |J|),

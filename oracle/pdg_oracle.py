@@ -30,7 +30,37 @@ class _Problem(C.Structure):
         ("alpha", C.c_double), ("bctype", C.c_int * 6),
         ("K", _dp), ("c", _dp), ("nmodes", C.c_int), ("modes", _dp),
         ("fq", _dp), ("fc", _dp), ("gq", _dp), ("jq", _dp), ("oq", _dp),
+        ("nl_deg", C.c_int), ("nl_coef", C.c_double * 5), ("xlin", _dp),
     ]
+
+
+class NewtonOpts(C.Structure):
+    _fields_ = [
+        ("reduction", C.c_double), ("absolute_limit", C.c_double),
+        ("max_iterations", C.c_int), ("force_iteration", C.c_int),
+        ("min_linear_reduction", C.c_double), ("fixed_linear_reduction", C.c_int),
+        ("line_search", C.c_int), ("line_search_max_iterations", C.c_int),
+        ("line_search_damping", C.c_double), ("line_search_accept_best", C.c_int),
+        ("linear_maxit", C.c_int),
+    ]
+
+
+class NewtonResult(C.Structure):
+    _fields_ = [
+        ("converged", C.c_int), ("iterations", C.c_int),
+        ("first_defect", C.c_double), ("defect", C.c_double),
+        ("reduction", C.c_double), ("conv_rate", C.c_double),
+        ("linear_iterations", C.c_int), ("status", C.c_int),
+    ]
+
+
+def newton_opts(**kw):
+    """NewtonMethod defaults (solver/newton.hh:654-669, terminate.hh:74-75,
+    linesearch.hh:206-208)."""
+    o = NewtonOpts(1e-8, 1e-12, 40, 0, 1e-3, 0, 1, 10, 0.5, 0, 5000)
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
 
 
 class Result(C.Structure):
@@ -104,6 +134,8 @@ def lib():
                                               C.c_int, C.c_int, C.c_double, _ip]),
             "pdgo_prec_apply_cfg": (C.c_int, [P, C.POINTER(PrecConfig), _dp, _dp, _ip, _dp,
                                               C.c_int, _dp, _dp, _ip]),
+            "pdgo_newton": (C.c_int, [P, C.c_int, C.POINTER(PrecConfig), C.POINTER(NewtonOpts),
+                                      _dp, C.POINTER(NewtonResult)]),
             "pdgo_solve_linear_problem_prec": (C.c_int, [P, C.c_int, C.c_int,
                                                          C.POINTER(PrecConfig), _dp, C.c_double,
                                                          C.c_double, C.c_int,
@@ -274,6 +306,26 @@ class Problem:
         st = lib().pdgo_solve_linear_problem(self.ref, 0 if solver == "cg" else 1, op,
                                              _ptr(x), reduction, min_defect, maxit,
                                              C.byref(res))
+        return x, res, st
+
+    def set_nonlinearity(self, coef):
+        """q(u) = sum_m coef[m] u^m (coef None removes it)."""
+        if coef is None:
+            self.s.nl_deg = 0
+            return
+        self.s.nl_deg = len(coef) - 1
+        for m in range(5):
+            self.s.nl_coef[m] = coef[m] if m < len(coef) else 0.0
+
+    def set_linearization_point(self, x):
+        self._xlin = None if x is None else np.ascontiguousarray(x, dtype=np.float64).copy()
+        self.s.xlin = _ptr(self._xlin)
+
+    def newton(self, pc, x=None, solver="bicgstab", **kw):
+        x = np.zeros(self.ndof) if x is None else x
+        res = NewtonResult()
+        st = lib().pdgo_newton(self.ref, 0 if solver == "cg" else 1, C.byref(pc),
+                               C.byref(newton_opts(**kw)), _ptr(x), C.byref(res))
         return x, res, st
 
     def prec_apply_cfg(self, pc, d, transpose=False):

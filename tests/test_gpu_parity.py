@@ -100,6 +100,31 @@ def test_jacobian_apply_f32(pdg, oracle, dim, k, n):
     assert _rel(yt.cpu().double().numpy(), P.jacobian_apply(x)) <= TOL32
 
 
+@pytest.mark.parametrize("k,nc,method,weights,react,bct", [
+    (1, (7, 6, 5), 1, 0, True, None),
+    (2, (9, 5, 4), 1, 0, True, [1, -1, 1, -2, -1, 1]),
+    (3, (11, 4, 3), 0, 1, False, None),
+    (4, (5, 4, 3), 2, 0, True, [-1, 1, 1, 1, -2, 1]),
+    (2, (1, 1, 1), 1, 0, False, None),
+    (2, (43, 1, 2), 1, 0, True, None),
+])
+def test_jacobian_apply_f32_staged(pdg, oracle, k, nc, method, weights, react, bct):
+    # the 3D FP32 kernel stages runs of CPB consecutive cells and their y/z
+    # neighbour runs: grids larger than one run, runs that cross rows and
+    # planes, every boundary type, reaction, all methods
+    import torch
+    go, P, rng = _pair(pdg, oracle, 3, k, nc, seed=31 + k, method=method, weights=weights,
+                       bctype=bct, react=react)
+    x = rng.uniform(-1, 1, go.ndof)
+    y0 = rng.uniform(-1, 1, go.ndof)
+    xt = torch.tensor(x, dtype=torch.float32, device="cuda")
+    yt = torch.tensor(y0, dtype=torch.float32, device="cuda")
+    go.jacobian_apply_f32(xt, yt)     # accumulates: y0 + J x
+    torch.cuda.synchronize()
+    ref = P.jacobian_apply(x, y0.copy())
+    assert _rel(yt.cpu().double().numpy(), ref) <= TOL32
+
+
 def test_device_pointers_match_host(pdg, oracle):
     import torch
     go, P, rng = _pair(pdg, oracle, 3, 3, 3, seed=4)
@@ -112,7 +137,8 @@ def test_device_pointers_match_host(pdg, oracle):
     assert np.array_equal(yt.cpu().numpy(), y)
 
 
-@pytest.mark.parametrize("dim,k,n", [(2, 1, 8), (2, 3, 4), (3, 2, 3), (3, 3, 2)])
+@pytest.mark.parametrize("dim,k,n", [(2, 1, 8), (2, 3, 4), (2, 4, 3), (3, 2, 3), (3, 3, 2),
+                                     (3, 4, 2)])
 def test_residual_with_data(pdg, oracle, dim, k, n):
     go, P, rng = _pair(pdg, oracle, dim, k, n, seed=8, react=True)
     fq = rng.standard_normal((go.ncell, go.nq_volume))
@@ -240,8 +266,10 @@ def test_bicgstab_nonsymmetric_dense(pdg, oracle):
     assert _rel(u, uref) <= 1e-8
 
 
-def test_grad_logK_matches_oracle(pdg, oracle):
-    go, P, rng = _pair(pdg, oracle, 3, 2, 3, seed=31)
+@pytest.mark.parametrize("dim,k,n", [(2, 1, 5), (2, 4, 3), (3, 1, 3), (3, 2, 3), (3, 3, 2),
+                                     (3, 4, 2)])
+def test_grad_logK_matches_oracle(pdg, oracle, dim, k, n):
+    go, P, rng = _pair(pdg, oracle, dim, k, n, seed=31)
     g = rng.standard_normal(go.nq_boundary)
     go.set_boundary_data(g=g)
     P.set(gq=g)

@@ -175,3 +175,30 @@ def test_block_sor_and_iterative_jacobi_oracle(oracle):
     vex = np.linalg.solve(Dm, d)
     assert np.max(np.abs(vi - vex)) <= 1e-4 * np.max(np.abs(vex))
     assert its.min() >= 1 and its.max() <= 100
+
+
+def test_nonlinear_reference_problem_oracle(oracle):
+    """matrix_free_nonlinear.cc:386-405: Newton on q(u) = 2 u^2, g = |x|^2
+    (2D Q1 16^2, SIPG, weightsOn, alpha 3) reaches L2 error^2 < 1e-6; the
+    oracle's nonlinear Jacobian matches central differences of its residual."""
+    import numpy as np
+    n = 16
+    P = oracle.Problem(2, 1, (n, n), alpha=3.0)
+    P.set_nonlinearity([0.0, 0.0, 2.0])
+    xv = P.volume_points().reshape(-1, 2)
+    g = (xv ** 2).sum(1)
+    xb = P.boundary_points().reshape(-1, 2)
+    P.set(fq=-4.0 + 2.0 * g * g, gq=(xb ** 2).sum(1))
+    rng = np.random.default_rng(0)
+    x = rng.uniform(0, 1, P.ndof)
+    z = rng.uniform(-1, 1, P.ndof)
+    P.set_linearization_point(x)
+    Jz = P.jacobian_apply(z)
+    eps = 1e-6
+    fd = (P.residual(x + eps * z) - P.residual(x - eps * z)) / (2 * eps)
+    assert np.max(np.abs(Jz - fd)) <= 1e-8 * np.max(np.abs(fd))
+    P.set_linearization_point(None)
+    u, res, st = P.newton(oracle.prec_config(2), solver="bicgstab")
+    assert st == 0 and res.converged and res.iterations <= 6
+    xyz, w, val = P.eval_points(u, 6)
+    assert float((w * (val - (xyz ** 2).sum(-1)) ** 2).sum()) < 1e-6
