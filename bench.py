@@ -442,6 +442,10 @@ def prec_metrics(pdg, np, torch, stream):
     go.set_source(fc=np.ones(go.ncell))
     out = {"workload": "sipg3d_q2_64^3 (7.08M DoF), BiCGStab, reduction 1e-10",
            "sor_hyperplane_steps": 3 * n - 2}
+    # block-solver options of the reference's matrix-free test
+    # (matrix_free_linear.ini: block_inverse_solver reduction 1e-14, maxiter 100)
+    go.set_prec_options(block_reduction=1e-14, block_maxit=100)
+    out["block_solver"] = {"reduction": 1e-14, "maxit": 100}
     d = torch.rand(go.ndof, dtype=torch.float64, device=dev)
     v = torch.zeros_like(d)
     kinds = (("bj_fdm", pdg.PREC_BJ_FDM), ("bj_dense", pdg.PREC_BJ_DENSE),

@@ -625,6 +625,7 @@ __global__ void k_perm(long n, const double *__restrict__ src, int is_log,
 static void invalidate(pdg_context *ctx, bool operator_changed) {
   ctx->r0_valid = 0;
   if (operator_changed) {
+    ctx->op_gen++;
     ctx->rec_valid = 0;
     ctx->rec32_valid = 0;
     ctx->A_valid = 0;
@@ -683,6 +684,7 @@ int pdg_set_prec_options(pdg_context *ctx, const pdg_prec_options *o) {
   if (!(o->block_reduction > 0.0) || o->block_maxit < 1)
     return set_error(PDG_EINVAL, "bad block solver options");
   ctx->popt = *o;
+  ctx->op_gen++;
   return PDG_OK;
 }
 

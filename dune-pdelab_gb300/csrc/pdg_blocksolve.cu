@@ -277,24 +277,27 @@ int sor_setup(pdg_context *ctx) {
 void sor_free(pdg_context *ctx) {
   if (ctx->hp_cells) cudaFree(ctx->hp_cells);
   delete[] ctx->hp_off;
-  if (ctx->sor_a64) cudaFree(ctx->sor_a64);
-  if (ctx->sor_a32) cudaFree(ctx->sor_a32);
+  void *bufs[] = {ctx->sor_a64, ctx->sor_d64, ctx->sor_v64,
+                  ctx->sor_a32, ctx->sor_d32, ctx->sor_v32};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  for (int i = 0; i < 8; i++) {
+    cudaGraphExec_t &g = (&ctx->sor_graph[0][0][0])[i];
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
   ctx->hp_cells = nullptr;
   ctx->hp_off = nullptr;
-  ctx->sor_a64 = nullptr;
-  ctx->sor_a32 = nullptr;
+  ctx->sor_a64 = ctx->sor_d64 = ctx->sor_v64 = nullptr;
+  ctx->sor_a32 = ctx->sor_d32 = ctx->sor_v32 = nullptr;
   ctx->hp_n = 0;
 }
 
+// the sweep body on the given buffers: v = 0, then per hyperplane
+// a = d - (J v) on its cells and v = omega D^{-1} a there
 template <typename T>
-int sor_apply(pdg_context *ctx, const T *d, T *v, int transpose, const int *skip) {
-  PDG_TRY(sor_setup(ctx));
+static int sor_sweep(pdg_context *ctx, const T *d, T *v, T *a, int transpose, const int *skip) {
   const bool dbl = std::is_same<T, double>::value;
-  T *&a = [&]() -> T *& {
-    if constexpr (std::is_same<T, double>::value) return ctx->sor_a64;
-    else return ctx->sor_a32;
-  }();
-  if (!a) PDG_CUDA_TRY(cudaMalloc(&a, sizeof(T) * ctx->ndof));
   const T *K = dbl ? (const T *)ctx->K64 : (const T *)ctx->K32;
   const T *c = dbl ? (const T *)ctx->c64 : (const T *)ctx->c32;
   const T *tab = dbl ? (const T *)ctx->tab64 : (const T *)ctx->tab32;
@@ -311,6 +314,51 @@ int sor_apply(pdg_context *ctx, const T *d, T *v, int transpose, const int *skip
     // v_e = omega D_e^{-1} a_e
     PDG_TRY(block_solve<T>(ctx, a, v, transpose, skip, cl, (int)cnt, omega));
   }
+  return PDG_OK;
+}
+
+// The 2(nx+ny+nz-2) launches of a sweep are latency bound, so the sweep is
+// captured once per operator / preconditioner generation as a CUDA graph on
+// fixed input/output buffers and replayed: d is copied in, v copied out.
+// The first sweep of a generation runs eagerly (it builds any lazily
+// created per-cell records outside the capture).
+template <typename T>
+int sor_apply(pdg_context *ctx, const T *d, T *v, int transpose, const int *skip) {
+  PDG_TRY(sor_setup(ctx));
+  const int pi = std::is_same<T, double>::value ? 0 : 1;
+  T *&a = *reinterpret_cast<T **>(pi == 0 ? (void *)&ctx->sor_a64 : (void *)&ctx->sor_a32);
+  T *&D = *reinterpret_cast<T **>(pi == 0 ? (void *)&ctx->sor_d64 : (void *)&ctx->sor_d32);
+  T *&V = *reinterpret_cast<T **>(pi == 0 ? (void *)&ctx->sor_v64 : (void *)&ctx->sor_v32);
+  for (T **b : {&a, &D, &V})
+    if (!*b) PDG_CUDA_TRY(cudaMalloc(b, sizeof(T) * ctx->ndof));
+  const int tr = transpose ? 1 : 0, sk = skip ? 1 : 0;
+  cudaGraphExec_t &g = ctx->sor_graph[pi][tr][sk];
+  unsigned &gen = ctx->sor_graph_gen[pi][tr][sk];
+  if (!g || gen != ctx->op_gen) {
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+    // eager sweep (also the result of this call)
+    PDG_TRY(sor_sweep<T>(ctx, d, v, a, transpose, skip));
+    cudaGraph_t graph = nullptr;
+    PDG_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const int st = sor_sweep<T>(ctx, D, V, a, transpose, skip);
+    const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+    if (st != PDG_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return st;
+    }
+    PDG_CUDA_TRY(ce);
+    const cudaError_t ie = cudaGraphInstantiate(&g, graph, 0);
+    cudaGraphDestroy(graph);
+    PDG_CUDA_TRY(ie);
+    gen = ctx->op_gen;
+    return PDG_OK;
+  }
+  PDG_CUDA_TRY(cudaMemcpyAsync(D, d, sizeof(T) * ctx->ndof, cudaMemcpyDeviceToDevice, ctx->stream));
+  PDG_CUDA_TRY(cudaGraphLaunch(g, ctx->stream));
+  PDG_CUDA_TRY(cudaMemcpyAsync(v, V, sizeof(T) * ctx->ndof, cudaMemcpyDeviceToDevice, ctx->stream));
   return PDG_OK;
 }
 

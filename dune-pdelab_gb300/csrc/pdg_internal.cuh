@@ -170,8 +170,13 @@ struct pdg_context {
   int *hp_cells;
   long *hp_off;
   int hp_n;
-  double *sor_a64;
-  float *sor_a32;
+  double *sor_a64, *sor_d64, *sor_v64;
+  float *sor_a32, *sor_d32, *sor_v32;
+  // the sweep captured as a CUDA graph on fixed buffers, per
+  // [precision][transpose][with skip flag], valid for generation op_gen
+  cudaGraphExec_t sor_graph[2][2][2];
+  unsigned sor_graph_gen[2][2][2];
+  unsigned op_gen;         // bumped whenever the operator or a preconditioner changes
   double *r0K;             // K-proportional Dirichlet-data part of R(0)
 
   // reduction scratch (deterministic two-stage reductions)

@@ -534,6 +534,7 @@ int prec_setup_impl(pdg_context *ctx, int kind, int precision) {
   if (precision != PDG_F64 && precision != PDG_F32)
     return set_error(PDG_EINVAL, "precision must be PDG_F64 or PDG_F32");
   prec_free(ctx, precision);
+  ctx->op_gen++;
   if (kind == PDG_PREC_NONE) {
     ctx->prec[precision].kind = kind;
     ctx->prec[precision].ready = 1;

@@ -136,6 +136,32 @@ def test_adjoint_solve_with_sor(pdg, oracle):
     assert _rel(P.blocks_apply(A, lam, transpose=True), rhs) <= 1e-9
 
 
+def test_sor_graph_replay(pdg, oracle):
+    # the first sweep of a generation runs eagerly and captures a CUDA graph;
+    # later sweeps replay it; a coefficient change starts a new generation
+    go, P, rng = _pair(pdg, oracle, 3, 2, (4, 3, 3), seed=31)
+    prec = pdg.GridOperatorPreconditioner(go, kind=16 | 2)
+    prec.pre()
+    pc = oracle.prec_config(16 | 2)
+    for rep in range(3):
+        d = rng.uniform(-1, 1, go.ndof)
+        v = np.zeros(go.ndof)
+        prec.apply(v, d)
+        vref, _ = P.prec_apply_cfg(pc, d)
+        assert _rel(v, vref) <= 1e-9, rep
+    K2 = np.exp(rng.standard_normal(go.ncell))
+    go.set_permeability(K2)
+    P.set(K=K2)
+    prec = pdg.GridOperatorPreconditioner(go, kind=16 | 2)
+    prec.pre()
+    for rep in range(2):
+        d = rng.uniform(-1, 1, go.ndof)
+        v = np.zeros(go.ndof)
+        prec.apply(v, d)
+        vref, _ = P.prec_apply_cfg(pc, d)
+        assert _rel(v, vref) <= 1e-9, rep
+
+
 def test_prec_options_validation(pdg):
     go = pdg.GridOperator(3, 1, (2, 2, 2))
     with pytest.raises(pdg.PDGError):
