@@ -816,7 +816,8 @@ int pdg_destroy(pdg_context *c) {
                   c->jq, c->oq, c->r0, c->r0K, c->red_partials, c->red_out, c->d_flag,
                   c->stage_a, c->stage_b, c->rec64, c->conv64, c->conv32, c->convtab64,
                   c->convtab32, c->gm_V32, c->gm_V64, c->gm_F64, c->gm_partial, c->gm_coef,
-                  c->A64, c->rec32, c->nlW64, c->nlW32, c->nlB64, c->nlB32};
+                  c->A64, c->rec32, c->nlW64, c->nlW32, c->nlB64, c->nlB32,
+                  c->massW, c->massWi, c->massB, c->massBiT, c->cstage64, c->cstage32};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 10; i++)
@@ -1285,6 +1286,255 @@ int pdg_newton_solve(pdg_context *ctx, const pdg_newton_options *opt,
   for (auto &b : buf) cudaFree(b);
   const int so = stage_out<double>(ctx, su);
   return st != PDG_OK ? st : so;
+}
+
+int pdg_mass_apply(pdg_context *ctx, const double *x, double *y) {
+  PDG_CHECK_CTX(ctx);
+  if (!x || !y) return set_error(PDG_EINVAL, "null vector");
+  PDG_TRY(ensure_stage(ctx));
+  Staged<double> sx, sy;
+  PDG_TRY(stage_in<double>(ctx, x, ctx->ndof, ctx->stage_a, true, &sx));
+  PDG_TRY(stage_in<double>(ctx, y, ctx->ndof, ctx->stage_b, false, &sy));
+  PDG_TRY(mass_apply(ctx, sx.dev, sy.dev, 1.0, 0, 0));
+  PDG_TRY(stage_out<double>(ctx, sy));
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return PDG_OK;
+}
+
+// Tables of instationary/onestepparameter.hh (the published schemes:
+// theta method, Alexander's SDIRK 2 and 3, the fractional-step theta scheme,
+// Heun, Shu's SSP RK3, classical RK4), row r-1 = stage r.
+int pdg_onestep_table(int method, double theta, int *stages, double *A, double *B, double *D) {
+  if (!stages || !A || !B || !D) return set_error(PDG_EINVAL, "null argument");
+  double a[4][5] = {}, b[4][5] = {}, d[5] = {};
+  int s = 0;
+  switch (method) {
+    case PDG_ONESTEP_IMPLICIT_EULER: theta = 1.0; [[fallthrough]];
+    case PDG_ONESTEP_EXPLICIT_EULER:
+      if (method == PDG_ONESTEP_EXPLICIT_EULER) theta = 0.0;
+      [[fallthrough]];
+    case PDG_ONESTEP_THETA:
+      s = 1;
+      d[0] = 0.0; d[1] = 1.0;
+      a[0][0] = -1.0; a[0][1] = 1.0;
+      b[0][0] = 1.0 - theta; b[0][1] = theta;
+      break;
+    case PDG_ONESTEP_ALEXANDER2: {
+      const double al = 1.0 - 0.5 * std::sqrt(2.0);
+      s = 2;
+      d[0] = 0.0; d[1] = al; d[2] = 1.0;
+      a[0][0] = -1.0; a[0][1] = 1.0;
+      a[1][0] = -1.0; a[1][2] = 1.0;
+      b[0][1] = al;
+      b[1][1] = 1.0 - al; b[1][2] = al;
+      break;
+    }
+    case PDG_ONESTEP_ALEXANDER3: {
+      // alpha: root of alpha^3 - 3 alpha^2 + 1.5 alpha - 1/6 = 0 near 0.4359 (Newton)
+      double al = 0.4358665215;
+      for (int i = 0; i < 10; i++)
+        al = al - (al * (al * al - 3.0 * (al - 0.5)) - 1.0 / 6.0) / (3.0 * al * (al - 2.0) + 1.5);
+      const double tau2 = (1.0 + al) * 0.5;
+      const double b1 = -(6.0 * al * al - 16.0 * al + 1.0) * 0.25;
+      const double b2 = (6 * al * al - 20.0 * al + 5.0) * 0.25;
+      s = 3;
+      d[0] = 0.0; d[1] = al; d[2] = tau2; d[3] = 1.0;
+      a[0][0] = -1.0; a[0][1] = 1.0;
+      a[1][0] = -1.0; a[1][2] = 1.0;
+      a[2][0] = -1.0; a[2][3] = 1.0;
+      b[0][1] = al;
+      b[1][1] = tau2 - al; b[1][2] = al;
+      b[2][1] = b1; b[2][2] = b2; b[2][3] = al;
+      break;
+    }
+    case PDG_ONESTEP_FRACTIONAL_STEP: {
+      const double th = 1.0 - 0.5 * std::sqrt(2.0), thp = 1.0 - 2.0 * th;
+      const double al = 2.0 - std::sqrt(2.0), be = 1.0 - al;
+      s = 3;
+      d[0] = 0.0; d[1] = th; d[2] = 1.0 - th; d[3] = 1.0;
+      a[0][0] = -1.0; a[0][1] = 1.0;
+      a[1][1] = -1.0; a[1][2] = 1.0;
+      a[2][2] = -1.0; a[2][3] = 1.0;
+      b[0][0] = be * th; b[0][1] = al * th;
+      b[1][1] = al * thp; b[1][2] = al * th;
+      b[2][2] = be * th; b[2][3] = al * th;
+      break;
+    }
+    case PDG_ONESTEP_HEUN:
+      s = 2;
+      d[0] = 0.0; d[1] = 1.0; d[2] = 1.0;
+      a[0][0] = -1.0; a[0][1] = 1.0;
+      a[1][0] = -0.5; a[1][1] = -0.5; a[1][2] = 1.0;
+      b[0][0] = 1.0;
+      b[1][1] = 0.5;
+      break;
+    case PDG_ONESTEP_SHU3:
+      s = 3;
+      d[0] = 0.0; d[1] = 1.0; d[2] = 0.5; d[3] = 1.0;
+      a[0][0] = -1.0; a[0][1] = 1.0;
+      a[1][0] = -0.75; a[1][1] = -0.25; a[1][2] = 1.0;
+      a[2][0] = -1.0 / 3.0; a[2][2] = -2.0 / 3.0; a[2][3] = 1.0;
+      b[0][0] = 1.0;
+      b[1][1] = 0.25;
+      b[2][2] = 2.0 / 3.0;
+      break;
+    case PDG_ONESTEP_RK4:
+      s = 4;
+      d[0] = 0.0; d[1] = 0.5; d[2] = 0.5; d[3] = 1.0; d[4] = 1.0;
+      for (int r = 0; r < 4; r++) { a[r][0] = -1.0; a[r][r + 1] = 1.0; }
+      b[0][0] = 0.5;
+      b[1][1] = 0.5;
+      b[2][2] = 1.0;
+      b[3][0] = 1.0 / 6.0; b[3][1] = 1.0 / 3.0; b[3][2] = 1.0 / 3.0; b[3][3] = 1.0 / 6.0;
+      break;
+    default:
+      return set_error(PDG_EINVAL, "unknown one-step method");
+  }
+  *stages = s;
+  for (int r = 0; r < s; r++)
+    for (int i = 0; i <= s; i++) {
+      A[r * (s + 1) + i] = a[r][i];
+      B[r * (s + 1) + i] = b[r][i];
+    }
+  for (int i = 0; i <= s; i++) D[i] = d[i];
+  return PDG_OK;
+}
+
+__global__ void k_shift_c(long n, const double *c, double sigma, double *c64, float *c32) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = (c ? c[i] : 0.0) + sigma;
+  c64[i] = v;
+  c32[i] = (float)v;
+}
+
+// Use J + sigma M as the operator: reaction c -> c + sigma (the mass term
+// int u psi is the reaction term with unit coefficient).  sigma = 0 with
+// `restore` puts the original coefficient back.
+static int set_mass_shift(pdg_context *ctx, double sigma, bool restore, double *c_orig64,
+                          float *c_orig32) {
+  if (restore) {
+    ctx->c64 = c_orig64;
+    ctx->c32 = c_orig32;
+    ctx->mass_shift = 0.0;
+    invalidate(ctx, true);
+    return PDG_OK;
+  }
+  if (!ctx->cstage64) {
+    PDG_CUDA_TRY(cudaMalloc(&ctx->cstage64, sizeof(double) * ctx->ncell));
+    PDG_CUDA_TRY(cudaMalloc(&ctx->cstage32, sizeof(float) * ctx->ncell));
+  }
+  k_shift_c<<<(unsigned)((ctx->ncell + 255) / 256), 256, 0, ctx->stream>>>(
+      ctx->ncell, c_orig64, sigma, ctx->cstage64, ctx->cstage32);
+  PDG_CUDA_TRY(cudaGetLastError());
+  ctx->c64 = ctx->cstage64;
+  ctx->c32 = ctx->cstage32;
+  ctx->mass_shift = sigma;
+  invalidate(ctx, true);
+  return PDG_OK;
+}
+
+static int onestep_run(pdg_context *ctx, int s, const double *A, const double *B, double dt,
+                       const pdg_solver_options *lin, const double *xold, double *xnew,
+                       pdg_onestep_result *res, std::vector<double *> &buf) {
+  const long n = ctx->ndof;
+  // buf: X[1..s-1] stage values, RX[0..s-1] = R(x_j), MX[0..s-1] = M x_j, C, r, z
+  double **X = buf.data();                 // X[0] unused (xold), X[s] = xnew
+  double **RX = X + s + 1, **MX = RX + s;
+  double *C = buf[3 * s + 1], *r = buf[3 * s + 2], *z = buf[3 * s + 3];
+  const double *x0 = xold;
+  auto xs = [&](int j) -> const double * { return j == 0 ? x0 : (j == s ? xnew : X[j]); };
+  // R(x) = (J + shift M) x - shift M x + R(0) with whatever shift is active
+  auto spatial_residual = [&](const double *x, double *out, double *mx) -> int {
+    PDG_TRY(mass_apply(ctx, x, mx, 1.0, 0, 0));
+    PDG_TRY(ensure_r0(ctx));
+    PDG_TRY(op_launch<double>(ctx, x, out, ctx->r0, 1.0, 0, 0, nullptr));
+    if (ctx->mass_shift != 0.0) PDG_TRY(vec_axpy(ctx, n, -ctx->mass_shift, mx, out));
+    return PDG_OK;
+  };
+  PDG_TRY(spatial_residual(x0, RX[0], MX[0]));
+  for (int rr = 1; rr <= s; rr++) {
+    const double *a = A + (rr - 1) * (s + 1), *b = B + (rr - 1) * (s + 1);
+    // constant part C = sum_{j<r} [b_rj dt R(x_j) + a_rj M x_j]
+    PDG_TRY(vec_fill<double>(ctx, n, C, 0.0));
+    for (int j = 0; j < rr; j++) {
+      if (b[j] != 0.0) PDG_TRY(vec_axpy(ctx, n, b[j] * dt, RX[j], C));
+      if (a[j] != 0.0) PDG_TRY(vec_axpy(ctx, n, a[j], MX[j], C));
+    }
+    double *xr = const_cast<double *>(xs(rr));
+    const double arr = a[rr], brr = b[rr];
+    if (brr == 0.0) {
+      // explicit stage: a_rr M x_r = -C
+      if (arr == 0.0) return set_error(PDG_EINVAL, "singular one-step stage");
+      PDG_TRY(mass_apply(ctx, C, xr, -1.0 / arr, 0, 1));
+    } else {
+      // implicit stage: (J + sigma M) x = -C/(b_rr dt) - R(0), sigma = a_rr/(b_rr dt);
+      // residual form from the previous stage value as initial guess
+      const double sigma = arr / (brr * dt);
+      if (sigma != ctx->mass_shift || !ctx->mass_shift_on) {
+        PDG_TRY(set_mass_shift(ctx, sigma, false, ctx->c_orig64, ctx->c_orig32));
+        ctx->mass_shift_on = 1;
+      }
+      PDG_TRY(vec_copy<double>(ctx, n, xs(rr - 1), xr));
+      PDG_TRY(ensure_r0(ctx));
+      PDG_TRY(op_launch<double>(ctx, xr, r, ctx->r0, 1.0, 0, 0, nullptr));
+      PDG_TRY(vec_axpy(ctx, n, 1.0 / (brr * dt), C, r));
+      PDG_TRY(vec_fill<double>(ctx, n, z, 0.0));
+      pdg_solver_result lr;
+      std::memset(&lr, 0, sizeof(lr));
+      const int st = solve_correction(ctx, lin, z, r, 0, &lr);
+      res->linear_solver_iterations += lr.iterations;
+      if (st != PDG_OK) return st;
+      PDG_TRY(vec_axpy(ctx, n, -1.0, z, xr));
+    }
+    if (rr < s) PDG_TRY(spatial_residual(xr, RX[rr], MX[rr]));
+  }
+  res->stages = s;
+  return PDG_OK;
+}
+
+int pdg_onestep_apply(pdg_context *ctx, int stages, const double *A, const double *B,
+                      const double *D, double dt, const pdg_solver_options *lin,
+                      const double *xold, double *xnew, pdg_onestep_result *res) {
+  PDG_CHECK_CTX(ctx);
+  if (!A || !B || !D || !lin || !xold || !xnew || !res)
+    return set_error(PDG_EINVAL, "null argument");
+  if (stages < 1 || stages > 4 || !(dt > 0)) return set_error(PDG_EINVAL, "bad stages or dt");
+  PDG_TRY(check_opts(lin));
+  if (ctx->nl_deg > 0)
+    return set_error(PDG_EUNSUPPORTED, "one-step methods with a nonlinear operator");
+  std::memset(res, 0, sizeof(*res));
+  PDG_TRY(ensure_stage(ctx));
+  PDG_TRY(ensure_work(ctx, lin->mixed != 0));
+  const long n = ctx->ndof;
+  Staged<double> so, sn;
+  PDG_TRY(stage_in<double>(ctx, xold, n, ctx->stage_a, true, &so));
+  PDG_TRY(stage_in<double>(ctx, xnew, n, ctx->stage_b, false, &sn));
+  std::vector<double *> buf(3 * stages + 4, nullptr);
+  for (auto &p : buf)
+    if (cudaMalloc(&p, sizeof(double) * n) != cudaSuccess) {
+      for (auto &q : buf)
+        if (q) cudaFree(q);
+      return set_error(PDG_ECUDA, "out of device memory for the stages");
+    }
+  ctx->c_orig64 = ctx->c64;
+  ctx->c_orig32 = ctx->c32;
+  ctx->mass_shift = 0.0;
+  ctx->mass_shift_on = 0;
+  cudaEventRecord(ctx->ev0, ctx->stream);
+  int st = onestep_run(ctx, stages, A, B, dt, lin, so.dev, sn.dev, res, buf);
+  cudaEventRecord(ctx->ev1, ctx->stream);
+  cudaEventSynchronize(ctx->ev1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  res->elapsed = ms * 1e-3;
+  if (ctx->mass_shift_on) set_mass_shift(ctx, 0.0, true, ctx->c_orig64, ctx->c_orig32);
+  ctx->mass_shift_on = 0;
+  for (auto &p : buf) cudaFree(p);
+  res->status = st;
+  if (st != PDG_OK) return st;
+  PDG_TRY(stage_out<double>(ctx, sn));
+  return PDG_OK;
 }
 
 int pdg_jacobian_assemble(pdg_context *ctx) {

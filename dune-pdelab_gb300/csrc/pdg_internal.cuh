@@ -155,6 +155,13 @@ struct pdg_context {
   double *nlW64, *nlB64;
   float *nlW32, *nlB32;
   int nl_point;            // weights valid for the current linearization point
+  // DG mass matrix (temporal operator): point weights, their inverses, B, B^{-T}
+  double *massW, *massWi, *massB, *massBiT;
+  // one-step stages: reaction shifted by sigma = a_rr / (b_rr dt)
+  double *cstage64, *c_orig64;
+  float *cstage32, *c_orig32;
+  double mass_shift;
+  int mass_shift_on;
   int nl_off;              // temporarily exclude the term (residual evaluation)
 
   // assembled Jacobian: [ncell][2d+1][nb][nb], column-major blocks
@@ -250,6 +257,9 @@ int nl_set_point(pdg_context *ctx, const double *x);
 int nl_residual(pdg_context *ctx, const double *x, double *r);
 template <typename T>
 int nl_apply(pdg_context *ctx, const ApplyArgs<T> &a);
+// y = (accumulate ? y : 0) + alpha M x, or M^{-1} x (block-diagonal DG mass)
+int mass_apply(pdg_context *ctx, const double *x, double *y, double alpha, int accumulate,
+               int inverse);
 
 // assembled Jacobian (probing the matrix-free operator) and its block product
 int assemble_jacobian(pdg_context *ctx);

@@ -14,7 +14,9 @@
 // as three (two) sum-factorised passes forward and back.  The term is
 // symmetric and cell-local, so it enters the transposed apply and the
 // diagonal blocks unchanged.
+#include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "pdg_internal.cuh"
 #include "pdg_vec.cuh"
@@ -309,35 +311,112 @@ int nl_residual(pdg_context *ctx, const double *x, double *r) {
 }
 
 template <typename T, int D, int N>
-static int nl_apply_dn(pdg_context *ctx, const ApplyArgs<T> &a) {
+static int weighted_apply_dn(pdg_context *ctx, const T *W, const T *B, const ApplyArgs<T> &a) {
   constexpr int TPC = D == 3 ? N * N : N;
   constexpr int CPB = 128 / TPC > 0 ? 128 / TPC : 1;
   const long work = a.cells ? a.ncells : ctx->ncell;
   if (work <= 0) return PDG_OK;
-  const bool dbl = std::is_same<T, double>::value;
-  const T *W = dbl ? (const T *)ctx->nlW64 : (const T *)ctx->nlW32;
-  const T *B = dbl ? (const T *)ctx->nlB64 : (const T *)ctx->nlB32;
   k_nl_apply<T, D, N><<<(unsigned)((work + CPB - 1) / CPB), 128, 0, ctx->stream>>>(
       ctx->ncell, W, B, a.x, a.y, a.alpha, a.cells, a.ncells, a.skip);
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
 }
 
+// y += alpha (X^T)^d diag(W) X^d x per cell, X an N x N table on the device
 template <typename T>
-int nl_apply(pdg_context *ctx, const ApplyArgs<T> &a) {
-  if (ctx->nl_deg <= 0 || !ctx->nl_point || ctx->nl_off) return PDG_OK;
+int weighted_apply(pdg_context *ctx, const T *W, const T *X, const ApplyArgs<T> &a) {
   switch (ctx->dim * 10 + ctx->k) {
-    case 21: return nl_apply_dn<T, 2, 2>(ctx, a);
-    case 22: return nl_apply_dn<T, 2, 3>(ctx, a);
-    case 23: return nl_apply_dn<T, 2, 4>(ctx, a);
-    case 24: return nl_apply_dn<T, 2, 5>(ctx, a);
-    case 31: return nl_apply_dn<T, 3, 2>(ctx, a);
-    case 32: return nl_apply_dn<T, 3, 3>(ctx, a);
-    case 33: return nl_apply_dn<T, 3, 4>(ctx, a);
-    case 34: return nl_apply_dn<T, 3, 5>(ctx, a);
+    case 21: return weighted_apply_dn<T, 2, 2>(ctx, W, X, a);
+    case 22: return weighted_apply_dn<T, 2, 3>(ctx, W, X, a);
+    case 23: return weighted_apply_dn<T, 2, 4>(ctx, W, X, a);
+    case 24: return weighted_apply_dn<T, 2, 5>(ctx, W, X, a);
+    case 31: return weighted_apply_dn<T, 3, 2>(ctx, W, X, a);
+    case 32: return weighted_apply_dn<T, 3, 3>(ctx, W, X, a);
+    case 33: return weighted_apply_dn<T, 3, 4>(ctx, W, X, a);
+    case 34: return weighted_apply_dn<T, 3, 5>(ctx, W, X, a);
     default: return set_error(PDG_EUNSUPPORTED, "dim/degree not compiled in");
   }
 }
+template int weighted_apply<double>(pdg_context *, const double *, const double *,
+                                    const ApplyArgs<double> &);
+
+// The DG mass matrix (the temporal operator of one-step methods, int u psi)
+// and its inverse per cell, both through the weighted tensor kernel:
+//   M = (B^T)^d diag(w |J|) B^d,   M^{-1} = (B^{-1})^d diag(1/(w |J|)) (B^{-T})^d,
+// B[q][a] = phi_a(xi_q) (square, invertible: k+1 Gauss points, k+1 nodes).
+static int ensure_mass(pdg_context *ctx) {
+  if (ctx->massW) return PDG_OK;
+  const RhsTables r = make_rhs_tables(ctx);
+  const int N = ctx->N, D = ctx->dim;
+  const int NB = D == 3 ? N * N * N : N * N;
+  double detJ = 1.0;
+  for (int j = 0; j < D; j++) detJ *= ctx->h[j];
+  std::vector<double> w(NB), wi(NB);
+  for (int q = 0; q < NB; q++) {
+    const int qx = q % N, qy = (q / N) % N, qz = D == 3 ? q / (N * N) : 0;
+    w[q] = r.w[qx] * r.w[qy] * (D == 3 ? r.w[qz] : 1.0) * detJ;
+    wi[q] = 1.0 / w[q];
+  }
+  // B^{-T}: invert B (Gauss-Jordan with partial pivoting, N <= 5), transpose
+  double a[kMaxN1][2 * kMaxN1];
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < 2 * N; j++) a[i][j] = j < N ? r.B[i * N + j] : (j - N == i ? 1.0 : 0.0);
+  for (int c = 0; c < N; c++) {
+    int p = c;
+    for (int i = c + 1; i < N; i++)
+      if (std::fabs(a[i][c]) > std::fabs(a[p][c])) p = i;
+    for (int j = 0; j < 2 * N; j++) std::swap(a[c][j], a[p][j]);
+    const double inv = 1.0 / a[c][c];
+    for (int j = 0; j < 2 * N; j++) a[c][j] *= inv;
+    for (int i = 0; i < N; i++)
+      if (i != c) {
+        const double f = a[i][c];
+        for (int j = 0; j < 2 * N; j++) a[i][j] -= f * a[c][j];
+      }
+  }
+  std::vector<double> BinvT(N * N), Bt(N * N);
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++) {
+      BinvT[i * N + j] = a[j][N + i];   // (B^{-1})^T
+      Bt[i * N + j] = r.B[i * N + j];
+    }
+  std::vector<double> W(ctx->ndof), Wi(ctx->ndof);
+  for (long e = 0; e < ctx->ncell; e++)
+    for (int q = 0; q < NB; q++) {
+      W[e * NB + q] = w[q];
+      Wi[e * NB + q] = wi[q];
+    }
+  PDG_CUDA_TRY(cudaMalloc(&ctx->massW, sizeof(double) * ctx->ndof));
+  PDG_CUDA_TRY(cudaMalloc(&ctx->massWi, sizeof(double) * ctx->ndof));
+  PDG_CUDA_TRY(cudaMalloc(&ctx->massB, sizeof(double) * N * N));
+  PDG_CUDA_TRY(cudaMalloc(&ctx->massBiT, sizeof(double) * N * N));
+  PDG_CUDA_TRY(cudaMemcpy(ctx->massW, W.data(), sizeof(double) * ctx->ndof, cudaMemcpyHostToDevice));
+  PDG_CUDA_TRY(cudaMemcpy(ctx->massWi, Wi.data(), sizeof(double) * ctx->ndof, cudaMemcpyHostToDevice));
+  PDG_CUDA_TRY(cudaMemcpy(ctx->massB, Bt.data(), sizeof(double) * N * N, cudaMemcpyHostToDevice));
+  PDG_CUDA_TRY(cudaMemcpy(ctx->massBiT, BinvT.data(), sizeof(double) * N * N, cudaMemcpyHostToDevice));
+  return PDG_OK;
+}
+
+// y = (accumulate ? y : 0) + alpha M x   (M^{-1} with `inverse`)
+int mass_apply(pdg_context *ctx, const double *x, double *y, double alpha, int accumulate,
+               int inverse) {
+  PDG_TRY(ensure_mass(ctx));
+  if (!accumulate) PDG_TRY(vec_fill<double>(ctx, ctx->ndof, y, 0.0));
+  ApplyArgs<double> a{x, y, nullptr, alpha, 1, 0, 0, nullptr};
+  return inverse ? weighted_apply<double>(ctx, ctx->massWi, ctx->massBiT, a)
+                 : weighted_apply<double>(ctx, ctx->massW, ctx->massB, a);
+}
+
+template <typename T>
+int nl_apply(pdg_context *ctx, const ApplyArgs<T> &a) {
+  if (ctx->nl_deg <= 0 || !ctx->nl_point || ctx->nl_off) return PDG_OK;
+  const bool dbl = std::is_same<T, double>::value;
+  const T *W = dbl ? (const T *)ctx->nlW64 : (const T *)ctx->nlW32;
+  const T *B = dbl ? (const T *)ctx->nlB64 : (const T *)ctx->nlB32;
+  return weighted_apply<T>(ctx, W, B, a);
+}
+template int weighted_apply<float>(pdg_context *, const float *, const float *,
+                                   const ApplyArgs<float> &);
 
 template int nl_apply<double>(pdg_context *, const ApplyArgs<double> &);
 template int nl_apply<float>(pdg_context *, const ApplyArgs<float> &);

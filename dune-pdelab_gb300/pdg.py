@@ -32,6 +32,8 @@ LIB_PATH = os.path.join(HERE, "_build", "libpdg.so")
 PDG_OK, PDG_EINVAL, PDG_ECUDA, PDG_ENOTCONVERGED, PDG_EBREAKDOWN = 0, 1, 2, 3, 4
 PDG_ESTATE, PDG_EUNSUPPORTED, PDG_EOUTFLOW, PDG_ENONFINITE, PDG_ETIMEOUT = 5, 6, 7, 8, 9
 PDG_ELINESEARCH = 10
+(ONESTEP_THETA, IMPLICIT_EULER, EXPLICIT_EULER, ALEXANDER2, ALEXANDER3, FRACTIONAL_STEP, HEUN,
+ SHU3, RK4) = range(9)
 NIPG, SIPG, IIPG = 0, 1, 2
 WEIGHTS_ON, WEIGHTS_OFF = 0, 1
 BC_DIRICHLET, BC_NEUMANN, BC_OUTFLOW, BC_NONE = 1, -1, -2, -3
@@ -91,6 +93,11 @@ class NewtonResult(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class OneStepResult(C.Structure):
+    _fields_ = [("stages", C.c_int), ("linear_solver_iterations", C.c_int),
+                ("elapsed", C.c_double), ("status", C.c_int)]
+
+
 class SolverResult(C.Structure):
     _fields_ = [("converged", C.c_int), ("iterations", C.c_int), ("elapsed", C.c_double),
                 ("reduction", C.c_double), ("conv_rate", C.c_double),
@@ -148,6 +155,11 @@ _SIGS = {
     "pdg_default_newton_options": (None, [C.POINTER(NewtonOptions)]),
     "pdg_newton_solve": (C.c_int, [_vp, C.POINTER(NewtonOptions), C.POINTER(SolverOptions), _vp,
                                    C.POINTER(NewtonResult)]),
+    "pdg_mass_apply": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_onestep_table": (C.c_int, [C.c_int, C.c_double, C.POINTER(C.c_int), _vp, _vp, _vp]),
+    "pdg_onestep_apply": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, C.c_double,
+                                    C.POINTER(SolverOptions), _vp, _vp,
+                                    C.POINTER(OneStepResult)]),
     "pdg_jacobian_assemble": (C.c_int, [_vp]),
     "pdg_jacobian_pattern": (C.c_int, [_vp, C.POINTER(C.c_long)]),
     "pdg_jacobian_export": (C.c_int, [_vp, _vp, _vp, _vp]),
@@ -406,6 +418,11 @@ class GridOperator:
         _check(load().pdg_matrix_apply(self._h, _ptr(x), _ptr(y)))
         return y
 
+    def mass_apply(self, x, y):
+        """y = M x (DG mass matrix)"""
+        _check(load().pdg_mass_apply(self._h, _ptr(x), _ptr(y)))
+        return y
+
     def grad_source(self, lam, g):
         _check(load().pdg_grad_source(self._h, _ptr(lam), _ptr(g)))
         return g
@@ -483,6 +500,45 @@ class ISTLBackend_SEQ_MatrixFree_Base:
 
     def norm(self, v):
         return self.go.norm(v)
+
+    def result(self):
+        return self.res
+
+
+def onestep_table(method, theta=1.0):
+    """(A, B, D) of a TimeSteppingParameterInterface scheme: A, B [s][s+1], D [s+1]."""
+    st = C.c_int()
+    A = np.zeros(20)
+    B = np.zeros(20)
+    D = np.zeros(5)
+    _check(load().pdg_onestep_table(method, float(theta), C.byref(st), A.ctypes.data,
+                                    B.ctypes.data, D.ctypes.data))
+    s = st.value
+    return A[:s * (s + 1)].reshape(s, s + 1).copy(), B[:s * (s + 1)].reshape(s, s + 1).copy(), \
+        D[:s + 1].copy()
+
+
+class OneStepMethod:
+    """OneStepMethod(method, igos, pdesolver) (instationary/implicitonestep.hh):
+    apply(time, dt, xold, xnew) advances one step; `method` is a scheme id
+    (IMPLICIT_EULER, ALEXANDER2, ...) or explicit (A, B, D) tables."""
+
+    def __init__(self, method, go: GridOperator, ls: "ISTLBackend_SEQ_MatrixFree_Base",
+                 theta=1.0):
+        self.go, self.ls = go, ls
+        self.A, self.B, self.D = (onestep_table(method, theta) if np.isscalar(method)
+                                  else [np.ascontiguousarray(t, dtype=np.float64) for t in method])
+        self.res = OneStepResult()
+
+    def apply(self, time, dt, xold, xnew):
+        s = self.A.shape[0]
+        A = np.ascontiguousarray(self.A, dtype=np.float64)
+        B = np.ascontiguousarray(self.B, dtype=np.float64)
+        D = np.ascontiguousarray(self.D, dtype=np.float64)
+        _check(load().pdg_onestep_apply(self.go.handle, s, A.ctypes.data, B.ctypes.data,
+                                        D.ctypes.data, float(dt), C.byref(self.ls.opts),
+                                        _ptr(xold), _ptr(xnew), C.byref(self.res)))
+        return time + dt
 
     def result(self):
         return self.res

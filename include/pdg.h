@@ -355,6 +355,49 @@ int pdg_newton_solve(pdg_context *ctx, const pdg_newton_options *opt,
                      const pdg_solver_options *lin, double *u, pdg_newton_result *res);
 
 /* ---------------------------------------------------------------- */
+/* instationary one-step methods                                     */
+/* ---------------------------------------------------------------- */
+
+/* y = M x with the DG mass matrix (the temporal L2 operator int u psi of
+   the one-step grid operator, gridoperator/onestep.hh). */
+int pdg_mass_apply(pdg_context *ctx, const double *x, double *y);
+
+/* TimeSteppingParameterInterface implementations
+   (instationary/onestepparameter.hh): */
+enum {
+  PDG_ONESTEP_THETA = 0,          /* OneStepThetaParameter(theta) */
+  PDG_ONESTEP_IMPLICIT_EULER = 1, /* theta = 1 */
+  PDG_ONESTEP_EXPLICIT_EULER = 2, /* theta = 0 */
+  PDG_ONESTEP_ALEXANDER2 = 3,
+  PDG_ONESTEP_ALEXANDER3 = 4,
+  PDG_ONESTEP_FRACTIONAL_STEP = 5,
+  PDG_ONESTEP_HEUN = 6,
+  PDG_ONESTEP_SHU3 = 7,
+  PDG_ONESTEP_RK4 = 8
+};
+/* The method's tables: *stages = s, A and B [s][s+1] (row r-1 holds
+   a(r, 0..s), b(r, 0..s)), D [s+1]; arrays of at least 4*5 and 5 values. */
+int pdg_onestep_table(int method, double theta, int *stages, double *A, double *B,
+                      double *D);
+typedef struct pdg_onestep_result {
+  int stages;
+  int linear_solver_iterations;
+  double elapsed;
+  int status;
+} pdg_onestep_result;
+/* OneStepMethod::apply(time, dt, xold, xnew) (instationary/implicitonestep.hh:
+   144-275): stage r solves
+     sum_{j<r} [a_rj M x_j + b_rj dt R(x_j)] + a_rr M x_r + b_rr dt R(x_r) = 0
+   (residual weights of the one-step local assembler with
+   MultiplyOperator0ByDT, gridoperator/onestep/prestageengine.hh:181-227);
+   implicit stages by the Krylov solver `lin` on the operator J + a_rr/(b_rr dt) M,
+   explicit stages (b_rr = 0) by the exact block-diagonal mass inverse.  The
+   spatial data (f, g, j, o) are time-independent. */
+int pdg_onestep_apply(pdg_context *ctx, int stages, const double *A, const double *B,
+                      const double *D, double dt, const pdg_solver_options *lin,
+                      const double *xold, double *xnew, pdg_onestep_result *res);
+
+/* ---------------------------------------------------------------- */
 /* assembled Jacobian                                                */
 /* ---------------------------------------------------------------- */
 

@@ -1390,6 +1390,140 @@ out:
   return st;
 }
 
+int pdgo_mass_apply(const pdgo_problem *p, const double *x, double *y) {
+  tables T;
+  if (tables_init(p, &T)) return PDGO_EARG;
+  const int d = T.d, nb = T.nb;
+  const long nc = pdgo_ncell(p);
+  double detJ = 1.0;
+  for (int j = 0; j < d; j++) detJ *= cell_h(p, j);
+  for (long e = 0; e < nc; e++) {
+    double *ye = &y[e * nb];
+    for (int i = 0; i < nb; i++) ye[i] = 0.0;
+    for (int q = 0; q < T.nqv; q++) {
+      const double *phi = &T.vphi[q * nb];
+      double u = 0.0;
+      for (int i = 0; i < nb; i++) u += x[e * nb + i] * phi[i];
+      for (int i = 0; i < nb; i++) ye[i] += u * phi[i] * T.vw[q] * detJ;
+    }
+  }
+  tables_free(&T);
+  return PDGO_OK;
+}
+
+/* per-cell mass block (identical for all cells of the uniform grid) */
+static int mass_block(const pdgo_problem *p, double *Mb) {
+  tables T;
+  if (tables_init(p, &T)) return PDGO_EARG;
+  const int d = T.d, nb = T.nb;
+  double detJ = 1.0;
+  for (int j = 0; j < d; j++) detJ *= cell_h(p, j);
+  memset(Mb, 0, sizeof(double) * nb * nb);
+  for (int q = 0; q < T.nqv; q++) {
+    const double *phi = &T.vphi[q * nb];
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < nb; j++) Mb[i * nb + j] += phi[i] * phi[j] * T.vw[q] * detJ;
+  }
+  tables_free(&T);
+  return PDGO_OK;
+}
+
+int pdgo_onestep(pdgo_problem *p, int s, const double *A, const double *B, double dt,
+                 int solver, const pdgo_prec_config *pc, double reduction, int maxit,
+                 const double *xold, double *xnew, int *linear_iterations) {
+  const long n = pdgo_ndof(p), nc = pdgo_ncell(p);
+  const int nb = pdgo_nbasis(p);
+  if (s < 1 || s > 4) return PDGO_EARG;
+  double *X[5], *RX[5], *MX[5];
+  for (int j = 0; j <= s; j++) {
+    X[j] = j == 0 ? (double *)xold : (j == s ? xnew : calloc(n, sizeof(double)));
+    RX[j] = calloc(n, sizeof(double));
+    MX[j] = calloc(n, sizeof(double));
+  }
+  double *Cv = calloc(n, sizeof(double)), *r = calloc(n, sizeof(double));
+  double *z = calloc(n, sizeof(double)), *cs = calloc(nc, sizeof(double));
+  double *Mb = malloc(sizeof(double) * nb * nb), *Mlu = NULL, *diag = NULL, *lu = NULL;
+  double *ablocks = NULL;
+  int *Mpiv = malloc(sizeof(int) * nb), *piv = NULL;
+  const double *c_orig = p->c;
+  int st = mass_block(p, Mb);
+  if (st) goto out;
+  Mlu = malloc(sizeof(double) * nb * nb);
+  memcpy(Mlu, Mb, sizeof(double) * nb * nb);
+  st = pdgo_lu_factor(nb, 1, Mlu, Mpiv);
+  if (st) goto out;
+  if (linear_iterations) *linear_iterations = 0;
+  /* R(x_0), M x_0 with the original coefficients */
+  st = pdgo_residual(p, X[0], RX[0]);
+  if (st) goto out;
+  pdgo_mass_apply(p, X[0], MX[0]);
+  for (int rr = 1; rr <= s; rr++) {
+    const double *a = A + (rr - 1) * (s + 1), *b = B + (rr - 1) * (s + 1);
+    memset(Cv, 0, sizeof(double) * n);
+    for (int j = 0; j < rr; j++)
+      for (long i = 0; i < n; i++) Cv[i] += b[j] * dt * RX[j][i] + a[j] * MX[j][i];
+    const double arr = a[rr], brr = b[rr];
+    if (brr == 0.0) {
+      for (long i = 0; i < n; i++) Cv[i] *= -1.0 / arr;
+      pdgo_lu_apply(nb, 1, Mlu, Mpiv, Cv, X[rr]);   /* one block at a time */
+      for (long e = 1; e < nc; e++) pdgo_lu_apply(nb, 1, Mlu, Mpiv, &Cv[e * nb], &X[rr][e * nb]);
+    } else {
+      const double sigma = arr / (brr * dt);
+      for (long e = 0; e < nc; e++) cs[e] = (c_orig ? c_orig[e] : 0.0) + sigma;
+      p->c = cs;
+      /* preconditioner on the shifted operator */
+      free(diag); free(lu); free(piv); free(ablocks);
+      diag = malloc(sizeof(double) * nc * nb * nb);
+      lu = NULL; piv = NULL; ablocks = NULL;
+      st = pdgo_block_diagonal(p, diag);
+      if (st) goto out;
+      const int base = pc->kind & 15;
+      if (base == 1 || base == 2) {
+        lu = malloc(sizeof(double) * nc * nb * nb);
+        piv = malloc(sizeof(int) * nc * nb);
+        memcpy(lu, diag, sizeof(double) * nc * nb * nb);
+        st = pdgo_lu_factor(nb, nc, lu, piv);
+        if (st) goto out;
+      }
+      if (pc->kind & 16) {
+        ablocks = malloc(sizeof(double) * nc * (2 * p->dim + 1) * nb * nb);
+        st = pdgo_assemble_jacobian(p, ablocks);
+        if (st) goto out;
+      }
+      memcpy(X[rr], X[rr - 1], sizeof(double) * n);
+      memset(r, 0, sizeof(double) * n);
+      st = pdgo_residual(p, X[rr], r);            /* J_sigma x + R(0) */
+      if (st) goto out;
+      for (long i = 0; i < n; i++) r[i] += Cv[i] / (brr * dt);
+      memset(z, 0, sizeof(double) * n);
+      opctx oc = {p, 0, NULL, lu, piv, n, nb, pc, diag, ablocks, 0};
+      pdgo_result lr;
+      st = solver == 0 ? cg_run(&oc, z, r, reduction, maxit, &lr)
+                       : bicgstab_run(&oc, z, r, reduction, maxit, &lr);
+      if (linear_iterations) *linear_iterations += lr.iterations;
+      if (st) goto out;
+      for (long i = 0; i < n; i++) X[rr][i] -= z[i];
+      p->c = c_orig;
+    }
+    if (rr < s) {
+      p->c = c_orig;
+      st = pdgo_residual(p, X[rr], RX[rr]);
+      if (st) goto out;
+      pdgo_mass_apply(p, X[rr], MX[rr]);
+    }
+  }
+out:
+  p->c = c_orig;
+  for (int j = 0; j <= s; j++) {
+    if (j != 0 && j != s) free(X[j]);
+    free(RX[j]);
+    free(MX[j]);
+  }
+  free(Cv); free(r); free(z); free(cs); free(Mb); free(Mlu); free(Mpiv);
+  free(diag); free(lu); free(piv); free(ablocks);
+  return st;
+}
+
 /* NewtonMethod::apply (solver/newton.hh:177-335) restated. */
 int pdgo_newton(pdgo_problem *p, int solver, const pdgo_prec_config *pc,
                 const pdgo_newton_opts *o, double *x, pdgo_newton_result *res) {

@@ -204,6 +204,19 @@ typedef struct pdgo_newton_result {
 int pdgo_newton(pdgo_problem *p, int solver, const pdgo_prec_config *pc,
                 const pdgo_newton_opts *o, double *x, pdgo_newton_result *res);
 
+/* y = M x: the DG mass matrix int u psi (L2 temporal operator), per cell
+   at the volume quadrature points. */
+int pdgo_mass_apply(const pdgo_problem *p, const double *x, double *y);
+/* OneStepMethod::apply (instationary/implicitonestep.hh:144-275) with the
+   one-step residual weights (gridoperator/onestep/prestageengine.hh):
+   stage r solves sum_{j<=r} [a_rj M x_j + b_rj dt R(x_j)] = 0; implicit
+   stages by residual-form Krylov (CG 0 / BiCGStab 1) with the configured
+   preconditioner on J + a_rr/(b_rr dt) M, explicit stages by the per-cell
+   mass inverse.  A, B [s][s+1] row-major. */
+int pdgo_onestep(pdgo_problem *p, int s, const double *A, const double *B, double dt,
+                 int solver, const pdgo_prec_config *pc, double reduction, int maxit,
+                 const double *xold, double *xnew, int *linear_iterations);
+
 /* Evaluate u_h at an m-point tensor Gauss rule in every cell:
    xyz [ncell][m^d][dim], w [ncell][m^d] (weights times |J|),
    val [ncell][m^d]. */

@@ -134,6 +134,10 @@ def lib():
                                               C.c_int, C.c_int, C.c_double, _ip]),
             "pdgo_prec_apply_cfg": (C.c_int, [P, C.POINTER(PrecConfig), _dp, _dp, _ip, _dp,
                                               C.c_int, _dp, _dp, _ip]),
+            "pdgo_mass_apply": (C.c_int, [P, _dp, _dp]),
+            "pdgo_onestep": (C.c_int, [P, C.c_int, _dp, _dp, C.c_double, C.c_int,
+                                       C.POINTER(PrecConfig), C.c_double, C.c_int, _dp, _dp,
+                                       _ip]),
             "pdgo_newton": (C.c_int, [P, C.c_int, C.POINTER(PrecConfig), C.POINTER(NewtonOpts),
                                       _dp, C.POINTER(NewtonResult)]),
             "pdgo_solve_linear_problem_prec": (C.c_int, [P, C.c_int, C.c_int,
@@ -307,6 +311,23 @@ class Problem:
                                              _ptr(x), reduction, min_defect, maxit,
                                              C.byref(res))
         return x, res, st
+
+    def mass_apply(self, x):
+        y = np.zeros(self.ndof)
+        _check(lib().pdgo_mass_apply(self.ref, _ptr(np.ascontiguousarray(x)), _ptr(y)))
+        return y
+
+    def onestep(self, A, B, dt, xold, pc, solver="cg", reduction=1e-12, maxit=5000):
+        """One step of the one-step method with tables A, B [s][s+1]."""
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        xnew = np.zeros(self.ndof)
+        its = np.zeros(1, dtype=np.int32)
+        _check(lib().pdgo_onestep(self.ref, A.shape[0], _ptr(A), _ptr(B), dt,
+                                  0 if solver == "cg" else 1, C.byref(pc), reduction, maxit,
+                                  _ptr(np.ascontiguousarray(xold, dtype=np.float64)), _ptr(xnew),
+                                  its.ctypes.data_as(_ip)))
+        return xnew, int(its[0])
 
     def set_nonlinearity(self, coef):
         """q(u) = sum_m coef[m] u^m (coef None removes it)."""

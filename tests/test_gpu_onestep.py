@@ -1,0 +1,94 @@
+"""Instationary one-step methods (OneStepMethod with the
+TimeSteppingParameterInterface schemes) and the DG mass operator on the GPU
+against the oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def pdg():
+    import __graft_entry__
+    __graft_entry__.build()
+    import pdg as m
+    return m
+
+
+def _pair(pdg, oracle, dim, k, nc, seed, react=True):
+    rng = np.random.default_rng(seed)
+    ncell = int(np.prod(nc))
+    K = np.exp(0.5 * rng.standard_normal(ncell))
+    go = pdg.GridOperator(dim, k, nc, alpha=3.0)
+    go.set_permeability(K)
+    P = oracle.Problem(dim, k, nc, alpha=3.0, K=K)
+    if react:
+        c = rng.uniform(0.5, 1.5, ncell)
+        go.set_reaction(c)
+        P.set(c=c)
+    fc = rng.uniform(0.5, 1.5, ncell)
+    go.set_source(fc=fc)
+    P.set(fc=fc)
+    return go, P, rng
+
+
+@pytest.mark.parametrize("dim,k,nc", [(2, 1, (5, 4)), (2, 4, (3, 3)), (3, 2, (3, 4, 2)),
+                                      (3, 4, (2, 2, 2))])
+def test_mass_apply(pdg, oracle, dim, k, nc):
+    go, P, rng = _pair(pdg, oracle, dim, k, nc, seed=61)
+    x = rng.uniform(-1, 1, go.ndof)
+    assert _rel(go.mass_apply(x, np.zeros(go.ndof)), P.mass_apply(x)) <= 1e-13
+
+
+METHODS = ["IMPLICIT_EULER", "EXPLICIT_EULER", "ALEXANDER2", "ALEXANDER3", "FRACTIONAL_STEP",
+           "HEUN", "SHU3", "RK4"]
+
+
+@pytest.mark.parametrize("name", METHODS + ["THETA"])
+def test_onestep_matches_oracle(pdg, oracle, name):
+    go, P, rng = _pair(pdg, oracle, 3, 2, (3, 3, 2), seed=63)
+    method = getattr(pdg, name) if name != "THETA" else pdg.ONESTEP_THETA
+    A, B, D = pdg.onestep_table(method, theta=0.5)
+    implicit = B[np.arange(B.shape[0]), np.arange(1, B.shape[0] + 1)].any()
+    dt = 2e-3 if implicit else 2e-5
+    ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG,
+                                             preconditioner=pdg.PREC_BJ_FDM)
+    ls.opts.reduction = 1e-13
+    osm = pdg.OneStepMethod(method, go, ls, theta=0.5)
+    x = rng.uniform(-1, 1, go.ndof)
+    xo = x.copy()
+    t = 0.0
+    for _ in range(3):
+        xn = np.zeros(go.ndof)
+        t = osm.apply(t, dt, x, xn)
+        x = xn
+        xo, _ = P.onestep(A, B, dt, xo, oracle.prec_config(2), reduction=1e-13)
+    assert _rel(x, xo) <= 1e-9
+    # the operator is restored after the step
+    y = go.residual(xo, np.zeros(go.ndof))
+    assert _rel(y, P.residual(xo)) <= 1e-12
+
+
+def test_onestep_mixed_sor_nonsymmetric(pdg, oracle):
+    # Alexander2 with convection: BiCGStab, FP32 block SOR inside FGMRES
+    go, P, rng = _pair(pdg, oracle, 3, 2, (4, 3, 3), seed=65)
+    modes = pdg.fourier_velocity_modes(65)
+    go.set_velocity_modes(modes)
+    P.set_modes(modes)
+    A, B, D = pdg.onestep_table(pdg.ALEXANDER2)
+    ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.BICGSTAB,
+                                             preconditioner=pdg.PREC_SOR | pdg.PREC_BJ_DENSE,
+                                             mixed=True, inner_reduction=1e-1)
+    ls.opts.reduction = 1e-12
+    ls.opts.inner_maxit = 30
+    osm = pdg.OneStepMethod(pdg.ALEXANDER2, go, ls)
+    x = rng.uniform(-1, 1, go.ndof)
+    xn = np.zeros(go.ndof)
+    osm.apply(0.0, 1e-2, x, xn)
+    xo, _ = P.onestep(A, B, 1e-2, x, oracle.prec_config(2), solver="bicgstab", reduction=1e-13)
+    assert _rel(xn, xo) <= 1e-9
+    assert osm.result().stages == 2 and osm.result().linear_solver_iterations > 0

@@ -202,3 +202,43 @@ def test_nonlinear_reference_problem_oracle(oracle):
     assert st == 0 and res.converged and res.iterations <= 6
     xyz, w, val = P.eval_points(u, 6)
     assert float((w * (val - (xyz ** 2).sum(-1)) ** 2).sum()) < 1e-6
+
+
+def test_onestep_orders_oracle(oracle):
+    """The oracle's one-step methods (tables of instationary/onestepparameter.hh)
+    converge to the exact semi-discrete solution exp(-M^{-1}J t) at their
+    orders: implicit Euler 1, Crank-Nicolson 2, Alexander2 2, Heun 2, RK4 4."""
+    import numpy as np
+    scipy_linalg = __import__("pytest").importorskip("scipy.linalg")
+    n = 4
+    P = oracle.Problem(2, 1, (n, n), alpha=3.0)
+    P.set(fc=np.ones(n * n))
+    N = P.ndof
+    E = np.eye(N)
+    J = np.column_stack([P.jacobian_apply(E[i]) for i in range(N)])
+    M = np.column_stack([P.mass_apply(E[i]) for i in range(N)])
+    L = np.linalg.solve(M, J)
+    ustar = np.linalg.solve(J, -P.residual(np.zeros(N)))
+    u0 = np.sin(np.arange(N))
+    al = 1 - 0.5 * np.sqrt(2)
+    cases = {
+        "IE": (np.array([[-1, 1.]]), np.array([[0, 1.]]), 1, 0.05, (8, 16, 32)),
+        "CN": (np.array([[-1, 1.]]), np.array([[0.5, 0.5]]), 2, 0.05, (16, 32, 64)),
+        "A2": (np.array([[-1, 1, 0], [-1, 0, 1.]]), np.array([[0, al, 0], [0, 1 - al, al]]), 2,
+               0.05, (8, 16, 32)),
+        "Heun": (np.array([[-1, 1, 0], [-0.5, -0.5, 1.]]), np.array([[1, 0, 0], [0, 0.5, 0.]]), 2,
+                 0.01, (40, 80, 160)),
+        "RK4": (np.array([[-1, 1, 0, 0, 0], [-1, 0, 1, 0, 0], [-1, 0, 0, 1, 0], [-1, 0, 0, 0, 1.]]),
+                np.array([[.5, 0, 0, 0, 0], [0, .5, 0, 0, 0], [0, 0, 1, 0, 0],
+                          [1 / 6, 1 / 3, 1 / 3, 1 / 6, 0]]), 4, 0.01, (40, 80, 160)),
+    }
+    for name, (A, B, order, T, steps) in cases.items():
+        ue = ustar + scipy_linalg.expm(-L * T) @ (u0 - ustar)
+        errs = []
+        for m in steps:
+            x = u0.copy()
+            for _ in range(m):
+                x, _ = P.onestep(A, B, T / m, x, oracle.prec_config(2), reduction=1e-13)
+            errs.append(np.abs(x - ue).max())
+        rate = np.log2(errs[-2] / errs[-1])
+        assert abs(rate - order) < 0.25, (name, errs)
