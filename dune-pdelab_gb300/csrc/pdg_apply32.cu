@@ -1,5 +1,5 @@
 // pdg_apply32.cu -- the FP32 cell operator of the mixed-precision inner
-// solve (3D), laid out for shared-memory throughput.
+// solve (3D, degrees 1 and 2), laid out for shared-memory throughput.
 //
 // Same operator as k_apply (pdg_apply.cu; reference: ConvectionDiffusionDG::
 // jacobian_apply_volume / _skeleton / _boundary, localoperator/
@@ -25,6 +25,7 @@
 //     out = (Mhat_y (x) Mhat_x) Z + sum_z' Mhat_z[z][z'] P_z'
 //
 // The output is staged in shared memory and written back coalesced.
+#include <cstdint>
 #include <mutex>
 
 #include "pdg_internal.cuh"
@@ -43,10 +44,14 @@ struct P32Cfg {
   static constexpr int CPB = 128 / N;                 // cells per CTA
   static constexpr int THREADS = CPB * N;
   static constexpr int REC = 3 * N2 + 30;             // A'_x, A'_y, A'_z, 5 per face
-  // shared floats: own run (CPB+2 cells), 4 neighbour runs, P, records
+  // shared floats: own run (CPB+2 cells), 4 neighbour runs, P, records;
+  // the staged runs carry 4 floats of slack (16-byte phase of their source)
   static constexpr int OWN = (CPB + 2) * NB;
   static constexpr int RUN = CPB * NB;
-  static constexpr int SMEM = OWN + 5 * RUN + CPB * REC;
+  static constexpr int OWNP = (OWN + 4 + 3) / 4 * 4, RUNP = (RUN + 4 + 3) / 4 * 4;
+  static constexpr int RECP = (CPB * REC + 4 + 3) / 4 * 4;
+  static constexpr int RUN4 = (RUN + 3) / 4 * 4;       // P, keeps RS 16-byte aligned
+  static constexpr int SMEM = OWNP + 4 * RUNP + RUN4 + RECP;
 };
 
 // face coupling of a neighbour trace (val, dv) into (s1, s2); cf = {hp ke,
@@ -78,13 +83,13 @@ __global__ void __launch_bounds__(P32Cfg<N>::THREADS)
   constexpr int N2 = C::N2, NB = C::NB, CPB = C::CPB, REC = C::REC;
   extern __shared__ __align__(16) float sm[];
   if (a.skip && *a.skip) return;
-  float *OWN = sm;                     // cells e0-1 .. e0+CPB
-  float *YL = OWN + C::OWN;            // cells e - nx
-  float *YH = YL + C::RUN;             // cells e + nx
-  float *ZL = YH + C::RUN;             // cells e - nx ny
-  float *ZH = ZL + C::RUN;             // cells e + nx ny
-  float *PS = ZH + C::RUN;             // stage-1 planes P
-  float *RS = PS + C::RUN;             // records
+  float *OWN0 = sm;                    // cells e0-1 .. e0+CPB
+  float *YL0 = OWN0 + C::OWNP;         // cells e - nx
+  float *YH0 = YL0 + C::RUNP;          // cells e + nx
+  float *ZL0 = YH0 + C::RUNP;          // cells e - nx ny
+  float *ZH0 = ZL0 + C::RUNP;          // cells e + nx ny
+  float *PS = ZH0 + C::RUNP;           // stage-1 planes P
+  float *RS0 = PS + C::RUN4;           // records
 
   const long e0 = (long)blockIdx.x * CPB;
   const long ncell = p.ncell;
@@ -94,29 +99,41 @@ __global__ void __launch_bounds__(P32Cfg<N>::THREADS)
   const bool coupled = !a.diag_only;
 
   // ---- coalesced staging: asynchronous global -> shared copies (cp.async),
-  // all in flight at once, one wait before the barrier ----
-  {
-    auto stage = [&](float *dst, const float *src, long g0, long lim, int count, bool on) {
-      for (int i = threadIdx.x; i < count; i += C::THREADS) {
-        const long g = g0 + i;
-        if (on && g >= 0 && g < lim) {
-          const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + i);
-          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(src + g)
-                       : "memory");
-        } else {
-          dst[i] = 0.f;
+  // all in flight at once, one wait before the barrier.  A run of source
+  // elements [g0, g0+count) lands at dst[ph + i] with ph = g0 mod 4, so that
+  // source and destination share their 16-byte phase and whole 16-byte
+  // chunks are copied; chunks that reach outside [0, lim) go element-wise.
+  // Returns the run's base pointer (dst + ph). ----
+  auto stage = [&](float *dst, const float *src, long g0, long lim, int count,
+                   bool on) -> float * {
+    const int ph = (int)(((g0 % 4) + 4) % 4);
+    const long ga = g0 - ph;
+    const int nch = (ph + count + 3) / 4;
+    const bool vec_ok = (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+    for (int c = threadIdx.x; c < nch; c += C::THREADS) {
+      const long gc = ga + 4L * c;
+      if (on && vec_ok && gc >= 0 && gc + 4 <= lim) {
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + 4 * c);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src + gc)
+                     : "memory");
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const long g = gc + j;
+          dst[4 * c + j] = (on && g >= 0 && g < lim) ? src[g] : 0.f;
         }
       }
-    };
-    stage(OWN, x, (e0 - 1) * NB, ndof, C::OWN, true);
-    stage(YL, x, (e0 - sx) * NB, ndof, C::RUN, coupled);
-    stage(YH, x, (e0 + sx) * NB, ndof, C::RUN, coupled);
-    stage(ZL, x, (e0 - sxy) * NB, ndof, C::RUN, coupled);
-    stage(ZH, x, (e0 + sxy) * NB, ndof, C::RUN, coupled);
-    stage(RS, rec, e0 * REC, ncell * REC, CPB * REC, true);
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-  }
+    }
+    return dst + ph;
+  };
+  float *OWN = stage(OWN0, x, (e0 - 1) * NB, ndof, C::OWN, true);
+  float *YL = stage(YL0, x, (e0 - sx) * NB, ndof, C::RUN, coupled);
+  float *YH = stage(YH0, x, (e0 + sx) * NB, ndof, C::RUN, coupled);
+  float *ZL = stage(ZL0, x, (e0 - sxy) * NB, ndof, C::RUN, coupled);
+  float *ZH = stage(ZH0, x, (e0 + sxy) * NB, ndof, C::RUN, coupled);
+  float *RS = stage(RS0, rec, e0 * REC, ncell * REC, CPB * REC, true);
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();
 
   const int t = threadIdx.x, cs = t / N, z = t - cs * N;
@@ -296,7 +313,7 @@ __global__ void __launch_bounds__(P32Cfg<N>::THREADS)
 
   // ---- coalesced write-back through shared memory (the YL run is free) ----
   __syncthreads();
-  float *O = YL;
+  float *O = YL0;
 #pragma unroll
   for (int y = 0; y < N; y++)
 #pragma unroll
@@ -368,9 +385,7 @@ int launch_apply32_3d(pdg_context *ctx, const ApplyArgs<float> &a, const OpParam
   switch (ctx->N) {
     case 2: return launch32_n<2>(ctx, a, p, rec);
     case 3: return launch32_n<3>(ctx, a, p, rec);
-    case 4: return launch32_n<4>(ctx, a, p, rec);
-    case 5: return launch32_n<5>(ctx, a, p, rec);
-    default: return set_error(PDG_EUNSUPPORTED, "degree not compiled in");
+    default: return set_error(PDG_EUNSUPPORTED, "staged FP32 kernel: degree 1 or 2 only");
   }
 }
 
