@@ -519,6 +519,11 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
   if (std::is_same<T, double>::value && K == (const T *)ctx->K64) {
     PDG_TRY(ensure_record(ctx));
     rec = (const T *)ctx->rec64;
+  } else if (std::is_same<T, float>::value && ctx->dim == 3 && K == (const T *)ctx->K32) {
+    // FP32 records (rounded from the FP64 arithmetic): no coefficient
+    // assembly or division in the apply
+    PDG_TRY(ensure_record32(ctx));
+    rec = (const T *)ctx->rec32;
   }
   const int key = ctx->dim * 10 + ctx->k;
   int st;
