@@ -809,6 +809,11 @@ int pdg_destroy(pdg_context *c) {
   if (!c) return PDG_OK;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->pipe_h2d) {
+    cudaStreamSynchronize(c->pipe_h2d);
+    cudaStreamSynchronize(c->pipe_d2h);
+    cudaStreamSynchronize(c->pipe_k2);
+  }
   prec_free(c, 0);
   prec_free(c, 1);
   sor_free(c);
@@ -828,6 +833,13 @@ int pdg_destroy(pdg_context *c) {
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  if (c->pipe_h2d) {
+    cudaStreamDestroy(c->pipe_h2d);
+    cudaStreamDestroy(c->pipe_d2h);
+    cudaStreamDestroy(c->pipe_k2);
+    for (cudaEvent_t e : c->pipe_ev)
+      if (e) cudaEventDestroy(e);
+  }
   delete c;
   return PDG_OK;
 }
@@ -970,6 +982,111 @@ static int ensure_stage(pdg_context *ctx) {
   return PDG_OK;
 }
 
+// ---- host-buffer applies pipelined over slabs of cells --------------------
+// Copying x in, applying and copying y out one after another costs the copies
+// on top of the kernel.  The grid is cut into slabs of whole planes of the
+// slowest direction (contiguous cell and DOF ranges); slab s is applied once
+// slabs s and s+1 are on the device (its faces read one neighbour plane) and
+// copied out while slab s+1 is applied, so the copies in, the kernels and the
+// copies out overlap, ordered by events.  Consecutive slabs are applied on
+// two alternating streams: they write disjoint ranges of y, and the last,
+// partly filled wave of one slab's grid overlaps the first of the next.
+constexpr int kMaxSlabs = 16;
+constexpr long kMinSlabCells = 16384;
+
+static int cuda_status(cudaError_t e) {
+  return e == cudaSuccess ? PDG_OK
+                          : set_error(PDG_ECUDA, std::string("host-buffer apply: ") +
+                                                     cudaGetErrorString(e));
+}
+
+static int pipe_ready(pdg_context *ctx) {
+  if (ctx->pipe_h2d) return PDG_OK;
+  PDG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->pipe_h2d, cudaStreamNonBlocking));
+  PDG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->pipe_d2h, cudaStreamNonBlocking));
+  PDG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->pipe_k2, cudaStreamNonBlocking));
+  for (int i = 0; i < 2 * kMaxSlabs + 3; i++)
+    PDG_CUDA_TRY(cudaEventCreateWithFlags(&ctx->pipe_ev[i], cudaEventDisableTiming));
+  return PDG_OK;
+}
+
+// number of slabs (1: no pipelining) and planes per slab
+static int pipe_slabs(const pdg_context *ctx, long *planes_per_slab) {
+  const long planes = ctx->cfg.cells[ctx->dim - 1];
+  long s = ctx->ncell / kMinSlabCells;
+  if (s > kMaxSlabs) s = kMaxSlabs;
+  if (s > planes) s = planes;
+  if (s < 2) return 1;
+  const long pps = (planes + s - 1) / s;
+  *planes_per_slab = pps;
+  return (int)((planes + pps - 1) / pps);
+}
+
+// y = (acc ? y : 0) + alpha J x + add with x and/or y in host memory;
+// xdev/ydev: the device copies (staging buffers for host vectors)
+static int apply_pipelined(pdg_context *ctx, const double *x, double *y, const double *xdev,
+                           double *ydev, bool hx, bool hy, const double *add, double alpha,
+                           int acc, int transpose, int nslab, long pps) {
+  PDG_TRY(pipe_ready(ctx));
+  PDG_TRY(prepare_apply64(ctx));
+  const long plane = ctx->ncell / ctx->cfg.cells[ctx->dim - 1];
+  const long nb = ctx->nb;
+  cudaEvent_t *ev_in = ctx->pipe_ev, *ev_out = ctx->pipe_ev + kMaxSlabs;
+  cudaEvent_t ev_start = ctx->pipe_ev[2 * kMaxSlabs], ev_end = ctx->pipe_ev[2 * kMaxSlabs + 1];
+  cudaEvent_t ev_k2 = ctx->pipe_ev[2 * kMaxSlabs + 2];
+  // the side streams start after the work already queued on the context stream
+  PDG_CUDA_TRY(cudaEventRecord(ev_start, ctx->stream));
+  PDG_CUDA_TRY(cudaStreamWaitEvent(ctx->pipe_h2d, ev_start, 0));
+  PDG_CUDA_TRY(cudaStreamWaitEvent(ctx->pipe_d2h, ev_start, 0));
+  PDG_CUDA_TRY(cudaStreamWaitEvent(ctx->pipe_k2, ev_start, 0));
+  cudaStream_t const ctx_stream = ctx->stream;
+  auto range = [&](int s, long *c0, long *c1) {
+    *c0 = s * pps * plane;
+    *c1 = std::min(ctx->ncell, (s + 1) * pps * plane);
+  };
+  for (int s = 0; s < nslab; s++) {
+    long c0, c1;
+    range(s, &c0, &c1);
+    const size_t off = (size_t)(c0 * nb), bytes = sizeof(double) * (size_t)((c1 - c0) * nb);
+    if (hx)
+      PDG_CUDA_TRY(cudaMemcpyAsync((double *)xdev + off, x + off, bytes, cudaMemcpyHostToDevice,
+                                   ctx->pipe_h2d));
+    if (hy && acc)
+      PDG_CUDA_TRY(cudaMemcpyAsync(ydev + off, y + off, bytes, cudaMemcpyHostToDevice,
+                                   ctx->pipe_h2d));
+    PDG_CUDA_TRY(cudaEventRecord(ev_in[s], ctx->pipe_h2d));
+  }
+  int st = PDG_OK;
+  for (int s = 0; s < nslab && st == PDG_OK; s++) {
+    long c0, c1;
+    range(s, &c0, &c1);
+    // the launchers enqueue on ctx->stream: point it at this slab's stream
+    ctx->stream = (s & 1) ? ctx->pipe_k2 : ctx_stream;
+    if ((st = cuda_status(cudaStreamWaitEvent(ctx->stream, ev_in[std::min(s + 1, nslab - 1)],
+                                              0))))
+      break;
+    ApplyArgs<double> a{xdev, ydev, add, alpha, acc, transpose, 0, nullptr, nullptr,
+                        (int)(c1 - c0), (int)c0};
+    if ((st = launch_apply<double>(ctx, a, ctx->K64, ctx->c64, ctx->tab64))) break;
+    if (hy) {
+      const size_t off = (size_t)(c0 * nb), bytes = sizeof(double) * (size_t)((c1 - c0) * nb);
+      if ((st = cuda_status(cudaEventRecord(ev_out[s], ctx->stream))) ||
+          (st = cuda_status(cudaStreamWaitEvent(ctx->pipe_d2h, ev_out[s], 0))) ||
+          (st = cuda_status(cudaMemcpyAsync(y + off, ydev + off, bytes, cudaMemcpyDeviceToHost,
+                                            ctx->pipe_d2h))))
+        break;
+    }
+  }
+  ctx->stream = ctx_stream;
+  PDG_TRY(st);
+  PDG_CUDA_TRY(cudaEventRecord(ev_k2, ctx->pipe_k2));
+  PDG_CUDA_TRY(cudaEventRecord(ev_end, ctx->pipe_d2h));
+  PDG_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ev_k2, 0));
+  PDG_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ev_end, 0));
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return PDG_OK;
+}
+
 // y = (acc ? y : 0) + alpha J x + (with_r0 ? R(0) : 0), host or device vectors
 static int apply_entry(pdg_context *ctx, const double *x, double *y, double alpha, int acc,
                        int transpose, bool with_r0) {
@@ -978,6 +1095,11 @@ static int apply_entry(pdg_context *ctx, const double *x, double *y, double alph
   if (with_r0) PDG_TRY(ensure_r0(ctx));
   const bool hx = !is_device_ptr(x), hy = !is_device_ptr(y);
   if (hx || hy) PDG_TRY(ensure_stage(ctx));
+  long pps = 0;
+  const int nslab = (hx || hy) ? pipe_slabs(ctx, &pps) : 1;
+  if (nslab > 1 && !ctx->use_matrix && !ctx->ops32 && ctx->nl_deg == 0)
+    return apply_pipelined(ctx, x, y, hx ? ctx->stage_a : x, hy ? ctx->stage_b : y, hx, hy,
+                           with_r0 ? ctx->r0 : nullptr, alpha, acc, transpose, nslab, pps);
   Staged<double> sx, sy;
   PDG_TRY(stage_in<double>(ctx, x, ctx->ndof, ctx->stage_a, true, &sx));
   PDG_TRY(stage_in<double>(ctx, y, ctx->ndof, ctx->stage_b, acc != 0, &sy));

@@ -52,6 +52,18 @@ struct Cfg {
   static constexpr int TAB = 2 * N2 + 2 * N;
 };
 
+// Padding (elements) added to the per-cell shared region of k_apply so that
+// the cells that share a warp fall on different shared-memory banks; chosen
+// by counting the wavefronts of the kernel's shared accesses per padding
+// (e.g. 3D Q3 FP32: 544 floats per cell put both cells of a warp on the same
+// banks, 16 more halve the wavefronts).
+template <typename T, int D, int N>
+constexpr int cell_pad() {
+  if (D != 3) return 0;
+  if (sizeof(T) == 4) return N == 3 ? 6 : N == 4 ? 16 : N == 5 ? 30 : 0;
+  return N == 3 ? 2 : N == 5 ? 14 : 0;
+}
+
 // tangential face scale of direction dir (product of the other cell sizes)
 template <typename T, int D>
 __device__ __forceinline__ T hperp(const OpParams<T> &p, int dir) {
@@ -128,6 +140,7 @@ __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
     k_apply(const OpParams<T> p, const ApplyArgs<T> a, const T *__restrict__ rec) {
   using C = Cfg<D, N>;
   constexpr int N2 = C::N2, NB = C::NB, TPC = C::TPC, CPB = C::CPB, NF = C::NF;
+  constexpr int PER_CELL = C::PER_CELL + cell_pad<T, D, N>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *tM = reinterpret_cast<T *>(smem_raw);
   T *tS = tM + N2;
@@ -136,7 +149,7 @@ __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
   const int t = threadIdx.x;
   const int cs = t / TPC;
   const int l = t - cs * TPC;
-  T *cellmem = tM + C::TAB + cs * C::PER_CELL;
+  T *cellmem = tM + C::TAB + cs * PER_CELL;
   T *ue = cellmem;
   T *Xs = ue + NB;
   T *Ys = Xs + (D == 3 ? NB : 0);
@@ -150,8 +163,9 @@ __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
   for (int i = t; i < C::TAB; i += blockDim.x) tM[i] = p.tab[i];
 
   const int li = blockIdx.x * CPB + cs;         // cell counts fit 31 bits
-  const bool active = a.cells ? li < a.ncells : li < p.ncell;
-  const int e = a.cells ? (active ? a.cells[li] : 0) : li;
+  const bool ranged = !a.cells && a.ncells > 0;
+  const bool active = (a.cells || ranged) ? li < a.ncells : li < p.ncell;
+  const int e = a.cells ? (active ? a.cells[li] : 0) : (ranged ? a.cell0 + li : li);
   const int ee = active ? e : 0;
   int ix[3];
   cell_coords(p, (unsigned)ee, ix);
@@ -426,7 +440,7 @@ template <typename T, int D, int N>
 static int launch_apply_dn(pdg_context *ctx, const ApplyArgs<T> &a, const OpParams<T> &p,
                            const T *rec) {
   using C = Cfg<D, N>;
-  const size_t smem = sizeof(T) * (C::TAB + C::CPB * C::PER_CELL);
+  const size_t smem = sizeof(T) * (C::TAB + C::CPB * (C::PER_CELL + cell_pad<T, D, N>()));
   static int attr_done = -1;
   if (attr_done != ctx->device) {
     PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply<T, D, N>,
@@ -434,7 +448,7 @@ static int launch_apply_dn(pdg_context *ctx, const ApplyArgs<T> &a, const OpPara
                                       (int)smem));
     attr_done = ctx->device;
   }
-  const long work = a.cells ? a.ncells : ctx->ncell;
+  const long work = (a.cells || a.ncells > 0) ? a.ncells : ctx->ncell;
   if (work <= 0) return PDG_OK;
   const long blocks = (work + C::CPB - 1) / C::CPB;
   k_apply<T, D, N><<<(unsigned)blocks, C::THREADS, smem, ctx->stream>>>(p, a, rec);
@@ -500,6 +514,10 @@ static int ensure_record(pdg_context *ctx) {
   return st;
 }
 
+// the FP64 operator's lazily built per-cell records, built now (before
+// launches are spread over several streams)
+int prepare_apply64(pdg_context *ctx) { return ensure_record(ctx); }
+
 template <typename T>
 int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c,
                  const T *tab) {
@@ -508,7 +526,7 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
     // the staged kernel wins for N <= 3 (Q1, Q2: 78 vs 126 us at 64^3 Q2);
     // at N >= 4 its shared-memory runs cut occupancy below the generic
     // kernel's (Q3 96^3: 1170 vs 828 us; Q4 48^3: 324 vs 206 us)
-    if (ctx->dim == 3 && ctx->N <= 3 && !a.cells && K == ctx->K32) {
+    if (ctx->dim == 3 && ctx->N <= 3 && !a.cells && a.ncells == 0 && K == ctx->K32) {
       PDG_TRY(ensure_record32(ctx));
       PDG_TRY(launch_apply32_3d(ctx, a, p, ctx->rec32));
       if (ctx->vel.nmodes > 0) PDG_TRY(launch_convection<T>(ctx, a));

@@ -119,8 +119,9 @@ __global__ void __launch_bounds__(CCfg<N>::THREADS)
   if (a.skip && *a.skip) return;
   for (int i = t; i < C::TAB; i += blockDim.x) tB[i] = tabBD[i];
   const long li = (long)blockIdx.x * CPB + cs;
-  const bool active = a.cells ? li < a.ncells : li < p.ncell;
-  const long e = a.cells ? (active ? (long)a.cells[li] : 0) : li;
+  const bool ranged = !a.cells && a.ncells > 0;
+  const bool active = (a.cells || ranged) ? li < a.ncells : li < p.ncell;
+  const long e = a.cells ? (active ? (long)a.cells[li] : 0) : (ranged ? (long)a.cell0 + li : li);
   const long ee = active ? e : 0;
   int ix[3];
   {
@@ -448,7 +449,7 @@ static int conv_launch_n(pdg_context *ctx, const ApplyArgs<T> &a) {
                                  dbl ? (const T *)ctx->tab64 : (const T *)ctx->tab32);
   const T *rec = dbl ? (const T *)ctx->conv64 : (const T *)ctx->conv32;
   const T *tab = dbl ? (const T *)ctx->convtab64 : (const T *)ctx->convtab32;
-  const long work = a.cells ? a.ncells : ctx->ncell;
+  const long work = (a.cells || a.ncells > 0) ? a.ncells : ctx->ncell;
   if (work <= 0) return PDG_OK;
   const unsigned blocks = (unsigned)((work + C::CPB - 1) / C::CPB);
   k_conv<T, N><<<blocks, C::THREADS, smem, ctx->stream>>>(p, a, rec, tab);

@@ -96,6 +96,7 @@ struct ApplyArgs {
   const int *skip; // if non-null and *skip != 0 the launch does nothing
   const int *cells; // if non-null: only these cells (ncells of them) are computed
   int ncells;
+  int cell0;        // cells null and ncells > 0: the cell range [cell0, cell0 + ncells)
 };
 
 // One cell-block Jacobi preconditioner instance (per precision).
@@ -193,6 +194,9 @@ struct pdg_context {
 
   // staging buffers for host pointers
   double *stage_a, *stage_b;
+  // host-buffer applies pipelined over slabs: copy streams and their events
+  cudaStream_t pipe_h2d, pipe_d2h, pipe_k2;
+  cudaEvent_t pipe_ev[35];
 
   // solver work vectors (lazily allocated)
   double *w64[10];
@@ -211,6 +215,7 @@ template <typename T>
 int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c,
                  const T *tab);
 int launch_rhs(pdg_context *ctx);
+int prepare_apply64(pdg_context *ctx);
 // 3D FP32 operator with staged neighbour runs (all cells, coupled or diag_only)
 int launch_apply32_3d(pdg_context *ctx, const ApplyArgs<float> &a, const OpParams<float> &p,
                       const float *rec);

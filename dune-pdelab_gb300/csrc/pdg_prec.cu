@@ -149,6 +149,16 @@ struct PCfg {
   static constexpr int PER_CELL = 2 * NB + D * N2 + D * N;
 };
 
+// Padding (elements) of the per-cell shared region of k_fdm_apply that puts
+// the cells sharing a warp on different shared-memory banks (chosen by
+// counting the wavefronts of the kernel's shared accesses per padding).
+template <typename T, int D, int N>
+constexpr int fdm_pad() {
+  if (D != 3) return 0;
+  if (sizeof(T) == 4) return N == 2 ? 2 : N == 3 ? 15 : N == 4 ? 20 : N == 5 ? 5 : 0;
+  return N == 2 ? 2 : N == 3 ? 2 : N == 5 ? 5 : 0;
+}
+
 template <typename T, int D, int N>
 __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
     k_fdm_apply(long ncell, const T *__restrict__ Q, const T *__restrict__ L,
@@ -159,7 +169,7 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
   if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int t = threadIdx.x, cs = t / TPC, l = t - cs * TPC;
-  T *S0 = reinterpret_cast<T *>(smem_raw) + cs * C::PER_CELL;
+  T *S0 = reinterpret_cast<T *>(smem_raw) + cs * (C::PER_CELL + fdm_pad<T, D, N>());
   T *S1 = S0 + NB;
   T *Qs = S1 + NB;       // [D][N2]
   T *Ls = Qs + D * N2;   // [D][N]
@@ -563,7 +573,7 @@ template <typename T, int D, int N>
 static int fdm_apply_dn(pdg_context *ctx, const T *d, T *v, const int *skip, const int *cells,
                         int ncells, T scale) {
   using C = PCfg<D, N>;
-  const size_t smem = sizeof(T) * C::CPB * C::PER_CELL;
+  const size_t smem = sizeof(T) * C::CPB * (C::PER_CELL + fdm_pad<T, D, N>());
   const long work = cells ? ncells : ctx->ncell;
   if (work <= 0) return PDG_OK;
   const unsigned blocks = (unsigned)((work + C::CPB - 1) / C::CPB);
