@@ -47,6 +47,101 @@ static double dlag(int k, int i, double x) {
     }
   return r;
 }
+
+// The nodal basis the kernels work in: Lagrange polynomials on the Gauss-
+// Lobatto points for PDG_BASIS_LOBATTO (GaussLobattoLagrangePolynomials::p /
+// dp, finiteelement/qkdglobatto.hh:69-107), else on the equidistant nodes
+// (the Legendre basis maps onto the latter, pdg_basis.cu).
+static double nlag(const pdg_context *c, int i, double x) {
+  if (c->basis != PDG_BASIS_LOBATTO) return lag(c->k, i, x);
+  const double *xi = c->nodes;
+  double r = 1.0;
+  for (int j = 0; j <= c->k; j++)
+    if (j != i) r *= (x - xi[j]) / (xi[i] - xi[j]);
+  return r;
+}
+static double ndlag(const pdg_context *c, int i, double x) {
+  if (c->basis != PDG_BASIS_LOBATTO) return dlag(c->k, i, x);
+  const double *xi = c->nodes;
+  double r = 0.0;
+  for (int j = 0; j <= c->k; j++)
+    if (j != i) {
+      double prod = 1.0 / (xi[i] - xi[j]);
+      for (int l = 0; l <= c->k; l++)
+        if (l != i && l != j) prod *= (x - xi[l]) / (xi[i] - xi[l]);
+      r += prod;
+    }
+  return r;
+}
+
+// Gauss-Lobatto points on [0,1], ascending (the rule of the Lobatto basis,
+// qkdglobatto.hh:27-67): the end points and the roots of P'_n, n = m-1, by
+// Newton's method on P'_n with P''_n from Legendre's equation
+// (1-z^2) P''_n = 2 z P'_n - n(n+1) P_n, started at cos(pi j/n).
+static void gauss_lobatto_points(int m, double *x) {
+  const int n = m - 1;
+  for (int j = 0; j <= n; j++) {
+    long double z = cosl(3.14159265358979323846264338327950288L * j / n);
+    if (j > 0 && j < n) {
+      for (int it = 0; it < 100; it++) {
+        long double p0 = 1.0L, p1 = 0.0L;
+        for (int i = 1; i <= n; i++) {
+          const long double p2 = p1;
+          p1 = p0;
+          p0 = ((2.0L * i - 1.0L) * z * p1 - (i - 1.0L) * p2) / i;
+        }
+        const long double dp = n * (p1 - z * p0) / (1.0L - z * z);
+        const long double d2 = (2.0L * z * dp - n * (n + 1.0L) * p0) / (1.0L - z * z);
+        const long double dz = dp / d2;
+        z -= dz;
+        if (fabsl(dz) < 1e-19L) break;
+      }
+    }
+    x[j] = (double)((1.0L - z) * 0.5L);
+  }
+  x[0] = 0.0;
+  x[n] = 1.0;
+}
+
+// Legendre polynomials on [0,1] at x (DGLegendreLocalBasis's 1D factors,
+// qkdglegendre.hh:80-88): P_0 = 1, P_1 = 2x-1, recurrence in n.
+static void legendre01(int k, double x, double *v) {
+  v[0] = 1.0;
+  if (k >= 1) v[1] = 2 * x - 1;
+  for (int n = 2; n <= k; n++)
+    v[n] = ((2 * n - 1) * (2 * x - 1) * v[n - 1] - (n - 1) * v[n - 2]) / n;
+}
+
+// T[j][i] = P_i(j/k) and its inverse (Gauss-Jordan with partial pivoting),
+// row-major, into t[0 .. N*N) and t[N*N .. 2 N*N)
+static void legendre_change_of_basis(int k, double *t) {
+  const int N = k + 1;
+  double a[kMaxN1][2 * kMaxN1];
+  for (int j = 0; j < N; j++) {
+    double v[kMaxN1];
+    legendre01(k, (double)j / k, v);
+    for (int i = 0; i < N; i++) {
+      t[j * N + i] = v[i];
+      a[j][i] = v[i];
+      a[j][N + i] = i == j ? 1.0 : 0.0;
+    }
+  }
+  for (int c = 0; c < N; c++) {
+    int piv = c;
+    for (int r = c + 1; r < N; r++)
+      if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+    for (int q = 0; q < 2 * N; q++) std::swap(a[c][q], a[piv][q]);
+    const double inv = 1.0 / a[c][c];
+    for (int q = 0; q < 2 * N; q++) a[c][q] *= inv;
+    for (int r = 0; r < N; r++)
+      if (r != c) {
+        const double f = a[r][c];
+        for (int q = 0; q < 2 * N; q++) a[r][q] -= f * a[c][q];
+      }
+  }
+  for (int j = 0; j < N; j++)
+    for (int i = 0; i < N; i++) t[N * N + j * N + i] = a[j][N + i];
+}
 // Gauss-Legendre points/weights on [0,1] (Newton on P_m, long double).
 static void gauss_legendre(int m, double *x, double *w) {
   for (int i = 0; i < m; i++) {
@@ -76,18 +171,18 @@ static void gauss_legendre(int m, double *x, double *w) {
   }
 }
 
-double lagrange_derivative(int k, int i, double x) { return dlag(k, i, x); }
+double lagrange_derivative(const pdg_context *ctx, int i, double x) { return ndlag(ctx, i, x); }
 
 RhsTables make_rhs_tables(const pdg_context *ctx) {
   RhsTables t;
   std::memset(&t, 0, sizeof(t));
-  const int N = ctx->N, k = ctx->k;
+  const int N = ctx->N;
   gauss_legendre(N, t.x, t.w);
   for (int q = 0; q < N; q++)
-    for (int a = 0; a < N; a++) t.B[q * N + a] = lag(k, a, t.x[q]);
+    for (int a = 0; a < N; a++) t.B[q * N + a] = nlag(ctx, a, t.x[q]);
   for (int a = 0; a < N; a++) {
-    t.d0[a] = dlag(k, a, 0.0);
-    t.d1[a] = dlag(k, a, 1.0);
+    t.d0[a] = ndlag(ctx, a, 0.0);
+    t.d1[a] = ndlag(ctx, a, 1.0);
   }
   return t;
 }
@@ -146,6 +241,14 @@ static int prec_op(pdg_context *ctx, const T *d, T *v, int transpose, const int 
 static int ensure_r0(pdg_context *ctx) {
   if (!ctx->r0_valid) {
     PDG_TRY(launch_rhs(ctx));
+    if (ctx->basis == PDG_BASIS_LEGENDRE) {
+      // R(0) is a residual: r_L = T^T r_nodal per cell (the K-proportional
+      // part kept for the log-K gradient stays nodal, it meets nodal lambda)
+      PDG_TRY(basis_change<double>(ctx, 0, 1, ctx->r0, ctx->legw64[0], 1.0, 0, nullptr,
+                                   nullptr));
+      PDG_CUDA_TRY(cudaMemcpyAsync(ctx->r0, ctx->legw64[0], sizeof(double) * ctx->ndof,
+                                   cudaMemcpyDeviceToDevice, ctx->stream));
+    }
     ctx->r0_valid = 1;
   }
   return PDG_OK;
@@ -722,6 +825,8 @@ int pdg_create(const pdg_config *cfg, pdg_context **out) {
     if (b != PDG_BC_DIRICHLET && b != PDG_BC_NEUMANN && b != PDG_BC_OUTFLOW && b != PDG_BC_NONE)
       return set_error(PDG_EINVAL, "bad boundary type");
   }
+  if (cfg->basis < PDG_BASIS_LAGRANGE || cfg->basis > PDG_BASIS_LOBATTO)
+    return set_error(PDG_EINVAL, "bad basis");
   PDG_CUDA_TRY(cudaSetDevice(cfg->device));
   pdg_context *c = new pdg_context;
   std::memset(c, 0, sizeof(*c));
@@ -731,6 +836,10 @@ int pdg_create(const pdg_config *cfg, pdg_context **out) {
   c->dim = cfg->dim;
   c->k = cfg->degree;
   c->N = c->k + 1;
+  c->basis = cfg->basis;
+  if (c->basis == PDG_BASIS_LOBATTO) gauss_lobatto_points(c->N, c->nodes);
+  else
+    for (int j = 0; j < c->N; j++) c->nodes[j] = (double)j / c->k;
   c->nb = 1;
   c->nqv = 1;
   c->nqf = 1;
@@ -770,8 +879,8 @@ int pdg_create(const pdg_config *cfg, pdg_context **out) {
     for (int a = 0; a < N; a++) {
       double m = 0.0, s = 0.0;
       for (int q = 0; q < N; q++) {
-        m += t.w[q] * lag(c->k, i, t.x[q]) * lag(c->k, a, t.x[q]);
-        s += t.w[q] * dlag(c->k, i, t.x[q]) * dlag(c->k, a, t.x[q]);
+        m += t.w[q] * nlag(c, i, t.x[q]) * nlag(c, a, t.x[q]);
+        s += t.w[q] * ndlag(c, i, t.x[q]) * ndlag(c, a, t.x[q]);
       }
       tab[i * N + a] = m;
       tab[N * N + i * N + a] = s;
@@ -799,6 +908,20 @@ int pdg_create(const pdg_config *cfg, pdg_context **out) {
   cudaMemcpy(c->K32, ones32.data(), sizeof(float) * c->ncell, cudaMemcpyHostToDevice);
   cudaMemset(c->d_flag, 0, sizeof(int) * F_COUNT);
   cudaMemset(c->red_out, 0, sizeof(double) * S_COUNT);
+  if (c->basis == PDG_BASIS_LEGENDRE) {
+    double lt[2 * kMaxN1 * kMaxN1];
+    legendre_change_of_basis(c->k, lt);
+    std::vector<float> lt32(lt, lt + 2 * N * N);
+    if (cudaMalloc(&c->leg64, sizeof(double) * 2 * N * N) != cudaSuccess ||
+        cudaMalloc(&c->leg32, sizeof(float) * 2 * N * N) != cudaSuccess ||
+        cudaMalloc(&c->legw64[0], sizeof(double) * c->ndof) != cudaSuccess ||
+        cudaMalloc(&c->legw64[1], sizeof(double) * c->ndof) != cudaSuccess ||
+        cudaMalloc(&c->legw32[0], sizeof(float) * c->ndof) != cudaSuccess ||
+        cudaMalloc(&c->legw32[1], sizeof(float) * c->ndof) != cudaSuccess)
+      return fail(set_error(PDG_ECUDA, "device allocation failed"));
+    cudaMemcpy(c->leg64, lt, sizeof(double) * 2 * N * N, cudaMemcpyHostToDevice);
+    cudaMemcpy(c->leg32, lt32.data(), sizeof(float) * 2 * N * N, cudaMemcpyHostToDevice);
+  }
   if (cudaDeviceSynchronize() != cudaSuccess) return fail(set_error(PDG_ECUDA, "init failed"));
   c->r0_valid = 0;
   *out = c;
@@ -822,7 +945,8 @@ int pdg_destroy(pdg_context *c) {
                   c->stage_a, c->stage_b, c->rec64, c->conv64, c->conv32, c->convtab64,
                   c->convtab32, c->gm_V32, c->gm_V64, c->gm_F64, c->gm_partial, c->gm_coef,
                   c->A64, c->rec32, c->nlW64, c->nlW32, c->nlB64, c->nlB32,
-                  c->massW, c->massWi, c->massB, c->massBiT, c->cstage64, c->cstage32};
+                  c->massW, c->massWi, c->massB, c->massBiT, c->cstage64, c->cstage32,
+                  c->leg64, c->leg32, c->legw64[0], c->legw64[1], c->legw32[0], c->legw32[1]};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 10; i++)
@@ -1097,7 +1221,8 @@ static int apply_entry(pdg_context *ctx, const double *x, double *y, double alph
   if (hx || hy) PDG_TRY(ensure_stage(ctx));
   long pps = 0;
   const int nslab = (hx || hy) ? pipe_slabs(ctx, &pps) : 1;
-  if (nslab > 1 && !ctx->use_matrix && !ctx->ops32 && ctx->nl_deg == 0)
+  if (nslab > 1 && !ctx->use_matrix && !ctx->ops32 && ctx->nl_deg == 0 &&
+      ctx->basis != PDG_BASIS_LEGENDRE)
     return apply_pipelined(ctx, x, y, hx ? ctx->stage_a : x, hy ? ctx->stage_b : y, hx, hy,
                            with_r0 ? ctx->r0 : nullptr, alpha, acc, transpose, nslab, pps);
   Staged<double> sx, sy;
@@ -1239,6 +1364,8 @@ static int check_opts(const pdg_solver_options *o) {
 int pdg_set_nonlinearity(pdg_context *ctx, int degree, const double *coef) {
   PDG_CHECK_CTX(ctx);
   if (coef && (degree < 1 || degree > 4)) return set_error(PDG_EINVAL, "degree must be 1..4");
+  if (coef && ctx->basis == PDG_BASIS_LEGENDRE)
+    return set_error(PDG_EUNSUPPORTED, "the nonlinear volume term needs a nodal basis");
   ctx->nl_deg = coef ? degree : 0;
   for (int m = 0; m < 5; m++) ctx->nl_coef[m] = (coef && m <= degree) ? coef[m] : 0.0;
   ctx->nl_point = 0;

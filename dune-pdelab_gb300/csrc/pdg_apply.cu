@@ -518,9 +518,34 @@ static int ensure_record(pdg_context *ctx) {
 // launches are spread over several streams)
 int prepare_apply64(pdg_context *ctx) { return ensure_record(ctx); }
 
+// Legendre basis: y = acc*y + alpha T^T J_nodal T x + add (pdg_basis.cu)
+template <typename T>
+static int launch_apply_modal(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c,
+                              const T *tab) {
+  if (a.cells || a.ncells > 0)
+    return set_error(PDG_EUNSUPPORTED, "cell subsets of the operator (block SOR) need a nodal basis");
+  const bool dbl = std::is_same<T, double>::value;
+  T *w0 = dbl ? (T *)ctx->legw64[0] : (T *)ctx->legw32[0];
+  T *w1 = dbl ? (T *)ctx->legw64[1] : (T *)ctx->legw32[1];
+  PDG_TRY(basis_change<T>(ctx, 0, 0, a.x, w0, T(1), 0, nullptr, a.skip));
+  ApplyArgs<T> b = a;
+  b.x = w0;
+  b.y = w1;
+  b.add = nullptr;
+  b.alpha = T(1);
+  b.accumulate = 0;
+  ctx->leg_nodal = 1;
+  const int st = launch_apply<T>(ctx, b, K, c, tab);
+  ctx->leg_nodal = 0;
+  PDG_TRY(st);
+  return basis_change<T>(ctx, 0, 1, w1, a.y, a.alpha, a.accumulate, a.add, a.skip);
+}
+
 template <typename T>
 int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c,
                  const T *tab) {
+  if (ctx->basis == PDG_BASIS_LEGENDRE && !ctx->leg_nodal)
+    return launch_apply_modal<T>(ctx, a, K, c, tab);
   OpParams<T> p = make_params<T>(ctx, K, c, tab);
   if constexpr (std::is_same<T, float>::value) {
     // the staged kernel wins for N <= 3 (Q1, Q2: 78 vs 126 us at 64^3 Q2);

@@ -349,17 +349,18 @@ static EdgeTab make_edge_tab_uncached(const pdg_context *ctx) {
   return t;
 }
 
-// the tables depend on the degree only: built once per degree
+// the tables depend on the degree and the nodal basis only: built once each
 static const EdgeTab &edge_tab(const pdg_context *ctx) {
   static std::mutex mu;
-  static EdgeTab tabs[kMaxN1 + 1];
-  static bool ready[kMaxN1 + 1] = {};
+  static EdgeTab tabs[3][kMaxN1 + 1];
+  static bool ready[3][kMaxN1 + 1] = {};
   std::lock_guard<std::mutex> lock(mu);
-  if (!ready[ctx->N]) {
-    tabs[ctx->N] = make_edge_tab_uncached(ctx);
-    ready[ctx->N] = true;
+  const int b = ctx->basis;
+  if (!ready[b][ctx->N]) {
+    tabs[b][ctx->N] = make_edge_tab_uncached(ctx);
+    ready[b][ctx->N] = true;
   }
-  return tabs[ctx->N];
+  return tabs[b][ctx->N];
 }
 
 template <int N>

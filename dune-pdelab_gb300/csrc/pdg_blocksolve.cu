@@ -238,6 +238,8 @@ template int bj_iterative_apply<float>(pdg_context *, const float *, float *, in
 // ---------------------------------------------------------------------------
 
 int sor_setup(pdg_context *ctx) {
+  if (ctx->basis == PDG_BASIS_LEGENDRE)
+    return set_error(PDG_EUNSUPPORTED, "block SOR needs a nodal basis");
   if (ctx->hp_cells) return PDG_OK;
   const int d = ctx->dim;
   const long nx = ctx->cfg.cells[0], ny = ctx->cfg.cells[1];

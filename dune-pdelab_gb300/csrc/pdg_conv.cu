@@ -399,7 +399,7 @@ static int conv_setup_n(pdg_context *ctx) {
     for (int q = 0; q < N; q++)
       for (int aa = 0; aa < N; aa++) {
         h[q * N + aa] = tb.B[q * N + aa];
-        h[N * N + q * N + aa] = lagrange_derivative(ctx->k, aa, tb.x[q]);
+        h[N * N + q * N + aa] = lagrange_derivative(ctx, aa, tb.x[q]);
       }
     for (int i = 0; i < 2 * N * N; i++) h32[i] = (float)h[i];
     PDG_CUDA_TRY(cudaMalloc(&ctx->convtab64, sizeof(h)));

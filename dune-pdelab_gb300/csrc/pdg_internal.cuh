@@ -192,6 +192,18 @@ struct pdg_context {
   double *red_out;         // [16] device results
   double *h_red;           // pinned host mirror [16]
 
+  // local basis (PDG_BASIS_*).  Nodal bases: the k+1 nodes on [0,1].  The
+  // modal (Legendre) basis runs the nodal kernels between changes of basis:
+  // leg64/leg32 hold T[j][i] = P_i(j/k) and T^{-1} (2 N*N values); legw*
+  // are nodal work vectors; leg_nodal marks a launch already in nodal form.
+  int basis;
+  double nodes[8];
+  double *leg64;
+  float *leg32;
+  double *legw64[2];
+  float *legw32[2];
+  int leg_nodal;
+
   // staging buffers for host pointers
   double *stage_a, *stage_b;
   // host-buffer applies pipelined over slabs: copy streams and their events
@@ -216,6 +228,11 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
                  const T *tab);
 int launch_rhs(pdg_context *ctx);
 int prepare_apply64(pdg_context *ctx);
+// per-cell change of basis out = acc*out + alpha (M (x) M (x) M) in + add with
+// M = T (which 0) or T^{-1} (which 1), transposed if `transpose`
+template <typename T>
+int basis_change(pdg_context *ctx, int which, int transpose, const T *in, T *out, T alpha,
+                 int acc, const T *add, const int *skip);
 // 3D FP32 operator with staged neighbour runs (all cells, coupled or diag_only)
 int launch_apply32_3d(pdg_context *ctx, const ApplyArgs<float> &a, const OpParams<float> &p,
                       const float *rec);
@@ -255,7 +272,7 @@ struct RhsTables {
 };
 RhsTables make_rhs_tables(const pdg_context *ctx);
 double *rhs_r0K(pdg_context *ctx, bool alloc);
-double lagrange_derivative(int k, int i, double x);
+double lagrange_derivative(const pdg_context *ctx, int i, double x);
 
 // nonlinear volume term: linearization point, residual part, Jacobian part
 int nl_set_point(pdg_context *ctx, const double *x);

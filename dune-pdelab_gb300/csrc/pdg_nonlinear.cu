@@ -401,6 +401,17 @@ static int ensure_mass(pdg_context *ctx) {
 int mass_apply(pdg_context *ctx, const double *x, double *y, double alpha, int accumulate,
                int inverse) {
   PDG_TRY(ensure_mass(ctx));
+  if (ctx->basis == PDG_BASIS_LEGENDRE) {
+    // M_L = T^T M T and M_L^{-1} = T^{-1} M^{-1} T^{-T} (pdg_basis.cu)
+    double *w0 = ctx->legw64[0], *w1 = ctx->legw64[1];
+    PDG_TRY(basis_change<double>(ctx, inverse, inverse, x, w0, 1.0, 0, nullptr, nullptr));
+    PDG_TRY(vec_fill<double>(ctx, ctx->ndof, w1, 0.0));
+    ApplyArgs<double> a{w0, w1, nullptr, 1.0, 1, 0, 0, nullptr};
+    PDG_TRY(inverse ? weighted_apply<double>(ctx, ctx->massWi, ctx->massBiT, a)
+                    : weighted_apply<double>(ctx, ctx->massW, ctx->massB, a));
+    return basis_change<double>(ctx, inverse, !inverse, w1, y, alpha, accumulate, nullptr,
+                                nullptr);
+  }
   if (!accumulate) PDG_TRY(vec_fill<double>(ctx, ctx->ndof, y, 0.0));
   ApplyArgs<double> a{x, y, nullptr, alpha, 1, 0, 0, nullptr};
   return inverse ? weighted_apply<double>(ctx, ctx->massWi, ctx->massBiT, a)

@@ -603,6 +603,22 @@ __global__ void k_scale_cells(long ncell, int nb, const T *__restrict__ d, T *__
 // v_e = scale * D_e^{-1} d_e (D_e^{-T} with `transpose`) on the listed cells
 // (all cells if `cells` is null), with the block solver of the instance.
 template <typename T>
+static int fdm_dispatch(pdg_context *ctx, const T *d, T *v, const int *skip, const int *cells,
+                        int ncells, T scale) {
+  switch (ctx->dim * 10 + ctx->k) {
+    case 21: return fdm_apply_dn<T, 2, 2>(ctx, d, v, skip, cells, ncells, scale);
+    case 22: return fdm_apply_dn<T, 2, 3>(ctx, d, v, skip, cells, ncells, scale);
+    case 23: return fdm_apply_dn<T, 2, 4>(ctx, d, v, skip, cells, ncells, scale);
+    case 24: return fdm_apply_dn<T, 2, 5>(ctx, d, v, skip, cells, ncells, scale);
+    case 31: return fdm_apply_dn<T, 3, 2>(ctx, d, v, skip, cells, ncells, scale);
+    case 32: return fdm_apply_dn<T, 3, 3>(ctx, d, v, skip, cells, ncells, scale);
+    case 33: return fdm_apply_dn<T, 3, 4>(ctx, d, v, skip, cells, ncells, scale);
+    case 34: return fdm_apply_dn<T, 3, 5>(ctx, d, v, skip, cells, ncells, scale);
+    default: return set_error(PDG_EUNSUPPORTED, "dim/degree not compiled in");
+  }
+}
+
+template <typename T>
 int block_solve(pdg_context *ctx, const T *d, T *v, int transpose, const int *skip,
                 const int *cells, int ncells, T scale) {
   const int pi = std::is_same<T, double>::value ? PDG_F64 : PDG_F32;
@@ -628,18 +644,18 @@ int block_solve(pdg_context *ctx, const T *d, T *v, int transpose, const int *sk
   }
   if (base == PDG_PREC_BJ_ITERATIVE)
     return bj_iterative_apply<T>(ctx, d, v, transpose, skip, cells, ncells, scale);
-  // FDM blocks are symmetric: D^{-T} = D^{-1}
-  switch (ctx->dim * 10 + ctx->k) {
-    case 21: return fdm_apply_dn<T, 2, 2>(ctx, d, v, skip, cells, ncells, scale);
-    case 22: return fdm_apply_dn<T, 2, 3>(ctx, d, v, skip, cells, ncells, scale);
-    case 23: return fdm_apply_dn<T, 2, 4>(ctx, d, v, skip, cells, ncells, scale);
-    case 24: return fdm_apply_dn<T, 2, 5>(ctx, d, v, skip, cells, ncells, scale);
-    case 31: return fdm_apply_dn<T, 3, 2>(ctx, d, v, skip, cells, ncells, scale);
-    case 32: return fdm_apply_dn<T, 3, 3>(ctx, d, v, skip, cells, ncells, scale);
-    case 33: return fdm_apply_dn<T, 3, 4>(ctx, d, v, skip, cells, ncells, scale);
-    case 34: return fdm_apply_dn<T, 3, 5>(ctx, d, v, skip, cells, ncells, scale);
-    default: return set_error(PDG_EUNSUPPORTED, "dim/degree not compiled in");
+  if (ctx->basis == PDG_BASIS_LEGENDRE) {
+    // the FDM factors invert the nodal block: D_L^{-1} = T^{-1} D^{-1} T^{-T}
+    if (cells) return set_error(PDG_EUNSUPPORTED, "block SOR needs a nodal basis");
+    const bool dbl = std::is_same<T, double>::value;
+    T *w0 = dbl ? (T *)ctx->legw64[0] : (T *)ctx->legw32[0];
+    T *w1 = dbl ? (T *)ctx->legw64[1] : (T *)ctx->legw32[1];
+    PDG_TRY(basis_change<T>(ctx, 1, 1, d, w0, T(1), 0, nullptr, skip));
+    PDG_TRY(fdm_dispatch<T>(ctx, w0, w1, skip, nullptr, 0, T(1)));
+    return basis_change<T>(ctx, 1, 0, w1, v, scale, 0, nullptr, skip);
   }
+  // FDM blocks are symmetric: D^{-T} = D^{-1}
+  return fdm_dispatch<T>(ctx, d, v, skip, cells, ncells, scale);
 }
 
 template <typename T>

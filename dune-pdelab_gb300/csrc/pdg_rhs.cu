@@ -368,6 +368,13 @@ int launch_rhs(pdg_context *ctx) {
 }
 
 int launch_grad_logK(pdg_context *ctx, const double *u, const double *lam, double *g) {
+  if (ctx->basis == PDG_BASIS_LEGENDRE) {
+    // lambda_L^T dA_L u_L = (T lambda_L)^T dA (T u_L): nodal coefficients
+    PDG_TRY(basis_change<double>(ctx, 0, 0, u, ctx->legw64[0], 1.0, 0, nullptr, nullptr));
+    PDG_TRY(basis_change<double>(ctx, 0, 0, lam, ctx->legw64[1], 1.0, 0, nullptr, nullptr));
+    u = ctx->legw64[0];
+    lam = ctx->legw64[1];
+  }
   OpParams<double> p = make_params<double>(ctx, ctx->K64, ctx->c64, ctx->tab64);
   const double *r0K = rhs_r0K(ctx, false);
   const unsigned blocks = (unsigned)((ctx->ncell + 63) / 64);
@@ -380,6 +387,10 @@ int launch_grad_logK(pdg_context *ctx, const double *u, const double *lam, doubl
 }
 
 int launch_grad_source(pdg_context *ctx, const double *lam, double *g) {
+  if (ctx->basis == PDG_BASIS_LEGENDRE) {
+    PDG_TRY(basis_change<double>(ctx, 0, 0, lam, ctx->legw64[1], 1.0, 0, nullptr, nullptr));
+    lam = ctx->legw64[1];
+  }
   RhsTables tb = make_rhs_tables(ctx);
   double detJ = 1.0;
   for (int j = 0; j < ctx->dim; j++) detJ *= ctx->h[j];

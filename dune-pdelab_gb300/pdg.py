@@ -41,6 +41,7 @@ CG, BICGSTAB, GMRES = 0, 1, 2
 PREC_NONE, PREC_BJ_FDM, PREC_BJ_DENSE, PREC_BJ_ITERATIVE = 0, 1, 2, 3
 PREC_SOR = 16          # OR-ed with a block kind: one block-SOR sweep
 F64, F32 = 0, 1
+LAGRANGE, LEGENDRE, LOBATTO = 0, 1, 2     # QkDGBasisPolynomial
 
 
 class PDGError(RuntimeError):
@@ -52,7 +53,8 @@ class PDGError(RuntimeError):
 class Config(C.Structure):
     _fields_ = [("dim", C.c_int), ("degree", C.c_int), ("cells", C.c_int * 3),
                 ("extent", C.c_double * 3), ("method", C.c_int), ("weights", C.c_int),
-                ("alpha", C.c_double), ("bctype", C.c_int * 6), ("device", C.c_int)]
+                ("alpha", C.c_double), ("bctype", C.c_int * 6), ("device", C.c_int),
+                ("basis", C.c_int)]
 
 
 class SolverOptions(C.Structure):
@@ -257,7 +259,7 @@ class GridOperator:
     + GridOperator of the reference, as a single context."""
 
     def __init__(self, dim, degree, cells, extent=None, method=SIPG, weights=WEIGHTS_ON,
-                 alpha=1.0, bctype=None, device=0):
+                 alpha=1.0, bctype=None, device=0, basis=LAGRANGE):
         cfg = Config()
         cfg.dim, cfg.degree = dim, degree
         cells = list(cells) + [1] * (3 - len(cells))
@@ -271,8 +273,9 @@ class GridOperator:
         for j in range(6):
             cfg.bctype[j] = bct[j] if j < len(bct) else BC_DIRICHLET
         cfg.device = device
+        cfg.basis = basis
         self.cfg = cfg
-        self.dim, self.degree = dim, degree
+        self.dim, self.degree, self.basis = dim, degree, basis
         self._h = _vp()
         _check(load().pdg_create(C.byref(cfg), C.byref(self._h)))
         nc, nb, nd, nq, nbp = C.c_long(), C.c_int(), C.c_long(), C.c_int(), C.c_long()

@@ -95,6 +95,14 @@ typedef struct pdg_prec_options {
 } pdg_prec_options;
 /* precisions */
 enum { PDG_F64 = 0, PDG_F32 = 1 };
+/* local DG bases: QkDGBasisPolynomial (finiteelementmap/qkdg.hh:18).
+   LAGRANGE: equidistant nodes j/k (qkdglagrange.hh:55-79); LEGENDRE:
+   Legendre polynomials on [0,1] (qkdglegendre.hh:76-113), vectors hold
+   modal coefficients; LOBATTO: Lagrange polynomials on the Gauss-Lobatto
+   points, ascending (qkdglobatto.hh:21-117).  With LEGENDRE the nonlinear
+   volume term, block SOR and explicit one-step stages are not available
+   (PDG_EUNSUPPORTED). */
+enum { PDG_BASIS_LAGRANGE = 0, PDG_BASIS_LEGENDRE = 1, PDG_BASIS_LOBATTO = 2 };
 
 typedef struct pdg_context pdg_context;
 
@@ -112,6 +120,8 @@ typedef struct pdg_config {
   double alpha;            /* penalty factor */
   int bctype[6];           /* boundary type per side -x,+x,-y,+y,-z,+z */
   int device;              /* CUDA device ordinal */
+  int basis;               /* PDG_BASIS_*: the QkDGBasisPolynomial of the
+                              QkDGLocalFiniteElementMap */
 } pdg_config;
 
 /* Solver options: ISTLBackend_SEQ_MatrixFree_Base(go, precgo, maxiter,

@@ -65,6 +65,7 @@ struct Config : pdg_config {
     alpha = 1.0;   // ConvectionDiffusionDG default (convectiondiffusiondg.hh:87-91)
     for (int &b : bctype) b = PDG_BC_DIRICHLET;
     device = 0;
+    basis = PDG_BASIS_LAGRANGE;
   }
 };
 

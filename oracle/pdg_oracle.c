@@ -56,6 +56,116 @@ double pdgo_dlagrange(int k, int i, double x) {
   return result;
 }
 
+/* Gauss-Lobatto rule with m >= 2 points on [0,1], ascending (the rule the
+   Lobatto basis takes its nodes from, qkdglobatto.hh:27-67; dune-geometry's
+   QuadratureType::GaussLobatto, restated): the end points and the roots of
+   P'_{m-1}, found by Newton iteration on P'_n with P''_n from Legendre's
+   equation (1-z^2) P''_n = 2 z P'_n - n(n+1) P_n, started at the
+   Chebyshev-Gauss-Lobatto points cos(pi j/n); weights 2/(n(n+1) P_n(z)^2)
+   on [-1,1] (Abramowitz & Stegun 25.4.32), halved on [0,1]. */
+static void legendre_pn(int n, long double z, long double *pn, long double *pn1) {
+  long double p0 = 1.0L, p1 = 0.0L;
+  for (int j = 1; j <= n; j++) {
+    long double p2 = p1;
+    p1 = p0;
+    p0 = ((2.0L * j - 1.0L) * z * p1 - (j - 1.0L) * p2) / j;
+  }
+  *pn = p0;
+  *pn1 = p1;
+}
+
+int pdgo_gauss_lobatto(int m, double *x, double *w) {
+  if (m < 2 || m > 32) return PDGO_EARG;
+  const int n = m - 1;
+  const long double pi = 3.14159265358979323846264338327950288L;
+  for (int j = 0; j <= n; j++) {
+    long double z = cosl(pi * j / n);
+    if (j > 0 && j < n) {
+      for (int it = 0; it < 100; it++) {
+        long double pn, pn1;
+        legendre_pn(n, z, &pn, &pn1);
+        const long double dp = n * (pn1 - z * pn) / (1.0L - z * z);
+        const long double d2 = (2.0L * z * dp - n * (n + 1.0L) * pn) / (1.0L - z * z);
+        const long double dz = dp / d2;
+        z -= dz;
+        if (fabsl(dz) < 1e-19L) break;
+      }
+    }
+    long double pn, pn1;
+    legendre_pn(n, z, &pn, &pn1);
+    x[j] = (double)((1.0L - z) * 0.5L);
+    w[j] = (double)(1.0L / (n * (n + 1.0L) * pn * pn));
+  }
+  return PDGO_OK;
+}
+
+/* DGLegendreLocalBasis 1D factor (qkdglegendre.hh:80-113): Legendre
+   polynomials on [0,1], P_0 = 1, P_1 = 2x-1,
+   P_n = ((2n-1)(2x-1) P_{n-1} - (n-1) P_{n-2}) / n,
+   P'_n = (2x-1) P'_{n-1} + 2n P_{n-1}. */
+static void legendre01(int k, double x, double *v, double *dv) {
+  v[0] = 1.0;
+  dv[0] = 0.0;
+  if (k >= 1) {
+    v[1] = 2 * x - 1;
+    dv[1] = 2.0;
+  }
+  for (int n = 2; n <= k; n++) {
+    v[n] = ((2 * n - 1) * (2 * x - 1) * v[n - 1] - (n - 1) * v[n - 2]) / n;
+    dv[n] = (2 * x - 1) * dv[n - 1] + 2 * n * v[n - 1];
+  }
+}
+
+/* GaussLobattoLagrangePolynomials (qkdglobatto.hh:21-117): Lagrange
+   polynomials on the k+1 Gauss-Lobatto points, ascending. */
+static const double *lobatto_nodes(int k) {
+  static double nodes[MAXK + 1][MAXN1];
+  static int ready[MAXK + 1];
+  if (!ready[k]) {
+    double w[MAXN1];
+    pdgo_gauss_lobatto(k + 1, nodes[k], w);
+    ready[k] = 1;
+  }
+  return nodes[k];
+}
+
+double pdgo_basis1d(int basis, int k, int i, double x) {
+  if (basis == PDGO_LEGENDRE) {
+    double v[MAXN1], dv[MAXN1];
+    legendre01(k, x, v, dv);
+    return v[i];
+  }
+  if (basis == PDGO_LOBATTO) {
+    const double *xi = lobatto_nodes(k);
+    double r = 1.0;
+    for (int j = 0; j <= k; j++)
+      if (j != i) r *= (x - xi[j]) / (xi[i] - xi[j]);
+    return r;
+  }
+  return pdgo_lagrange(k, i, x);
+}
+
+double pdgo_dbasis1d(int basis, int k, int i, double x) {
+  if (basis == PDGO_LEGENDRE) {
+    double v[MAXN1], dv[MAXN1];
+    legendre01(k, x, v, dv);
+    return dv[i];
+  }
+  if (basis == PDGO_LOBATTO) {
+    const double *xi = lobatto_nodes(k);
+    double r = 0.0;
+    for (int j = 0; j <= k; j++)
+      if (j != i) {
+        double prod = 1.0 / (xi[i] - xi[j]);
+        for (int l = 0; l <= k; l++)
+          if (l != i && l != j) prod *= (x - xi[l]) / (xi[i] - xi[l]);
+        r += prod;
+      }
+    return r;
+  }
+  return pdgo_dlagrange(k, i, x);
+}
+
 /* Gauss-Legendre rule with m points on [0,1] (dune-geometry's default
    QuadratureType::GaussLegendre, selected by quadratureRule() at
    common/quadraturerules.hh:110-120).  Newton on P_m in long double. */
@@ -118,20 +228,23 @@ static int get_theta(int method, double *theta) {
 }
 
 /* QkLocalBasis::evaluateFunction / evaluateJacobian
-   (qkdglagrange.hh:153-198) with multiindex (qkdglagrange.hh:118-128) */
-static void eval_basis(int d, int k, const double *xi, double *phi, double *js) {
+   (qkdglagrange.hh:153-198) with multiindex (qkdglagrange.hh:118-128);
+   DGLegendreLocalBasis (qkdglegendre.hh:236-328, same multiindex,
+   :63-73) and QkGLLocalBasis (qkdglobatto.hh:130-220) have the same tensor
+   structure with other 1D factors. */
+static void eval_basis(int basis, int d, int k, const double *xi, double *phi, double *js) {
   int n1 = k + 1, nb = 1;
   for (int j = 0; j < d; j++) nb *= n1;
   for (int i = 0; i < nb; i++) {
     int alpha[MAXD], t = i;
     for (int j = 0; j < d; j++) { alpha[j] = t % n1; t /= n1; }
     double v = 1.0;
-    for (int j = 0; j < d; j++) v *= pdgo_lagrange(k, alpha[j], xi[j]);
+    for (int j = 0; j < d; j++) v *= pdgo_basis1d(basis, k, alpha[j], xi[j]);
     phi[i] = v;
     for (int j = 0; j < d; j++) {
-      double g = pdgo_dlagrange(k, alpha[j], xi[j]);
+      double g = pdgo_dbasis1d(basis, k, alpha[j], xi[j]);
       for (int l = 0; l < d; l++)
-        if (l != j) g *= pdgo_lagrange(k, alpha[l], xi[l]);
+        if (l != j) g *= pdgo_basis1d(basis, k, alpha[l], xi[l]);
       js[i * d + j] = g;
     }
   }
@@ -173,7 +286,7 @@ static int tables_init(const pdgo_problem *p, tables *T) {
       w *= T->gw[a];
     }
     T->vw[q] = w;
-    eval_basis(d, k, &T->vloc[q * d], &T->vphi[q * nb], &T->vjs[q * nb * d]);
+    eval_basis(p->basis, d, k, &T->vloc[q * d], &T->vphi[q * nb], &T->vjs[q * nb * d]);
   }
   for (int f = 0; f < 2 * d; f++) {
     int dir = f / 2, hi = f % 2;
@@ -189,7 +302,7 @@ static int tables_init(const pdgo_problem *p, tables *T) {
         w *= T->gw[a];
       }
       T->fw[f * nqf + q] = w;
-      eval_basis(d, k, loc, &T->fphi[(f * nqf + q) * nb], &T->fjs[(f * nqf + q) * nb * d]);
+      eval_basis(p->basis, d, k, loc, &T->fphi[(f * nqf + q) * nb], &T->fjs[(f * nqf + q) * nb * d]);
     }
   }
   return PDGO_OK;
@@ -1657,7 +1770,7 @@ int pdgo_eval_points(const pdgo_problem *p, const double *u, int m, double *xyz,
       double wt = 1.0;
       int t = q;
       for (int j = 0; j < d; j++) { int a = t % m; t /= m; loc[j] = gx[a]; wt *= gw[a]; }
-      eval_basis(d, k, loc, phi, js);
+      eval_basis(p->basis, d, k, loc, phi, js);
       double s = 0.0;
       for (int i = 0; i < nb; i++) s += u[e * nb + i] * phi[i];
       val[e * mq + q] = s;

@@ -43,6 +43,8 @@ enum { PDGO_BC_DIRICHLET = 1, PDGO_BC_NEUMANN = -1, PDGO_BC_OUTFLOW = -2,
 enum { PDGO_NIPG = 0, PDGO_SIPG = 1, PDGO_IIPG = 2 };
 /* ConvectionDiffusionDGWeights::Type (convectiondiffusiondg.hh:34-37) */
 enum { PDGO_WEIGHTS_ON = 0, PDGO_WEIGHTS_OFF = 1 };
+/* QkDGBasisPolynomial (finiteelementmap/qkdg.hh:18) */
+enum { PDGO_LAGRANGE = 0, PDGO_LEGENDRE = 1, PDGO_LOBATTO = 2 };
 
 /* status codes */
 enum { PDGO_OK = 0, PDGO_EARG = 1, PDGO_EOUTFLOW_ON_INFLOW = 2,
@@ -75,6 +77,10 @@ typedef struct pdgo_problem {
   int nl_deg;
   double nl_coef[5];
   const double *xlin;
+  /* local basis of the QkDG space (QkDGBasisPolynomial,
+     finiteelementmap/qkdg.hh:18): PDGO_LAGRANGE (default), PDGO_LEGENDRE,
+     PDGO_LOBATTO */
+  int basis;
 } pdgo_problem;
 
 typedef struct pdgo_result {
@@ -102,6 +108,11 @@ int pdgo_gauss_legendre(int m, double *x, double *w);
 /* Lagrange basis p_i(x) / dp_i(x) of degree k at equidistant nodes */
 double pdgo_lagrange(int k, int i, double x);
 double pdgo_dlagrange(int k, int i, double x);
+/* 1D basis function i of degree k of the given kind and its derivative */
+double pdgo_basis1d(int basis, int k, int i, double x);
+double pdgo_dbasis1d(int basis, int k, int i, double x);
+/* Gauss-Lobatto points and weights on [0,1], m >= 2, ascending */
+int pdgo_gauss_lobatto(int m, double *x, double *w);
 
 /* coordinates of every volume quadrature point, [ncell][nq^d][dim] */
 int pdgo_volume_points(const pdgo_problem *p, double *xyz);

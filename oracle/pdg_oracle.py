@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libpdg_oracle.so")
 BC_DIRICHLET, BC_NEUMANN, BC_OUTFLOW, BC_NONE = 1, -1, -2, -3
 NIPG, SIPG, IIPG = 0, 1, 2
 WEIGHTS_ON, WEIGHTS_OFF = 0, 1
+LAGRANGE, LEGENDRE, LOBATTO = 0, 1, 2     # QkDGBasisPolynomial
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -31,6 +32,7 @@ class _Problem(C.Structure):
         ("K", _dp), ("c", _dp), ("nmodes", C.c_int), ("modes", _dp),
         ("fq", _dp), ("fc", _dp), ("gq", _dp), ("jq", _dp), ("oq", _dp),
         ("nl_deg", C.c_int), ("nl_coef", C.c_double * 5), ("xlin", _dp),
+        ("basis", C.c_int),
     ]
 
 
@@ -113,6 +115,9 @@ def lib():
             "pdgo_gauss_legendre": (C.c_int, [C.c_int, _dp, _dp]),
             "pdgo_lagrange": (C.c_double, [C.c_int, C.c_int, C.c_double]),
             "pdgo_dlagrange": (C.c_double, [C.c_int, C.c_int, C.c_double]),
+            "pdgo_basis1d": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_double]),
+            "pdgo_dbasis1d": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_double]),
+            "pdgo_gauss_lobatto": (C.c_int, [C.c_int, _dp, _dp]),
             "pdgo_volume_points": (C.c_int, [P, _dp]),
             "pdgo_boundary_points": (C.c_int, [P, _dp]),
             "pdgo_jacobian_apply": (C.c_int, [P, _dp, _dp]),
@@ -166,6 +171,18 @@ def gauss_legendre(m):
     return x, w
 
 
+def gauss_lobatto(m):
+    x = np.zeros(m)
+    w = np.zeros(m)
+    lib().pdgo_gauss_lobatto(m, _ptr(x), _ptr(w))
+    return x, w
+
+
+def basis1d(basis, k, i, x, derivative=False):
+    f = lib().pdgo_dbasis1d if derivative else lib().pdgo_basis1d
+    return f(basis, k, i, x)
+
+
 class Problem:
     """SIPG/NIPG/IIPG ConvectionDiffusionDG problem on a structured grid.
 
@@ -174,8 +191,8 @@ class Problem:
 
     def __init__(self, dim, k, nc, L=None, method=SIPG, weights=WEIGHTS_ON,
                  alpha=1.0, bctype=None, K=None, c=None, modes=None,
-                 fq=None, fc=None, gq=None, jq=None, oq=None):
-        self.dim, self.k = dim, k
+                 fq=None, fc=None, gq=None, jq=None, oq=None, basis=LAGRANGE):
+        self.dim, self.k, self.basis = dim, k, basis
         self.nc = tuple(nc) + (1,) * (3 - len(nc))
         self.L = tuple(L) if L is not None else (1.0,) * dim
         self.L = self.L + (1.0,) * (3 - len(self.L))
@@ -189,6 +206,7 @@ class Problem:
             s.nc[j] = self.nc[j]
             s.L[j] = self.L[j]
         s.method, s.weights, s.alpha = method, weights, self.alpha
+        s.basis = basis
         for j in range(6):
             s.bctype[j] = self.bctype[j] if j < len(self.bctype) else BC_DIRICHLET
         self.set(K=K, c=c, fq=fq, fc=fc, gq=gq, jq=jq, oq=oq)
