@@ -548,10 +548,10 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
     return launch_apply_modal<T>(ctx, a, K, c, tab);
   OpParams<T> p = make_params<T>(ctx, K, c, tab);
   if constexpr (std::is_same<T, float>::value) {
-    // the staged kernel wins for N <= 3 (Q1, Q2: 78 vs 126 us at 64^3 Q2);
-    // at N >= 4 its shared-memory runs cut occupancy below the generic
-    // kernel's (Q3 96^3: 1170 vs 828 us; Q4 48^3: 324 vs 206 us)
-    if (ctx->dim == 3 && ctx->N <= 3 && !a.cells && a.ncells == 0 && K == ctx->K32) {
+    // the staged kernels (plane per thread) win for N <= 4: Q1, Q2 (78 vs
+    // 126 us at 64^3 Q2) and the Q3 variant with swizzled 16-byte rows; at
+    // N = 5 the generic kernel is used
+    if (ctx->dim == 3 && ctx->N <= 4 && !a.cells && a.ncells == 0 && K == ctx->K32) {
       PDG_TRY(ensure_record32(ctx));
       PDG_TRY(launch_apply32_3d(ctx, a, p, ctx->rec32));
       if (ctx->vel.nmodes > 0) PDG_TRY(launch_convection<T>(ctx, a));

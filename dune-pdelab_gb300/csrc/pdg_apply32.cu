@@ -1,5 +1,5 @@
 // pdg_apply32.cu -- the FP32 cell operator of the mixed-precision inner
-// solve (3D, degrees 1 and 2), laid out for shared-memory throughput.
+// solve (3D, degrees 1 to 3), laid out for shared-memory throughput.
 //
 // Same operator as k_apply (pdg_apply.cu; reference: ConvectionDiffusionDG::
 // jacobian_apply_volume / _skeleton / _boundary, localoperator/
@@ -331,6 +331,359 @@ __global__ void __launch_bounds__(P32Cfg<N>::THREADS)
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Q3 (N = 4) variant.  A row of a cell (4 floats along x at fixed y, z) is one
+// 16-byte vector, so every exchange goes through 128-bit shared accesses.
+// Staged runs are stored with the row swizzle swz(): a quarter warp (two
+// cells x four planes) then reads eight distinct 16-byte bank groups for
+// every row pattern of the kernel (own / neighbour planes, all planes of one
+// row, P planes), and consecutive staging stores stay conflict-free.
+// The z faces are not staged: thread z loads row y = z of the four planes of
+// each z neighbour straight from global memory (64 contiguous bytes per cell),
+// forms the face terms of the face points of that row and hands them to the
+// other planes through a small shared array.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int swz(int r) { return r ^ (((r >> 3) & 1) | (((r >> 4) & 1) << 1)); }
+
+struct Q3Cfg {
+  static constexpr int N = 4, N2 = 16, NB = 64, CPB = 32, THREADS = 128;
+  static constexpr int REC = 3 * N2 + 30;
+  // shared layout in 16-byte rows
+  static constexpr int OWN = (CPB + 2) * 16, RUN = CPB * 16, FS = 4 * CPB * 4;
+  static constexpr int RECR = (CPB * REC + 4 + 3) / 4;   // records (+ phase slack)
+  static constexpr int ROWS = OWN + 2 * RUN + RUN + FS + RECR;
+};
+
+__device__ __forceinline__ float4 ld4(const float *p, bool vec) {
+  if (vec) return *reinterpret_cast<const float4 *>(p);
+  return make_float4(p[0], p[1], p[2], p[3]);
+}
+
+__global__ void __launch_bounds__(Q3Cfg::THREADS)
+    k_apply32_q3(const OpParams<float> p, const ApplyArgs<float> a, const float *__restrict__ rec,
+                 const EdgeTab tb) {
+  using C = Q3Cfg;
+  constexpr int N = 4, N2 = 16, NB = 64, CPB = C::CPB, REC = C::REC;
+  extern __shared__ __align__(16) float4 sm4[];
+  if (a.skip && *a.skip) return;
+  float4 *OWN = sm4;                 // cells e0-1 .. e0+CPB, swizzled rows
+  float4 *YL = OWN + C::OWN;         // cells e - nx
+  float4 *YH = YL + C::RUN;          // cells e + nx
+  float4 *PS = YH + C::RUN;          // stage-1 planes P
+  float4 *FS = PS + C::RUN;          // z-face terms [lo s1, lo s2, hi s1, hi s2][cell][row]
+  float *RS0 = reinterpret_cast<float *>(FS + C::FS);
+
+  const long e0 = (long)blockIdx.x * CPB;
+  const long ncell = p.ncell;
+  const long sx = p.nc[0], sxy = (long)p.nc[0] * p.nc[1];
+  const float *__restrict__ x = a.x;
+  const bool coupled = !a.diag_only;
+  const bool vec = (reinterpret_cast<uintptr_t>(x) & 15) == 0;
+
+  // rows of cells [c0, c0 + ncells) into dst (swizzled); absent cells read 0
+  auto stage_rows = [&](float4 *dst, long c0, int ncells, bool on) {
+    for (int r = threadIdx.x; r < ncells * 16; r += C::THREADS) {
+      const long cell = c0 + (r >> 4);
+      float4 *d = dst + swz(r);
+      if (on && cell >= 0 && cell < ncell) {
+        const float *src = x + cell * NB + (r & 15) * 4;
+        if (vec) {
+          const unsigned sa = (unsigned)__cvta_generic_to_shared(d);
+          asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src)
+                       : "memory");
+        } else {
+          *d = make_float4(src[0], src[1], src[2], src[3]);
+        }
+      } else {
+        *d = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+  };
+  stage_rows(OWN, e0 - 1, CPB + 2, true);
+  stage_rows(YL, e0 - sx, CPB, coupled);
+  stage_rows(YH, e0 + sx, CPB, coupled);
+  float *RS;
+  {
+    // records: one contiguous run, copied in 16-byte chunks in phase with
+    // their source (element-wise where a chunk leaves the array)
+    const long g0 = e0 * REC, lim = ncell * REC;
+    const int ph = (int)(g0 & 3);
+    const long ga = g0 - ph;
+    const int nch = (ph + CPB * REC + 3) / 4;
+    const bool rvec = (reinterpret_cast<uintptr_t>(rec) & 15) == 0;
+    for (int c = threadIdx.x; c < nch; c += C::THREADS) {
+      const long gc = ga + 4L * c;
+      if (rvec && gc >= 0 && gc + 4 <= lim) {
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(RS0 + 4 * c);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(rec + gc)
+                     : "memory");
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const long g = gc + j;
+          RS0[4 * c + j] = (g >= 0 && g < lim) ? rec[g] : 0.f;
+        }
+      }
+    }
+    RS = RS0 + ph;
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+
+  const int t = threadIdx.x, cs = t >> 2, z = t & 3;
+  const long e = e0 + cs;
+  const bool active = e < ncell;
+  const long ee = active ? e : 0;
+  int ix[3];
+  coords32(p, (unsigned)ee, ix);
+  const bool has[6] = {coupled && ix[0] > 0, coupled && ix[0] + 1 < p.nc[0],
+                       coupled && ix[1] > 0, coupled && ix[1] + 1 < p.nc[1],
+                       coupled && ix[2] > 0, coupled && ix[2] + 1 < p.nc[2]};
+  const bool tr = a.transpose != 0;
+
+  // z-neighbour rows (plane q, row z) straight from global memory, issued
+  // before the wait so they overlap the staging copies
+  float4 zl[N], zh[N];
+#pragma unroll
+  for (int q = 0; q < N; q++) {
+    zl[q] = has[4] ? ld4(x + (ee - sxy) * NB + q * N2 + z * N, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
+    zh[q] = has[5] ? ld4(x + (ee + sxy) * NB + q * N2 + z * N, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads();
+
+  const float *R = RS + cs * REC;
+  const float *cf = R + 3 * N2;
+  auto A = [&](int dir, int i, int q) -> float {
+    return R[dir * N2 + (tr ? q * N + i : i * N + q)];
+  };
+  auto row = [](const float4 &v, int i) -> float {
+    return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+  };
+
+  // ---- z faces of the face points of row z ----
+  {
+    float s1l[N], s2l[N], s1h[N], s2h[N];
+#pragma unroll
+    for (int xx = 0; xx < N; xx++) {
+      float dvl = 0.f, dvh = 0.f;
+#pragma unroll
+      for (int q = 0; q < N; q++) {
+        dvl += tb.d1[q] * row(zl[q], xx);
+        dvh += tb.d0[q] * row(zh[q], xx);
+      }
+      face_s(cf + 20, false, tr, row(zl[N - 1], xx), dvl, s1l[xx], s2l[xx]);
+      face_s(cf + 25, true, tr, row(zh[0], xx), dvh, s1h[xx], s2h[xx]);
+      if (!has[4]) { s1l[xx] = 0.f; s2l[xx] = 0.f; }
+      if (!has[5]) { s1h[xx] = 0.f; s2h[xx] = 0.f; }
+    }
+    FS[(0 * CPB + cs) * 4 + z] = make_float4(s1l[0], s1l[1], s1l[2], s1l[3]);
+    FS[(1 * CPB + cs) * 4 + z] = make_float4(s2l[0], s2l[1], s2l[2], s2l[3]);
+    FS[(2 * CPB + cs) * 4 + z] = make_float4(s1h[0], s1h[1], s1h[2], s1h[3]);
+    FS[(3 * CPB + cs) * 4 + z] = make_float4(s2h[0], s2h[1], s2h[2], s2h[3]);
+  }
+
+  // ---- stage 1: plane z ----
+  float u[N][N];
+#pragma unroll
+  for (int y = 0; y < N; y++) {
+    const float4 v = OWN[swz((cs + 1) * 16 + z * 4 + y)];
+    u[y][0] = v.x; u[y][1] = v.y; u[y][2] = v.z; u[y][3] = v.w;
+  }
+  float xs1l[N], xs2l[N], xs1h[N], xs2h[N];
+#pragma unroll
+  for (int y = 0; y < N; y++) {
+    const float4 l = OWN[swz(cs * 16 + z * 4 + y)];
+    const float4 h = OWN[swz((cs + 2) * 16 + z * 4 + y)];
+    const float dvl = tb.d1[0] * l.x + tb.d1[1] * l.y + tb.d1[2] * l.z + tb.d1[3] * l.w;
+    const float dvh = tb.d0[0] * h.x + tb.d0[1] * h.y + tb.d0[2] * h.z + tb.d0[3] * h.w;
+    face_s(cf + 0, false, tr, l.w, dvl, xs1l[y], xs2l[y]);
+    face_s(cf + 5, true, tr, h.x, dvh, xs1h[y], xs2h[y]);
+    if (!has[0]) { xs1l[y] = 0.f; xs2l[y] = 0.f; }
+    if (!has[1]) { xs1h[y] = 0.f; xs2h[y] = 0.f; }
+  }
+  float ys1l[N], ys2l[N], ys1h[N], ys2h[N];
+  {
+    float yl[N][N], yh[N][N];
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      const float4 l = YL[swz(cs * 16 + z * 4 + y)];
+      const float4 h = YH[swz(cs * 16 + z * 4 + y)];
+      yl[y][0] = l.x; yl[y][1] = l.y; yl[y][2] = l.z; yl[y][3] = l.w;
+      yh[y][0] = h.x; yh[y][1] = h.y; yh[y][2] = h.z; yh[y][3] = h.w;
+    }
+#pragma unroll
+    for (int xx = 0; xx < N; xx++) {
+      float dvl = 0.f, dvh = 0.f;
+#pragma unroll
+      for (int q = 0; q < N; q++) {
+        dvl += tb.d1[q] * yl[q][xx];
+        dvh += tb.d0[q] * yh[q][xx];
+      }
+      face_s(cf + 10, false, tr, yl[N - 1][xx], dvl, ys1l[xx], ys2l[xx]);
+      face_s(cf + 15, true, tr, yh[0][xx], dvh, ys1h[xx], ys2h[xx]);
+      if (!has[2]) { ys1l[xx] = 0.f; ys2l[xx] = 0.f; }
+      if (!has[3]) { ys1h[xx] = 0.f; ys2h[xx] = 0.f; }
+    }
+  }
+  float P[N][N];
+  {
+    float X[N][N];
+#pragma unroll
+    for (int y = 0; y < N; y++)
+#pragma unroll
+      for (int xx = 0; xx < N; xx++) {
+        float s = 0.f;
+#pragma unroll
+        for (int q = 0; q < N; q++) s += A(0, xx, q) * u[y][q];
+        if (xx == 0) s += xs1l[y];
+        s += tb.d0[xx] * xs2l[y];
+        if (xx == N - 1) s += xs1h[y];
+        s += tb.d1[xx] * xs2h[y];
+        X[y][xx] = s;
+      }
+#pragma unroll
+    for (int y = 0; y < N; y++)
+#pragma unroll
+      for (int xx = 0; xx < N; xx++) {
+        float s = 0.f;
+#pragma unroll
+        for (int r = 0; r < N; r++) s += tb.M[y * N + r] * X[r][xx];
+        P[y][xx] = s;
+      }
+  }
+  {
+    float Y[N][N];
+#pragma unroll
+    for (int y = 0; y < N; y++)
+#pragma unroll
+      for (int xx = 0; xx < N; xx++) {
+        float s = 0.f;
+#pragma unroll
+        for (int q = 0; q < N; q++) s += A(1, y, q) * u[q][xx];
+        if (y == 0) s += ys1l[xx];
+        s += tb.d0[y] * ys2l[xx];
+        if (y == N - 1) s += ys1h[xx];
+        s += tb.d1[y] * ys2h[xx];
+        Y[y][xx] = s;
+      }
+#pragma unroll
+    for (int y = 0; y < N; y++)
+#pragma unroll
+      for (int xx = 0; xx < N; xx++) {
+        float s = P[y][xx];
+#pragma unroll
+        for (int r = 0; r < N; r++) s += tb.M[xx * N + r] * Y[y][r];
+        P[y][xx] = s;
+      }
+  }
+#pragma unroll
+  for (int y = 0; y < N; y++)
+    PS[swz(cs * 16 + z * 4 + y)] = make_float4(P[y][0], P[y][1], P[y][2], P[y][3]);
+  __syncthreads();
+
+  // ---- stage 2: z contractions ----
+  float Zp[N][N];
+  {
+    float az[N];
+#pragma unroll
+    for (int q = 0; q < N; q++) az[q] = A(2, z, q);
+    const float d0z = tb.d0[z], d1z = tb.d1[z];
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < N; q++) {
+        const float4 v = OWN[swz((cs + 1) * 16 + q * 4 + y)];
+        acc.x += az[q] * v.x; acc.y += az[q] * v.y; acc.z += az[q] * v.z; acc.w += az[q] * v.w;
+      }
+      const float4 s2l = FS[(1 * CPB + cs) * 4 + y], s2h = FS[(3 * CPB + cs) * 4 + y];
+      acc.x += d0z * s2l.x + d1z * s2h.x;
+      acc.y += d0z * s2l.y + d1z * s2h.y;
+      acc.z += d0z * s2l.z + d1z * s2h.z;
+      acc.w += d0z * s2l.w + d1z * s2h.w;
+      if (z == 0) {
+        const float4 s1 = FS[(0 * CPB + cs) * 4 + y];
+        acc.x += s1.x; acc.y += s1.y; acc.z += s1.z; acc.w += s1.w;
+      }
+      if (z == N - 1) {
+        const float4 s1 = FS[(2 * CPB + cs) * 4 + y];
+        acc.x += s1.x; acc.y += s1.y; acc.z += s1.z; acc.w += s1.w;
+      }
+      Zp[y][0] = acc.x; Zp[y][1] = acc.y; Zp[y][2] = acc.z; Zp[y][3] = acc.w;
+    }
+  }
+  float out[N][N];
+  {
+    float T1[N][N];   // Mhat_x along x
+#pragma unroll
+    for (int y = 0; y < N; y++)
+#pragma unroll
+      for (int xx = 0; xx < N; xx++) {
+        float s = 0.f;
+#pragma unroll
+        for (int r = 0; r < N; r++) s += tb.M[xx * N + r] * Zp[y][r];
+        T1[y][xx] = s;
+      }
+    float mz[N];
+#pragma unroll
+    for (int q = 0; q < N; q++) mz[q] = tb.M[z * N + q];
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < N; q++) {
+        const float4 v = PS[swz(cs * 16 + q * 4 + y)];
+        acc.x += mz[q] * v.x; acc.y += mz[q] * v.y; acc.z += mz[q] * v.z; acc.w += mz[q] * v.w;
+      }
+#pragma unroll
+      for (int r = 0; r < N; r++) {
+        const float m = tb.M[y * N + r];
+        acc.x += m * T1[r][0]; acc.y += m * T1[r][1]; acc.z += m * T1[r][2]; acc.w += m * T1[r][3];
+      }
+      out[y][0] = acc.x; out[y][1] = acc.y; out[y][2] = acc.z; out[y][3] = acc.w;
+    }
+  }
+
+  // ---- coalesced write-back through shared memory (the YL run is free) ----
+  __syncthreads();
+#pragma unroll
+  for (int y = 0; y < N; y++)
+    YL[swz(cs * 16 + z * 4 + y)] = make_float4(out[y][0], out[y][1], out[y][2], out[y][3]);
+  __syncthreads();
+  const long ob = e0 * NB;
+  const long ndof = ncell * NB;
+  const float alpha = a.alpha;
+  const bool yvec = ((reinterpret_cast<uintptr_t>(a.y) | reinterpret_cast<uintptr_t>(a.add)) & 15) == 0;
+  for (int r = threadIdx.x; r < C::RUN; r += C::THREADS) {
+    const long g = ob + 4L * r;
+    if (g >= ndof) break;
+    const float4 o = YL[swz(r)];
+    float4 v = make_float4(alpha * o.x, alpha * o.y, alpha * o.z, alpha * o.w);
+    if (yvec) {
+      float4 *yp = reinterpret_cast<float4 *>(a.y + g);
+      if (a.accumulate) {
+        const float4 w = *yp;
+        v.x += w.x; v.y += w.y; v.z += w.z; v.w += w.w;
+      }
+      if (a.add) {
+        const float4 w = *reinterpret_cast<const float4 *>(a.add + g);
+        v.x += w.x; v.y += w.y; v.z += w.z; v.w += w.w;
+      }
+      *yp = v;
+    } else {
+      float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        float rr = vv[j];
+        if (a.accumulate) rr += a.y[g + j];
+        if (a.add) rr += a.add[g + j];
+        a.y[g + j] = rr;
+      }
+    }
+  }
+}
+
 static EdgeTab make_edge_tab_uncached(const pdg_context *ctx) {
   EdgeTab t{};
   const RhsTables r = make_rhs_tables(ctx);
@@ -381,12 +734,29 @@ static int launch32_n(pdg_context *ctx, const ApplyArgs<float> &a, const OpParam
   return PDG_OK;
 }
 
+static int launch32_q3(pdg_context *ctx, const ApplyArgs<float> &a, const OpParams<float> &p,
+                       const float *rec) {
+  const size_t smem = 16 * Q3Cfg::ROWS;
+  static int attr_dev = -1;
+  if (attr_dev != ctx->device) {
+    PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply32_q3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    attr_dev = ctx->device;
+  }
+  const EdgeTab &tb = edge_tab(ctx);
+  const unsigned blocks = (unsigned)((ctx->ncell + Q3Cfg::CPB - 1) / Q3Cfg::CPB);
+  k_apply32_q3<<<blocks, Q3Cfg::THREADS, smem, ctx->stream>>>(p, a, rec, tb);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+
 int launch_apply32_3d(pdg_context *ctx, const ApplyArgs<float> &a, const OpParams<float> &p,
                       const float *rec) {
   switch (ctx->N) {
     case 2: return launch32_n<2>(ctx, a, p, rec);
     case 3: return launch32_n<3>(ctx, a, p, rec);
-    default: return set_error(PDG_EUNSUPPORTED, "staged FP32 kernel: degree 1 or 2 only");
+    case 4: return launch32_q3(ctx, a, p, rec);
+    default: return set_error(PDG_EUNSUPPORTED, "staged FP32 kernel: degrees 1 to 3");
   }
 }
 

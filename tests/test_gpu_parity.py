@@ -107,6 +107,10 @@ def test_jacobian_apply_f32(pdg, oracle, dim, k, n):
     (4, (5, 4, 3), 2, 0, True, [-1, 1, 1, 1, -2, 1]),
     (2, (1, 1, 1), 1, 0, False, None),
     (2, (43, 1, 2), 1, 0, True, None),
+    (3, (13, 7, 5), 1, 0, True, [1, -1, -2, 1, 1, -1]),
+    (3, (33, 2, 3), 2, 1, False, None),
+    (3, (1, 1, 1), 1, 0, False, None),
+    (3, (5, 9, 11), 0, 0, True, None),
 ])
 def test_jacobian_apply_f32_staged(pdg, oracle, k, nc, method, weights, react, bct):
     # the 3D FP32 kernel stages runs of CPB consecutive cells and their y/z
@@ -300,3 +304,25 @@ def test_errors_are_status_codes(pdg):
     u = np.zeros(go.ndof)
     pdg.StationaryLinearProblemSolver(go, ls, u, 1e-12).apply()
     assert not ls.result().converged and ls.result().iterations == 1
+
+
+@pytest.mark.parametrize("k,nc", [(2, (6, 5, 4)), (3, (7, 5, 4))])
+def test_mixed_adjoint_solve_uses_fp32_transpose(pdg, oracle, k, nc):
+    # NIPG: J^T != J, so the FP32 inner solves of the mixed adjoint solve run
+    # the transposed FP32 operator; the FP64 outer loop must land on the
+    # FP64 adjoint solution
+    go, P, rng = _pair(pdg, oracle, 3, k, nc, seed=60 + k, method=0, react=True)
+    rhs = rng.uniform(-1, 1, go.ndof)
+    lam = {}
+    for mixed in (0, 1):
+        o = pdg.default_options(method=pdg.BICGSTAB, preconditioner=pdg.PREC_BJ_DENSE,
+                                reduction=1e-11, mixed=mixed, maxit=20000)
+        pdg.GridOperatorPreconditioner(go, kind=pdg.PREC_BJ_DENSE,
+                                       precision=pdg.F32 if mixed else pdg.F64).pre()
+        lam[mixed] = np.zeros(go.ndof)
+        assert go.adjoint_solve(rhs, lam[mixed], o).converged
+    assert _rel(lam[1], lam[0]) <= 1e-8
+    # the FP64 adjoint solution against the oracle's transposed operator
+    A = P.assemble_jacobian()
+    r = P.blocks_apply(A, lam[0], transpose=True)
+    assert np.linalg.norm(r - rhs) <= 1e-9 * np.linalg.norm(rhs)
