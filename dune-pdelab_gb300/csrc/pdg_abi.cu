@@ -308,6 +308,30 @@ struct KrylovOut {
   double def0, def;
 };
 
+// The inner FP32 CG can fuse its two dot products into the kernels that
+// produce one operand: <p, q> into the staged FP32 operator writing q = A p,
+// <z, r> into the FDM block Jacobi writing z = M^{-1} r.  Only where those are
+// the kernels that run: 3D, degree <= 3, plain diffusion-reaction operator
+// (no convection, nonlinear term, modal basis or assembled matrix) and the
+// FDM block Jacobi.
+static bool cg_fusable(const pdg_context *ctx) {
+  return ctx->dim == 3 && ctx->N <= 4 && ctx->vel.nmodes == 0 && ctx->nl_deg == 0 &&
+         ctx->basis != PDG_BASIS_LEGENDRE && !ctx->use_matrix &&
+         ctx->prec[PDG_F32].ready && ctx->prec[PDG_F32].kind == PDG_PREC_BJ_FDM;
+}
+
+static int ensure_fuse(pdg_context *ctx) {
+  if (ctx->fuse_part) return PDG_OK;
+  // the fused kernels run at least 8 cells per block
+  const long maxb = ctx->ncell / 8 + 2;
+  const long ngroups = (maxb + kFuseGroup - 1) / kFuseGroup;
+  PDG_CUDA_TRY(cudaMalloc(&ctx->fuse_part, sizeof(double) * 2 * (maxb + ngroups)));
+  PDG_CUDA_TRY(cudaMalloc(&ctx->fuse_cnt, sizeof(int) * ngroups));
+  PDG_CUDA_TRY(cudaMemsetAsync(ctx->fuse_cnt, 0, sizeof(int) * ngroups, ctx->stream));
+  ctx->fuse_max_blocks = maxb;
+  return PDG_OK;
+}
+
 // dune-istl CGSolver::apply restated on the device.  x: initial guess and
 // result; b: right-hand side, overwritten by the defect.  w0, w1: work.
 template <typename T>
@@ -327,13 +351,31 @@ static int cg_device(pdg_context *ctx, T *x, T *b, T *p, T *q, double reduction,
   int i = 1;
   const int batch = 8;
   bool done = false;
+  const bool fuse = std::is_same<T, float>::value && cg_fusable(ctx);
+  if (fuse) PDG_TRY(ensure_fuse(ctx));
   for (; i <= maxit && !done; i++) {
     PDG_TRY(set_iter(ctx, rc, (double)i));
-    PDG_TRY(op_launch<T>(ctx, p, q, nullptr, T(1), 0, transpose, skip));          // q = A p
-    PDG_TRY(dot<T>(ctx, rc, p, q, nullptr, nullptr, FIN_CG_LAMBDA, -1, -1, true)); // lambda
+    if (fuse) {
+      // q = A p with lambda = rholast / <p, q> in the same launch
+      ctx->fuse_fin = FIN_CG_LAMBDA;
+      const int st = op_launch<T>(ctx, p, q, nullptr, T(1), 0, transpose, skip);
+      ctx->fuse_fin = 0;
+      PDG_TRY(st);
+    } else {
+      PDG_TRY(op_launch<T>(ctx, p, q, nullptr, T(1), 0, transpose, skip));          // q = A p
+      PDG_TRY(dot<T>(ctx, rc, p, q, nullptr, nullptr, FIN_CG_LAMBDA, -1, -1, true)); // lambda
+    }
     PDG_TRY(cg_update_xr<T>(ctx, rc, ctx->ndof, x, b, p, q));                     // x, b, def
-    PDG_TRY(prec_op<T>(ctx, b, q, transpose, skip));                        // q = M^-1 b
-    PDG_TRY(dot<T>(ctx, rc, q, b, nullptr, nullptr, FIN_CG_BETA, -1, -1, true));   // beta
+    if (fuse) {
+      // q = M^{-1} b with beta = <q, b> / rholast in the same launch
+      ctx->fuse_fin = FIN_CG_BETA;
+      const int st = prec_op<T>(ctx, b, q, transpose, skip);
+      ctx->fuse_fin = 0;
+      PDG_TRY(st);
+    } else {
+      PDG_TRY(prec_op<T>(ctx, b, q, transpose, skip));                        // q = M^-1 b
+      PDG_TRY(dot<T>(ctx, rc, q, b, nullptr, nullptr, FIN_CG_BETA, -1, -1, true));   // beta
+    }
     PDG_TRY(cg_update_p<T>(ctx, rc, ctx->ndof, p, q));                             // p = q + beta p
     if (i % batch == 0 || i == maxit || i == 1) {
       PDG_TRY(fetch_state(ctx, scal, flags));
@@ -946,7 +988,8 @@ int pdg_destroy(pdg_context *c) {
                   c->convtab32, c->gm_V32, c->gm_V64, c->gm_F64, c->gm_partial, c->gm_coef,
                   c->A64, c->rec32, c->nlW64, c->nlW32, c->nlB64, c->nlB32,
                   c->massW, c->massWi, c->massB, c->massBiT, c->cstage64, c->cstage32,
-                  c->leg64, c->leg32, c->legw64[0], c->legw64[1], c->legw32[0], c->legw32[1]};
+                  c->leg64, c->leg32, c->legw64[0], c->legw64[1], c->legw32[0], c->legw32[1],
+                  c->fuse_part, c->fuse_cnt};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 10; i++)

@@ -28,7 +28,7 @@
 #include <cstdint>
 #include <mutex>
 
-#include "pdg_internal.cuh"
+#include "pdg_vec.cuh"
 
 namespace pdg {
 
@@ -321,6 +321,7 @@ __global__ void __launch_bounds__(P32Cfg<N>::THREADS)
   __syncthreads();
   const long ob = e0 * NB;
   const float alpha = a.alpha;
+  float part = 0.f;
   for (int i = threadIdx.x; i < C::RUN; i += C::THREADS) {
     const long g = ob + i;
     if (g >= ndof) break;
@@ -328,7 +329,12 @@ __global__ void __launch_bounds__(P32Cfg<N>::THREADS)
     if (a.accumulate) r += a.y[g];
     if (a.add) r += a.add[g];
     a.y[g] = r;
+    part += OWN[NB + i] * r;
   }
+  if (a.dot_part)
+    reduce_tail_grouped<128>(a.dot_part, a.dot_max_blocks, a.dot_cnt,
+                             RedCtx{nullptr, a.dot_scal, a.dot_flags}, (double)part, 0.0,
+                             a.dot_fin, -1, -1);
 }
 
 
@@ -655,10 +661,12 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS)
   const long ndof = ncell * NB;
   const float alpha = a.alpha;
   const bool yvec = ((reinterpret_cast<uintptr_t>(a.y) | reinterpret_cast<uintptr_t>(a.add)) & 15) == 0;
+  float part = 0.f;
   for (int r = threadIdx.x; r < C::RUN; r += C::THREADS) {
     const long g = ob + 4L * r;
     if (g >= ndof) break;
     const float4 o = YL[swz(r)];
+    const float4 pin = OWN[swz(16 + r)];
     float4 v = make_float4(alpha * o.x, alpha * o.y, alpha * o.z, alpha * o.w);
     if (yvec) {
       float4 *yp = reinterpret_cast<float4 *>(a.y + g);
@@ -679,9 +687,16 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS)
         if (a.accumulate) rr += a.y[g + j];
         if (a.add) rr += a.add[g + j];
         a.y[g + j] = rr;
+        vv[j] = rr;
       }
+      v = make_float4(vv[0], vv[1], vv[2], vv[3]);
     }
+    part += pin.x * v.x + pin.y * v.y + pin.z * v.z + pin.w * v.w;
   }
+  if (a.dot_part)
+    reduce_tail_grouped<Q3Cfg::THREADS>(a.dot_part, a.dot_max_blocks, a.dot_cnt,
+                                        RedCtx{nullptr, a.dot_scal, a.dot_flags}, (double)part,
+                                        0.0, a.dot_fin, -1, -1);
 }
 
 static EdgeTab make_edge_tab_uncached(const pdg_context *ctx) {
@@ -750,8 +765,17 @@ static int launch32_q3(pdg_context *ctx, const ApplyArgs<float> &a, const OpPara
   return PDG_OK;
 }
 
-int launch_apply32_3d(pdg_context *ctx, const ApplyArgs<float> &a, const OpParams<float> &p,
+int launch_apply32_3d(pdg_context *ctx, const ApplyArgs<float> &a0, const OpParams<float> &p,
                       const float *rec) {
+  ApplyArgs<float> a = a0;
+  if (ctx->fuse_fin) {
+    a.dot_part = ctx->fuse_part;
+    a.dot_max_blocks = ctx->fuse_max_blocks;
+    a.dot_cnt = ctx->fuse_cnt;
+    a.dot_scal = ctx->red_out;
+    a.dot_flags = ctx->d_flag;
+    a.dot_fin = ctx->fuse_fin;
+  }
   switch (ctx->N) {
     case 2: return launch32_n<2>(ctx, a, p, rec);
     case 3: return launch32_n<3>(ctx, a, p, rec);

@@ -97,6 +97,14 @@ struct ApplyArgs {
   const int *cells; // if non-null: only these cells (ncells of them) are computed
   int ncells;
   int cell0;        // cells null and ncells > 0: the cell range [cell0, cell0 + ncells)
+  // fused dot product <x, y_out> (staged FP32 operator): block partials into
+  // dot_part, finisher dot_fin on the Krylov scalars dot_scal / dot_flags
+  double *dot_part;
+  long dot_max_blocks;
+  int *dot_cnt;
+  double *dot_scal;
+  int *dot_flags;
+  int dot_fin;
 };
 
 // One cell-block Jacobi preconditioner instance (per precision).
@@ -203,6 +211,15 @@ struct pdg_context {
   double *legw64[2];
   float *legw32[2];
   int leg_nodal;
+
+  // dot products fused into the FP32 operator / FDM block Jacobi of the
+  // inner CG: fuse_fin != 0 asks the next such launch for <in, out> with that
+  // finisher; block and group partials in fuse_part, group counters in
+  // fuse_cnt (reduce_tail_grouped)
+  double *fuse_part;
+  long fuse_max_blocks;
+  int *fuse_cnt;
+  int fuse_fin;
 
   // staging buffers for host pointers
   double *stage_a, *stage_b;

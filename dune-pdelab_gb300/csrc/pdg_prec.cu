@@ -163,7 +163,9 @@ template <typename T, int D, int N>
 __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
     k_fdm_apply(long ncell, const T *__restrict__ Q, const T *__restrict__ L,
                 const T *__restrict__ d, T *__restrict__ v, const int *__restrict__ skip,
-                const int *__restrict__ cells, int ncells, T scale) {
+                const int *__restrict__ cells, int ncells, T scale, double *dot_part,
+                long dot_max_blocks, int *dot_cnt, double *dot_scal, int *dot_flags,
+                int dot_fin) {
   using C = PCfg<D, N>;
   constexpr int N2 = C::N2, NB = C::NB, TPC = C::TPC, CPB = C::CPB;
   if (skip && *skip) return;
@@ -182,6 +184,7 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
   T col[N];
 #pragma unroll
   for (int z = 0; z < N; z++) col[z] = d[(size_t)ee * NB + z * TPC + l];
+  T part = T(0);   // <d, v> of this thread's entries (fused dot product)
   __syncthreads();
   if constexpr (D == 3) {
     const int tx = l % N, ty = l / N;
@@ -244,6 +247,7 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
 #pragma unroll
         for (int zp = 0; zp < N; zp++) s += Qz[z * N + zp] * a[zp];
         v[(size_t)e * NB + z * N2 + l] = scale * s;
+        part += col[z] * (scale * s);
       }
     }
   } else {
@@ -284,9 +288,14 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
 #pragma unroll
         for (int yp = 0; yp < N; yp++) s += Qy[y * N + yp] * a[yp];
         v[(size_t)e * NB + y * N + tx] = scale * s;
+        part += col[y] * (scale * s);
       }
     }
   }
+  if (dot_part)
+    reduce_tail_grouped<C::THREADS>(dot_part, dot_max_blocks, dot_cnt,
+                                    RedCtx{nullptr, dot_scal, dot_flags}, (double)part, 0.0,
+                                    dot_fin, -1, -1);
 }
 
 // ---------------------------------------------------------------------------
@@ -577,10 +586,12 @@ static int fdm_apply_dn(pdg_context *ctx, const T *d, T *v, const int *skip, con
   const long work = cells ? ncells : ctx->ncell;
   if (work <= 0) return PDG_OK;
   const unsigned blocks = (unsigned)((work + C::CPB - 1) / C::CPB);
+  const bool fuse = ctx->fuse_fin != 0;
   k_fdm_apply<T, D, N><<<blocks, C::THREADS, smem, ctx->stream>>>(
       ctx->ncell, (const T *)ctx->prec[std::is_same<T, double>::value ? 0 : 1].Q,
       (const T *)ctx->prec[std::is_same<T, double>::value ? 0 : 1].L, d, v, skip, cells, ncells,
-      scale);
+      scale, fuse ? ctx->fuse_part : nullptr, ctx->fuse_max_blocks, ctx->fuse_cnt, ctx->red_out,
+      ctx->d_flag, ctx->fuse_fin);
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
 }

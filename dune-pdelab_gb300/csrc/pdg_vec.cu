@@ -31,73 +31,6 @@ __device__ __forceinline__ void block_sum2(double &a, double &b) {
   }
 }
 
-__device__ void run_finisher(const RedCtx &rc, int fin, int slot0, int slot1, double d0,
-                             double d1) {
-  double *s = rc.scal;
-  int *fl = rc.flags;
-  switch (fin) {
-    case FIN_STORE:
-      if (slot0 >= 0) s[slot0] = d0;
-      if (slot1 >= 0) s[slot1] = d1;
-      break;
-    case FIN_NORM:
-      s[slot0] = sqrt(d0);
-      break;
-    case FIN_DEF0: {
-      const double def = sqrt(d0);
-      s[S_DEF0] = def;
-      s[S_DEF] = def;
-      if (!isfinite(def)) fl[F_STATE] = 2;
-      else if (def < def * s[S_RED] || def < 1e-30) fl[F_STATE] = 1;
-      break;
-    }
-    case FIN_DEF: {
-      const double def = sqrt(d0);
-      s[S_DEF] = def;
-      if (!isfinite(def)) fl[F_STATE] = 2;
-      else if (def < s[S_DEF0] * s[S_RED] || def < 1e-30) fl[F_STATE] = 1;
-      if (slot0 == S_RHO) s[S_RHO] = s[S_RHONEW];   // BiCGStab: rho = rho_new
-      break;
-    }
-    case FIN_CG_LAMBDA:
-      s[S_ALPHA] = s[S_RHO] / d0;
-      break;
-    case FIN_CG_BETA:
-      s[S_BETA] = d0 / s[S_RHO];
-      s[S_RHO] = d0;
-      break;
-    // BiCGSTABSolver breakdown tests are absolute (rho, omega <= 1e-80,
-    // |h| < 1e-80).  With S_GUARD > 0 (FP32 inner solves, whose dot products
-    // carry ~1e-7 relative noise) a relative test is added:
-    // |<rt, r>| or |<rt, v>| below S_GUARD |rt| |r| (|rt| |v|) is treated as a
-    // breakdown, and the solve stops with the last finite iterate.
-    case FIN_BI_RHONEW:
-      s[S_RHONEW] = d0;
-      if (fabs(s[S_RHO]) <= 1e-80 || fabs(s[S_OMEGA]) <= 1e-80 || !isfinite(d0) ||
-          (s[S_GUARD] > 0 && fabs(d0) < s[S_GUARD] * s[S_DEF0] * s[S_DEF]))
-        fl[F_STATE] = 3;
-      else
-        s[S_BETA] = (d0 / s[S_RHO]) * (s[S_ALPHA] / s[S_OMEGA]);
-      break;
-    case FIN_BI_ALPHA:
-      s[S_H] = d0;
-      if (fabs(d0) < 1e-80 || !isfinite(d0) ||
-          (s[S_GUARD] > 0 && fabs(d0) < s[S_GUARD] * s[S_DEF0] * sqrt(d1)))
-        fl[F_STATE] = 3;
-      else
-        s[S_ALPHA] = s[S_RHONEW] / d0;
-      break;
-    case FIN_BI_OMEGA:
-      s[S_TR] = d0;
-      s[S_TT] = d1;
-      if (!(d1 > 0.0) || !isfinite(d0 / d1)) fl[F_STATE] = 3;
-      else s[S_OMEGA] = d0 / d1;
-      break;
-    default:
-      break;
-  }
-}
-
 // Shared tail of every reducing kernel: publish the block partial, let the
 // last block add all partials in block order and run the finisher.
 __device__ __forceinline__ void reduce_tail(const RedCtx &rc, double s0, double s1, int fin,

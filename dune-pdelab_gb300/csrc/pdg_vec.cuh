@@ -60,6 +60,164 @@ struct RedCtx {
   int *flags;         // [F_COUNT]
 };
 
+// Finisher of a reduction: updates the Krylov scalars (dune-istl's
+// CGSolver / BiCGSTABSolver recurrences and breakdown tests) from the two
+// reduced sums d0, d1.
+__device__ inline void run_finisher(const RedCtx &rc, int fin, int slot0, int slot1, double d0,
+                             double d1) {
+  double *s = rc.scal;
+  int *fl = rc.flags;
+  switch (fin) {
+    case FIN_STORE:
+      if (slot0 >= 0) s[slot0] = d0;
+      if (slot1 >= 0) s[slot1] = d1;
+      break;
+    case FIN_NORM:
+      s[slot0] = sqrt(d0);
+      break;
+    case FIN_DEF0: {
+      const double def = sqrt(d0);
+      s[S_DEF0] = def;
+      s[S_DEF] = def;
+      if (!isfinite(def)) fl[F_STATE] = 2;
+      else if (def < def * s[S_RED] || def < 1e-30) fl[F_STATE] = 1;
+      break;
+    }
+    case FIN_DEF: {
+      const double def = sqrt(d0);
+      s[S_DEF] = def;
+      if (!isfinite(def)) fl[F_STATE] = 2;
+      else if (def < s[S_DEF0] * s[S_RED] || def < 1e-30) fl[F_STATE] = 1;
+      if (slot0 == S_RHO) s[S_RHO] = s[S_RHONEW];   // BiCGStab: rho = rho_new
+      break;
+    }
+    case FIN_CG_LAMBDA:
+      s[S_ALPHA] = s[S_RHO] / d0;
+      break;
+    case FIN_CG_BETA:
+      s[S_BETA] = d0 / s[S_RHO];
+      s[S_RHO] = d0;
+      break;
+    // BiCGSTABSolver breakdown tests are absolute (rho, omega <= 1e-80,
+    // |h| < 1e-80).  With S_GUARD > 0 (FP32 inner solves, whose dot products
+    // carry ~1e-7 relative noise) a relative test is added:
+    // |<rt, r>| or |<rt, v>| below S_GUARD |rt| |r| (|rt| |v|) is treated as a
+    // breakdown, and the solve stops with the last finite iterate.
+    case FIN_BI_RHONEW:
+      s[S_RHONEW] = d0;
+      if (fabs(s[S_RHO]) <= 1e-80 || fabs(s[S_OMEGA]) <= 1e-80 || !isfinite(d0) ||
+          (s[S_GUARD] > 0 && fabs(d0) < s[S_GUARD] * s[S_DEF0] * s[S_DEF]))
+        fl[F_STATE] = 3;
+      else
+        s[S_BETA] = (d0 / s[S_RHO]) * (s[S_ALPHA] / s[S_OMEGA]);
+      break;
+    case FIN_BI_ALPHA:
+      s[S_H] = d0;
+      if (fabs(d0) < 1e-80 || !isfinite(d0) ||
+          (s[S_GUARD] > 0 && fabs(d0) < s[S_GUARD] * s[S_DEF0] * sqrt(d1)))
+        fl[F_STATE] = 3;
+      else
+        s[S_ALPHA] = s[S_RHONEW] / d0;
+      break;
+    case FIN_BI_OMEGA:
+      s[S_TR] = d0;
+      s[S_TT] = d1;
+      if (!(d1 > 0.0) || !isfinite(d0 / d1)) fl[F_STATE] = 3;
+      else s[S_OMEGA] = d0 / d1;
+      break;
+    default:
+      break;
+  }
+}
+
+
+// ---- reductions fused into other kernels ----------------------------------
+// A kernel that produces one operand of a dot product (the operator writing
+// q = A p, the block preconditioner writing z = M^{-1} r) adds the product of
+// its own output with the other operand per block.  Same determinism as the
+// dot kernels: block partials in a per-kernel array, the last block adds
+// them in block order and runs the finisher.  Blocks of any size <= MAXT.
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int MAXT>
+__device__ __forceinline__ void block_sum2_any(double &a, double &b) {
+  __shared__ double sa[MAXT], sb[MAXT];
+  __syncthreads();   // the arrays may still be read by a previous call
+  sa[threadIdx.x] = a;
+  sb[threadIdx.x] = b;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double x = 0.0, y = 0.0;
+    for (unsigned i = threadIdx.x; i < blockDim.x; i += 32) {
+      x += sa[i];
+      y += sb[i];
+    }
+    a = warp_sum_d(x);
+    b = warp_sum_d(y);
+  }
+}
+
+// Two-level tail for grids of many blocks: the last block of each group of
+// kFuseGroup blocks adds the group's partials in block order into a group
+// partial; the last group to finish adds the group partials in group order
+// and runs the finisher.  The order of every sum is fixed, so the result does
+// not depend on which block finishes last.  Layout of `part`: 2 doubles per
+// block, then 2 per group from offset 2 * max_blocks; `cnt`: one int per
+// group, zero between launches (each group's last block resets its own).
+constexpr int kFuseGroup = 256;
+
+template <int MAXT>
+__device__ __forceinline__ void reduce_tail_grouped(double *part, long max_blocks, int *cnt,
+                                                    const RedCtx &rc, double s0, double s1,
+                                                    int fin, int slot0, int slot1) {
+  __shared__ bool last;
+  block_sum2_any<MAXT>(s0, s1);
+  const int b = (int)blockIdx.x, g = b / kFuseGroup;
+  const int ngroups = (int)((gridDim.x + kFuseGroup - 1) / kFuseGroup);
+  const int gsize = min(kFuseGroup, (int)gridDim.x - g * kFuseGroup);
+  if (threadIdx.x == 0) {
+    part[2 * b] = s0;
+    part[2 * b + 1] = s1;
+    __threadfence();
+    last = atomicAdd(&cnt[g], 1) == gsize - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double a = 0.0, c = 0.0;
+  for (int i = threadIdx.x; i < gsize; i += blockDim.x) {
+    a += __ldcg(part + 2 * (g * kFuseGroup + i));
+    c += __ldcg(part + 2 * (g * kFuseGroup + i) + 1);
+  }
+  block_sum2_any<MAXT>(a, c);
+  double *gpart = part + 2 * max_blocks;
+  if (threadIdx.x == 0) {
+    gpart[2 * g] = a;
+    gpart[2 * g + 1] = c;
+    cnt[g] = 0;
+    __threadfence();
+    last = atomicAdd(&rc.flags[F_COUNTER], 1) == ngroups - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  a = 0.0;
+  c = 0.0;
+  for (int i = threadIdx.x; i < ngroups; i += blockDim.x) {
+    a += __ldcg(gpart + 2 * i);
+    c += __ldcg(gpart + 2 * i + 1);
+  }
+  block_sum2_any<MAXT>(a, c);
+  if (threadIdx.x == 0) {
+    run_finisher(rc, fin, slot0, slot1, a, c);
+    rc.flags[F_COUNTER] = 0;
+  }
+}
+
 int red_dot(pdg_context *ctx, const RedCtx &rc, long n, const double *a, const double *b,
             const double *c, const double *d, int fin, int slot0, int slot1, bool respect_flag);
 int red_dot_f32(pdg_context *ctx, const RedCtx &rc, long n, const float *a, const float *b,

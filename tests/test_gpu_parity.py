@@ -326,3 +326,25 @@ def test_mixed_adjoint_solve_uses_fp32_transpose(pdg, oracle, k, nc):
     A = P.assemble_jacobian()
     r = P.blocks_apply(A, lam[0], transpose=True)
     assert np.linalg.norm(r - rhs) <= 1e-9 * np.linalg.norm(rhs)
+
+
+@pytest.mark.parametrize("k,nc", [(1, (9, 7, 6)), (2, (6, 5, 4)), (3, (5, 4, 4))])
+def test_mixed_cg_fused_dots_match_unfused(pdg, oracle, k, nc):
+    # The FP32 inner CG computes <p, A p> inside the operator kernel and
+    # <M^-1 r, r> inside the FDM block Jacobi kernel.  The dense block Jacobi
+    # is the same exact block inverse but takes the separate dot kernels, so
+    # both runs must agree (iteration counts up to FP32 rounding).
+    go, P, rng = _pair(pdg, oracle, 3, k, nc, seed=70 + k, react=True)
+    go.set_source(fc=rng.standard_normal(go.ncell))
+    sols, its = {}, {}
+    for kind in (pdg.PREC_BJ_FDM, pdg.PREC_BJ_DENSE):
+        pdg.GridOperatorPreconditioner(go, kind=kind, precision=pdg.F32).pre()
+        ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG, preconditioner=kind,
+                                                 mixed=True, inner_reduction=1e-4)
+        u = np.zeros(go.ndof)
+        slp = pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10)
+        slp.apply()
+        assert slp.result().converged
+        sols[kind], its[kind] = u, slp.result().iterations
+    assert abs(its[pdg.PREC_BJ_FDM] - its[pdg.PREC_BJ_DENSE]) <= max(2, its[pdg.PREC_BJ_DENSE] // 20)
+    assert _rel(sols[pdg.PREC_BJ_FDM], sols[pdg.PREC_BJ_DENSE]) <= 1e-8
