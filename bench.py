@@ -37,6 +37,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 METRIC = "GDoF/s matrix-free SIPG apply; time-to-1e-10 solve, mixed vs FP64 on GB300; grad/solve"
 WORKLOAD = dict(dim=3, degree=2, cells=64, alpha=3.0, seed=2)
+DATA = "synthetic (seeded log-normal K per cell, x ~ U(-1,1))"
 
 
 def flops_per_cell(dim, N):
@@ -249,9 +250,10 @@ def run_reference(args, world, rank):
         "metric": METRIC, "value": value, "unit": "GDoF/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded log-normal K, x ~ U(-1,1))",
-        "config": {"workload": f"sipg3d_q{wl['degree']}_{n}^3_fp64_apply", "ndof": ndof,
-                   "l2": "n/a (CPU)"},
+        "data": DATA,
+        "config": {"workload": f"sipg3d_q{wl['degree']}_{n}^3_f64_apply", "ndof": ndof,
+                   "cells": ncell, "degree": wl["degree"], "alpha": wl["alpha"],
+                   "l2": "n/a (host memory)", "parallelism": f"{cores} host processes"},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "GDoF/s", "cores": cores, "kind": "port",
                          "sample": f"{args.steps} full FP64 jacobian_apply of the {n}^3 grid, "
@@ -399,7 +401,7 @@ def run_gb300(args, world, rank, local):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": args.precision,
-        "data": "synthetic (seeded log-normal K per cell, x ~ U(-1,1))",
+        "data": DATA,
         "config": {"workload": wname, "ndof": ndof, "cells": ncell,
                    "degree": WORKLOAD["degree"], "alpha": 3.0,
                    "l2": f"{npairs} rotating x/y pairs ({npairs * 2 * esz * ndof / 1e6:.0f} MB "
