@@ -9,10 +9,12 @@ Dirichlet boundary, alpha = 3 (sigma = 3 k (k+d-1)).  Metric: GDoF/s.
 Also reported on the same line: the end-to-end number through the C ABI
 with host buffers (H2D input, D2H result every step), the roofline of the
 operator kernel (FP64 pipe; measured DFMA peak), the CPU baseline (the
-oracle restating the reference's loop structure, one core), and the solve
-metrics of the same problem: time to 1e-10 relative residual for the FP64
+oracle restating the reference's loop structure, one core), the solve
+metrics of the same problem (time to 1e-10 relative residual for the FP64
 CG + cell-block-Jacobi solve and for the FP32-apply / FP64-defect-correction
-solve, and the adjoint gradient cost relative to one forward solve.
+solve, and the adjoint gradient cost relative to one forward solve), and the
+same two solves on the 96^3 Q3 grid (56.6M DoF, box-filtered log-normal K)
+with the errors of the mixed solution against the FP64 one.
 
 ``--impl reference`` times the reference's CPU algorithm (the oracle port:
 PDELab itself cannot be built here) on all host cores for the same
@@ -383,8 +385,10 @@ def run_gb300(args, world, rank, local):
     extras = {}
     if not args.no_solves:
         extras = solve_metrics(pdg, np, torch, go, stream, logK)
-    if args.extended:
-        legs = set(args.legs.split(","))
+    # the 96^3 Q3 mixed-vs-FP64 solve is part of the default line; the other
+    # legs need --extended
+    legs = set(args.legs.split(",")) if args.extended else (set() if args.no_solves else {"c3"})
+    if legs:
         for leg, key, fn in (("c3", "solve_q3_96", c3_metrics), ("c4", "adjoint_q2_64", c4_metrics),
                              ("c5", "cdr_q4_48", c5_metrics), ("prec", "block_prec_q2_64", prec_metrics),
                              ("asm", "assembled_q2_32", assembled_metrics)):
@@ -816,8 +820,10 @@ def main():
     ap.add_argument("--no-solves", action="store_true", help="skip solve/adjoint metrics")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--extended", action="store_true",
-                    help="also run the 96^3 Q3 solves (c3), the 64^3 adjoint checks (c4) and "
-                         "the 48^3 Q4 convection-diffusion-reaction solves and gradients (c5)")
+                    help="run the legs in --legs (default: the 96^3 Q3 solves (c3), the 64^3 "
+                         "adjoint checks (c4) and the 48^3 Q4 convection-diffusion-reaction "
+                         "solves and gradients (c5)); without it only c3 runs, unless "
+                         "--no-solves")
     ap.add_argument("--legs", default="c3,c4,c5", help="subset of the extended legs")
     ap.add_argument("--no-probe", action="store_true",
                     help="skip the FMA peak probe (profiling runs); roofline frac is then null")
