@@ -290,6 +290,7 @@ __global__ void k_init_solve(double *scal, int *flags, double red, double guard 
   scal[S_OMEGA] = 1.0;
   flags[F_STATE] = 0;
   flags[F_COUNTER] = 0;
+  flags[F_XPEND] = 0;
 }
 
 template <typename T>
@@ -358,30 +359,32 @@ static int cg_device(pdg_context *ctx, T *x, T *b, T *p, T *q, double reduction,
     if (fuse) {
       // q = A p with lambda = rholast / <p, q> in the same launch
       ctx->fuse_fin = FIN_CG_LAMBDA;
-      const int st = op_launch<T>(ctx, p, q, nullptr, T(1), 0, transpose, skip);
+      int st = op_launch<T>(ctx, p, q, nullptr, T(1), 0, transpose, skip);
       ctx->fuse_fin = 0;
       PDG_TRY(st);
+      // one block-Jacobi launch: b -= lambda q, defect check, q = M^{-1} b,
+      // beta = <q, b> / rholast; then x += lambda p and p = q + beta p
+      ctx->fuse_fin = FIN_CG_DEF_BETA;
+      ctx->fuse_q = q;
+      st = prec_op<T>(ctx, b, q, transpose, skip);
+      ctx->fuse_fin = 0;
+      ctx->fuse_q = nullptr;
+      PDG_TRY(st);
+      PDG_TRY(cg_update_px<T>(ctx, rc, ctx->ndof, x, p, q));
     } else {
       PDG_TRY(op_launch<T>(ctx, p, q, nullptr, T(1), 0, transpose, skip));          // q = A p
       PDG_TRY(dot<T>(ctx, rc, p, q, nullptr, nullptr, FIN_CG_LAMBDA, -1, -1, true)); // lambda
-    }
-    PDG_TRY(cg_update_xr<T>(ctx, rc, ctx->ndof, x, b, p, q));                     // x, b, def
-    if (fuse) {
-      // q = M^{-1} b with beta = <q, b> / rholast in the same launch
-      ctx->fuse_fin = FIN_CG_BETA;
-      const int st = prec_op<T>(ctx, b, q, transpose, skip);
-      ctx->fuse_fin = 0;
-      PDG_TRY(st);
-    } else {
+      PDG_TRY(cg_update_xr<T>(ctx, rc, ctx->ndof, x, b, p, q));                   // x, b, def
       PDG_TRY(prec_op<T>(ctx, b, q, transpose, skip));                        // q = M^-1 b
       PDG_TRY(dot<T>(ctx, rc, q, b, nullptr, nullptr, FIN_CG_BETA, -1, -1, true));   // beta
+      PDG_TRY(cg_update_p<T>(ctx, rc, ctx->ndof, p, q));                           // p = q + beta p
     }
-    PDG_TRY(cg_update_p<T>(ctx, rc, ctx->ndof, p, q));                             // p = q + beta p
     if (i % batch == 0 || i == maxit || i == 1) {
       PDG_TRY(fetch_state(ctx, scal, flags));
       if (flags[F_STATE]) done = true;
     }
   }
+  if (fuse) PDG_TRY(cg_finish_x<T>(ctx, rc, ctx->ndof, x, p));
   PDG_TRY(fetch_state(ctx, scal, flags));
   out->state = flags[F_STATE];
   out->def0 = scal[S_DEF0];

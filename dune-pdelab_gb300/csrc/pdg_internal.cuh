@@ -220,6 +220,7 @@ struct pdg_context {
   long fuse_max_blocks;
   int *fuse_cnt;
   int fuse_fin;
+  void *fuse_q;            // FIN_CG_DEF_BETA: the FDM launch first does b -= lambda q
 
   // staging buffers for host pointers
   double *stage_a, *stage_b;

@@ -161,11 +161,13 @@ constexpr int fdm_pad() {
 
 template <typename T, int D, int N>
 __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
-    k_fdm_apply(long ncell, const T *__restrict__ Q, const T *__restrict__ L,
-                const T *__restrict__ d, T *__restrict__ v, const int *__restrict__ skip,
-                const int *__restrict__ cells, int ncells, T scale, double *dot_part,
-                long dot_max_blocks, int *dot_cnt, double *dot_scal, int *dot_flags,
-                int dot_fin) {
+    k_fdm_apply(long ncell, const T *__restrict__ Q, const T *__restrict__ L, T *d, T *v,
+                const int *__restrict__ skip, const int *__restrict__ cells, int ncells, T scale,
+                double *dot_part, long dot_max_blocks, int *dot_cnt, double *dot_scal,
+                int *dot_flags, int dot_fin, const T *rq) {
+  // rq != null (fused CG): first d -= lambda rq (lambda = dot_scal[S_ALPHA]),
+  // written back; the fused dot then carries |d|^2 and <d, v>.  d, v and rq
+  // may alias element-wise: every entry is read and written by one thread.
   using C = PCfg<D, N>;
   constexpr int N2 = C::N2, NB = C::NB, TPC = C::TPC, CPB = C::CPB;
   if (skip && *skip) return;
@@ -184,7 +186,18 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
   T col[N];
 #pragma unroll
   for (int z = 0; z < N; z++) col[z] = d[(size_t)ee * NB + z * TPC + l];
-  T part = T(0);   // <d, v> of this thread's entries (fused dot product)
+  T part = T(0), part2 = T(0);   // <d, v> (and |d|^2) of this thread's entries
+  if (rq) {
+    const T lambda = (T)dot_scal[S_ALPHA];
+#pragma unroll
+    for (int z = 0; z < N; z++) {
+      const size_t i = (size_t)ee * NB + z * TPC + l;
+      col[z] -= lambda * rq[i];
+      if (active) d[i] = col[z];
+      part2 += col[z] * col[z];
+    }
+    if (!active) part2 = T(0);
+  }
   __syncthreads();
   if constexpr (D == 3) {
     const int tx = l % N, ty = l / N;
@@ -292,10 +305,17 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
       }
     }
   }
-  if (dot_part)
+  if (dot_part) {
+    // FIN_CG_DEF_BETA takes (|d|^2, <d, v>); the plain fused dot (<d, v>)
+    double s0 = (double)part, s1 = 0.0;
+    if (rq) {
+      s0 = (double)part2;
+      s1 = (double)part;
+    }
     reduce_tail_grouped<C::THREADS>(dot_part, dot_max_blocks, dot_cnt,
-                                    RedCtx{nullptr, dot_scal, dot_flags}, (double)part, 0.0,
-                                    dot_fin, -1, -1);
+                                    RedCtx{nullptr, dot_scal, dot_flags}, s0, s1, dot_fin, -1,
+                                    -1);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -589,9 +609,10 @@ static int fdm_apply_dn(pdg_context *ctx, const T *d, T *v, const int *skip, con
   const bool fuse = ctx->fuse_fin != 0;
   k_fdm_apply<T, D, N><<<blocks, C::THREADS, smem, ctx->stream>>>(
       ctx->ncell, (const T *)ctx->prec[std::is_same<T, double>::value ? 0 : 1].Q,
-      (const T *)ctx->prec[std::is_same<T, double>::value ? 0 : 1].L, d, v, skip, cells, ncells,
-      scale, fuse ? ctx->fuse_part : nullptr, ctx->fuse_max_blocks, ctx->fuse_cnt, ctx->red_out,
-      ctx->d_flag, ctx->fuse_fin);
+      (const T *)ctx->prec[std::is_same<T, double>::value ? 0 : 1].L, const_cast<T *>(d), v, skip,
+      cells, ncells, scale, fuse ? ctx->fuse_part : nullptr, ctx->fuse_max_blocks, ctx->fuse_cnt,
+      ctx->red_out, ctx->d_flag, ctx->fuse_fin,
+      (fuse && ctx->fuse_fin == FIN_CG_DEF_BETA) ? (const T *)ctx->fuse_q : nullptr);
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
 }

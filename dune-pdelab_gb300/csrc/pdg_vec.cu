@@ -129,6 +129,31 @@ __global__ void k_cg_p(long n, T *__restrict__ p, const T *__restrict__ z, RedCt
     p[i] = beta * p[i] + z[i];
 }
 
+// fused CG: x += lambda p ; p = z + beta p
+template <typename T>
+__global__ void k_cg_px(long n, T *__restrict__ x, T *__restrict__ p, const T *__restrict__ z,
+                        RedCtx rc) {
+  if (rc.flags[F_STATE]) return;
+  const T lambda = (T)rc.scal[S_ALPHA], beta = (T)rc.scal[S_BETA];
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const T pi = p[i];
+    x[i] += lambda * pi;
+    p[i] = beta * pi + z[i];
+  }
+}
+
+// x += lambda p for the iteration that stopped the fused CG (its px launch
+// was skipped)
+template <typename T>
+__global__ void k_cg_xfin(long n, T *__restrict__ x, const T *__restrict__ p, RedCtx rc) {
+  if (!rc.flags[F_XPEND]) return;
+  const T lambda = (T)rc.scal[S_ALPHA];
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    x[i] += lambda * p[i];
+}
+
 // BiCGSTABSolver: p = r (first half step) or p = beta (p - omega v) + r
 template <typename T>
 __global__ void k_bi_p(long n, T *__restrict__ p, const T *__restrict__ r,
@@ -183,6 +208,18 @@ int cg_update_p(pdg_context *ctx, const RedCtx &rc, long n, T *p, const T *z) {
   return PDG_OK;
 }
 template <typename T>
+int cg_update_px(pdg_context *ctx, const RedCtx &rc, long n, T *x, T *p, const T *z) {
+  k_cg_px<T><<<ew_grid(n), 256, 0, ctx->stream>>>(n, x, p, z, rc);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+template <typename T>
+int cg_finish_x(pdg_context *ctx, const RedCtx &rc, long n, T *x, const T *p) {
+  k_cg_xfin<T><<<ew_grid(n), 256, 0, ctx->stream>>>(n, x, p, rc);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+template <typename T>
 int bi_update_p(pdg_context *ctx, const RedCtx &rc, long n, T *p, const T *r, const T *v,
                 int first) {
   k_bi_p<T><<<ew_grid(n), 256, 0, ctx->stream>>>(n, p, r, v, rc, first);
@@ -213,6 +250,8 @@ int set_iter(pdg_context *ctx, const RedCtx &rc, double it) {
   template int cg_update_xr<T>(pdg_context *, const RedCtx &, long, T *, T *, const T *,    \
                                const T *);                                                  \
   template int cg_update_p<T>(pdg_context *, const RedCtx &, long, T *, const T *);         \
+  template int cg_update_px<T>(pdg_context *, const RedCtx &, long, T *, T *, const T *);   \
+  template int cg_finish_x<T>(pdg_context *, const RedCtx &, long, T *, const T *);         \
   template int bi_update_p<T>(pdg_context *, const RedCtx &, long, T *, const T *,          \
                               const T *, int);                                              \
   template int bi_update_half<T>(pdg_context *, const RedCtx &, long, T *, T *, const T *,  \

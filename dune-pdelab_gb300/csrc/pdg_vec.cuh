@@ -39,8 +39,9 @@ enum Slot {
 };
 
 // flag words (int): [0] state (0 running, 1 converged, 2 non-finite,
-// 3 breakdown), [1] reduction counter (last-block detection)
-enum { F_STATE = 0, F_COUNTER = 1, F_COUNT = 4 };
+// 3 breakdown), [1] reduction counter (last-block detection), [2] the CG
+// x update of the stopping iteration is still to be applied
+enum { F_STATE = 0, F_COUNTER = 1, F_XPEND = 2, F_COUNT = 4 };
 
 enum Finisher {
   FIN_STORE = 0,        // scal[slot0] = d0 ; scal[slot1] = d1
@@ -51,7 +52,9 @@ enum Finisher {
   FIN_BI_RHONEW = 5,    // rho_new = d0; breakdown checks
   FIN_BI_ALPHA = 6,     // h = d0; alpha = rho_new / h
   FIN_BI_OMEGA = 7,     // omega = d0 / d1
-  FIN_NORM = 8          // scal[slot0] = sqrt(d0)
+  FIN_NORM = 8,         // scal[slot0] = sqrt(d0)
+  FIN_CG_DEF_BETA = 9   // def = sqrt(d0) + convergence check; beta = d1 / rholast;
+                        // rholast = d1; a stop marks the iteration's x update pending
 };
 
 struct RedCtx {
@@ -98,6 +101,18 @@ __device__ inline void run_finisher(const RedCtx &rc, int fin, int slot0, int sl
       s[S_BETA] = d0 / s[S_RHO];
       s[S_RHO] = d0;
       break;
+    case FIN_CG_DEF_BETA: {
+      // CGSolver: the defect check after b -= lambda q, then (when it goes
+      // on) rho = <M^{-1} b, b>, beta = rho / rholast
+      const double def = sqrt(d0);
+      s[S_DEF] = def;
+      if (!isfinite(def)) fl[F_STATE] = 2;
+      else if (def < s[S_DEF0] * s[S_RED] || def < 1e-30) fl[F_STATE] = 1;
+      if (fl[F_STATE]) fl[F_XPEND] = 1;
+      s[S_BETA] = d1 / s[S_RHO];
+      s[S_RHO] = d1;
+      break;
+    }
     // BiCGSTABSolver breakdown tests are absolute (rho, omega <= 1e-80,
     // |h| < 1e-80).  With S_GUARD > 0 (FP32 inner solves, whose dot products
     // carry ~1e-7 relative noise) a relative test is added:
@@ -230,6 +245,13 @@ int cg_update_xr(pdg_context *ctx, const RedCtx &rc, long n, T *x, T *r, const T
                  const T *q);   // x += lambda p; r -= lambda q; def check
 template <typename T>
 int cg_update_p(pdg_context *ctx, const RedCtx &rc, long n, T *p, const T *z);  // p = z + beta p
+// fused CG: x += lambda p ; p = z + beta p (the residual update and defect
+// check ran in the preconditioner kernel) and, after the loop, the x update of
+// the stopping iteration
+template <typename T>
+int cg_update_px(pdg_context *ctx, const RedCtx &rc, long n, T *x, T *p, const T *z);
+template <typename T>
+int cg_finish_x(pdg_context *ctx, const RedCtx &rc, long n, T *x, const T *p);
 template <typename T>
 int bi_update_p(pdg_context *ctx, const RedCtx &rc, long n, T *p, const T *r, const T *v,
                 int first);   // p = r (first) or p = beta (p - omega v) + r

@@ -328,8 +328,9 @@ def test_mixed_adjoint_solve_uses_fp32_transpose(pdg, oracle, k, nc):
     assert np.linalg.norm(r - rhs) <= 1e-9 * np.linalg.norm(rhs)
 
 
-@pytest.mark.parametrize("k,nc", [(1, (9, 7, 6)), (2, (6, 5, 4)), (3, (5, 4, 4))])
-def test_mixed_cg_fused_dots_match_unfused(pdg, oracle, k, nc):
+@pytest.mark.parametrize("k,nc,inner_maxit", [(1, (9, 7, 6), 0), (2, (6, 5, 4), 0),
+                                               (3, (5, 4, 4), 0), (2, (6, 5, 4), 20)])
+def test_mixed_cg_fused_dots_match_unfused(pdg, oracle, k, nc, inner_maxit):
     # The FP32 inner CG computes <p, A p> inside the operator kernel and
     # <M^-1 r, r> inside the FDM block Jacobi kernel.  The dense block Jacobi
     # is the same exact block inverse but takes the separate dot kernels, so
@@ -340,7 +341,11 @@ def test_mixed_cg_fused_dots_match_unfused(pdg, oracle, k, nc):
     for kind in (pdg.PREC_BJ_FDM, pdg.PREC_BJ_DENSE):
         pdg.GridOperatorPreconditioner(go, kind=kind, precision=pdg.F32).pre()
         ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG, preconditioner=kind,
-                                                 mixed=True, inner_reduction=1e-4)
+                                                 mixed=True, inner_reduction=1e-4,
+                                                 maxiter=20000)
+        if inner_maxit:       # inner solves stopped by the iteration cap
+            ls.opts.inner_maxit = inner_maxit
+            ls.opts.max_outer = 2000
         u = np.zeros(go.ndof)
         slp = pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10)
         slp.apply()
