@@ -355,10 +355,12 @@ __device__ __forceinline__ int swz(int r) { return r ^ (((r >> 3) & 1) | (((r >>
 struct Q3Cfg {
   static constexpr int N = 4, N2 = 16, NB = 64, CPB = 32, THREADS = 128;
   static constexpr int REC = 3 * N2 + 30;
-  // shared layout in 16-byte rows
+  // shared layout in 16-byte rows; once the y-neighbour rows are read, the
+  // P planes reuse the YL run and the z-face terms (FS rows) the YH run
   static constexpr int OWN = (CPB + 2) * 16, RUN = CPB * 16, FS = 4 * CPB * 4;
   static constexpr int RECR = (CPB * REC + 4 + 3) / 4;   // records (+ phase slack)
-  static constexpr int ROWS = OWN + 2 * RUN + RUN + FS + RECR;
+  static constexpr int ROWS = OWN + 2 * RUN + RECR;
+  static_assert(FS <= RUN, "z-face terms must fit the YH run");
 };
 
 __device__ __forceinline__ float4 ld4(const float *p, bool vec) {
@@ -366,7 +368,10 @@ __device__ __forceinline__ float4 ld4(const float *p, bool vec) {
   return make_float4(p[0], p[1], p[2], p[3]);
 }
 
-__global__ void __launch_bounds__(Q3Cfg::THREADS)
+// 6 blocks of 128 threads per SM (35 KB of shared memory each): 333 us at
+// 96^3 Q3, against 351 us with the compiler's free register choice (96
+// registers, 5 blocks per SM) and 378 us without the aliased runs
+__global__ void __launch_bounds__(Q3Cfg::THREADS, 6)
     k_apply32_q3(const OpParams<float> p, const ApplyArgs<float> a, const float *__restrict__ rec,
                  const EdgeTab tb) {
   using C = Q3Cfg;
@@ -374,11 +379,11 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS)
   extern __shared__ __align__(16) float4 sm4[];
   if (a.skip && *a.skip) return;
   float4 *OWN = sm4;                 // cells e0-1 .. e0+CPB, swizzled rows
-  float4 *YL = OWN + C::OWN;         // cells e - nx
-  float4 *YH = YL + C::RUN;          // cells e + nx
-  float4 *PS = YH + C::RUN;          // stage-1 planes P
-  float4 *FS = PS + C::RUN;          // z-face terms [lo s1, lo s2, hi s1, hi s2][cell][row]
-  float *RS0 = reinterpret_cast<float *>(FS + C::FS);
+  float4 *YL = OWN + C::OWN;         // cells e - nx; then the stage-1 planes P
+  float4 *YH = YL + C::RUN;          // cells e + nx; then the z-face terms
+  float4 *PS = YL;                   // [cell][plane][row], swizzled
+  float4 *FS = YH;                   // [lo s1, lo s2, hi s1, hi s2][cell][row]
+  float *RS0 = reinterpret_cast<float *>(YH + C::RUN);
 
   const long e0 = (long)blockIdx.x * CPB;
   const long ncell = p.ncell;
@@ -447,14 +452,6 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS)
                        coupled && ix[2] > 0, coupled && ix[2] + 1 < p.nc[2]};
   const bool tr = a.transpose != 0;
 
-  // z-neighbour rows (plane q, row z) straight from global memory, issued
-  // before the wait so they overlap the staging copies
-  float4 zl[N], zh[N];
-#pragma unroll
-  for (int q = 0; q < N; q++) {
-    zl[q] = has[4] ? ld4(x + (ee - sxy) * NB + q * N2 + z * N, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
-    zh[q] = has[5] ? ld4(x + (ee + sxy) * NB + q * N2 + z * N, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
-  }
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();
 
@@ -466,28 +463,6 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS)
   auto row = [](const float4 &v, int i) -> float {
     return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
   };
-
-  // ---- z faces of the face points of row z ----
-  {
-    float s1l[N], s2l[N], s1h[N], s2h[N];
-#pragma unroll
-    for (int xx = 0; xx < N; xx++) {
-      float dvl = 0.f, dvh = 0.f;
-#pragma unroll
-      for (int q = 0; q < N; q++) {
-        dvl += tb.d1[q] * row(zl[q], xx);
-        dvh += tb.d0[q] * row(zh[q], xx);
-      }
-      face_s(cf + 20, false, tr, row(zl[N - 1], xx), dvl, s1l[xx], s2l[xx]);
-      face_s(cf + 25, true, tr, row(zh[0], xx), dvh, s1h[xx], s2h[xx]);
-      if (!has[4]) { s1l[xx] = 0.f; s2l[xx] = 0.f; }
-      if (!has[5]) { s1h[xx] = 0.f; s2h[xx] = 0.f; }
-    }
-    FS[(0 * CPB + cs) * 4 + z] = make_float4(s1l[0], s1l[1], s1l[2], s1l[3]);
-    FS[(1 * CPB + cs) * 4 + z] = make_float4(s2l[0], s2l[1], s2l[2], s2l[3]);
-    FS[(2 * CPB + cs) * 4 + z] = make_float4(s1h[0], s1h[1], s1h[2], s1h[3]);
-    FS[(3 * CPB + cs) * 4 + z] = make_float4(s2h[0], s2h[1], s2h[2], s2h[3]);
-  }
 
   // ---- stage 1: plane z ----
   float u[N][N];
@@ -532,6 +507,40 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS)
       if (!has[3]) { ys1h[xx] = 0.f; ys2h[xx] = 0.f; }
     }
   }
+  // every thread has read its y-neighbour rows: YL and YH are free
+  __syncthreads();
+
+  // ---- z faces of the face points of row z ----
+  {
+    // z-neighbour rows (plane q, row z) straight from global memory
+    float4 zl[N], zh[N];
+#pragma unroll
+    for (int q = 0; q < N; q++) {
+      zl[q] = has[4] ? ld4(x + (ee - sxy) * NB + q * N2 + z * N, vec)
+                     : make_float4(0.f, 0.f, 0.f, 0.f);
+      zh[q] = has[5] ? ld4(x + (ee + sxy) * NB + q * N2 + z * N, vec)
+                     : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    float s1l[N], s2l[N], s1h[N], s2h[N];
+#pragma unroll
+    for (int xx = 0; xx < N; xx++) {
+      float dvl = 0.f, dvh = 0.f;
+#pragma unroll
+      for (int q = 0; q < N; q++) {
+        dvl += tb.d1[q] * row(zl[q], xx);
+        dvh += tb.d0[q] * row(zh[q], xx);
+      }
+      face_s(cf + 20, false, tr, row(zl[N - 1], xx), dvl, s1l[xx], s2l[xx]);
+      face_s(cf + 25, true, tr, row(zh[0], xx), dvh, s1h[xx], s2h[xx]);
+      if (!has[4]) { s1l[xx] = 0.f; s2l[xx] = 0.f; }
+      if (!has[5]) { s1h[xx] = 0.f; s2h[xx] = 0.f; }
+    }
+    FS[(0 * CPB + cs) * 4 + z] = make_float4(s1l[0], s1l[1], s1l[2], s1l[3]);
+    FS[(1 * CPB + cs) * 4 + z] = make_float4(s2l[0], s2l[1], s2l[2], s2l[3]);
+    FS[(2 * CPB + cs) * 4 + z] = make_float4(s1h[0], s1h[1], s1h[2], s1h[3]);
+    FS[(3 * CPB + cs) * 4 + z] = make_float4(s2h[0], s2h[1], s2h[2], s2h[3]);
+  }
+
   float P[N][N];
   {
     float X[N][N];
