@@ -2,6 +2,7 @@
 // fused Krylov vector updates (dune-istl CGSolver / BiCGSTABSolver
 // recurrences), and precision conversions for defect correction.
 #include <cmath>
+#include <cstdint>
 
 #include "pdg_vec.cuh"
 
@@ -207,9 +208,36 @@ int cg_update_p(pdg_context *ctx, const RedCtx &rc, long n, T *p, const T *z) {
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
 }
+// FP32 vectors, 16-byte accesses (n4 = n / 4 float4 elements)
+__global__ void k_cg_px4(long n4, float4 *__restrict__ x, float4 *__restrict__ p,
+                         const float4 *__restrict__ z, RedCtx rc) {
+  if (rc.flags[F_STATE]) return;
+  const float lambda = (float)rc.scal[S_ALPHA], beta = (float)rc.scal[S_BETA];
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+    const float4 pi = p[i], zi = z[i];
+    float4 xi = x[i];
+    xi.x += lambda * pi.x; xi.y += lambda * pi.y; xi.z += lambda * pi.z; xi.w += lambda * pi.w;
+    x[i] = xi;
+    p[i] = make_float4(beta * pi.x + zi.x, beta * pi.y + zi.y, beta * pi.z + zi.z,
+                       beta * pi.w + zi.w);
+  }
+}
+
 template <typename T>
 int cg_update_px(pdg_context *ctx, const RedCtx &rc, long n, T *x, T *p, const T *z) {
-  k_cg_px<T><<<ew_grid(n), 256, 0, ctx->stream>>>(n, x, p, z, rc);
+  const bool vec = std::is_same<T, float>::value && n % 4 == 0 &&
+                   ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(p) |
+                     reinterpret_cast<uintptr_t>(z)) & 15) == 0;
+  if (vec) {
+    long g = (n / 4 + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    k_cg_px4<<<(unsigned)g, 256, 0, ctx->stream>>>(n / 4, reinterpret_cast<float4 *>(x),
+                                                   reinterpret_cast<float4 *>(p),
+                                                   reinterpret_cast<const float4 *>(z), rc);
+  } else {
+    k_cg_px<T><<<ew_grid(n), 256, 0, ctx->stream>>>(n, x, p, z, rc);
+  }
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
 }
