@@ -120,6 +120,38 @@ def dist_setup():
     return world, rank, local
 
 
+# ---- replicas on N GPUs: host logic shared by the arms ---------------------
+# The path does not shard across GPUs here (one GPU per box): every rank runs
+# the whole workload as an independent replica; the job's time is that of its
+# slowest rank and its throughput counts the units of all ranks.
+def max_over_ranks(x, world, device=None):
+    """Maximum of x over the ranks (float; x itself when world == 1)."""
+    if world == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, units_per_rank, seconds):
+    """Whole-job rate: the units of all ranks over the slowest rank's time."""
+    return world * units_per_rank / seconds
+
+
+def gather_checksums(value, world, device=None):
+    """All ranks' checksums of their replica results (a list of floats)."""
+    if world == 1:
+        return [float(value)]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    out = [torch.zeros_like(t) for _ in range(world)]
+    dist.all_gather(out, t)
+    return [float(o.item()) for o in out]
+
+
 def make_problem(pdg, np, device, wl=WORKLOAD):
     n = wl["cells"]
     go = pdg.GridOperator(wl["dim"], wl["degree"], (n,) * wl["dim"], alpha=wl["alpha"],
@@ -328,12 +360,12 @@ def run_gb300(args, world, rank, local):
             torch.cuda.synchronize()
             barrier()
         ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * ndof / (ms * 1e-3) / 1e9
+    ms = max_over_ranks(ms, world, dev)
+    value = job_throughput(world, ndof, ms * 1e-3) / 1e9
     clocks = clk.summary()
+    # replicas compute the same apply: their results must agree bit for bit
+    sums = gather_checksums(float(ys[0].double().sum().item()), world, dev)
+    replicas_identical = all(x == sums[0] for x in sums)
 
     # end to end through the public API with host (pinned) buffers
     xh = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
@@ -346,11 +378,8 @@ def run_gb300(args, world, rank, local):
     for _ in range(args.steps):
         op.apply(xh, yh)       # H2D x, kernel, D2H y, synchronise
     t_e2e = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([t_e2e], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(t.item())
-    e2e = {"value": world * ndof * args.steps / t_e2e / 1e9, "unit": "GDoF/s",
+    t_e2e = max_over_ranks(t_e2e, world, dev)
+    e2e = {"value": job_throughput(world, ndof * args.steps, t_e2e) / 1e9, "unit": "GDoF/s",
            "h2d_bytes_per_step": ndof * 8, "d2h_bytes_per_step": ndof * 8}
 
     if rank != 0:
@@ -412,6 +441,7 @@ def run_gb300(args, world, rank, local):
                          f"> 129 MB L2)",
                    "parallelism": f"replicas x{world}"},
         "e2e": e2e, "gpu_launches": args.steps, "clocks": clocks, "roofline": roofline,
+        "replicas_identical": replicas_identical,
         "cpu_baseline": cpu,
     }
     line.update(extras)
