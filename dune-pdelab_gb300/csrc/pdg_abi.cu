@@ -823,6 +823,7 @@ void pdg_default_prec_options(pdg_prec_options *o) {
   o->block_maxit = 100;
   o->block_precondition = 1;
   o->block_weight = 1.0;
+  o->dense_fp16 = 0;
 }
 
 int pdg_set_prec_options(pdg_context *ctx, const pdg_prec_options *o) {

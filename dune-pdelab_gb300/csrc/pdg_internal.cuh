@@ -115,6 +115,8 @@ struct PrecData {
   void *blk;       // iterative block Jacobi: diagonal blocks, column-major [ncell][nb*nb]
   void *invdiag;   // and the inverses of their diagonals [ncell][nb]
   int *iters;      // block-solve iteration counts of the last apply [ncell]
+  void *inv16;     // FP16 dense inverses (dense_fp16), scaled by invscale [ncell]
+  float *invscale;
 };
 
 }  // namespace pdg

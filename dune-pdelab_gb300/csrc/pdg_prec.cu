@@ -22,6 +22,7 @@
 //    with partial pivoting; the apply is a dense per-cell matvec.  Exact for
 //    every block (non-symmetric methods, reaction, convection).
 #include <cmath>
+#include <cuda_fp16.h>
 #include <vector>
 
 #include "pdg_ops.cuh"
@@ -435,6 +436,91 @@ __global__ void k_dense_apply(long ncell, int nb, const T *__restrict__ invT,
   }
 }
 
+// FP16 copy of the FP32 block inverses: per block the largest magnitude as
+// an FP32 scale, entries divided by it and rounded to FP16 (relative rounding
+// 2^-11 of the block's largest entry).  Columns are padded to nbp = nb rounded
+// up to 4 entries (zeros), so four rows of a column are one 8-byte load.  One
+// block per CTA.
+__global__ void k_inv_to_half(int nb, int nbp, const float *__restrict__ inv,
+                              __half *__restrict__ inv16, float *__restrict__ scale) {
+  __shared__ float red[32];
+  const long e = blockIdx.x;
+  const long n2 = (long)nb * nb;
+  const float *B = inv + e * n2;
+  float m = 0.f;
+  for (long i = threadIdx.x; i < n2; i += blockDim.x) m = fmaxf(m, fabsf(B[i]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) red[0] = m;
+  }
+  __syncthreads();
+  const float s = red[0] > 0.f ? red[0] : 1.f;
+  const float is = 1.f / s;
+  __half *O = inv16 + e * (long)nb * nbp;
+  for (long k = threadIdx.x; k < (long)nb * nbp; k += blockDim.x) {
+    const int j = (int)(k / nbp), i = (int)(k - (long)j * nbp);
+    O[k] = __float2half_rn(i < nb ? B[(long)j * nb + i] * is : 0.f);
+  }
+  if (threadIdx.x == 0) scale[e] = s;
+}
+
+// v = scale * s_e * B16_e d  (B16 column-major with column stride nbp, FP16),
+// FP32 vectors.  Thread (rg, jg): rows 4rg..4rg+3 over the columns j = jg mod
+// JG, one 8-byte load per column; the JG partial sums of a row are added in
+// shared memory.  The transposed apply reads rows of B^T (columns of B) with
+// scalar loads.
+constexpr int kDenseH = 128;   // threads per block of the FP16 apply
+__global__ void __launch_bounds__(kDenseH)
+    k_dense_apply_h(long ncell, int nb, int nbp, const __half *__restrict__ inv16,
+                    const float *__restrict__ bscale, const float *__restrict__ d,
+                    float *__restrict__ v, int transpose, const int *__restrict__ skip,
+                    const int *__restrict__ cells, float scale) {
+  if (skip && *skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *ds = reinterpret_cast<float *>(smem_raw);   // [nb]
+  float *part = ds + nbp;                             // [JG][nbp]
+  const long e = cells ? (long)cells[blockIdx.x] : (long)blockIdx.x;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) ds[i] = d[e * nb + i];
+  __syncthreads();
+  const __half *B = inv16 + e * (long)nb * nbp;
+  const float sc = scale * bscale[e];
+  if (!transpose) {
+    const int ngroups = nbp / 4;                  // row groups
+    const int JG = blockDim.x / ngroups;          // column subsets (>= 1)
+    const int rg = threadIdx.x % ngroups, jg = threadIdx.x / ngroups;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    if (jg < JG) {
+      for (int j = jg; j < nb; j += JG) {
+        const uint2 w = *reinterpret_cast<const uint2 *>(B + (long)j * nbp + 4 * rg);
+        const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&w.x));
+        const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&w.y));
+        const float dj = ds[j];
+        s0 += a.x * dj; s1 += a.y * dj; s2 += b.x * dj; s3 += b.y * dj;
+      }
+      float *pp = part + jg * nbp + 4 * rg;
+      pp[0] = s0; pp[1] = s1; pp[2] = s2; pp[3] = s3;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+      float r = 0.f;
+      for (int g = 0; g < JG; g++) r += part[g * nbp + i];
+      v[e * nb + i] = sc * r;
+    }
+  } else {
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+      float r = 0.f;
+      for (int j = 0; j < nb; j++) r += __half2float(B[(long)i * nbp + j]) * ds[j];
+      v[e * nb + i] = sc * r;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -555,6 +641,17 @@ static int dense_setup(pdg_context *ctx, int precision) {
   PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   cudaFree(D); cudaFree(bad);
   if (hbad) return set_error(PDG_EINVAL, "singular diagonal block");
+  if (precision == PDG_F32 && ctx->popt.dense_fp16) {
+    const int nbp = (nb + 3) / 4 * 4;
+    PDG_CUDA_TRY(cudaMalloc(&pd.inv16, (size_t)nc * nb * nbp * sizeof(__half)));
+    PDG_CUDA_TRY(cudaMalloc(&pd.invscale, nc * sizeof(float)));
+    k_inv_to_half<<<(unsigned)nc, 128, 0, ctx->stream>>>(nb, nbp, (const float *)pd.inv,
+                                                        (__half *)pd.inv16, pd.invscale);
+    PDG_CUDA_TRY(cudaGetLastError());
+    PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    cudaFree(pd.inv);
+    pd.inv = nullptr;
+  }
   return PDG_OK;
 }
 
@@ -566,7 +663,9 @@ void prec_free(pdg_context *ctx, int precision) {
   if (pd.blk) cudaFree(pd.blk);
   if (pd.invdiag) cudaFree(pd.invdiag);
   if (pd.iters) cudaFree(pd.iters);
-  pd = PrecData{0, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  if (pd.inv16) cudaFree(pd.inv16);
+  if (pd.invscale) cudaFree(pd.invscale);
+  pd = PrecData{0, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 }
 
 int prec_setup_impl(pdg_context *ctx, int kind, int precision) {
@@ -669,6 +768,19 @@ int block_solve(pdg_context *ctx, const T *d, T *v, int transpose, const int *sk
   if (base == PDG_PREC_BJ_DENSE) {
     const int nb = ctx->nb;
     const int threads = ((nb + 31) / 32) * 32;
+    if constexpr (std::is_same<T, float>::value) {
+      if (pd.inv16) {
+        // blocks up to nb = 512 (degree 7 in 3D): at least one column subset
+        const int nbp = (nb + 3) / 4 * 4;
+        if (nbp / 4 > kDenseH) return set_error(PDG_EUNSUPPORTED, "FP16 dense blocks: nb > 512");
+        const size_t sm = sizeof(float) * (nbp + (kDenseH / (nbp / 4)) * nbp);
+        k_dense_apply_h<<<(unsigned)work, kDenseH, sm, ctx->stream>>>(
+            ctx->ncell, nb, nbp, (const __half *)pd.inv16, pd.invscale, d, v, transpose, skip,
+            cells, scale);
+        PDG_CUDA_TRY(cudaGetLastError());
+        return PDG_OK;
+      }
+    }
     k_dense_apply<T><<<(unsigned)work, threads, sizeof(T) * nb, ctx->stream>>>(
         ctx->ncell, nb, (const T *)pd.inv, d, v, transpose, skip, cells, scale);
     PDG_CUDA_TRY(cudaGetLastError());

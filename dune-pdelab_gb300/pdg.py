@@ -71,7 +71,7 @@ class PrecOptions(C.Structure):
     """BlockSORPreconditionerLocalOperator omega + BlockSolverOptions."""
     _fields_ = [("omega", C.c_double), ("block_reduction", C.c_double),
                 ("block_maxit", C.c_int), ("block_precondition", C.c_int),
-                ("block_weight", C.c_double)]
+                ("block_weight", C.c_double), ("dense_fp16", C.c_int)]
 
 
 class NewtonOptions(C.Structure):

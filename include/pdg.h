@@ -92,6 +92,11 @@ typedef struct pdg_prec_options {
   int block_maxit;         /* iteration cap of each block solve (100) */
   int block_precondition;  /* point-Jacobi inside the block solve (1) */
   double block_weight;     /* weight of that point Jacobi (1.0) */
+  int dense_fp16;          /* PDG_PREC_BJ_DENSE in PDG_F32 precision: store each
+                              block inverse in FP16 with one FP32 scale per block
+                              (half the bytes per apply); no counterpart in the
+                              reference, for the inner solves of mixed precision
+                              (0) */
 } pdg_prec_options;
 /* precisions */
 enum { PDG_F64 = 0, PDG_F32 = 1 };

@@ -178,3 +178,49 @@ def test_mixed_flexible_adjoint_solve(pdg, oracle):
     assert res.converged and res.outer_iterations >= 1
     A = P.assemble_jacobian()
     assert _rel(P.blocks_apply(A, lam, transpose=True), rhs) <= 1e-9
+
+
+def test_dense_block_jacobi_fp16_storage(pdg, oracle):
+    # FP32 dense block Jacobi with the inverses stored in FP16 (one FP32 scale
+    # per block): within FP16 rounding of the FP32 inverse, and the mixed
+    # BiCGStab solve that uses it for its inner solves reaches the FP64 solution
+    import torch
+    go, P, rng = _pair(pdg, oracle, 3, (4, 4, 3), seed=81)
+    go.set_source(fc=np.ones(go.ncell))
+    d = torch.tensor(rng.uniform(-1, 1, go.ndof), dtype=torch.float32, device="cuda")
+    out = {}
+    for half in (0, 1):
+        go.set_prec_options(dense_fp16=half)
+        prec = pdg.GridOperatorPreconditioner(go, kind=pdg.PREC_BJ_DENSE, precision=pdg.F32)
+        prec.pre()
+        v = torch.zeros_like(d)
+        torch.cuda.synchronize()
+        prec.apply(v, d)
+        torch.cuda.synchronize()
+        out[half] = v.cpu().double().numpy()
+    assert _rel(out[1], out[0]) <= 4e-3
+    assert _rel(out[1], out[0]) > 0          # the FP16 path really ran
+    # mixed solve (FP64 flexible GMRES around FP32 BiCGStab) with FP16 blocks
+    go.set_prec_options(dense_fp16=1)
+    sols = {}
+    for mixed in (0, 1):
+        pdg.GridOperatorPreconditioner(go, kind=pdg.PREC_BJ_DENSE,
+                                       precision=pdg.F32 if mixed else pdg.F64).pre()
+        ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.BICGSTAB,
+                                                 preconditioner=pdg.PREC_BJ_DENSE, mixed=mixed,
+                                                 maxiter=5000, inner_reduction=1e-1)
+        u = np.zeros(go.ndof)
+        slp = pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10)
+        slp.apply()
+        assert slp.result().converged
+        sols[mixed] = u
+    assert _rel(sols[1], sols[0]) <= 1e-8
+    # the transposed FP16 block apply, inside the mixed adjoint solve
+    rhs = rng.uniform(-1, 1, go.ndof)
+    lam = {}
+    for mixed in (0, 1):
+        o = pdg.default_options(method=pdg.BICGSTAB, preconditioner=pdg.PREC_BJ_DENSE,
+                                reduction=1e-11, mixed=mixed, maxit=20000, inner_reduction=1e-1)
+        lam[mixed] = np.zeros(go.ndof)
+        assert go.adjoint_solve(rhs, lam[mixed], o).converged
+    assert _rel(lam[1], lam[0]) <= 1e-8
