@@ -159,6 +159,11 @@ def make_problem(pdg, np, device, wl=WORKLOAD):
     rng = np.random.default_rng(wl["seed"])
     logK = rng.standard_normal(go.ncell)
     go.set_permeability(logK, is_log=True)
+    if wl.get("convection"):
+        # the convection-diffusion-reaction operator of the 48^3 Q4 leg:
+        # upwind b = curl of a seeded 8-mode Fourier potential, c = 1
+        go.set_reaction(np.ones(go.ncell))
+        go.set_velocity_modes(pdg.fourier_velocity_modes(5))
     return go, logK
 
 
@@ -394,7 +399,8 @@ def run_gb300(args, world, rank, local):
     achieved = fl / (ms * 1e-3) / 1e12
     alg_bytes = 2 * esz * ndof + esz * ncell
     pk = peaks["fp32" if f32 else "fp64"]
-    wname = f"sipg3d_q{WORKLOAD['degree']}_{WORKLOAD['cells']}^3_{args.precision}_apply"
+    wname = (f"{'cdr' if WORKLOAD.get('convection') else 'sipg'}3d_q{WORKLOAD['degree']}_"
+             f"{WORKLOAD['cells']}^3_{args.precision}_apply")
     roofline = {
         "bound": "fp32" if f32 else "fp64", "achieved": achieved, "peak": pk,
         "unit": "TFLOP/s", "frac": achieved / pk if pk else None,
@@ -866,11 +872,16 @@ def main():
     ap.add_argument("--degree", type=int, default=None, help="override polynomial degree")
     ap.add_argument("--precision", choices=["f64", "f32"], default="f64",
                     help="operator precision of the timed steps")
+    ap.add_argument("--convection", action="store_true",
+                    help="time the convection-diffusion-reaction operator (upwind velocity "
+                         "and reaction of the 48^3 Q4 leg) instead of pure diffusion")
     args = ap.parse_args()
     if args.cells:
         WORKLOAD["cells"] = args.cells
     if args.degree:
         WORKLOAD["degree"] = args.degree
+    if args.convection:
+        WORKLOAD["convection"] = True
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_setup()

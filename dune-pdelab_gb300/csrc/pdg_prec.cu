@@ -22,6 +22,7 @@
 //    with partial pivoting; the apply is a dense per-cell matvec.  Exact for
 //    every block (non-symmetric methods, reaction, convection).
 #include <cmath>
+#include <cstdint>
 #include <cuda_fp16.h>
 #include <vector>
 
@@ -521,6 +522,219 @@ __global__ void __launch_bounds__(kDenseH)
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// FDM apply, 3D Q3 FP32 (the inner solves of the mixed-precision CG): one
+// z-plane of one cell per thread.  The x and y contractions of the plane run in
+// registers; the two z contractions go through one shared exchange buffer of
+// 16-byte rows with the operator's row swizzle (conflict-free for a quarter warp
+// of two cells x four planes).  d and, with the fused CG residual update, q are
+// staged with coalesced 16-byte copies; the update b -= lambda q runs as one
+// coalesced pass before the plane work.  Same fused dot products as k_fdm_apply.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int fswz(int r) { return r ^ (((r >> 3) & 1) | (((r >> 4) & 1) << 1)); }
+
+struct FdmQ3Cfg {
+  static constexpr int N = 4, NB = 64, CPB = 32, THREADS = 128;
+  static constexpr int RUN = CPB * 16;               // 16-byte rows of a run of cells
+  static constexpr int QROWS = CPB * 12, LROWS = CPB * 3;
+  static constexpr int ROWS = 2 * RUN + QROWS + LROWS;
+};
+
+__global__ void __launch_bounds__(FdmQ3Cfg::THREADS)
+    k_fdm32_q3(long ncell, const float *__restrict__ Q, const float *__restrict__ L, float *d,
+               float *v, const int *__restrict__ skip, float scale, double *dot_part,
+               long dot_max_blocks, int *dot_cnt, double *dot_scal, int *dot_flags, int dot_fin,
+               const float *rq) {
+  using C = FdmQ3Cfg;
+  constexpr int N = 4, NB = 64, CPB = C::CPB;
+  extern __shared__ __align__(16) float4 fsm[];
+  if (skip && *skip) return;
+  float4 *DR = fsm;                     // d (then b - lambda q) of the run, swizzled
+  float4 *PR = DR + C::RUN;             // q of the run, then the z-exchange planes
+  float4 *QS = PR + C::RUN;             // factors Q [cell][dir][4 rows]
+  float4 *LS = QS + C::QROWS;           // eigenvalues L [cell][dir]
+  const long e0 = (long)blockIdx.x * CPB;
+  const long ndof = ncell * NB;
+  const bool vec = ((reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(v) |
+                     reinterpret_cast<uintptr_t>(rq)) & 15) == 0;
+  auto cp16 = [](float4 *dst, const float *src) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src) : "memory");
+  };
+  for (int r = threadIdx.x; r < C::RUN; r += C::THREADS) {
+    const long g = e0 * NB + 4L * r;
+    float4 *dd = DR + fswz(r), *dq = PR + fswz(r);
+    if (g < ndof) {
+      if (vec) {
+        cp16(dd, d + g);
+        if (rq) cp16(dq, rq + g);
+      } else {
+        *dd = make_float4(d[g], d[g + 1], d[g + 2], d[g + 3]);
+        if (rq) *dq = make_float4(rq[g], rq[g + 1], rq[g + 2], rq[g + 3]);
+      }
+    } else {
+      *dd = make_float4(0.f, 0.f, 0.f, 0.f);
+      *dq = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+  // factors: contiguous runs, 16-byte aligned (48 and 12 floats per cell, 32 cells)
+  const long cmax = ncell - e0 < CPB ? ncell - e0 : CPB;
+  for (int r = threadIdx.x; r < C::QROWS; r += C::THREADS) {
+    if (r < cmax * 12) cp16(QS + r, Q + e0 * 48 + 4L * r);
+    else QS[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  for (int r = threadIdx.x; r < C::LROWS; r += C::THREADS) {
+    if (r < cmax * 3) cp16(LS + r, L + e0 * 12 + 4L * r);
+    else LS[r] = make_float4(1.f, 1.f, 1.f, 1.f);
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads();
+
+  float part2 = 0.f;   // |b - lambda q|^2 (fused CG residual update)
+  if (rq) {
+    const float lambda = (float)dot_scal[S_ALPHA];
+    for (int r = threadIdx.x; r < C::RUN; r += C::THREADS) {
+      const long g = e0 * NB + 4L * r;
+      if (g >= ndof) break;
+      const float4 a = DR[fswz(r)], q = PR[fswz(r)];
+      const float4 b = make_float4(a.x - lambda * q.x, a.y - lambda * q.y, a.z - lambda * q.z,
+                                   a.w - lambda * q.w);
+      DR[fswz(r)] = b;
+      if (vec) *reinterpret_cast<float4 *>(d + g) = b;
+      else { d[g] = b.x; d[g + 1] = b.y; d[g + 2] = b.z; d[g + 3] = b.w; }
+      part2 += b.x * b.x + b.y * b.y + b.z * b.z + b.w * b.w;
+    }
+    __syncthreads();
+  }
+
+  const int t = threadIdx.x, cs = t >> 2, z = t & 3;
+  const float4 *Qc = QS + cs * 12;   // Qx rows 0..3, Qy rows 4..7, Qz rows 8..11
+  auto el = [](const float4 &w, int i) -> float {
+    return i == 0 ? w.x : (i == 1 ? w.y : (i == 2 ? w.z : w.w));
+  };
+  float u[N][N];
+#pragma unroll
+  for (int y = 0; y < N; y++) {
+    const float4 w = DR[fswz(cs * 16 + z * 4 + y)];
+    u[y][0] = w.x; u[y][1] = w.y; u[y][2] = w.z; u[y][3] = w.w;
+  }
+  // forward x then y (registers): w[y'][x'] = sum_y Qy[y][y'] sum_x Qx[x][x'] u[y][x]
+  {
+    float t1[N][N];
+#pragma unroll
+    for (int y = 0; y < N; y++)
+#pragma unroll
+      for (int xp = 0; xp < N; xp++) {
+        float s = 0.f;
+#pragma unroll
+        for (int x = 0; x < N; x++) s += el(Qc[x], xp) * u[y][x];
+        t1[y][xp] = s;
+      }
+#pragma unroll
+    for (int yp = 0; yp < N; yp++)
+#pragma unroll
+      for (int xp = 0; xp < N; xp++) {
+        float s = 0.f;
+#pragma unroll
+        for (int y = 0; y < N; y++) s += el(Qc[4 + y], yp) * t1[y][xp];
+        u[yp][xp] = s;
+      }
+  }
+#pragma unroll
+  for (int y = 0; y < N; y++) PR[fswz(cs * 16 + z * 4 + y)] = make_float4(u[y][0], u[y][1], u[y][2], u[y][3]);
+  __syncthreads();
+  // forward z + scaling: c_z'[y][x] = sum_z Qz[z][z'] w_z[y][x] / (Lx[x] + Ly[y] + Lz[z'])
+  {
+    float qzc[N];
+#pragma unroll
+    for (int zz = 0; zz < N; zz++) qzc[zz] = el(Qc[8 + zz], z);
+    const float4 lx = LS[cs * 3], ly = LS[cs * 3 + 1];
+    const float lz = el(LS[cs * 3 + 2], z);
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int zz = 0; zz < N; zz++) {
+        const float4 w = PR[fswz(cs * 16 + zz * 4 + y)];
+        acc.x += qzc[zz] * w.x; acc.y += qzc[zz] * w.y; acc.z += qzc[zz] * w.z; acc.w += qzc[zz] * w.w;
+      }
+      const float lyz = el(ly, y) + lz;
+      u[y][0] = __fdividef(acc.x, lx.x + lyz);
+      u[y][1] = __fdividef(acc.y, lx.y + lyz);
+      u[y][2] = __fdividef(acc.z, lx.z + lyz);
+      u[y][3] = __fdividef(acc.w, lx.w + lyz);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int y = 0; y < N; y++) PR[fswz(cs * 16 + z * 4 + y)] = make_float4(u[y][0], u[y][1], u[y][2], u[y][3]);
+  __syncthreads();
+  // backward z: e_z[y][x] = sum_z' Qz[z][z'] c_z'[y][x]
+  {
+    const float4 qzr = Qc[8 + z];
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int zz = 0; zz < N; zz++) {
+        const float4 w = PR[fswz(cs * 16 + zz * 4 + y)];
+        const float qq = el(qzr, zz);
+        acc.x += qq * w.x; acc.y += qq * w.y; acc.z += qq * w.z; acc.w += qq * w.w;
+      }
+      u[y][0] = acc.x; u[y][1] = acc.y; u[y][2] = acc.z; u[y][3] = acc.w;
+    }
+  }
+  // backward y then x (registers): g[y][x] = sum_x' Qx[x][x'] sum_y' Qy[y][y'] e[y'][x']
+  float g[N][N];
+  {
+    float t1[N][N];
+#pragma unroll
+    for (int y = 0; y < N; y++)
+#pragma unroll
+      for (int x = 0; x < N; x++) {
+        float s = 0.f;
+#pragma unroll
+        for (int yp = 0; yp < N; yp++) s += el(Qc[4 + y], yp) * u[yp][x];
+        t1[y][x] = s;
+      }
+#pragma unroll
+    for (int y = 0; y < N; y++)
+#pragma unroll
+      for (int x = 0; x < N; x++) {
+        float s = 0.f;
+#pragma unroll
+        for (int xp = 0; xp < N; xp++) s += el(Qc[x], xp) * t1[y][xp];
+        g[y][x] = s;
+      }
+  }
+  // coalesced write-back through the exchange buffer; fused <d, v>
+  __syncthreads();
+#pragma unroll
+  for (int y = 0; y < N; y++) PR[fswz(cs * 16 + z * 4 + y)] = make_float4(g[y][0], g[y][1], g[y][2], g[y][3]);
+  __syncthreads();
+  float part = 0.f;
+  for (int r = threadIdx.x; r < C::RUN; r += C::THREADS) {
+    const long gi = e0 * NB + 4L * r;
+    if (gi >= ndof) break;
+    const float4 o = PR[fswz(r)], dd = DR[fswz(r)];
+    const float4 w = make_float4(scale * o.x, scale * o.y, scale * o.z, scale * o.w);
+    if (vec) *reinterpret_cast<float4 *>(v + gi) = w;
+    else { v[gi] = w.x; v[gi + 1] = w.y; v[gi + 2] = w.z; v[gi + 3] = w.w; }
+    part += dd.x * w.x + dd.y * w.y + dd.z * w.z + dd.w * w.w;
+  }
+  if (dot_part) {
+    double s0 = (double)part, s1 = 0.0;
+    if (rq) {
+      s0 = (double)part2;
+      s1 = (double)part;
+    }
+    reduce_tail_grouped<C::THREADS>(dot_part, dot_max_blocks, dot_cnt,
+                                    RedCtx{nullptr, dot_scal, dot_flags}, s0, s1, dot_fin, -1, -1);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -700,6 +914,27 @@ int prec_setup_impl(pdg_context *ctx, int kind, int precision) {
 template <typename T, int D, int N>
 static int fdm_apply_dn(pdg_context *ctx, const T *d, T *v, const int *skip, const int *cells,
                         int ncells, T scale) {
+  if constexpr (std::is_same<T, float>::value && D == 3 && N == 4) {
+    if (!cells) {
+      using Q = FdmQ3Cfg;
+      const size_t smem = 16 * Q::ROWS;
+      static int attr_dev = -1;
+      if (attr_dev != ctx->device) {
+        PDG_CUDA_TRY(cudaFuncSetAttribute(k_fdm32_q3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+        attr_dev = ctx->device;
+      }
+      const bool fuse = ctx->fuse_fin != 0;
+      const unsigned blocks = (unsigned)((ctx->ncell + Q::CPB - 1) / Q::CPB);
+      k_fdm32_q3<<<blocks, Q::THREADS, smem, ctx->stream>>>(
+          ctx->ncell, (const float *)ctx->prec[PDG_F32].Q, (const float *)ctx->prec[PDG_F32].L,
+          const_cast<float *>(d), v, skip, scale, fuse ? ctx->fuse_part : nullptr,
+          ctx->fuse_max_blocks, ctx->fuse_cnt, ctx->red_out, ctx->d_flag, ctx->fuse_fin,
+          (fuse && ctx->fuse_fin == FIN_CG_DEF_BETA) ? (const float *)ctx->fuse_q : nullptr);
+      PDG_CUDA_TRY(cudaGetLastError());
+      return PDG_OK;
+    }
+  }
   using C = PCfg<D, N>;
   const size_t smem = sizeof(T) * C::CPB * (C::PER_CELL + fdm_pad<T, D, N>());
   const long work = cells ? ncells : ctx->ncell;

@@ -353,3 +353,24 @@ def test_mixed_cg_fused_dots_match_unfused(pdg, oracle, k, nc, inner_maxit):
         sols[kind], its[kind] = u, slp.result().iterations
     assert abs(its[pdg.PREC_BJ_FDM] - its[pdg.PREC_BJ_DENSE]) <= max(2, its[pdg.PREC_BJ_DENSE] // 20)
     assert _rel(sols[pdg.PREC_BJ_FDM], sols[pdg.PREC_BJ_DENSE]) <= 1e-8
+
+
+@pytest.mark.parametrize("k,nc", [(3, (7, 5, 3)), (3, (40, 3, 2)), (3, (1, 1, 1)), (2, (6, 5, 4))])
+def test_block_jacobi_fdm_f32(pdg, oracle, k, nc):
+    # the FP32 FDM block Jacobi (Q3: one z-plane per thread, partial blocks of
+    # 32 cells) against the FP64 one
+    import torch
+    go, P, rng = _pair(pdg, oracle, 3, k, nc, seed=90 + k, react=True)
+    d = rng.uniform(-1, 1, go.ndof)
+    ref = np.zeros(go.ndof)
+    p64 = pdg.GridOperatorPreconditioner(go, kind=pdg.PREC_BJ_FDM, precision=pdg.F64)
+    p64.pre()
+    p64.apply(ref, d)
+    p32 = pdg.GridOperatorPreconditioner(go, kind=pdg.PREC_BJ_FDM, precision=pdg.F32)
+    p32.pre()
+    dt = torch.tensor(d, dtype=torch.float32, device="cuda")
+    vt = torch.zeros_like(dt)
+    torch.cuda.synchronize()
+    p32.apply(vt, dt)
+    torch.cuda.synchronize()
+    assert _rel(vt.cpu().double().numpy(), ref) <= TOL32
