@@ -32,7 +32,9 @@ struct CCfg {
   static constexpr int N2 = N * N, NB = N * N * N, TPC = N * N;
   static constexpr int CPB = (128 / TPC) > 0 ? (128 / TPC) : 1;
   static constexpr int THREADS = CPB * TPC;
-  static constexpr int PER_CELL = 4 * NB + 6 * N2;   // S0..S3, face fluxes
+  // S0..S3, then the face region: fluxes / face test results, own and
+  // neighbour partial traces (the latter two reused for the partial tests)
+  static constexpr int PER_CELL = 4 * NB + 18 * N2;
   static constexpr int TAB = 2 * N2;                 // B[q][a], D[q][a]
   static constexpr int VREC = 3 * NB;                // G_dir(q)
   static constexpr int FREC = 6 * N2;                // F_f(p)
@@ -115,7 +117,8 @@ __global__ void __launch_bounds__(CCfg<N>::THREADS)
   const int t = threadIdx.x, cs = t / TPC, l = t - cs * TPC;
   T *S0 = tB + C::TAB + cs * C::PER_CELL;
   T *S1 = S0 + NB, *S2 = S1 + NB, *S3 = S2 + NB;
-  T *fl = S3 + NB;                           // [6][N2]
+  T *fl = S3 + NB;                           // [6][N2] fluxes, then face test results
+  T *Ue = fl + 6 * N2, *Un = Ue + 6 * N2;    // [6][N2] partial traces (own, neighbour)
   if (a.skip && *a.skip) return;
   for (int i = t; i < C::TAB; i += blockDim.x) tB[i] = tabBD[i];
   const long li = (long)blockIdx.x * CPB + cs;
@@ -315,40 +318,57 @@ __global__ void __launch_bounds__(CCfg<N>::THREADS)
   }
 
   // ---------------- faces ----------------
-  // thread l evaluates face point p = l (tangential lexicographic) of every face
+  // Traces at the face points and the test with the face basis are
+  // sum-factorised through shared memory (the volume part has released
+  // S0..S2): thread l = (pa, pb) first contracts row pb of a node layer with
+  // B[pa][.], then column pa of the partial results with B[pb][.].
   const int pa = l % N, pb = l / N;
+  const int st[3] = {1, N, N2};
+  long nbr[6];
+#pragma unroll
+  for (int f = 0; f < 6; f++) {
+    const int dir = f >> 1, hi = f & 1;
+    if (hi) nbr[f] = ix[dir] + 1 < p.nc[dir] ? ee + stride[dir] : -1;
+    else nbr[f] = ix[dir] > 0 ? ee - stride[dir] : -1;
+  }
+  T Bp[N], Bq[N];   // B[pa][.] and B[pb][.] (face point -> node layer)
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    Bp[i] = tB[pa * N + i];
+    Bq[i] = tB[pb * N + i];
+  }
+  // per face, U[j][pa] = sum_i B[pa][i] layer[j][i] into Ue (own), Un (neighbour)
 #pragma unroll 1
   for (int f = 0; f < 6; f++) {
     const int dir = f >> 1, hi = f & 1;
-    long nb;
-    if (hi) nb = ix[dir] + 1 < p.nc[dir] ? ee + stride[dir] : -1;
-    else nb = ix[dir] > 0 ? ee - stride[dir] : -1;
     const int od0 = dir == 0 ? 1 : 0, od1 = dir == 2 ? 1 : 2;   // tangential dirs
-    const int st[3] = {1, N, N2};
     const int lay_e = hi ? N - 1 : 0, lay_n = hi ? 0 : N - 1;
-    // traces at point (pa along od0, pb along od1)
+    // row j = pb of the own and the neighbour's node layer
+    T se = T(0), sn = T(0);
+    const int rowe = lay_e * st[dir] + pb * st[od1], rown = lay_n * st[dir] + pb * st[od1];
+#pragma unroll
+    for (int i = 0; i < N; i++) se += Bp[i] * S3[rowe + i * st[od0]];
+    if (nbr[f] >= 0 && !a.diag_only) {
+      const T *xn = a.x + nbr[f] * NB;
+#pragma unroll
+      for (int i = 0; i < N; i++) sn += Bp[i] * xn[rown + i * st[od0]];
+    }
+    Ue[f * N2 + pb * N + pa] = se;
+    Un[f * N2 + pb * N + pa] = sn;
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int f = 0; f < 6; f++) {
     T ue = T(0), un = T(0);
 #pragma unroll
-    for (int j = 0; j < N; j++)
-#pragma unroll
-      for (int i = 0; i < N; i++) {
-        const T wgt = tB[pa * N + i] * tB[pb * N + j];
-        ue += wgt * S3[lay_e * st[dir] + i * st[od0] + j * st[od1]];
-      }
-    const bool use_nb = nb >= 0 && !a.diag_only;
-    if (use_nb) {
-      const T *xn = a.x + nb * NB;
-#pragma unroll
-      for (int j = 0; j < N; j++)
-#pragma unroll
-        for (int i = 0; i < N; i++) {
-          const T wgt = tB[pa * N + i] * tB[pb * N + j];
-          un += wgt * xn[lay_n * st[dir] + i * st[od0] + j * st[od1]];
-        }
+    for (int j = 0; j < N; j++) {
+      ue += Bq[j] * Ue[f * N2 + j * N + pa];
+      un += Bq[j] * Un[f * N2 + j * N + pa];
     }
     const T bnw = rec[C::VREC + f * N2 + l];
     T flux = T(0);
-    if (nb >= 0) {
+    if (nbr[f] >= 0) {
+      if (a.diag_only) un = T(0);
       if (!a.transpose) flux = (bnw >= T(0) ? ue : un) * bnw;
       else flux = bnw >= T(0) ? (ue - un) * bnw : T(0);
     } else {
@@ -359,7 +379,36 @@ __global__ void __launch_bounds__(CCfg<N>::THREADS)
     fl[f * N2 + l] = flux;
   }
   __syncthreads();
-  // test: node (tx, ty, z); face f contributes to its node layer
+  // test with the face basis: W[j][pa] = sum_i B[i][pa] flux[j][i] (into S2),
+  // then R[pb][pa] = sum_j B[j][pb] W[j][pa] (into fl, in place per face)
+  T Cp[N], Cq[N];   // B[.][pa] and B[.][pb]
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    Cp[i] = tB[i * N + pa];
+    Cq[i] = tB[i * N + pb];
+  }
+  T *Wt = Ue;       // [6][N2]; Ue's last reads were before the previous barrier
+#pragma unroll 1
+  for (int f = 0; f < 6; f++) {
+    T w = T(0);
+#pragma unroll
+    for (int i = 0; i < N; i++) w += Cp[i] * fl[f * N2 + pb * N + i];
+    Wt[f * N2 + pb * N + pa] = w;
+  }
+  __syncthreads();
+  T Rf[6];
+#pragma unroll
+  for (int f = 0; f < 6; f++) {
+    T rr = T(0);
+#pragma unroll
+    for (int j = 0; j < N; j++) rr += Cq[j] * Wt[f * N2 + j * N + pa];
+    Rf[f] = rr;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int f = 0; f < 6; f++) fl[f * N2 + pb * N + pa] = Rf[f];   // R[f][n1][n0]
+  __syncthreads();
+  // node (tx, ty, z) on the layer of face f receives R[f][n1][n0]
 #pragma unroll
   for (int z = 0; z < N; z++) {
     T s = T(0);
@@ -369,11 +418,7 @@ __global__ void __launch_bounds__(CCfg<N>::THREADS)
       const int dir = f >> 1, hi = f & 1;
       if (node[dir] != (hi ? N - 1 : 0)) continue;
       const int od0 = dir == 0 ? 1 : 0, od1 = dir == 2 ? 1 : 2;
-      const int n0 = node[od0], n1 = node[od1];
-#pragma unroll
-      for (int j = 0; j < N; j++)
-#pragma unroll
-        for (int i = 0; i < N; i++) s += tB[i * N + n0] * tB[j * N + n1] * fl[f * N2 + j * N + i];
+      s += fl[f * N2 + node[od1] * N + node[od0]];
     }
     r[z] += s;
   }
