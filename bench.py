@@ -344,6 +344,12 @@ def run_gb300(args, world, rank, local):
     ys = [torch.zeros(ndof, dtype=dt_, device=dev) for _ in range(npairs)]
     torch.cuda.synchronize()
     step_fn = (lambda x, y: go.jacobian_apply_f32(x, y)) if f32 else op.apply
+    if args.step == "prec":
+        # profiling runs: the FDM block-Jacobi apply in the step's precision
+        prec = pdg.GridOperatorPreconditioner(go, kind=pdg.PREC_BJ_FDM,
+                                              precision=pdg.F32 if f32 else pdg.F64)
+        prec.pre()
+        step_fn = lambda x, y: prec.apply(y, x)
 
     def barrier():
         if world > 1:
@@ -872,6 +878,9 @@ def main():
     ap.add_argument("--degree", type=int, default=None, help="override polynomial degree")
     ap.add_argument("--precision", choices=["f64", "f32"], default="f64",
                     help="operator precision of the timed steps")
+    ap.add_argument("--step", choices=["apply", "prec"], default="apply",
+                    help="profiling runs: time the FDM block-Jacobi apply instead of the "
+                         "operator (the roofline fields then describe the operator only)")
     ap.add_argument("--convection", action="store_true",
                     help="time the convection-diffusion-reaction operator (upwind velocity "
                          "and reaction of the 48^3 Q4 leg) instead of pure diffusion")

@@ -34,7 +34,13 @@ struct CCfg {
   static constexpr int THREADS = CPB * TPC;
   // S0..S3, then the face region: fluxes / face test results, own and
   // neighbour partial traces (the latter two reused for the partial tests)
-  static constexpr int PER_CELL = 4 * NB + 18 * N2;
+  static constexpr int PER_CELL_RAW = 4 * NB + 18 * N2;
+  // padding that puts the cells of a warp on different shared-memory banks
+  // (counted wavefronts of the volume part's accesses, 4-byte elements)
+  static constexpr int PAD = N == 2 ? 4 : N == 3 ? 27 : N == 4 ? 16 : N == 5 ? 3 : 0;
+  // (FP32; FP64 keeps the raw stride)
+  template <typename T>
+  static constexpr int per_cell() { return sizeof(T) == 4 ? PER_CELL_RAW + PAD : PER_CELL_RAW; }
   static constexpr int TAB = 2 * N2;                 // B[q][a], D[q][a]
   static constexpr int VREC = 3 * NB;                // G_dir(q)
   static constexpr int FREC = 6 * N2;                // F_f(p)
@@ -115,7 +121,7 @@ __global__ void __launch_bounds__(CCfg<N>::THREADS)
   T *tB = reinterpret_cast<T *>(smem_raw);   // B[q][a]
   T *tD = tB + N2;                           // D[q][a] (xi-derivative)
   const int t = threadIdx.x, cs = t / TPC, l = t - cs * TPC;
-  T *S0 = tB + C::TAB + cs * C::PER_CELL;
+  T *S0 = tB + C::TAB + cs * C::template per_cell<T>();
   T *S1 = S0 + NB, *S2 = S1 + NB, *S3 = S2 + NB;
   T *fl = S3 + NB;                           // [6][N2] fluxes, then face test results
   T *Ue = fl + 6 * N2, *Un = Ue + 6 * N2;    // [6][N2] partial traces (own, neighbour)
@@ -482,7 +488,7 @@ int conv_setup(pdg_context *ctx) {
 template <typename T, int N>
 static int conv_launch_n(pdg_context *ctx, const ApplyArgs<T> &a) {
   using C = CCfg<N>;
-  const size_t smem = sizeof(T) * (C::TAB + C::CPB * C::PER_CELL);
+  const size_t smem = sizeof(T) * (C::TAB + C::CPB * C::template per_cell<T>());
   static int attr_dev = -1;
   if (attr_dev != ctx->device) {
     PDG_CUDA_TRY(cudaFuncSetAttribute(k_conv<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -537,7 +537,10 @@ __device__ __forceinline__ int fswz(int r) { return r ^ (((r >> 3) & 1) | (((r >
 struct FdmQ3Cfg {
   static constexpr int N = 4, NB = 64, CPB = 32, THREADS = 128;
   static constexpr int RUN = CPB * 16;               // 16-byte rows of a run of cells
-  static constexpr int QROWS = CPB * 12, LROWS = CPB * 3;
+  // factor rows per cell: 12 (Qx, Qy, Qz), stored with a stride of 13 so that
+  // the scalar factor reads of the cells sharing a warp fall on distinct banks
+  static constexpr int QSTRIDE = 13;
+  static constexpr int QROWS = CPB * QSTRIDE, LROWS = CPB * 3;
   static constexpr int ROWS = 2 * RUN + QROWS + LROWS;
 };
 
@@ -580,9 +583,10 @@ __global__ void __launch_bounds__(FdmQ3Cfg::THREADS)
   }
   // factors: contiguous runs, 16-byte aligned (48 and 12 floats per cell, 32 cells)
   const long cmax = ncell - e0 < CPB ? ncell - e0 : CPB;
-  for (int r = threadIdx.x; r < C::QROWS; r += C::THREADS) {
-    if (r < cmax * 12) cp16(QS + r, Q + e0 * 48 + 4L * r);
-    else QS[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int r = threadIdx.x; r < CPB * 12; r += C::THREADS) {
+    float4 *dst = QS + (r / 12) * C::QSTRIDE + r % 12;
+    if (r < cmax * 12) cp16(dst, Q + e0 * 48 + 4L * r);
+    else *dst = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   for (int r = threadIdx.x; r < C::LROWS; r += C::THREADS) {
     if (r < cmax * 3) cp16(LS + r, L + e0 * 12 + 4L * r);
@@ -610,7 +614,7 @@ __global__ void __launch_bounds__(FdmQ3Cfg::THREADS)
   }
 
   const int t = threadIdx.x, cs = t >> 2, z = t & 3;
-  const float4 *Qc = QS + cs * 12;   // Qx rows 0..3, Qy rows 4..7, Qz rows 8..11
+  const float4 *Qc = QS + cs * C::QSTRIDE;   // Qx rows 0..3, Qy rows 4..7, Qz rows 8..11
   auto el = [](const float4 &w, int i) -> float {
     return i == 0 ? w.x : (i == 1 ? w.y : (i == 2 ? w.z : w.w));
   };
