@@ -832,6 +832,11 @@ int pdg_set_prec_options(pdg_context *ctx, const pdg_prec_options *o) {
   if (!(o->omega > 0.0 && o->omega < 2.0)) return set_error(PDG_EINVAL, "omega must be in (0,2)");
   if (!(o->block_reduction > 0.0) || o->block_maxit < 1)
     return set_error(PDG_EINVAL, "bad block solver options");
+  // the FP32 dense block inverses are stored per dense_fp16: a set-up made
+  // under the other setting is dropped (the next solve sets it up again)
+  if (o->dense_fp16 != ctx->popt.dense_fp16 &&
+      (ctx->prec[PDG_F32].kind & PDG_PREC_BLOCK_MASK) == PDG_PREC_BJ_DENSE)
+    prec_free(ctx, PDG_F32);
   ctx->popt = *o;
   ctx->op_gen++;
   return PDG_OK;
