@@ -277,6 +277,7 @@ static int fetch_state(pdg_context *ctx, double *scal, int *flags) {
   PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   if (scal) std::memcpy(scal, ctx->h_red, sizeof(double) * S_COUNT);
   if (flags) std::memcpy(flags, hf, sizeof(int) * F_COUNT);
+  if (hf[F_TMA]) return set_error(PDG_ETIMEOUT, "TMA staging of the FP32 operator timed out");
   return PDG_OK;
 }
 

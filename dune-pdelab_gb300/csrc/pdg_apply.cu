@@ -471,8 +471,10 @@ static int record_dn(pdg_context *ctx) {
 template <int N>
 static int record32_n(pdg_context *ctx) {
   using C = Cfg<3, N>;
+  // 16 floats of slack: bulk copies of a record run round their size up to
+  // 16 bytes
   if (!ctx->rec32)
-    PDG_CUDA_TRY(cudaMalloc(&ctx->rec32, sizeof(float) * C::REC * ctx->ncell));
+    PDG_CUDA_TRY(cudaMalloc(&ctx->rec32, sizeof(float) * (C::REC * ctx->ncell + 16)));
   OpParams<double> p = make_params<double>(ctx, ctx->K64, ctx->c64, ctx->tab64);
   const unsigned blocks = (unsigned)((ctx->ncell + 127) / 128);
   k_cell_record<float, 3, N><<<blocks, 128, 0, ctx->stream>>>(p, ctx->rec32);

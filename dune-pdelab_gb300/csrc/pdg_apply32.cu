@@ -25,7 +25,10 @@
 //     out = (Mhat_y (x) Mhat_x) Z + sum_z' Mhat_z[z][z'] P_z'
 //
 // The output is staged in shared memory and written back coalesced.
+#include <cuda.h>
+
 #include <cstdint>
+#include <cstring>
 #include <mutex>
 
 #include "pdg_vec.cuh"
@@ -341,16 +344,21 @@ __global__ void __launch_bounds__(P32Cfg<N>::THREADS)
 // ---------------------------------------------------------------------------
 // Q3 (N = 4) variant.  A row of a cell (4 floats along x at fixed y, z) is one
 // 16-byte vector, so every exchange goes through 128-bit shared accesses.
-// Staged runs are stored with the row swizzle swz(): a quarter warp (two
-// cells x four planes) then reads eight distinct 16-byte bank groups for
-// every row pattern of the kernel (own / neighbour planes, all planes of one
-// row, P planes), and consecutive staging stores stay conflict-free.
+// Staged runs are stored with the row swizzle swz(), the 128-byte pattern of
+// the tensor memory accelerator (16-byte chunk c of 128-byte line L at chunk
+// c ^ (L mod 8), buffers 1024-byte aligned): a quarter warp (two cells x four
+// planes) then reads eight distinct 16-byte bank groups for every row pattern
+// of the kernel (own / neighbour planes, all planes of one row, P planes), and
+// consecutive staging stores stay conflict-free.  With 16-byte aligned
+// vectors the runs are loaded by TMA tensor copies (the vector as a 2D tensor
+// of 128-byte lines; lines outside it read as zeros) and the record run by a
+// bulk copy, all completing on one mbarrier.
 // The z faces are not staged: thread z loads row y = z of the four planes of
 // each z neighbour straight from global memory (64 contiguous bytes per cell),
 // forms the face terms of the face points of that row and hands them to the
 // other planes through a small shared array.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int swz(int r) { return r ^ (((r >> 3) & 1) | (((r >> 4) & 1) << 1)); }
+__device__ __forceinline__ int swz(int r) { return (r & ~7) | ((r & 7) ^ ((r >> 3) & 7)); }
 
 struct Q3Cfg {
   static constexpr int N = 4, N2 = 16, NB = 64, CPB = 32, THREADS = 128;
@@ -359,9 +367,60 @@ struct Q3Cfg {
   // P planes reuse the YL run and the z-face terms (FS rows) the YH run
   static constexpr int OWN = (CPB + 2) * 16, RUN = CPB * 16, FS = 4 * CPB * 4;
   static constexpr int RECR = (CPB * REC + 4 + 3) / 4;   // records (+ phase slack)
-  static constexpr int ROWS = OWN + 2 * RUN + RECR;
+  // byte offsets from a 1024-byte aligned base (the swizzle atom)
+  static constexpr int OWN_B = 0, OWN_BYTES = (OWN * 16 + 1023) / 1024 * 1024;
+  static constexpr int YL_B = OWN_B + OWN_BYTES, YH_B = YL_B + RUN * 16;
+  static constexpr int REC_B = YH_B + RUN * 16;
+  static constexpr int SMEM = 1024 + REC_B + RECR * 16;   // + alignment slack
+  static constexpr int LINES_OWN = (CPB + 2) * 2, LINES_RUN = CPB * 2;   // 128-byte lines
   static_assert(FS <= RUN, "z-face terms must fit the YH run");
+  static_assert((RUN * 16) % 1024 == 0, "runs must keep the 1024-byte alignment");
 };
+
+// ---- TMA / mbarrier helpers (inline PTX) ------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+// true once phase `parity` of the barrier completed; at most `limit` polls
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int limit) {
+  for (int it = 0; it < limit; it++) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap *map, int c0, int c1,
+                                            unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_load(unsigned dst, const void *src, unsigned bytes,
+                                          unsigned bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(dst), "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+// polls of the staging barrier before a launch gives up (far above any
+// real copy time); the kernel then records the failure and returns
+constexpr int kTmaPolls = 1 << 22;
 
 __device__ __forceinline__ float4 ld4(const float *p, bool vec) {
   if (vec) return *reinterpret_cast<const float4 *>(p);
@@ -371,19 +430,24 @@ __device__ __forceinline__ float4 ld4(const float *p, bool vec) {
 // 6 blocks of 128 threads per SM (35 KB of shared memory each): 333 us at
 // 96^3 Q3, against 351 us with the compiler's free register choice (96
 // registers, 5 blocks per SM) and 378 us without the aliased runs
+template <bool kTma>
 __global__ void __launch_bounds__(Q3Cfg::THREADS, 6)
     k_apply32_q3(const OpParams<float> p, const ApplyArgs<float> a, const float *__restrict__ rec,
-                 const EdgeTab tb) {
+                 const EdgeTab tb, const __grid_constant__ CUtensorMap map_own,
+                 const __grid_constant__ CUtensorMap map_run, int *tma_err) {
   using C = Q3Cfg;
   constexpr int N = 4, N2 = 16, NB = 64, CPB = C::CPB, REC = C::REC;
-  extern __shared__ __align__(16) float4 sm4[];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ __align__(8) unsigned long long stage_bar;
   if (a.skip && *a.skip) return;
-  float4 *OWN = sm4;                 // cells e0-1 .. e0+CPB, swizzled rows
-  float4 *YL = OWN + C::OWN;         // cells e - nx; then the stage-1 planes P
-  float4 *YH = YL + C::RUN;          // cells e + nx; then the z-face terms
+  unsigned char *base = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smraw) + 1023) & ~static_cast<uintptr_t>(1023));
+  float4 *OWN = reinterpret_cast<float4 *>(base + C::OWN_B);   // cells e0-1 .. e0+CPB
+  float4 *YL = reinterpret_cast<float4 *>(base + C::YL_B);     // cells e - nx; then P
+  float4 *YH = reinterpret_cast<float4 *>(base + C::YH_B);     // cells e + nx; then z faces
   float4 *PS = YL;                   // [cell][plane][row], swizzled
   float4 *FS = YH;                   // [lo s1, lo s2, hi s1, hi s2][cell][row]
-  float *RS0 = reinterpret_cast<float *>(YH + C::RUN);
+  float *RS0 = reinterpret_cast<float *>(base + C::REC_B);
 
   const long e0 = (long)blockIdx.x * CPB;
   const long ncell = p.ncell;
@@ -411,10 +475,34 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS, 6)
       }
     }
   };
+  float *RS = RS0;
+  if constexpr (kTma) {
+    // one elected thread issues the copies; everyone waits on the barrier
+    const unsigned bar = smem_u32(&stage_bar);
+    const long ncp = ncell - e0 < CPB ? ncell - e0 : CPB;
+    const unsigned rbytes = (unsigned)((ncp * REC * 4 + 15) / 16 * 16);
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const unsigned lines = (unsigned)C::LINES_OWN + (coupled ? 2u * C::LINES_RUN : 0u);
+      mbar_expect_tx(bar, lines * 128u + rbytes);
+      tma_load_2d(smem_u32(OWN), &map_own, 0, (int)((e0 - 1) * 2), bar);
+      if (coupled) {
+        tma_load_2d(smem_u32(YL), &map_run, 0, (int)((e0 - sx) * 2), bar);
+        tma_load_2d(smem_u32(YH), &map_run, 0, (int)((e0 + sx) * 2), bar);
+      }
+      bulk_load(smem_u32(RS0), rec + e0 * REC, rbytes, bar);
+    }
+    if (!mbar_wait(bar, 0, kTmaPolls)) {
+      // record the failure, give the copies a last chance to land, leave
+      if (threadIdx.x == 0) atomicExch(tma_err, 1);
+      mbar_wait(bar, 0, kTmaPolls);
+      return;
+    }
+  } else {
   stage_rows(OWN, e0 - 1, CPB + 2, true);
   stage_rows(YL, e0 - sx, CPB, coupled);
   stage_rows(YH, e0 + sx, CPB, coupled);
-  float *RS;
   {
     // records: one contiguous run, copied in 16-byte chunks in phase with
     // their source (element-wise where a chunk leaves the array)
@@ -440,6 +528,7 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS, 6)
     RS = RS0 + ph;
   }
   asm volatile("cp.async.commit_group;\n" ::: "memory");
+  }
 
   const int t = threadIdx.x, cs = t >> 2, z = t & 3;
   const long e = e0 + cs;
@@ -702,10 +791,12 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS, 6)
     }
     part += pin.x * v.x + pin.y * v.y + pin.z * v.z + pin.w * v.w;
   }
+  // block sums in the YH run (its z-face terms were consumed in stage 2): no
+  // static shared arrays, six blocks per SM
   if (a.dot_part)
-    reduce_tail_grouped<Q3Cfg::THREADS>(a.dot_part, a.dot_max_blocks, a.dot_cnt,
-                                        RedCtx{nullptr, a.dot_scal, a.dot_flags}, (double)part,
-                                        0.0, a.dot_fin, -1, -1);
+    reduce_tail_grouped<Q3Cfg::THREADS, true>(
+        a.dot_part, a.dot_max_blocks, a.dot_cnt, RedCtx{nullptr, a.dot_scal, a.dot_flags},
+        (double)part, 0.0, a.dot_fin, -1, -1, reinterpret_cast<double *>(YH));
 }
 
 static EdgeTab make_edge_tab_uncached(const pdg_context *ctx) {
@@ -758,18 +849,99 @@ static int launch32_n(pdg_context *ctx, const ApplyArgs<float> &a, const OpParam
   return PDG_OK;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+// A FP32 vector of ndof values as a 2D tensor of 128-byte lines (32 floats),
+// boxes of `lines` lines, the 128-byte swizzle, zeros outside
+static bool encode_lines(CUtensorMap *m, const float *x, long ndof, unsigned lines) {
+  const EncodeTiledFn fn = encode_tiled();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {32, (cuuint64_t)(ndof / 32)};
+  const cuuint64_t strides[1] = {128};
+  const cuuint32_t box[2] = {32, lines};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(x), dims, strides, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// the maps of the last few input vectors (a Krylov solve applies the
+// operator to the same few buffers); per host thread, so no locking
+struct LinesMaps {
+  const float *x;
+  long ndof;
+  CUtensorMap own, run;
+};
+static bool lines_maps(const float *x, long ndof, const CUtensorMap **own,
+                       const CUtensorMap **run) {
+  constexpr int kSlots = 8;
+  thread_local LinesMaps cache[kSlots];
+  thread_local int next = 0;
+  for (int i = 0; i < kSlots; i++)
+    if (cache[i].x == x && cache[i].ndof == ndof) {
+      *own = &cache[i].own;
+      *run = &cache[i].run;
+      return true;
+    }
+  LinesMaps &c = cache[next];
+  if (!encode_lines(&c.own, x, ndof, Q3Cfg::LINES_OWN) ||
+      !encode_lines(&c.run, x, ndof, Q3Cfg::LINES_RUN)) {
+    c.x = nullptr;
+    return false;
+  }
+  c.x = x;
+  c.ndof = ndof;
+  next = (next + 1) % kSlots;
+  *own = &c.own;
+  *run = &c.run;
+  return true;
+}
+
 static int launch32_q3(pdg_context *ctx, const ApplyArgs<float> &a, const OpParams<float> &p,
                        const float *rec) {
-  const size_t smem = 16 * Q3Cfg::ROWS;
+  const size_t smem = Q3Cfg::SMEM;
   static int attr_dev = -1;
   if (attr_dev != ctx->device) {
-    PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply32_q3, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+    PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply32_q3<true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply32_q3<false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_dev = ctx->device;
   }
   const EdgeTab &tb = edge_tab(ctx);
   const unsigned blocks = (unsigned)((ctx->ncell + Q3Cfg::CPB - 1) / Q3Cfg::CPB);
-  k_apply32_q3<<<blocks, Q3Cfg::THREADS, smem, ctx->stream>>>(p, a, rec, tb);
+  int *err = ctx->d_flag + F_TMA;
+  const CUtensorMap *own = nullptr, *run = nullptr;
+  // TMA needs a 16-byte aligned vector (and records, from cudaMalloc)
+  if ((reinterpret_cast<uintptr_t>(a.x) & 15) == 0 && (reinterpret_cast<uintptr_t>(rec) & 15) == 0 &&
+      lines_maps(a.x, ctx->ndof, &own, &run)) {
+    k_apply32_q3<true><<<blocks, Q3Cfg::THREADS, smem, ctx->stream>>>(p, a, rec, tb, *own, *run,
+                                                                      err);
+  } else {
+    CUtensorMap none;
+    std::memset(&none, 0, sizeof(none));
+    k_apply32_q3<false><<<blocks, Q3Cfg::THREADS, smem, ctx->stream>>>(p, a, rec, tb, none, none,
+                                                                       err);
+  }
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
 }

@@ -40,8 +40,9 @@ enum Slot {
 
 // flag words (int): [0] state (0 running, 1 converged, 2 non-finite,
 // 3 breakdown), [1] reduction counter (last-block detection), [2] the CG
-// x update of the stopping iteration is still to be applied
-enum { F_STATE = 0, F_COUNTER = 1, F_XPEND = 2, F_COUNT = 4 };
+// x update of the stopping iteration is still to be applied, [3] a kernel's
+// TMA staging did not complete within its poll limit (sticky)
+enum { F_STATE = 0, F_COUNTER = 1, F_XPEND = 2, F_TMA = 3, F_COUNT = 4 };
 
 enum Finisher {
   FIN_STORE = 0,        // scal[slot0] = d0 ; scal[slot1] = d1
@@ -159,8 +160,7 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 template <int MAXT>
-__device__ __forceinline__ void block_sum2_any(double &a, double &b) {
-  __shared__ double sa[MAXT], sb[MAXT];
+__device__ __forceinline__ void block_sum2_with(double &a, double &b, double *sa, double *sb) {
   __syncthreads();   // the arrays may still be read by a previous call
   sa[threadIdx.x] = a;
   sb[threadIdx.x] = b;
@@ -176,6 +176,20 @@ __device__ __forceinline__ void block_sum2_any(double &a, double &b) {
   }
 }
 
+template <int MAXT>
+__device__ __forceinline__ void block_sum2_any(double &a, double &b) {
+  __shared__ double sa[MAXT], sb[MAXT];
+  block_sum2_with<MAXT>(a, b, sa, sb);
+}
+
+// block sums through a caller-provided scratch of 2 * MAXT doubles (the
+// kernel's dynamic shared memory) or static arrays
+template <int MAXT, bool kScratch>
+__device__ __forceinline__ void block_sum2_sel(double &a, double &b, double *scratch) {
+  if constexpr (kScratch) block_sum2_with<MAXT>(a, b, scratch, scratch + MAXT);
+  else block_sum2_any<MAXT>(a, b);
+}
+
 // Two-level tail for grids of many blocks: the last block of each group of
 // kFuseGroup blocks adds the group's partials in block order into a group
 // partial; the last group to finish adds the group partials in group order
@@ -185,12 +199,13 @@ __device__ __forceinline__ void block_sum2_any(double &a, double &b) {
 // group, zero between launches (each group's last block resets its own).
 constexpr int kFuseGroup = 256;
 
-template <int MAXT>
+template <int MAXT, bool kScratch = false>
 __device__ __forceinline__ void reduce_tail_grouped(double *part, long max_blocks, int *cnt,
                                                     const RedCtx &rc, double s0, double s1,
-                                                    int fin, int slot0, int slot1) {
+                                                    int fin, int slot0, int slot1,
+                                                    double *scratch = nullptr) {
   __shared__ bool last;
-  block_sum2_any<MAXT>(s0, s1);
+  block_sum2_sel<MAXT, kScratch>(s0, s1, scratch);
   const int b = (int)blockIdx.x, g = b / kFuseGroup;
   const int ngroups = (int)((gridDim.x + kFuseGroup - 1) / kFuseGroup);
   const int gsize = min(kFuseGroup, (int)gridDim.x - g * kFuseGroup);
@@ -208,7 +223,7 @@ __device__ __forceinline__ void reduce_tail_grouped(double *part, long max_block
     a += __ldcg(part + 2 * (g * kFuseGroup + i));
     c += __ldcg(part + 2 * (g * kFuseGroup + i) + 1);
   }
-  block_sum2_any<MAXT>(a, c);
+  block_sum2_sel<MAXT, kScratch>(a, c, scratch);
   double *gpart = part + 2 * max_blocks;
   if (threadIdx.x == 0) {
     gpart[2 * g] = a;
@@ -226,7 +241,7 @@ __device__ __forceinline__ void reduce_tail_grouped(double *part, long max_block
     a += __ldcg(gpart + 2 * i);
     c += __ldcg(gpart + 2 * i + 1);
   }
-  block_sum2_any<MAXT>(a, c);
+  block_sum2_sel<MAXT, kScratch>(a, c, scratch);
   if (threadIdx.x == 0) {
     run_finisher(rc, fin, slot0, slot1, a, c);
     rc.flags[F_COUNTER] = 0;

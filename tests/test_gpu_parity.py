@@ -374,3 +374,22 @@ def test_block_jacobi_fdm_f32(pdg, oracle, k, nc):
     p32.apply(vt, dt)
     torch.cuda.synchronize()
     assert _rel(vt.cpu().double().numpy(), ref) <= TOL32
+
+
+def test_apply_f32_q3_unaligned_vectors(pdg, oracle):
+    # the Q3 FP32 operator stages its runs with TMA copies from 16-byte
+    # aligned vectors; vectors one float off that alignment take the
+    # per-thread copy path; both must agree with the oracle
+    import torch
+    go, P, rng = _pair(pdg, oracle, 3, 3, (9, 5, 4), seed=95, react=True)
+    x = rng.uniform(-1, 1, go.ndof)
+    ref = P.jacobian_apply(x)
+    for off in (0, 1):
+        xb = torch.zeros(go.ndof + 4, dtype=torch.float32, device="cuda")
+        yb = torch.zeros(go.ndof + 4, dtype=torch.float32, device="cuda")
+        xt, yt = xb[off:off + go.ndof], yb[off:off + go.ndof]
+        xt.copy_(torch.tensor(x, dtype=torch.float32))
+        torch.cuda.synchronize()
+        go.jacobian_apply_f32(xt, yt)
+        torch.cuda.synchronize()
+        assert _rel(yt.cpu().double().numpy(), ref) <= TOL32, off
