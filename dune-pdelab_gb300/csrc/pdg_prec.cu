@@ -427,13 +427,23 @@ __global__ void k_dense_apply(long ncell, int nb, const T *__restrict__ invT,
   for (int i = threadIdx.x; i < nb; i += blockDim.x) ds[i] = d[e * nb + i];
   __syncthreads();
   const T *B = invT + e * (long)nb * nb;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-    T s = T(0);
-    if (!transpose)
+  if (!transpose) {
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+      T s = T(0);
       for (int j = 0; j < nb; j++) s += B[j * nb + i] * ds[j];
-    else
-      for (int j = 0; j < nb; j++) s += B[i * nb + j] * ds[j];
-    v[e * nb + i] = scale * s;
+      v[e * nb + i] = scale * s;
+    }
+  } else {
+    // v_i = sum_j B[i nb + j] d_j (column i contiguous): one warp per output,
+    // lanes over j, warp sum
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int i = warp; i < nb; i += nwarps) {
+      T s = T(0);
+      for (int j = lane; j < nb; j += 32) s += B[i * nb + j] * ds[j];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) v[e * nb + i] = scale * s;
+    }
   }
 }
 
@@ -514,10 +524,23 @@ __global__ void __launch_bounds__(kDenseH)
       v[e * nb + i] = sc * r;
     }
   } else {
-    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    // v_i = sum_j B16[i nbp + j] d_j: one warp per output, each lane four
+    // consecutive j per 8-byte load (column i is contiguous), warp sum
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int i = warp; i < nb; i += nwarps) {
       float r = 0.f;
-      for (int j = 0; j < nb; j++) r += __half2float(B[(long)i * nbp + j]) * ds[j];
-      v[e * nb + i] = sc * r;
+      for (int j = 4 * lane; j < nb; j += 128) {
+        const uint2 w = *reinterpret_cast<const uint2 *>(B + (long)i * nbp + j);
+        const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&w.x));
+        const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&w.y));
+        r += a.x * ds[j];
+        if (j + 1 < nb) r += a.y * ds[j + 1];
+        if (j + 2 < nb) r += b.x * ds[j + 2];
+        if (j + 3 < nb) r += b.y * ds[j + 3];
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+      if (lane == 0) v[e * nb + i] = sc * r;
     }
   }
 }
