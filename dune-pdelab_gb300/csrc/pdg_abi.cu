@@ -1027,6 +1027,12 @@ int pdg_set_stream(pdg_context *ctx, void *stream) {
   return PDG_OK;
 }
 
+int pdg_get_stream(const pdg_context *ctx, void **stream) {
+  if (!ctx || !stream) return set_error(PDG_EINVAL, "null argument");
+  *stream = (void *)ctx->stream;
+  return PDG_OK;
+}
+
 int pdg_sizes(const pdg_context *ctx, long *ncell, int *nbasis, long *ndof, int *nqv,
               long *nbp) {
   if (!ctx) return set_error(PDG_EINVAL, "null context");

@@ -15,14 +15,21 @@ code keeps its shape:
   (dune/pdelab/stationary/linearproblem.hh:59-338).
 
 Vectors are numpy float64 arrays (host) or torch tensors on the GPU (device
-pointers are passed straight through).  Every failure raises ``PDGError``
+pointers are passed straight through).  Unless a stream is bound with
+``GridOperator.set_stream``, every call that can touch device buffers is
+ordered after the work already queued on torch's current stream, and torch's
+current stream waits for the call's work (events, no host synchronisation),
+so tensors made or read by torch around a call need no explicit
+``torch.cuda.synchronize()``.  Every failure raises ``PDGError``
 with the library's message, as the reference raises Dune exceptions.
 There is no CPU fallback: without the CUDA library nothing here works.
 """
 from __future__ import annotations
 
 import ctypes as C
+import functools
 import os
+import sys
 
 import numpy as np
 
@@ -118,6 +125,7 @@ _SIGS = {
     "pdg_last_error": (C.c_char_p, []),
     "pdg_default_solver_options": (None, [C.POINTER(SolverOptions)]),
     "pdg_set_stream": (C.c_int, [_vp, _vp]),
+    "pdg_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
     "pdg_sizes": (C.c_int, [_vp, C.POINTER(C.c_long), C.POINTER(C.c_int), C.POINTER(C.c_long),
                             C.POINTER(C.c_int), C.POINTER(C.c_long)]),
     "pdg_volume_points": (C.c_int, [_vp, _vp]),
@@ -192,6 +200,36 @@ def _check(st, allow=()):
         msg = load().pdg_last_error()
         raise PDGError(st, msg.decode() if msg else "")
     return st
+
+
+def _torch_streams(go):
+    """(torch's current stream, the context's stream as a torch stream) when
+    torch has initialised CUDA and no stream was bound explicitly, else None."""
+    torch = sys.modules.get("torch")
+    if torch is None or go._explicit_stream or not go._h or not torch.cuda.is_initialized():
+        return None
+    p = _vp()
+    _check(load().pdg_get_stream(go._h, C.byref(p)))
+    dev = torch.device("cuda", go.cfg.device)
+    if go._lib_stream is None or go._lib_stream[0] != p.value:
+        go._lib_stream = (p.value, torch.cuda.ExternalStream(p.value, device=dev))
+    return torch.cuda.current_stream(dev), go._lib_stream[1]
+
+
+def _stream_ordered(method):
+    """Order a call's work between torch's current stream and the context's."""
+    @functools.wraps(method)
+    def wrapper(self, *args, **kw):
+        s = _torch_streams(self if isinstance(self, GridOperator) else self.go)
+        if s is None:
+            return method(self, *args, **kw)
+        cur, lib = s
+        lib.wait_stream(cur)
+        try:
+            return method(self, *args, **kw)
+        finally:
+            cur.wait_stream(lib)
+    return wrapper
 
 
 def _ptr(v, dtype=np.float64):
@@ -276,6 +314,8 @@ class GridOperator:
         cfg.basis = basis
         self.cfg = cfg
         self.dim, self.degree, self.basis = dim, degree, basis
+        self._explicit_stream = False
+        self._lib_stream = None
         self._h = _vp()
         _check(load().pdg_create(C.byref(cfg), C.byref(self._h)))
         nc, nb, nd, nq, nbp = C.c_long(), C.c_int(), C.c_long(), C.c_int(), C.c_long()
@@ -299,6 +339,15 @@ class GridOperator:
     def handle(self):
         return self._h
 
+    def set_stream(self, stream):
+        """Bind the context to a CUDA stream (a torch stream or a raw
+        cudaStream_t address; None: the context's own stream again).  While a
+        stream is bound, the caller orders its work against it."""
+        ptr = getattr(stream, "cuda_stream", stream)
+        _check(load().pdg_set_stream(self._h, _vp(ptr) if ptr else None))
+        # torch's default stream (address 0) is followed through events instead
+        self._explicit_stream = bool(ptr)
+
     # -- geometry ---------------------------------------------------------
     def volume_points(self):
         out = np.zeros((self.ncell, self.nq_volume, self.dim))
@@ -311,6 +360,7 @@ class GridOperator:
         return out
 
     # -- parameters -------------------------------------------------------
+    @_stream_ordered
     def set_permeability(self, K, is_log=False):
         K = np.ascontiguousarray(K, dtype=np.float64) if isinstance(K, (list, np.ndarray)) else K
         _check(load().pdg_set_permeability(self._h, _ptr(K), int(is_log)))
@@ -335,36 +385,43 @@ class GridOperator:
         _check(load().pdg_set_boundary_data(self._h, *[_ptr(a) for a in arrs]))
 
     # -- GridOperator -----------------------------------------------------
+    @_stream_ordered
     def residual(self, x, r):
         """r += R(x)"""
         _check(load().pdg_residual(self._h, _ptr(x), _ptr(r)))
         return r
 
+    @_stream_ordered
     def jacobian_apply(self, z, y):
         """y += J z"""
         _check(load().pdg_jacobian_apply(self._h, _ptr(z), _ptr(y)))
         return y
 
+    @_stream_ordered
     def jacobian_apply_f32(self, z, y):
         """y += J z in FP32 (device tensors)"""
         _check(load().pdg_jacobian_apply_f32(self._h, _ptr(z, np.float32), _ptr(y, np.float32)))
         return y
 
+    @_stream_ordered
     def jacobian_apply_transpose(self, z, y):
         """y += J^T z"""
         _check(load().pdg_jacobian_apply_transpose(self._h, _ptr(z), _ptr(y)))
         return y
 
+    @_stream_ordered
     def norm(self, v):
         out = C.c_double()
         _check(load().pdg_norm(self._h, _ptr(v), C.byref(out)))
         return out.value
 
+    @_stream_ordered
     def dot(self, a, b):
         out = C.c_double()
         _check(load().pdg_dot(self._h, _ptr(a), _ptr(b), C.byref(out)))
         return out.value
 
+    @_stream_ordered
     def grad_logK(self, u, lam, g):
         _check(load().pdg_grad_logK(self._h, _ptr(u), _ptr(lam), _ptr(g)))
         return g
@@ -377,9 +434,11 @@ class GridOperator:
         c = np.ascontiguousarray(coef, dtype=np.float64)
         _check(load().pdg_set_nonlinearity(self._h, len(c) - 1, c.ctypes.data))
 
+    @_stream_ordered
     def set_linearization_point(self, x):
         _check(load().pdg_set_linearization_point(self._h, _ptr(x)))
 
+    @_stream_ordered
     def jacobian_apply_nonlinear(self, x, z, y):
         """y += J(x) z"""
         _check(load().pdg_jacobian_apply_nonlinear(self._h, _ptr(x), _ptr(z), _ptr(y)))
@@ -406,6 +465,7 @@ class GridOperator:
         _check(load().pdg_jacobian_pattern(self._h, C.byref(nnz)))
         return nnz.value
 
+    @_stream_ordered
     def jacobian_export(self, values=True):
         """(rowptr, colind, blocks[nnz, n, n]) in BCRS order; blocks row-major."""
         nnz = self.jacobian_pattern()
@@ -416,20 +476,24 @@ class GridOperator:
                                           _ptr(vals) if values else None))
         return rowptr, colind, vals
 
+    @_stream_ordered
     def matrix_apply(self, x, y):
         """y = A x with the assembled Jacobian"""
         _check(load().pdg_matrix_apply(self._h, _ptr(x), _ptr(y)))
         return y
 
+    @_stream_ordered
     def mass_apply(self, x, y):
         """y = M x (DG mass matrix)"""
         _check(load().pdg_mass_apply(self._h, _ptr(x), _ptr(y)))
         return y
 
+    @_stream_ordered
     def grad_source(self, lam, g):
         _check(load().pdg_grad_source(self._h, _ptr(lam), _ptr(g)))
         return g
 
+    @_stream_ordered
     def adjoint_solve(self, rhs, lam, options=None):
         o = options or default_options()
         res = SolverResult()
@@ -447,10 +511,12 @@ class OnTheFlyOperator:
     def __init__(self, go: GridOperator):
         self.go = go
 
+    @_stream_ordered
     def apply(self, x, y):
         """y = J x"""
         _check(load().pdg_apply(self.go.handle, _ptr(x), _ptr(y)))
 
+    @_stream_ordered
     def applyscaleadd(self, alpha, x, y):
         """y += alpha J x"""
         _check(load().pdg_applyscaleadd(self.go.handle, float(alpha), _ptr(x), _ptr(y)))
@@ -467,11 +533,13 @@ class GridOperatorPreconditioner:
         self.go, self.kind, self.precision = go, kind, precision
         self._ready = False
 
+    @_stream_ordered
     def pre(self, v=None, d=None):
         if not self._ready:
             _check(load().pdg_prec_setup(self.go.handle, self.kind, self.precision))
             self._ready = True
 
+    @_stream_ordered
     def apply(self, v, d):
         if self.precision == F64:
             _check(load().pdg_prec_apply(self.go.handle, _ptr(d), _ptr(v)))
@@ -496,11 +564,13 @@ class ISTLBackend_SEQ_MatrixFree_Base:
                                     inner_reduction=inner_reduction)
         self.res = SolverResult()
 
+    @_stream_ordered
     def apply(self, z, r, reduction):
         self.opts.reduction = reduction
         _check(load().pdg_krylov_solve(self.go.handle, C.byref(self.opts), _ptr(z), _ptr(r),
                                        C.byref(self.res)), allow=(PDG_ENOTCONVERGED,))
 
+    @_stream_ordered
     def norm(self, v):
         return self.go.norm(v)
 
@@ -533,6 +603,7 @@ class OneStepMethod:
                                   else [np.ascontiguousarray(t, dtype=np.float64) for t in method])
         self.res = OneStepResult()
 
+    @_stream_ordered
     def apply(self, time, dt, xold, xnew):
         s = self.A.shape[0]
         A = np.ascontiguousarray(self.A, dtype=np.float64)
@@ -557,6 +628,7 @@ class NewtonMethod:
         self.opts = newton_options(**kw)
         self.res = NewtonResult()
 
+    @_stream_ordered
     def apply(self, u):
         st = load().pdg_newton_solve(self.go.handle, C.byref(self.opts), C.byref(self.ls.opts),
                                      _ptr(u), C.byref(self.res))
@@ -576,6 +648,7 @@ class StationaryLinearProblemSolver:
         self.reduction, self.min_defect = reduction, min_defect
         self.res = SolverResult()
 
+    @_stream_ordered
     def apply(self, x=None):
         if x is not None:
             self.x = x

@@ -197,6 +197,12 @@ void pdg_default_solver_options(pdg_solver_options *opt);
    the context's own non-blocking stream). */
 int pdg_set_stream(pdg_context *ctx, void *stream);
 
+/* The stream the context currently works on (the one set by pdg_set_stream,
+   else its own).  No reference counterpart: a caller on another stream
+   (a framework's current stream) orders its own work against this one with
+   events before and after passing device buffers. */
+int pdg_get_stream(const pdg_context *ctx, void **stream);
+
 /* sizes: cells, basis functions per cell, DOFs, volume quadrature points
    per cell ((k+1)^d) and boundary quadrature points in total */
 int pdg_sizes(const pdg_context *ctx, long *ncell, int *nbasis, long *ndof,

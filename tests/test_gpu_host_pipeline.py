@@ -88,3 +88,40 @@ def test_host_apply_pinned_and_convection(env):
     torch.cuda.synchronize()
     assert torch.equal(y, yd.cpu())
     go.close()
+
+
+def test_device_calls_follow_torch_current_stream(env):
+    """Device tensors produced on torch's current stream behind a long kernel
+    (a bounded GPU sleep of ~20 ms) are read only once they are written, and
+    torch reads the results only after the call's work: the binding orders the
+    context's stream against torch's current stream with events, without an
+    explicit synchronisation in the caller."""
+    pdg, torch = env
+    go, rng = _go(pdg, 3, 2, (24, 24, 24), seed=4)
+    dev = torch.device("cuda", 0)
+    base = torch.tensor(rng.uniform(-1, 1, go.ndof), device=dev)
+    ref = torch.zeros_like(base)
+    torch.cuda.synchronize()
+    go.jacobian_apply(base, ref)
+    torch.cuda.synchronize()
+    for stream in (None, torch.cuda.Stream(dev)):
+        ctx = torch.cuda.stream(stream) if stream is not None else torch.cuda.stream(
+            torch.cuda.current_stream(dev))
+        with ctx:
+            torch.cuda._sleep(40_000_000)
+            x = base * 1.0                      # written after the sleep
+            y = torch.zeros_like(base)
+            go.jacobian_apply(x, y)
+            out = y.clone()                     # read on torch's stream
+        torch.cuda.synchronize()
+        assert torch.equal(out, ref)
+    # an explicitly bound stream is the caller's to order
+    s = torch.cuda.Stream(dev)
+    go.set_stream(s)
+    with torch.cuda.stream(s):
+        y = torch.zeros_like(base)
+        go.jacobian_apply(base, y)
+    s.synchronize()
+    assert torch.equal(y, ref)
+    go.set_stream(None)
+    go.close()
