@@ -47,6 +47,10 @@ struct Cfg {
   static constexpr int THREADS = CPB * TPC;
   static constexpr int NF = 2 * D;
   static constexpr int REC = D * N2 + 5 * NF;             // per-cell record
+  // 3D FP64 record: A'_dir, then per face the coefficients W_f[0..N] of the
+  // neighbour line (see k_cell_record), for the operator and for its transpose
+  static constexpr int NW = NF * (N + 1);
+  static constexpr int RECW = D * N2 + 2 * NW;
   // shared memory per cell (elements): ue, Xs, Ys, Zs, face data, record, raw coefs
   static constexpr int PER_CELL = (D == 3 ? 4 * NB : 2 * NB) + 4 * D * TPC + REC + 3 * NF;
   static constexpr int TAB = 2 * N2 + 2 * N;
@@ -96,8 +100,23 @@ __device__ __forceinline__ void cell_coords(const OpParams<T> &p, unsigned e, in
   ix[2] = (int)q1;
 }
 
+// True where the record carries per-face line coefficients instead of the
+// five scaled face coefficients: the 3D FP64 operator, bound by its FP64 pipe.
+template <typename T, int D>
+constexpr bool face_vectors() { return sizeof(T) == 8 && D == 3; }
+
 // Record of one cell (computed in FP64, stored in T): A'_dir row-major, then
-// five scaled coefficients per face.
+// five scaled coefficients per face {hp ke, hp ko, hp pen, th hp ke, th hp ko},
+// or, for the 3D FP64 operator, per face f the coefficients of the neighbour
+// line v (its N values along the face normal): the face terms of this cell are
+// s1 = sum_q W_f[q] v[q] and s2 = W_f[N] v[qv], with qv = N-1 for the
+// neighbour below and 0 above,
+//   W_f[q] = sg ko' td[q] - [q = qv] pen,   W_f[N] = sg ke'
+// (td: the derivative of the 1D basis at the shared face; ko', ke' = hp ko,
+// th hp ke for the operator and th hp ko, hp ke for its transpose; sg = +-1
+// by side and form).  The neighbour's normal derivative and face value are
+// folded into these coefficients, which takes 2 FP64 operations per face
+// point out of the apply.
 template <typename T, int D, int N>
 __global__ void k_cell_record(const OpParams<double> p, T *__restrict__ rec) {
   using C = Cfg<D, N>;
@@ -118,7 +137,7 @@ __global__ void k_cell_record(const OpParams<double> p, T *__restrict__ rec) {
     else nb = ix[dir] > 0 ? e - stride[dir] : -1;
     face_coefficients(p, f, Ke, nb, raw + 3 * f);
   }
-  T *r = rec + e * C::REC;
+  T *r = rec + e * (face_vectors<T, D>() ? C::RECW : C::REC);
 #pragma unroll
   for (int dir = 0; dir < D; dir++) {
     const double hp = hperp<double, D>(p, dir);
@@ -131,7 +150,19 @@ __global__ void k_cell_record(const OpParams<double> p, T *__restrict__ rec) {
   for (int f = 0; f < 2 * D; f++) {
     double c5[5];
     scale_face<double, D>(p, f, raw + 3 * f, c5);
-    for (int j = 0; j < 5; j++) r[D * N * N + 5 * f + j] = (T)c5[j];
+    if constexpr (face_vectors<T, D>()) {
+      const int hi = f & 1, qv = hi ? 0 : N - 1;
+      const double *td = hi ? td0 : td1;
+      for (int tr = 0; tr < 2; tr++) {
+        const double sg = (hi ^ tr) ? -1.0 : 1.0;
+        const double ko = tr ? c5[4] : c5[1];
+        T *w = r + D * N * N + tr * C::NW + f * (N + 1);
+        for (int q = 0; q < N; q++) w[q] = (T)(sg * ko * td[q] - (q == qv ? c5[2] : 0.0));
+        w[N] = (T)(sg * (tr ? c5[0] : c5[3]));
+      }
+    } else {
+      for (int j = 0; j < 5; j++) r[D * N * N + 5 * f + j] = (T)c5[j];
+    }
   }
 }
 
@@ -200,8 +231,16 @@ __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
     }
   }
   if (rec) {
-    const T *r = rec + (size_t)ee * C::REC;
-    for (int i = l; i < C::REC; i += TPC) Am[i] = r[i];
+    if constexpr (face_vectors<T, D>()) {
+      // A'_dir and the line coefficients of this launch's form (into the
+      // face-coefficient region: NW <= 5 NF + 3 NF)
+      const T *r = rec + (size_t)ee * C::RECW;
+      const int woff = a.transpose ? C::NW : 0;
+      for (int i = l; i < D * N2 + C::NW; i += TPC) Am[i] = r[i < D * N2 ? i : i + woff];
+    } else {
+      const T *r = rec + (size_t)ee * C::REC;
+      for (int i = l; i < C::REC; i += TPC) Am[i] = r[i];
+    }
   }
 #pragma unroll
   for (int z = 0; z < N; z++) ue[z * TPC + l] = col[z];
@@ -237,7 +276,14 @@ __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
   for (int f = 0; f < NF; f++) {
     const int hi = f & 1;
     T s1 = T(0), s2 = T(0);
-    if (nbr[f] >= 0 && !a.diag_only) {
+    if constexpr (face_vectors<T, D>()) {
+      if (nbr[f] >= 0 && !a.diag_only) {
+        const T *w = c5 + f * (N + 1);
+#pragma unroll
+        for (int q = 0; q < N; q++) s1 += w[q] * v[f][q];
+        s2 = w[N] * v[f][hi ? 0 : N - 1];
+      }
+    } else if (nbr[f] >= 0 && !a.diag_only) {
       const T *cf = c5 + 5 * f;   // hp ke, hp ko, hp pen, th hp ke, th hp ko
       T dv = T(0);
       if (!hi) {
@@ -448,6 +494,8 @@ static int launch_apply_dn(pdg_context *ctx, const ApplyArgs<T> &a, const OpPara
                                       (int)smem));
     attr_done = ctx->device;
   }
+  if (face_vectors<T, D>() && !rec)
+    return set_error(PDG_EUNSUPPORTED, "the 3D FP64 operator runs from its cell records");
   const long work = (a.cells || a.ncells > 0) ? a.ncells : ctx->ncell;
   if (work <= 0) return PDG_OK;
   const long blocks = (work + C::CPB - 1) / C::CPB;
@@ -460,7 +508,8 @@ template <int D, int N>
 static int record_dn(pdg_context *ctx) {
   using C = Cfg<D, N>;
   if (!ctx->rec64)
-    PDG_CUDA_TRY(cudaMalloc(&ctx->rec64, sizeof(double) * C::REC * ctx->ncell));
+    PDG_CUDA_TRY(cudaMalloc(&ctx->rec64, sizeof(double) * (face_vectors<double, D>() ? C::RECW : C::REC) *
+                                             ctx->ncell));
   OpParams<double> p = make_params<double>(ctx, ctx->K64, ctx->c64, ctx->tab64);
   const unsigned blocks = (unsigned)((ctx->ncell + 127) / 128);
   k_cell_record<double, D, N><<<blocks, 128, 0, ctx->stream>>>(p, ctx->rec64);
