@@ -51,7 +51,7 @@ def flops_per_cell(dim, N):
     return 2 * mac
 
 
-def survey_flops_per_dof(dim, N):
+def quadrature_flops_per_dof(dim, N):
     """Sum-factorised count of the reference algorithm (volume at quadrature
     points + both-sided face quadrature): 8 d N^{d+1} + 16 d^2 N^d per cell."""
     return (8 * dim * N ** (dim + 1) + 16 * dim * dim * N ** dim) / N ** dim
@@ -415,7 +415,7 @@ def run_gb300(args, world, rank, local):
                        "cores (libpdg_probe.so); MEASURED_PEAKS.json has no FP64/FP32 "
                        "CUDA-core figure",
         "flops_per_launch": fl, "flops_per_dof": fl / ndof,
-        "reference_algorithm_flops_per_dof": survey_flops_per_dof(3, N),
+        "reference_algorithm_flops_per_dof": quadrature_flops_per_dof(3, N),
         "algorithmic_bytes_per_launch": alg_bytes,
         "hbm_achieved_gbs": alg_bytes / (ms * 1e-3) / 1e9,
         "hbm_peak_gbs": mp_.get("hbm_gbs"),
