@@ -167,6 +167,42 @@ def make_problem(pdg, np, device, wl=WORKLOAD):
     return go, logK
 
 
+def link_bandwidth(torch, dev, xh, yh, reps=10):
+    """Pinned host<->device copy rates (GB/s) for one step's vectors: each
+    direction alone, and each way while both run at once on two streams."""
+    dx = torch.empty(xh.numel(), dtype=xh.dtype, device=dev)
+    dy = torch.empty(yh.numel(), dtype=yh.dtype, device=dev)
+    s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    nbytes = xh.numel() * xh.element_size()
+
+    def both():
+        cur = torch.cuda.current_stream(dev)
+        s1.wait_stream(cur)
+        s2.wait_stream(cur)
+        with torch.cuda.stream(s1):
+            dx.copy_(xh, non_blocking=True)
+        with torch.cuda.stream(s2):
+            yh.copy_(dy, non_blocking=True)
+        cur.wait_stream(s1)
+        cur.wait_stream(s2)
+
+    out = {}
+    for name, fn in (("h2d", lambda: dx.copy_(xh, non_blocking=True)),
+                     ("d2h", lambda: yh.copy_(dy, non_blocking=True)),
+                     ("concurrent_each_way", both)):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        out[name] = nbytes / (e0.elapsed_time(e1) / reps * 1e-3) / 1e9
+    return out
+
+
 def fma_peaks(pdg):
     import build_lib
     lib = ctypes.CDLL(build_lib.PROBE_LIB)
@@ -391,7 +427,10 @@ def run_gb300(args, world, rank, local):
     t_e2e = time.perf_counter() - t0
     t_e2e = max_over_ranks(t_e2e, world, dev)
     e2e = {"value": job_throughput(world, ndof * args.steps, t_e2e) / 1e9, "unit": "GDoF/s",
-           "h2d_bytes_per_step": ndof * 8, "d2h_bytes_per_step": ndof * 8}
+           "h2d_bytes_per_step": ndof * 8, "d2h_bytes_per_step": ndof * 8,
+           # the host link's rates for these buffers: the copies of a step
+           # overlap the kernel, so e2e is bound by max(kernel, copies) + edges
+           "link_gbs": link_bandwidth(torch, dev, xh, yh)}
 
     if rank != 0:
         go.close()
