@@ -25,10 +25,11 @@
 // with K_e and h_F = |T|/|F| (:717-727), theta = -1/+1/0 (:99-101).
 //
 // Per-cell data (A'_dir and five scaled coefficients per face) is either
-// read from a record precomputed once per coefficient field (FP64: its FP64
-// pipe is the bottleneck, the record removes all divisions and matrix
-// assembly from the apply) or formed on the fly (FP32: memory traffic is
-// the scarcer resource).
+// read from a record precomputed once per coefficient field or formed on
+// the fly (2D FP32).  The FP64 operator is bound by its FP64 pipe: the
+// record removes all divisions and matrix assembly from the apply, and in
+// 3D it carries per face the coefficients of the neighbour line (see
+// k_cell_record) so that each face point costs N + 1 FP64 operations.
 //
 // Thread mapping (d = 3): N*N threads per cell, thread (tx,ty) holds the
 // z-column u[.,ty,tx] in registers; x/y contractions go through shared
