@@ -4,15 +4,17 @@ The reference ships no golden vectors; these assertions are the pins:
   * dune/pdelab/test/matrixfree/matrix_free_linear.cc:387-393
   * dune/pdelab/test/testfastdgassembler.cc:160-175
   * dune/pdelab/test/testblocklocaloperatorwrapper.cc:200-276
+  * dune/pdelab/test/testconvectiondiffusiondg.cc:160-168
+  * dune/pdelab/test/testinstationaryfastdgassembler.cc:226-235
 """
 import numpy as np
 import pytest
 
 
-def _mfl_problem(O, n=16, k=1):
+def _mfl_problem(O, n=16, k=1, alpha=3.0):
     # PoissonProblem of matrix_free_linear.cc:28-60: g = exp(-|x-1/2|^2),
     # f = 4 (1 - c) g, SIPG, weightsOn, alpha = 3 (:104-108)
-    P = O.Problem(2, k, (n, n), alpha=3.0)
+    P = O.Problem(2, k, (n, n), alpha=alpha)
     vp = P.volume_points()
     c = (0.5 - vp[..., 0]) ** 2 + (0.5 - vp[..., 1]) ** 2
     P.set(fq=4 * (1 - c) * np.exp(-c))
@@ -242,3 +244,47 @@ def test_onestep_orders_oracle(oracle):
             errs.append(np.abs(x - ue).max())
         rate = np.log2(errs[-2] / errs[-1])
         assert abs(rate - order) < 0.25, (name, errs)
+
+
+def test_convectiondiffusiondg_default_constructor(oracle):
+    """testconvectiondiffusiondg.cc: the same Poisson problem with the local
+    operator's default arguments (SIPG, weightsOn, alpha = 1,
+    convectiondiffusiondg.hh:85-90) on 16x16 Q1, solved to reduction 1e-12
+    (SuperLU there, an assembled Krylov solve here): L2 error squared < 1e-6
+    (:160-168)."""
+    P = _mfl_problem(oracle, alpha=1.0)
+    u, res, st = P.solve(solver="bicgstab", op=1, reduction=1e-12)
+    assert st == 0 and res.converged
+    exact = lambda x: np.exp(-((0.5 - x[..., 0]) ** 2 + (0.5 - x[..., 1]) ** 2))
+    assert _l2err2(P, u, exact, 6) < 1e-6
+
+
+def test_instationary_fastdg_assembler(oracle):
+    """testinstationaryfastdgassembler.cc: ParameterA (g = exp(-|x|^2),
+    f = (2d - 4|x|^2) g, Dirichlet; :24-118) on the unit square refined to
+    8x8, Q1, SIPG weightsOn alpha = 2 (:144), L2 mass (:152), initial value the
+    nodal interpolant of g (:181), one Alexander2 step of dt = 0.1 to T = 0.1
+    (:204-221), CG to 1e-10: L2 error squared < 5e-6 against g (integration
+    order 12; :226-235)."""
+    n, k = 8, 1
+    P = oracle.Problem(2, k, (n, n), alpha=2.0)
+    vp = P.volume_points()
+    nrm = (vp ** 2).sum(-1)
+    P.set(fq=(4 - 4 * nrm) * np.exp(-nrm))
+    bp = P.boundary_points()
+    P.set(gq=np.exp(-(bp ** 2).sum(-1)))
+    h = 1.0 / n
+    x0 = np.zeros(P.ndof)
+    for cy in range(n):
+        for cx in range(n):
+            for j in range(k + 1):
+                for i in range(k + 1):
+                    X, Y = (cx + i / k) * h, (cy + j / k) * h
+                    x0[(cx + n * cy) * (k + 1) ** 2 + i + (k + 1) * j] = np.exp(-(X * X + Y * Y))
+    al = 1 - 0.5 * np.sqrt(2)          # Alexander2Parameter
+    A = np.array([[-1, 1, 0], [-1, 0, 1.]])
+    B = np.array([[0, al, 0], [0, 1 - al, al]])
+    x1, its = P.onestep(A, B, 0.1, x0, oracle.prec_config(1), solver="cg", reduction=1e-10)
+    assert its > 0
+    exact = lambda x: np.exp(-(x ** 2).sum(-1))
+    assert _l2err2(P, x1, exact, 7) < 5e-6
