@@ -92,3 +92,39 @@ def test_onestep_mixed_sor_nonsymmetric(pdg, oracle):
     xo, _ = P.onestep(A, B, 1e-2, x, oracle.prec_config(2), solver="bicgstab", reduction=1e-13)
     assert _rel(xn, xo) <= 1e-9
     assert osm.result().stages == 2 and osm.result().linear_solver_iterations > 0
+
+
+def test_instationary_reference_problem(pdg, oracle):
+    """testinstationaryfastdgassembler.cc:24-235 on the GPU: g = exp(-|x|^2),
+    f = (2d - 4|x|^2) g, 8x8 Q1, SIPG weightsOn alpha = 2, one Alexander2 step
+    of dt = 0.1 from the nodal interpolant of g; the step agrees with the
+    oracle's, and its L2 error squared against g is < 5e-6 (:226-235)."""
+    n, k = 8, 1
+    go = pdg.GridOperator(2, k, (n, n), alpha=2.0)
+    P = oracle.Problem(2, k, (n, n), alpha=2.0)
+    vp = P.volume_points()
+    nrm = (vp ** 2).sum(-1)
+    fq = (4 - 4 * nrm) * np.exp(-nrm)
+    gq = np.exp(-(P.boundary_points() ** 2).sum(-1))
+    go.set_source(fq=fq)
+    go.set_boundary_data(g=gq)
+    P.set(fq=fq, gq=gq)
+    x0 = np.zeros(go.ndof)
+    for cy in range(n):
+        for cx in range(n):
+            for j in range(k + 1):
+                for i in range(k + 1):
+                    X, Y = (cx + i / k) / n, (cy + j / k) / n
+                    x0[(cx + n * cy) * (k + 1) ** 2 + i + (k + 1) * j] = np.exp(-(X * X + Y * Y))
+    A, B, D = pdg.onestep_table(pdg.ALEXANDER2)
+    ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG,
+                                             preconditioner=pdg.PREC_BJ_FDM)
+    ls.opts.reduction = 1e-13
+    osm = pdg.OneStepMethod(pdg.ALEXANDER2, go, ls)
+    x1 = np.zeros(go.ndof)
+    osm.apply(0.0, 0.1, x0, x1)
+    xo, _ = P.onestep(A, B, 0.1, x0, oracle.prec_config(2), reduction=1e-13)
+    assert _rel(x1, xo) <= 1e-9
+    xyz, w, val = P.eval_points(x1, 7)
+    assert float((w * (val - np.exp(-(xyz ** 2).sum(-1))) ** 2).sum()) < 5e-6
+    go.close()
