@@ -189,12 +189,20 @@ typedef struct pdg_solver_result {
 /* Replaces building YaspGrid + GridFunctionSpace + ConvectionDiffusionDG +
    GridOperator (test/matrixfree/matrix_free_linear.cc:73-151). */
 int pdg_create(const pdg_config *cfg, pdg_context **out);
+/* Ends the objects pdg_create replaces (their destructors). */
 int pdg_destroy(pdg_context *ctx);
+/* Message of the last failure on the calling thread: the text the reference
+   puts in the Dune::Exception it throws (DUNE_THROW); no exception crosses
+   this boundary. */
 const char *pdg_last_error(void);
+/* Defaults of the solver options: maxiter 5000 as in the
+   ISTLBackend_SEQ_MatrixFree_Base constructor
+   (backend/istl/matrixfree/backends.hh:74-78). */
 void pdg_default_solver_options(pdg_solver_options *opt);
 
 /* Stream for all subsequent work (cudaStream_t passed as void*; NULL =
-   the context's own non-blocking stream). */
+   the context's own non-blocking stream).  No reference counterpart (the
+   reference runs on the host). */
 int pdg_set_stream(pdg_context *ctx, void *stream);
 
 /* The stream the context currently works on (the one set by pdg_set_stream,
@@ -204,14 +212,19 @@ int pdg_set_stream(pdg_context *ctx, void *stream);
 int pdg_get_stream(const pdg_context *ctx, void **stream);
 
 /* sizes: cells, basis functions per cell, DOFs, volume quadrature points
-   per cell ((k+1)^d) and boundary quadrature points in total */
+   per cell ((k+1)^d) and boundary quadrature points in total (the sizes of
+   GridFunctionSpace::size() and of the Blocking::fixed blocks,
+   backend/istl/descriptors.hh:26-47) */
 int pdg_sizes(const pdg_context *ctx, long *ncell, int *nbasis, long *ndof,
               int *nq_volume, long *nq_boundary);
 
 /* Quadrature-point coordinates (host output) so that callers evaluate
    their parameter functions where the operator integrates them:
    volume [ncell][(k+1)^d][dim]; boundary points grouped by side, faces
-   lexicographic over the remaining directions, (k+1)^(d-1) points each. */
+   lexicographic over the remaining directions, (k+1)^(d-1) points each.
+   No reference counterpart: the reference evaluates f, g, j, o inside the
+   local operator at the same Gauss points of order 2k
+   (convectiondiffusiondg.hh:1060-1061, :745-746). */
 int pdg_volume_points(const pdg_context *ctx, double *xyz);
 int pdg_boundary_points(const pdg_context *ctx, double *xyz);
 
@@ -244,7 +257,9 @@ int pdg_set_boundary_data(pdg_context *ctx, const double *g, const double *j,
 int pdg_residual(pdg_context *ctx, const double *x, double *r);
 /* GridOperator::jacobian_apply(z, y): y += J z  (gridoperator.hh:192-197) */
 int pdg_jacobian_apply(pdg_context *ctx, const double *z, double *y);
-/* Same in FP32 (the inner operator of the mixed-precision solve). */
+/* Same in FP32 (the inner operator of the mixed-precision solve).  No
+   reference counterpart: the reference computes in RF = double
+   (test/matrixfree/matrix_free_linear.cc:89). */
 int pdg_jacobian_apply_f32(pdg_context *ctx, const float *z, float *y);
 /* Transposed apply y += J^T z (adjoint; no reference counterpart, derived
    from jacobian_skeleton's sn/ns blocks, convectiondiffusiondg.hh:483-669) */
@@ -314,7 +329,10 @@ int pdg_krylov_solve(pdg_context *ctx, const pdg_solver_options *opt,
 int pdg_solve_linear_problem(pdg_context *ctx, const pdg_solver_options *opt,
                              double *x, pdg_solver_result *res);
 
-/* Defaults of pdg_prec_options (the reference's defaults). */
+/* Defaults of pdg_prec_options: the reference's (the iterative block
+   Jacobi's and block SOR's constructor arguments,
+   backend/istl/matrixfree/iterativeblockjacobipreconditioner.hh:302-310,
+   blocksorpreconditioner.hh:38-296). */
 void pdg_default_prec_options(pdg_prec_options *o);
 /* Options used by the next pdg_prec_setup (and every apply after it). */
 int pdg_set_prec_options(pdg_context *ctx, const pdg_prec_options *o);
@@ -379,12 +397,14 @@ int pdg_newton_solve(pdg_context *ctx, const pdg_newton_options *opt,
 /* instationary one-step methods                                     */
 /* ---------------------------------------------------------------- */
 
-/* y = M x with the DG mass matrix (the temporal L2 operator int u psi of
-   the one-step grid operator, gridoperator/onestep.hh). */
+/* y = M x with the DG mass matrix: the temporal operator L2
+   (localoperator/l2.hh:45-89, 149-152) of the one-step grid operator. */
 int pdg_mass_apply(pdg_context *ctx, const double *x, double *y);
 
 /* TimeSteppingParameterInterface implementations
-   (instationary/onestepparameter.hh): */
+   (instationary/onestepparameter.hh: theta :89, explicit / implicit Euler
+   :164 / :189, Heun :214, Shu3 :287, RK4 :364, Alexander2 :445,
+   fractional step :522, Alexander3 :605): */
 enum {
   PDG_ONESTEP_THETA = 0,          /* OneStepThetaParameter(theta) */
   PDG_ONESTEP_IMPLICIT_EULER = 1, /* theta = 1 */
@@ -429,7 +449,8 @@ int pdg_onestep_apply(pdg_context *ctx, int stages, const double *A, const doubl
    when a coefficient changes). */
 int pdg_jacobian_assemble(pdg_context *ctx);
 /* Number of nonzero blocks of the BCRS pattern (ncell + 2 * interior faces;
-   PDELab's pattern: the cell and its face neighbours). */
+   PDELab's pattern: the cell and its face neighbours, assembled by
+   GridOperator::jacobian, gridoperator/gridoperator.hh:184-189). */
 int pdg_jacobian_pattern(const pdg_context *ctx, long *nnz_blocks);
 /* Export in ISTL BCRSMatrix<FieldMatrix<double,n,n>> layout: rowptr
    [ncell+1] and colind [nnz_blocks] (host arrays; either may be NULL),
@@ -437,7 +458,9 @@ int pdg_jacobian_pattern(const pdg_context *ctx, long *nnz_blocks);
    cell order, column blocks ascending, each block row-major (test function
    i, trial function j). */
 int pdg_jacobian_export(pdg_context *ctx, long *rowptr, long *colind, double *values);
-/* y = A x with the assembled Jacobian (ISTL MatrixAdapter::apply). */
+/* y = A x with the assembled Jacobian (dune-istl MatrixAdapter::apply, the
+   operator of the matrix-based backends,
+   backend/istl/seqistlsolverbackend.hh:138). */
 int pdg_matrix_apply(pdg_context *ctx, const double *x, double *y);
 
 /* ---------------------------------------------------------------- */
