@@ -17,7 +17,15 @@
  *     alpha=2: L2 err^2 < 1e-8),
  *   - dune/pdelab/test/testblocklocaloperatorwrapper.cc:200-276 (block
  *     diagonal of the assembled Jacobian equals the block-diagonal
- *     wrapper's blocks to 1e-14).
+ *     wrapper's blocks to 1e-14),
+ *   - dune/pdelab/test/testconvectiondiffusiondg.cc:160-168 (the operator's
+ *     default arguments, alpha = 1: L2 err^2 < 1e-6),
+ *   - dune/pdelab/test/testinstationaryfastdgassembler.cc:226-235 (one
+ *     Alexander2 step on 8x8 Q1: L2 err^2 < 5e-6),
+ *   - dune/pdelab/test/matrixfree/matrix_free_nonlinear.cc:386-405 (Newton
+ *     on the nonlinear test problem),
+ *   - dune/pdelab/test/testdglegendre.cc:146-194 (Legendre, Lobatto and
+ *     Lagrange spaces give the same advection solution, L2 diff^2 < 1e-14).
  *
  * Everything follows the loop structure of the reference: per-point basis
  * evaluation, dense O(q*n) loops, one-sided face visits (inside = larger
