@@ -215,6 +215,14 @@ def fma_peaks(pdg):
             if lib.pdg_probe_fma_peak(prec, iters, ctypes.byref(v)) == 0:
                 best = max(best, v.value)
         out[name] = best
+    # the FP64 tensor-core path (mma.sync m8n8k4 f64), for comparison only
+    lib.pdg_probe_dmma_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    best = 0.0
+    for _ in range(3):
+        v = ctypes.c_double()
+        if lib.pdg_probe_dmma_peak(1000, ctypes.byref(v)) == 0:
+            best = max(best, v.value)
+    out["fp64_tensor_mma"] = best
     return out
 
 
@@ -460,16 +468,25 @@ def run_gb300(args, world, rank, local):
         "hbm_peak_gbs": mp_.get("hbm_gbs"),
         "hbm_frac": (alg_bytes / (ms * 1e-3) / 1e9) / mp_["hbm_gbs"] if mp_.get("hbm_gbs") else None,
         "fp32_fma_peak_tflops": peaks["fp32"],
+        "fp64_tensor_mma_peak_tflops": peaks.get("fp64_tensor_mma"),
     }
 
     extras = {}
     if not args.no_solves:
         extras = solve_metrics(pdg, np, torch, go, stream, logK)
-    # the 96^3 Q3 mixed-vs-FP64 solve is part of the default line; the other
-    # legs need --extended
-    legs = set(args.legs.split(",")) if args.extended else (set() if args.no_solves else {"c3"})
+    # the configurations' legs: C1 (2D Q1 solve beside the CPU solve), C3
+    # (96^3 Q3 mixed vs FP64), C4 (64^3 Q2 adjoint checks) and C5 (48^3 Q4
+    # convection-diffusion-reaction solves and gradients) are on the default
+    # line; --legs picks a subset, --extended adds the block-preconditioner
+    # and assembled-matrix legs
+    legs = set(args.legs.split(","))
+    if args.extended:
+        legs |= {"prec", "asm"}
+    if args.no_solves:
+        legs = set()
     if legs:
-        for leg, key, fn in (("c3", "solve_q3_96", c3_metrics), ("c4", "adjoint_q2_64", c4_metrics),
+        for leg, key, fn in (("c1", "solve_q1_2d_64", c1_metrics),
+                             ("c3", "solve_q3_96", c3_metrics), ("c4", "adjoint_q2_64", c4_metrics),
                              ("c5", "cdr_q4_48", c5_metrics), ("prec", "block_prec_q2_64", prec_metrics),
                              ("asm", "assembled_q2_32", assembled_metrics)):
             if leg not in legs:
@@ -610,6 +627,59 @@ def assembled_metrics(pdg, np, torch, stream):
         out[f"{key}_solve_s"] = time.perf_counter() - t0
         out[f"{key}_iterations"] = r.iterations
     go.close()
+    return out
+
+
+C1_SEED = 1
+
+
+def c1_problem(pdg, np, device):
+    """2D SIPG Poisson, Q1 on 64^2 cells of the unit square, K = 1, alpha = 3
+    (sigma = 3 k (k+d-1) = 6), homogeneous Dirichlet, f = sin(2 pi x)
+    sin(2 pi y) + eps_cell at the volume quadrature points, eps_cell i.i.d.
+    normal with variance 0.01 (N(mu, sigma^2) read as sigma^2 = 0.01, so
+    standard deviation 0.1), seeded.  Returns the GridOperator and f."""
+    n = 64
+    go = pdg.GridOperator(2, 1, (n, n), alpha=3.0, device=device)
+    vp = go.volume_points()
+    eps = np.random.default_rng(C1_SEED).normal(0.0, 0.1, go.ncell)
+    fq = np.sin(2 * np.pi * vp[..., 0]) * np.sin(2 * np.pi * vp[..., 1]) + eps[:, None]
+    go.set_source(fq=fq)
+    return go, fq
+
+
+def c1_metrics(pdg, np, torch, stream):
+    """The 2D Q1 64^2 problem: the GPU's CG + cell-block Jacobi solve to 1e-10
+    (FP64) beside the oracle's full CPU solve of the same problem on one
+    core (the reference's sequential path restated)."""
+    import pdg_oracle as O
+    go, fq = c1_problem(pdg, np, stream.device.index or 0)
+    go.set_stream(stream)
+    out = {"workload": "sipg2d_q1_64^2 (16,384 DoF), K=1, f=sin(2 pi x)sin(2 pi y)+N(0,0.1^2) "
+                       "per cell, CG + cell-block Jacobi (FDM), reduction 1e-10"}
+    ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG, preconditioner=pdg.PREC_BJ_FDM)
+    for rep in range(2):       # the first run includes the preconditioner set-up
+        u = torch.zeros(go.ndof, dtype=torch.float64, device=stream.device)
+        slp = pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        slp.apply()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out["gpu_first_solve_s" if rep == 0 else "gpu_solve_s"] = dt
+    r = slp.result()
+    out["gpu_iterations"] = r.iterations
+    out["gpu_converged"] = bool(r.converged)
+    go.close()
+    P = O.Problem(2, 1, (64, 64), alpha=3.0, fq=fq)
+    t0 = time.perf_counter()
+    uref, res, st = P.solve(solver="cg", op=0, reduction=1e-10)
+    out["cpu_solve_s"] = time.perf_counter() - t0
+    out["cpu_iterations"] = res.iterations
+    out["cpu_cores"] = 1
+    un = u.cpu().numpy()
+    out["gpu_vs_cpu_rel_max"] = float(np.max(np.abs(un - uref)) / np.max(np.abs(uref)))
+    out["speedup_gpu_vs_cpu"] = out["cpu_solve_s"] / out["gpu_solve_s"]
     return out
 
 
@@ -902,11 +972,12 @@ def main():
     ap.add_argument("--no-solves", action="store_true", help="skip solve/adjoint metrics")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--extended", action="store_true",
-                    help="run the legs in --legs (default: the 96^3 Q3 solves (c3), the 64^3 "
-                         "adjoint checks (c4) and the 48^3 Q4 convection-diffusion-reaction "
-                         "solves and gradients (c5)); without it only c3 runs, unless "
-                         "--no-solves")
-    ap.add_argument("--legs", default="c3,c4,c5", help="subset of the extended legs")
+                    help="also run the block-preconditioner (prec) and assembled-matrix (asm) "
+                         "legs")
+    ap.add_argument("--legs", default="c1,c3,c4,c5",
+                    help="configuration legs to run: c1 (2D Q1 64^2 solve and its CPU "
+                         "solve), c3 (96^3 Q3 mixed vs FP64), c4 (64^3 Q2 adjoint checks), c5 "
+                         "(48^3 Q4 convection-diffusion-reaction); prec, asm")
     ap.add_argument("--no-probe", action="store_true",
                     help="skip the FMA peak probe (profiling runs); roofline frac is then null")
     ap.add_argument("--solves-only", action="store_true",

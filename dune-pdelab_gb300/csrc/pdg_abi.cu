@@ -292,6 +292,7 @@ __global__ void k_init_solve(double *scal, int *flags, double red, double guard 
   flags[F_STATE] = 0;
   flags[F_COUNTER] = 0;
   flags[F_XPEND] = 0;
+  flags[F_TMA] = 0;   // a staging timeout is reported by the solve it happened in only
 }
 
 template <typename T>

@@ -1,13 +1,13 @@
 // pdg_noalloc.cu -- a dot product that allocates nothing.
 //
 // Who needs it: callers that cannot allocate device memory at the point of
-// the call.  Work recorded into a CUDA graph by stream capture cannot call
-// cudaMalloc while capturing; host solvers that own every buffer (for
-// example a dune-istl Krylov loop over device vectors, which asks for a dot
-// product or a norm in every iteration) may forbid library allocations
-// after set-up; memory-budgeted embeddings must not see hidden
-// allocations.  pdg_dot needs a context, and a context owns allocated
-// scratch; pdg_dot_noalloc needs neither.
+// the call.  Host solvers that own every buffer (for example a dune-istl
+// Krylov loop over device vectors, which asks for a dot product or a norm in
+// every iteration) may forbid library allocations after set-up, and
+// memory-budgeted embeddings must not see hidden allocations or the
+// synchronisation that cudaMalloc and cudaFree bring.  pdg_dot needs a
+// context, and a context owns allocated scratch; pdg_dot_noalloc needs
+// neither.
 //
 // How: the same deterministic two-stage reduction as the context-based dot
 // (block partial sums, the last block adds them in block order), with the
@@ -81,34 +81,72 @@ __global__ void __launch_bounds__(kNAThreads)
   }
 }
 
-// Device address of the scratch array per device, looked up once per device
-// with that device current (a host-side use of the symbol itself would name
-// host memory, not the device array).
+// Device address of the scratch array per device, looked up with that device
+// current (a host-side use of the symbol itself would name host memory, not
+// the device array).  The address belongs to the device's current context:
+// after cudaDeviceReset the runtime makes a new context, loads the module
+// again and the old address is gone, so the cache also keeps the unique id
+// of the context the address was taken in and looks the address up again
+// when that id changes.
 constexpr int kMaxDevices = 64;
 std::mutex g_na_mutex;
 double *g_na_ptr[kMaxDevices] = {};
+unsigned long long g_na_ctx[kMaxDevices] = {};
+
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
+
+// The unique id of the calling thread's current context (cuCtxGetId through
+// the runtime's driver entry point, no link against the driver library);
+// 0 if it cannot be had, which forces a fresh lookup on every call.
+unsigned long long current_context_id() {
+  static std::once_flag once;
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+    cudaGetLastError();
+  });
+  if (!get_current || !get_id) return 0;
+  void *ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
 
 int scratch_address(int dev, double **out) {
   if (dev < 0 || dev >= kMaxDevices) return set_error(PDG_EINVAL, "device ordinal out of range");
+  const unsigned long long ctx_id = current_context_id();
   std::lock_guard<std::mutex> lock(g_na_mutex);
-  if (!g_na_ptr[dev]) {
+  if (!g_na_ptr[dev] || ctx_id == 0 || g_na_ctx[dev] != ctx_id) {
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess)
       return set_error(PDG_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     g_na_ptr[dev] = static_cast<double *>(p);
+    g_na_ctx[dev] = ctx_id;
   }
   *out = g_na_ptr[dev];
   return PDG_OK;
 }
 
-bool on_device(const void *p) {
+// The device that owns p (device or managed memory), else -1.
+int owning_device(const void *p) {
   cudaPointerAttributes attr;
   if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return -1;
   }
-  return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+  if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged) return -1;
+  return attr.device;
 }
 
 }  // namespace
@@ -124,12 +162,17 @@ extern "C" int pdg_dot_noalloc(long n, const double *a, const double *b, double 
                      "partial sums of 65,536 elements); use pdg_dot");
   if (!result || (n > 0 && (!a || !b)))
     return set_error(PDG_EINVAL, "pdg_dot_noalloc: null pointer");
-  if (!on_device(result) || (n > 0 && (!on_device(a) || !on_device(b))))
-    return set_error(PDG_EINVAL, "pdg_dot_noalloc: a, b and result must be device pointers");
   int dev = 0;
   const cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess)
     return set_error(PDG_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  // every pointer must live on the current device, where the kernel runs
+  const int dr = owning_device(result);
+  if (dr < 0 || (n > 0 && (owning_device(a) < 0 || owning_device(b) < 0)))
+    return set_error(PDG_EINVAL, "pdg_dot_noalloc: a, b and result must be device pointers");
+  if (dr != dev || (n > 0 && (owning_device(a) != dev || owning_device(b) != dev)))
+    return set_error(PDG_EINVAL,
+                     "pdg_dot_noalloc: a, b and result must be on the current device");
   double *scratch = nullptr;
   const int st = scratch_address(dev, &scratch);
   if (st != PDG_OK) return st;

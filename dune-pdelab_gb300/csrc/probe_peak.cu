@@ -1,7 +1,10 @@
 // probe_peak.cu -- measurement helper for bench.py: sustained FP64 / FP32
 // fused-multiply-add throughput of this GPU's CUDA cores (not the product
 // path).  The operator kernels run on the FP64 / FP32 pipes, so these are
-// the roofline denominators for their arithmetic.
+// the roofline denominators for their arithmetic.  A second probe measures
+// the FP64 tensor-core path (warp-level mma.sync of f64 operands), the only
+// FP64 matrix instruction sm_103a has, to decide whether the FP64 operator's
+// small contractions could move there.
 //
 // Each thread runs 8 independent FMA chains for `iters` steps; the result
 // is written out so the compiler keeps the work.
@@ -40,6 +43,53 @@ static int run(int iters, double *tflops) {
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
   const double flops = 2.0 * 8 * 16 * (double)iters * threads * blocks;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+// Each warp keeps 8 independent m8n8k4 accumulators (D = A B + D, 512 flops
+// per warp instruction); A and B stay in registers.
+__global__ void k_dmma(int iters, double a, double b, double *out) {
+  double c[8][2];
+#pragma unroll
+  for (int u = 0; u < 8; u++) { c[u][0] = 0.0; c[u][1] = 0.0; }
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      asm volatile(
+          "mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+          : "+d"(c[u][0]), "+d"(c[u][1])
+          : "d"(a), "d"(b));
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int u = 0; u < 8; u++) s += c[u][0] + c[u][1];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+extern "C" int pdg_probe_dmma_peak(int iters, double *tflops) {
+  if (!tflops || iters < 10) return 1;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int threads = 256, blocks = sms * 8;
+  double *out = nullptr;
+  if (cudaMalloc(&out, sizeof(double) * threads * blocks) != cudaSuccess) return 2;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_dmma<<<blocks, threads>>>(iters / 10, 1e-3, 1e-3, out);   // warm-up
+  cudaEventRecord(e0);
+  k_dmma<<<blocks, threads>>>(iters, 1e-3, 1e-3, out);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  const double warps = (double)threads / 32 * blocks;
+  const double flops = 512.0 * 8 * (double)iters * warps;
   *tflops = flops / (ms * 1e-3) / 1e12;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -295,18 +295,22 @@ int pdg_dot(pdg_context *ctx, const double *a, const double *b, double *out);
 
 /* Dot product *result = sum_i a[i] b[i] of two device vectors that
    allocates nothing.  No counterpart in the reference.  For callers that
-   cannot allocate device memory when they call: work recorded by CUDA stream
-   capture (cudaMalloc is not allowed while capturing), host solvers that own
-   every buffer and forbid allocations after set-up.  No context is needed.
-   a, b and result are device pointers; the result is written on `stream`
-   (cudaStream_t as void*, NULL = legacy default stream).  The reduction
-   scratch is a file-scope device array of 1024 partial sums that every GPU
-   loading the library holds until exit; n <= PDG_DOT_NOALLOC_MAX_N
+   cannot allocate device memory when they call: host solvers that own every
+   buffer and forbid library allocations after set-up (a dune-istl Krylov
+   loop over device vectors asks for a dot product in every iteration), and
+   embeddings that budget device memory and must not see the hidden
+   allocations, or the synchronisation, of cudaMalloc and cudaFree.  No
+   context is needed.  a, b and result are device pointers on the current
+   device (others are rejected with PDG_EINVAL); the result is written on
+   `stream` (cudaStream_t as void*, NULL = legacy default stream).  The
+   reduction scratch is a file-scope device array of 1024 partial sums that
+   every GPU loading the library holds until exit; n <= PDG_DOT_NOALLOC_MAX_N
    (1024 chunks of 65,536 elements) and larger n is rejected with PDG_EINVAL.
-   The first call on a device looks up the array's device address with that
-   device current; make that first call before any stream capture.  All calls
-   share the one array: calls that overlap on the GPU (other streams, other
-   threads) race and must be serialised by the caller. */
+   The first call on a device (and the first call after cudaDeviceReset gave
+   the device a new context) looks up the array's device address with that
+   device current; make that first call before any stream capture.  All
+   calls share the one array: calls that overlap on the GPU (other streams,
+   other threads) race and must be serialised by the caller. */
 #define PDG_DOT_NOALLOC_MAX_N 67108864L
 int pdg_dot_noalloc(long n, const double *a, const double *b, double *result,
                     void *stream);

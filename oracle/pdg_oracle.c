@@ -374,6 +374,99 @@ static void velocity(const pdgo_problem *p, const double *xg, double *b) {
   }
 }
 
+/* ---- coefficients (ConvectionDiffusionModelProblem, convectiondiffusion-
+   parameter.hh:148-183): A as a d x d tensor, row-major ---- */
+static int pointwise_A(const pdgo_problem *p) { return p->Aq_vol && p->Aq_face; }
+static void A_scalar(int d, double k, double *A) {
+  for (int i = 0; i < d; i++)
+    for (int j = 0; j < d; j++) A[i * d + j] = i == j ? k : 0.0;
+}
+/* A(cell, centre) (:124-127, :305-309, :710-713) */
+static void A_centre(const pdgo_problem *p, long e, double *A) {
+  int d = p->dim;
+  if (p->Acell) memcpy(A, &p->Acell[e * d * d], sizeof(double) * d * d);
+  else A_scalar(d, Kof(p, e), A);
+}
+/* A(cell, volume point q) and A(cell, point q of the cell's face f) */
+static void A_vol_point(const pdgo_problem *p, int nqv, long e, int q, double *A) {
+  int d = p->dim;
+  memcpy(A, &p->Aq_vol[(e * nqv + q) * d * d], sizeof(double) * d * d);
+}
+static void A_face_point(const pdgo_problem *p, int nqf, long e, int f, int q, double *A) {
+  int d = p->dim;
+  memcpy(A, &p->Aq_face[((e * 2 * d + f) * nqf + q) * d * d], sizeof(double) * d * d);
+}
+/* y = A x (FieldMatrix::mv) */
+static void mat_vec(int d, const double *A, const double *x, double *y) {
+  for (int i = 0; i < d; i++) {
+    y[i] = 0.0;
+    for (int j = 0; j < d; j++) y[i] += A[i * d + j] * x[j];
+  }
+}
+/* y = A^T x */
+static void mat_tvec(int d, const double *A, const double *x, double *y) {
+  for (int i = 0; i < d; i++) {
+    y[i] = 0.0;
+    for (int j = 0; j < d; j++) y[i] += A[j * d + i] * x[j];
+  }
+}
+static double dotd(int d, const double *a, const double *b) {
+  double s = 0.0;
+  for (int j = 0; j < d; j++) s += a[j] * b[j];
+  return s;
+}
+/* c(cell, volume point q) (:181): per-cell c plus the per-point part */
+static double c_at(const pdgo_problem *p, int nqv, long e, int q) {
+  return (p->c ? p->c[e] : 0.0) + (p->cq ? p->cq[e * nqv + q] : 0.0);
+}
+
+/* face lattice: see pdgo_face_lattice_index in pdg_oracle.h */
+static long faces_in_plane(const pdgo_problem *p, int dir) {
+  long n = 1;
+  for (int j = 0; j < p->dim; j++)
+    if (j != dir) n *= p->nc[j];
+  return n;
+}
+long pdgo_nface_lattice(const pdgo_problem *p) {
+  long n = 0;
+  for (int dir = 0; dir < p->dim; dir++) n += (p->nc[dir] + 1) * faces_in_plane(p, dir);
+  return n;
+}
+long pdgo_face_lattice_index(const pdgo_problem *p, int dir, int plane, const int *ix) {
+  long off = 0;
+  for (int j = 0; j < dir; j++) off += (p->nc[j] + 1) * faces_in_plane(p, j);
+  long idx = 0;
+  for (int j = p->dim - 1; j >= 0; j--) {
+    if (j == dir) continue;
+    idx = idx * p->nc[j] + ix[j];
+  }
+  return off + (long)plane * faces_in_plane(p, dir) + idx;
+}
+
+/* b(cell, x) at volume point q of cell e (:178) and at point q of face f
+   of the inside cell e (:426, :797): per-point data when given, else the
+   Fourier-mode field at the point's coordinates xg */
+static int have_velocity(const pdgo_problem *p) {
+  return p->nmodes > 0 || (p->bq_vol && p->bq_face);
+}
+static void b_vol(const pdgo_problem *p, int nqv, long e, int q, const double *xg, double *b) {
+  if (p->bq_vol && p->bq_face) {
+    for (int j = 0; j < MAXD; j++) b[j] = j < p->dim ? p->bq_vol[(e * nqv + q) * p->dim + j] : 0.0;
+    return;
+  }
+  velocity(p, xg, b);
+}
+static void b_face(const pdgo_problem *p, int nqf, const int *ix, int f, int q, const double *xg,
+                   double *b) {
+  if (p->bq_vol && p->bq_face) {
+    int dir = f / 2, hi = f % 2;
+    long fi = pdgo_face_lattice_index(p, dir, ix[dir] + hi, ix);
+    for (int j = 0; j < MAXD; j++) b[j] = j < p->dim ? p->bq_face[(fi * nqf + q) * p->dim + j] : 0.0;
+    return;
+  }
+  velocity(p, xg, b);
+}
+
 int pdgo_volume_points(const pdgo_problem *p, double *xyz) {
   tables T;
   if (tables_init(p, &T)) return PDGO_EARG;
@@ -411,6 +504,45 @@ int pdgo_boundary_points(const pdgo_problem *p, double *xyz) {
   return PDGO_OK;
 }
 
+int pdgo_face_lattice_points(const pdgo_problem *p, double *xyz) {
+  tables T;
+  if (tables_init(p, &T)) return PDGO_EARG;
+  int d = T.d;
+  long nc = pdgo_ncell(p);
+  for (long e = 0; e < nc; e++) {
+    int ix[MAXD];
+    cell_index(p, e, ix);
+    for (int f = 0; f < 2 * d; f++) {
+      int dir = f / 2, hi = f % 2;
+      if (hi && ix[dir] != p->nc[dir] - 1) continue;   /* upper faces of the last cell only */
+      long fi = pdgo_face_lattice_index(p, dir, ix[dir] + hi, ix);
+      for (int q = 0; q < T.nqf; q++)
+        for (int j = 0; j < d; j++)
+          xyz[(fi * T.nqf + q) * d + j] = (ix[j] + T.floc[(f * T.nqf + q) * d + j]) * cell_h(p, j);
+    }
+  }
+  tables_free(&T);
+  return PDGO_OK;
+}
+
+int pdgo_cell_face_points(const pdgo_problem *p, double *xyz) {
+  tables T;
+  if (tables_init(p, &T)) return PDGO_EARG;
+  int d = T.d;
+  long nc = pdgo_ncell(p);
+  for (long e = 0; e < nc; e++) {
+    int ix[MAXD];
+    cell_index(p, e, ix);
+    for (int f = 0; f < 2 * d; f++)
+      for (int q = 0; q < T.nqf; q++)
+        for (int j = 0; j < d; j++)
+          xyz[((e * 2 * d + f) * T.nqf + q) * d + j] =
+              (ix[j] + T.floc[(f * T.nqf + q) * d + j]) * cell_h(p, j);
+  }
+  tables_free(&T);
+  return PDGO_OK;
+}
+
 /* ------------------------------------------------------------------ */
 /* local operator (residual / jacobian_apply form)                     */
 /* ------------------------------------------------------------------ */
@@ -429,11 +561,13 @@ static void alpha_volume(const pdgo_problem *p, const tables *T, long e,
   cell_index(p, e, ix);
   double h[MAXD], detJ = 1.0;
   for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); detJ *= h[j]; }
-  /* A at the cell centre (:124-127); scalar K -> A = K I */
-  double A = co && co->active ? co->Ks : Kof(p, e);
-  double cc = (co && co->active) ? 0.0 : (p->c ? p->c[e] : 0.0);
+  /* A at the cell centre (:124-127), per point if not constant (:143-146) */
+  int act = co && co->active;
+  double A[MAXD * MAXD];
+  if (act) A_scalar(d, co->Ks, A); else A_centre(p, e, A);
   double gradphi[MAXNB][MAXD];
   for (int q = 0; q < T->nqv; q++) {
+    if (!act && pointwise_A(p)) A_vol_point(p, T->nqv, e, q, A);
     const double *phi = &T->vphi[q * nb];
     const double *js = &T->vjs[q * nb * d];
     double u = 0.0;
@@ -444,13 +578,14 @@ static void alpha_volume(const pdgo_problem *p, const tables *T, long e,
     double gradu[MAXD] = {0, 0, 0}, Agradu[MAXD];
     for (int i = 0; i < nb; i++)
       for (int j = 0; j < d; j++) gradu[j] += x[i] * gradphi[i][j];
-    for (int j = 0; j < d; j++) Agradu[j] = A * gradu[j];
+    mat_vec(d, A, gradu, Agradu);
     double b[MAXD] = {0, 0, 0};
-    if (!(co && co->active) && p->nmodes > 0) {
+    if (!act && have_velocity(p)) {
       double xg[MAXD];
       for (int j = 0; j < d; j++) xg[j] = (ix[j] + T->vloc[q * d + j]) * h[j];
-      velocity(p, xg, b);
+      b_vol(p, T->nqv, e, q, xg, b);
     }
+    double cc = act ? 0.0 : c_at(p, T->nqv, e, q);
     double factor = T->vw[q] * detJ;
     for (int i = 0; i < nb; i++) {
       double ag = 0.0, bg = 0.0;
@@ -507,12 +642,12 @@ static void lambda_volume(const pdgo_problem *p, const tables *T, long e, double
   }
 }
 
-/* skeleton weights (convectiondiffusiondg.hh:308-346) */
-static void face_weights(const pdgo_problem *p, double Ks, double Kn, double hF,
+/* skeleton weights (convectiondiffusiondg.hh:308-346) from
+   delta = (A n).n of both sides */
+static void face_weights(const pdgo_problem *p, double delta_s, double delta_n, double hF,
                          double *omega_s, double *omega_n, double *penalty) {
   double harmonic_average;
   if (p->weights == PDGO_WEIGHTS_ON) {
-    double delta_s = Ks, delta_n = Kn;   /* (A n).n with A = K I, |n| = 1 */
     *omega_s = delta_n / (delta_s + delta_n + 1e-20);
     *omega_n = delta_s / (delta_s + delta_n + 1e-20);
     harmonic_average = 2.0 * delta_s * delta_n / (delta_s + delta_n + 1e-20);
@@ -524,31 +659,65 @@ static void face_weights(const pdgo_problem *p, double Ks, double Kn, double hF,
   *penalty = (p->alpha / hF) * harmonic_average * degree * (degree + p->dim - 1);
 }
 
+/* The coefficient state of one side pair of an interior face: A_s n, A_n n,
+   the weights and the penalty (:305-346), refreshed per point when A is not
+   constant per cell (:365-382). */
+typedef struct face_coef {
+  double As[MAXD * MAXD], An[MAXD * MAXD];
+  double AnFs[MAXD], AnFn[MAXD];
+  double omega_s, omega_n, penalty;
+} face_coef;
+
+static void face_coef_update(const pdgo_problem *p, int d, const double *nF, double hF,
+                             face_coef *fc) {
+  mat_vec(d, fc->As, nF, fc->AnFs);
+  mat_vec(d, fc->An, nF, fc->AnFn);
+  face_weights(p, dotd(d, fc->AnFs, nF), dotd(d, fc->AnFn, nF), hF, &fc->omega_s, &fc->omega_n,
+               &fc->penalty);
+}
+
+static void face_coef_init(const pdgo_problem *p, int d, long s, long n, const double *nF,
+                           double hF, const coef_override *co, face_coef *fc) {
+  if (co && co->active) { A_scalar(d, co->Ks, fc->As); A_scalar(d, co->Kn, fc->An); }
+  else { A_centre(p, s, fc->As); A_centre(p, n, fc->An); }
+  face_coef_update(p, d, nF, hF, fc);
+}
+
+static void face_coef_point(const pdgo_problem *p, int d, int nqf, long s, long n, int fs, int fn,
+                            int q, const double *nF, double hF, const coef_override *co,
+                            face_coef *fc) {
+  if ((co && co->active) || !pointwise_A(p)) return;
+  A_face_point(p, nqf, s, fs, q, fc->As);
+  A_face_point(p, nqf, n, fn, q, fc->An);
+  face_coef_update(p, d, nF, hF, fc);
+}
+
 /* alpha_skeleton (convectiondiffusiondg.hh:270-471) for the interior face
    between inside cell s and outside cell n; the face is normal to `dir`,
-   and n lies on side `hi_s` of s (0 = lower, 1 = upper). */
-static void alpha_skeleton(const pdgo_problem *p, const tables *T, long s, long n,
-                           int dir, int hi_s, const double *x_s, const double *x_n,
-                           double *r_s, double *r_n, const coef_override *co) {
+   and n lies on side `hi_s` of s (0 = lower, 1 = upper).  With transpose
+   set it adds J^T instead: the same point quantities, with the roles of
+   the trial traces (u, A n . grad u) and of the test traces (psi,
+   A n . grad psi) exchanged term by term. */
+static void skeleton_form(const pdgo_problem *p, const tables *T, long s, long n,
+                          int dir, int hi_s, const double *x_s, const double *x_n,
+                          double *r_s, double *r_n, const coef_override *co, int transpose) {
   int d = T->d, nb = T->nb, nqf = T->nqf;
   double h[MAXD], vol = 1.0;
   for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); vol *= h[j]; }
   double area = vol / h[dir];
-  double Ks = co && co->active ? co->Ks : Kof(p, s);
-  double Kn = co && co->active ? co->Kn : Kof(p, n);
   double vol_s = vol, vol_n = vol;                   /* uniform grid */
   double hF = (vol_s < vol_n ? vol_s : vol_n) / area; /* min(|T_s|,|T_n|)/|F| (:313) */
   double nF[MAXD] = {0, 0, 0};
   nF[dir] = hi_s ? 1.0 : -1.0;
-  double omega_s, omega_n, penalty;
-  face_weights(p, Ks, Kn, hF, &omega_s, &omega_n, &penalty);
-  double An_F_s[MAXD], An_F_n[MAXD];
-  for (int j = 0; j < d; j++) { An_F_s[j] = Ks * nF[j]; An_F_n[j] = Kn * nF[j]; }
+  face_coef fc;
+  face_coef_init(p, d, s, n, nF, hF, co, &fc);
   int fs = 2 * dir + hi_s, fn = 2 * dir + (1 - hi_s);
   int ixs[MAXD];
   cell_index(p, s, ixs);
-  double tgs[MAXNB][MAXD], tgn[MAXNB][MAXD];
+  int act = co && co->active;
+  double tgs[MAXNB][MAXD], tgn[MAXNB][MAXD], ans[MAXNB], ann[MAXNB];
   for (int q = 0; q < nqf; q++) {
+    face_coef_point(p, d, nqf, s, n, fs, fn, q, nF, hF, co, &fc);
     const double *phi_s = &T->fphi[(fs * nqf + q) * nb];
     const double *phi_n = &T->fphi[(fn * nqf + q) * nb];
     const double *js_s = &T->fjs[(fs * nqf + q) * nb * d];
@@ -558,68 +727,100 @@ static void alpha_skeleton(const pdgo_problem *p, const tables *T, long s, long 
     for (int i = 0; i < nb; i++) u_n += x_n[i] * phi_n[i];
     for (int i = 0; i < nb; i++)
       for (int j = 0; j < d; j++) { tgs[i][j] = js_s[i * d + j] / h[j]; tgn[i][j] = js_n[i * d + j] / h[j]; }
-    double gus[MAXD] = {0, 0, 0}, gun[MAXD] = {0, 0, 0};
-    for (int i = 0; i < nb; i++)
-      for (int j = 0; j < d; j++) { gus[j] += x_s[i] * tgs[i][j]; gun[j] += x_n[i] * tgn[i][j]; }
+    /* A n . grad(phi_i) on both sides */
+    for (int i = 0; i < nb; i++) { ans[i] = dotd(d, fc.AnFs, tgs[i]); ann[i] = dotd(d, fc.AnFn, tgn[i]); }
     double b[MAXD] = {0, 0, 0};
-    if (!(co && co->active) && p->nmodes > 0) {
+    if (!act && have_velocity(p)) {
       double xg[MAXD];
       for (int j = 0; j < d; j++) xg[j] = (ixs[j] + T->floc[(fs * nqf + q) * d + j]) * h[j];
-      velocity(p, xg, b);
+      b_face(p, nqf, ixs, fs, q, xg, b);
     }
-    double normalflux = 0.0;
-    for (int j = 0; j < d; j++) normalflux += b[j] * nF[j];
+    double normalflux = dotd(d, b, nF);
     double omegaup_s, omegaup_n;
     if (normalflux >= 0.0) { omegaup_s = 1.0; omegaup_n = 0.0; }
     else { omegaup_s = 0.0; omegaup_n = 1.0; }
     double factor = T->fw[fs * nqf + q] * area;
-    double term1 = (omegaup_s * u_s + omegaup_n * u_n) * normalflux * factor;
-    double Ags = 0.0, Agn = 0.0;
-    for (int j = 0; j < d; j++) { Ags += An_F_s[j] * gus[j]; Agn += An_F_n[j] * gun[j]; }
-    double term2 = -(omega_s * Ags + omega_n * Agn) * factor;
-    double term3 = (u_s - u_n) * factor;
-    double term4 = penalty * (u_s - u_n) * factor;
-    for (int i = 0; i < nb; i++) {
-      double ans = 0.0, ann = 0.0;
-      for (int j = 0; j < d; j++) { ans += An_F_s[j] * tgs[i][j]; ann += An_F_n[j] * tgn[i][j]; }
-      r_s[i] += term1 * phi_s[i];
-      r_n[i] += -term1 * phi_n[i];
-      r_s[i] += term2 * phi_s[i];
-      r_n[i] += -term2 * phi_n[i];
-      r_s[i] += term3 * T->theta * omega_s * ans;
-      r_n[i] += term3 * T->theta * omega_n * ann;
-      r_s[i] += term4 * phi_s[i];
-      r_n[i] += -term4 * phi_n[i];
+    double omega_s = fc.omega_s, omega_n = fc.omega_n, penalty = fc.penalty;
+    if (!transpose) {
+      double gus[MAXD] = {0, 0, 0}, gun[MAXD] = {0, 0, 0};
+      for (int i = 0; i < nb; i++)
+        for (int j = 0; j < d; j++) { gus[j] += x_s[i] * tgs[i][j]; gun[j] += x_n[i] * tgn[i][j]; }
+      /* A_s n . grad u_s, A_n n . grad u_n */
+      double Ags = dotd(d, fc.AnFs, gus), Agn = dotd(d, fc.AnFn, gun);
+      double term1 = (omegaup_s * u_s + omegaup_n * u_n) * normalflux * factor;
+      double term2 = -(omega_s * Ags + omega_n * Agn) * factor;
+      double term3 = (u_s - u_n) * factor;
+      double term4 = penalty * (u_s - u_n) * factor;
+      for (int i = 0; i < nb; i++) {
+        r_s[i] += term1 * phi_s[i];
+        r_n[i] += -term1 * phi_n[i];
+        r_s[i] += term2 * phi_s[i];
+        r_n[i] += -term2 * phi_n[i];
+        r_s[i] += term3 * T->theta * omega_s * ans[i];
+        r_n[i] += term3 * T->theta * omega_n * ann[i];
+        r_s[i] += term4 * phi_s[i];
+        r_n[i] += -term4 * phi_n[i];
+      }
+    } else {
+      /* x holds the test-side vector z: jump [z] = z_s - z_n of the value
+         traces and the weighted A n . grad z traces */
+      double jz = u_s - u_n;
+      double az = 0.0;
+      for (int i = 0; i < nb; i++) az += T->theta * (omega_s * x_s[i] * ans[i] + omega_n * x_n[i] * ann[i]);
+      for (int j = 0; j < nb; j++) {
+        /* term1: trial value of side s (n) times the upwind weight */
+        r_s[j] += omegaup_s * normalflux * factor * jz * phi_s[j];
+        r_n[j] += omegaup_n * normalflux * factor * jz * phi_n[j];
+        /* term2: trial A n . grad */
+        r_s[j] += -omega_s * factor * jz * ans[j];
+        r_n[j] += -omega_n * factor * jz * ann[j];
+        /* term3: trial jump against the test A n . grad traces */
+        r_s[j] += factor * az * phi_s[j];
+        r_n[j] += -factor * az * phi_n[j];
+        /* term4 */
+        r_s[j] += penalty * factor * jz * phi_s[j];
+        r_n[j] += -penalty * factor * jz * phi_n[j];
+      }
     }
   }
 }
 
+static void alpha_skeleton(const pdgo_problem *p, const tables *T, long s, long n,
+                           int dir, int hi_s, const double *x_s, const double *x_n,
+                           double *r_s, double *r_n, const coef_override *co) {
+  skeleton_form(p, T, s, n, dir, hi_s, x_s, x_n, r_s, r_n, co, 0);
+}
+
 /* residual_boundary_integral (convectiondiffusiondg.hh:683-879), called by
    alpha_boundary (:883-889, jacobian_apply=false) and
-   jacobian_apply_boundary (:892-899, jacobian_apply=true). */
-static int boundary_integral(const pdgo_problem *p, const tables *T, long e, int side,
-                             const double *x_s, double *r_s, int jacobian_apply,
-                             const coef_override *co) {
+   jacobian_apply_boundary (:892-899, jacobian_apply=true).  transpose = 1
+   (only with jacobian_apply) adds the transposed boundary form. */
+static int boundary_form(const pdgo_problem *p, const tables *T, long e, int side,
+                         const double *x_s, double *r_s, int jacobian_apply,
+                         const coef_override *co, int transpose) {
   int d = T->d, nb = T->nb, nqf = T->nqf;
   int dir = side / 2, hi = side % 2;
   double h[MAXD], vol = 1.0;
   for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); vol *= h[j]; }
   double area = vol / h[dir];
-  double Ks = co && co->active ? co->Ks : Kof(p, e);
   double hF = vol / area;
   double nF[MAXD] = {0, 0, 0};
   nF[dir] = hi ? 1.0 : -1.0;
-  double An_F_s[MAXD];
-  for (int j = 0; j < d; j++) An_F_s[j] = Ks * nF[j];
-  double harmonic_average = (p->weights == PDGO_WEIGHTS_ON) ? Ks : 1.0;
+  int act = co && co->active;
+  double A[MAXD * MAXD], An_F_s[MAXD];
+  if (act) A_scalar(d, co->Ks, A); else A_centre(p, e, A);
   int degree = p->k;
-  double penalty_factor = (p->alpha / hF) * harmonic_average * degree * (degree + d - 1);
   int ix[MAXD];
   cell_index(p, e, ix);
   long base = pdgo_bpts_offset(p, side) + boundary_face_index(p, ix, side) * nqf;
   int bctype = p->bctype[side];
-  double tg[MAXNB][MAXD];
+  double tg[MAXNB][MAXD], an[MAXNB];
   for (int q = 0; q < nqf; q++) {
+    /* A n and the penalty (:710-734), per point if A is not constant (:750-761) */
+    if (!act && pointwise_A(p)) A_face_point(p, nqf, e, side, q, A);
+    mat_vec(d, A, nF, An_F_s);
+    double harmonic_average = (p->weights == PDGO_WEIGHTS_ON) ? dotd(d, An_F_s, nF) : 1.0;
+    double penalty_factor = (p->alpha / hF) * harmonic_average * degree * (degree + d - 1);
     if (bctype == PDGO_BC_NONE) continue;
     const double *phi = &T->fphi[(side * nqf + q) * nb];
     const double *js = &T->fjs[(side * nqf + q) * nb * d];
@@ -634,16 +835,15 @@ static int boundary_integral(const pdgo_problem *p, const tables *T, long e, int
     double u_s = 0.0;
     for (int i = 0; i < nb; i++) u_s += x_s[i] * phi[i];
     double b[MAXD] = {0, 0, 0};
-    if (!(co && co->active) && p->nmodes > 0) {
+    if (!act && have_velocity(p)) {
       double xg[MAXD];
       for (int j = 0; j < d; j++) xg[j] = (ix[j] + T->floc[(side * nqf + q) * d + j]) * h[j];
-      velocity(p, xg, b);
+      b_face(p, nqf, ix, side, q, xg, b);
     }
-    double normalflux = 0.0;
-    for (int j = 0; j < d; j++) normalflux += b[j] * nF[j];
+    double normalflux = dotd(d, b, nF);
     if (bctype == PDGO_BC_OUTFLOW) {
       if (normalflux < -1e-30) return PDGO_EOUTFLOW_ON_INFLOW;
-      double term1 = u_s * normalflux * factor;
+      double term1 = u_s * normalflux * factor;   /* symmetric in test and trial */
       for (int i = 0; i < nb; i++) r_s[i] += term1 * phi[i];
       if (!jacobian_apply) {
         double ov = p->oq ? p->oq[base + q] : 0.0;
@@ -652,32 +852,84 @@ static int boundary_integral(const pdgo_problem *p, const tables *T, long e, int
       continue;
     }
     /* Dirichlet */
-    for (int i = 0; i < nb; i++)
+    for (int i = 0; i < nb; i++) {
       for (int j = 0; j < d; j++) tg[i][j] = js[i * d + j] / h[j];
-    double gu[MAXD] = {0, 0, 0};
-    for (int i = 0; i < nb; i++)
-      for (int j = 0; j < d; j++) gu[j] += x_s[i] * tg[i][j];
+      an[i] = dotd(d, An_F_s, tg[i]);
+    }
     double g = p->gq ? p->gq[base + q] : 0.0;
     if (jacobian_apply) g = 0.0;
     double omegaup_s, omegaup_n;
     if (normalflux >= 0.0) { omegaup_s = 1.0; omegaup_n = 0.0; }
     else { omegaup_s = 0.0; omegaup_n = 1.0; }
-    double term1 = (omegaup_s * u_s + omegaup_n * g) * normalflux * factor;
-    double Ag = 0.0;
-    for (int j = 0; j < d; j++) Ag += An_F_s[j] * gu[j];
-    double term2 = Ag * factor;
-    double term3 = (u_s - g) * factor;
-    double term4 = penalty_factor * (u_s - g) * factor;
-    for (int i = 0; i < nb; i++) {
-      double an = 0.0;
-      for (int j = 0; j < d; j++) an += An_F_s[j] * tg[i][j];
-      r_s[i] += term1 * phi[i];
-      r_s[i] += -term2 * phi[i];
-      r_s[i] += term3 * T->theta * an;
-      r_s[i] += term4 * phi[i];
+    if (!transpose) {
+      double gu[MAXD] = {0, 0, 0};
+      for (int i = 0; i < nb; i++)
+        for (int j = 0; j < d; j++) gu[j] += x_s[i] * tg[i][j];
+      double Ag = dotd(d, An_F_s, gu);
+      double term1 = (omegaup_s * u_s + omegaup_n * g) * normalflux * factor;
+      double term2 = Ag * factor;
+      double term3 = (u_s - g) * factor;
+      double term4 = penalty_factor * (u_s - g) * factor;
+      for (int i = 0; i < nb; i++) {
+        r_s[i] += term1 * phi[i];
+        r_s[i] += -term2 * phi[i];
+        r_s[i] += term3 * T->theta * an[i];
+        r_s[i] += term4 * phi[i];
+      }
+    } else {
+      double az = 0.0;
+      for (int i = 0; i < nb; i++) az += x_s[i] * an[i];
+      for (int j = 0; j < nb; j++) {
+        r_s[j] += omegaup_s * normalflux * factor * u_s * phi[j];
+        r_s[j] += -factor * u_s * an[j];
+        r_s[j] += T->theta * factor * az * phi[j];
+        r_s[j] += penalty_factor * factor * u_s * phi[j];
+      }
     }
   }
   return PDGO_OK;
+}
+
+static int boundary_integral(const pdgo_problem *p, const tables *T, long e, int side,
+                             const double *x_s, double *r_s, int jacobian_apply,
+                             const coef_override *co) {
+  return boundary_form(p, T, e, side, x_s, r_s, jacobian_apply, co, 0);
+}
+
+/* transposed jacobian_apply_volume: y_j += sum_q w [A grad phi_j . grad z
+   - phi_j b . grad z + c phi_j z] (the volume form with test and trial
+   exchanged) */
+static void volume_transpose(const pdgo_problem *p, const tables *T, long e,
+                             const double *z, double *y) {
+  int d = T->d, nb = T->nb;
+  int ix[MAXD];
+  cell_index(p, e, ix);
+  double h[MAXD], detJ = 1.0;
+  for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); detJ *= h[j]; }
+  double A[MAXD * MAXD];
+  A_centre(p, e, A);
+  double gradphi[MAXNB][MAXD];
+  for (int q = 0; q < T->nqv; q++) {
+    if (pointwise_A(p)) A_vol_point(p, T->nqv, e, q, A);
+    const double *phi = &T->vphi[q * nb];
+    const double *js = &T->vjs[q * nb * d];
+    double zq = 0.0, gz[MAXD] = {0, 0, 0}, Atgz[MAXD];
+    for (int i = 0; i < nb; i++) zq += z[i] * phi[i];
+    for (int i = 0; i < nb; i++)
+      for (int j = 0; j < d; j++) { gradphi[i][j] = js[i * d + j] / h[j]; gz[j] += z[i] * gradphi[i][j]; }
+    mat_tvec(d, A, gz, Atgz);    /* (A grad phi_j) . grad z = grad phi_j . (A^T grad z) */
+    double b[MAXD] = {0, 0, 0};
+    if (have_velocity(p)) {
+      double xg[MAXD];
+      for (int j = 0; j < d; j++) xg[j] = (ix[j] + T->vloc[q * d + j]) * h[j];
+      b_vol(p, T->nqv, e, q, xg, b);
+    }
+    double bz = dotd(d, b, gz);
+    double cc = c_at(p, T->nqv, e, q);
+    double factor = T->vw[q] * detJ;
+    for (int j = 0; j < nb; j++)
+      y[j] += (dotd(d, Atgz, gradphi[j]) - phi[j] * bz + cc * phi[j] * zq) * factor;
+  }
 }
 
 /* DefaultAssembler::assemble (gridoperator/default/assembler.hh:85-279):
@@ -722,6 +974,48 @@ int pdgo_jacobian_apply_range(const pdgo_problem *p, const double *z, double *y,
                               long e_begin, long e_end) {
   return assemble_vector(p, z, y, 1, e_begin, e_end);
 }
+/* y += J^T z over the traversal of assemble_vector: volume and boundary
+   blocks transposed in place, each interior face's four blocks transposed
+   and exchanged between the two sides.  The nonlinear Jacobian term
+   int q'(u_lin) z psi is symmetric and enters unchanged. */
+static int assemble_transpose(const pdgo_problem *p, const double *z, double *y, long e_begin,
+                              long e_end) {
+  tables T;
+  if (tables_init(p, &T)) return PDGO_EARG;
+  int d = T.d, nb = T.nb;
+  long nc = pdgo_ncell(p);
+  if (e_end > nc) e_end = nc;
+  int st = PDGO_OK;
+  for (long e = e_begin; e < e_end && !st; e++) {
+    int ix[MAXD];
+    cell_index(p, e, ix);
+    volume_transpose(p, &T, e, &z[e * nb], &y[e * nb]);
+    nl_volume(p, &T, e, &z[e * nb], &y[e * nb], 1);
+    for (int f = 0; f < 2 * d && !st; f++) {
+      int dir = f / 2, hi = f % 2;
+      int jx[MAXD];
+      memcpy(jx, ix, sizeof(jx));
+      jx[dir] += hi ? 1 : -1;
+      if (jx[dir] < 0 || jx[dir] >= p->nc[dir]) {
+        st = boundary_form(p, &T, e, f, &z[e * nb], &y[e * nb], 1, NULL, 1);
+        continue;
+      }
+      long n = cell_of(p, jx);
+      if (!(e > n)) continue;
+      skeleton_form(p, &T, e, n, dir, hi, &z[e * nb], &z[n * nb], &y[e * nb], &y[n * nb], NULL, 1);
+    }
+  }
+  tables_free(&T);
+  return st;
+}
+
+int pdgo_jacobian_apply_transpose(const pdgo_problem *p, const double *z, double *y) {
+  return assemble_transpose(p, z, y, 0, pdgo_ncell(p));
+}
+int pdgo_jacobian_apply_transpose_range(const pdgo_problem *p, const double *z, double *y,
+                                        long e_begin, long e_end) {
+  return assemble_transpose(p, z, y, e_begin, e_end);
+}
 int pdgo_residual(const pdgo_problem *p, const double *x, double *r) {
   return assemble_vector(p, x, r, 0, 0, pdgo_ncell(p));
 }
@@ -739,20 +1033,25 @@ static void jacobian_volume(const pdgo_problem *p, const tables *T, long e,
   cell_index(p, e, ix);
   double h[MAXD], detJ = 1.0;
   for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); detJ *= h[j]; }
-  double A = co && co->active ? co->Ks : Kof(p, e);
-  double cc = (co && co->active) ? 0.0 : (p->c ? p->c[e] : 0.0);
+  int act = co && co->active;
+  double A[MAXD * MAXD];
+  if (act) A_scalar(d, co->Ks, A); else A_centre(p, e, A);
   double gradphi[MAXNB][MAXD], Agradphi[MAXNB][MAXD];
   for (int q = 0; q < T->nqv; q++) {
+    if (!act && pointwise_A(p)) A_vol_point(p, T->nqv, e, q, A);
     const double *phi = &T->vphi[q * nb];
     const double *js = &T->vjs[q * nb * d];
-    for (int i = 0; i < nb; i++)
-      for (int j = 0; j < d; j++) { gradphi[i][j] = js[i * d + j] / h[j]; Agradphi[i][j] = A * gradphi[i][j]; }
+    for (int i = 0; i < nb; i++) {
+      for (int j = 0; j < d; j++) gradphi[i][j] = js[i * d + j] / h[j];
+      mat_vec(d, A, gradphi[i], Agradphi[i]);
+    }
     double b[MAXD] = {0, 0, 0};
-    if (!(co && co->active) && p->nmodes > 0) {
+    if (!act && have_velocity(p)) {
       double xg[MAXD];
       for (int j = 0; j < d; j++) xg[j] = (ix[j] + T->vloc[q * d + j]) * h[j];
-      velocity(p, xg, b);
+      b_vol(p, T->nqv, e, q, xg, b);
     }
+    double cc = act ? 0.0 : c_at(p, T->nqv, e, q);
     double factor = T->vw[q] * detJ;
     /* nonlinear part at the linearization point (jacobian_volume of
        nonlinearconvectiondiffusiondg.hh:178-223) */
@@ -781,21 +1080,20 @@ static void jacobian_skeleton(const pdgo_problem *p, const tables *T, long s, lo
   double h[MAXD], vol = 1.0;
   for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); vol *= h[j]; }
   double area = vol / h[dir];
-  double Ks = co && co->active ? co->Ks : Kof(p, s);
-  double Kn = co && co->active ? co->Kn : Kof(p, n);
   double hF = vol / area;
   double nF[MAXD] = {0, 0, 0};
   nF[dir] = hi_s ? 1.0 : -1.0;
-  double omega_s, omega_n, penalty;
-  face_weights(p, Ks, Kn, hF, &omega_s, &omega_n, &penalty);
-  double An_F_s[MAXD], An_F_n[MAXD];
-  for (int j = 0; j < d; j++) { An_F_s[j] = Ks * nF[j]; An_F_n[j] = Kn * nF[j]; }
+  face_coef fc;
+  face_coef_init(p, d, s, n, nF, hF, co, &fc);
   int fs = 2 * dir + hi_s, fn = 2 * dir + (1 - hi_s);
   int ixs[MAXD];
   cell_index(p, s, ixs);
   double tgs[MAXNB][MAXD], tgn[MAXNB][MAXD];
   double theta = T->theta;
   for (int q = 0; q < nqf; q++) {
+    face_coef_point(p, d, nqf, s, n, fs, fn, q, nF, hF, co, &fc);
+    const double *An_F_s = fc.AnFs, *An_F_n = fc.AnFn;
+    double omega_s = fc.omega_s, omega_n = fc.omega_n, penalty = fc.penalty;
     const double *phi_s = &T->fphi[(fs * nqf + q) * nb];
     const double *phi_n = &T->fphi[(fn * nqf + q) * nb];
     const double *js_s = &T->fjs[(fs * nqf + q) * nb * d];
@@ -803,10 +1101,10 @@ static void jacobian_skeleton(const pdgo_problem *p, const tables *T, long s, lo
     for (int i = 0; i < nb; i++)
       for (int j = 0; j < d; j++) { tgs[i][j] = js_s[i * d + j] / h[j]; tgn[i][j] = js_n[i * d + j] / h[j]; }
     double b[MAXD] = {0, 0, 0};
-    if (!(co && co->active) && p->nmodes > 0) {
+    if (!(co && co->active) && have_velocity(p)) {
       double xg[MAXD];
       for (int j = 0; j < d; j++) xg[j] = (ixs[j] + T->floc[(fs * nqf + q) * d + j]) * h[j];
-      velocity(p, xg, b);
+      b_face(p, nqf, ixs, fs, q, xg, b);
     }
     double normalflux = 0.0;
     for (int j = 0; j < d; j++) normalflux += b[j] * nF[j];
@@ -875,29 +1173,31 @@ static int jacobian_boundary(const pdgo_problem *p, const tables *T, long e, int
   double h[MAXD], vol = 1.0;
   for (int j = 0; j < d; j++) { h[j] = cell_h(p, j); vol *= h[j]; }
   double area = vol / h[dir];
-  double Ks = co && co->active ? co->Ks : Kof(p, e);
   double hF = vol / area;
   double nF[MAXD] = {0, 0, 0};
   nF[dir] = hi ? 1.0 : -1.0;
-  double An_F_s[MAXD];
-  for (int j = 0; j < d; j++) An_F_s[j] = Ks * nF[j];
-  double harmonic_average = (p->weights == PDGO_WEIGHTS_ON) ? Ks : 1.0;
+  int act = co && co->active;
+  double A[MAXD * MAXD], An_F_s[MAXD];
+  if (act) A_scalar(d, co->Ks, A); else A_centre(p, e, A);
   int degree = p->k;
-  double penalty_factor = (p->alpha / hF) * harmonic_average * degree * (degree + d - 1);
   int ix[MAXD];
   cell_index(p, e, ix);
   int bctype = p->bctype[side];
   double tg[MAXNB][MAXD], an[MAXNB];
   for (int q = 0; q < nqf; q++) {
+    if (!act && pointwise_A(p)) A_face_point(p, nqf, e, side, q, A);
+    mat_vec(d, A, nF, An_F_s);
+    double harmonic_average = (p->weights == PDGO_WEIGHTS_ON) ? dotd(d, An_F_s, nF) : 1.0;
+    double penalty_factor = (p->alpha / hF) * harmonic_average * degree * (degree + d - 1);
     if (bctype == PDGO_BC_NONE || bctype == PDGO_BC_NEUMANN) continue;
     const double *phi = &T->fphi[(side * nqf + q) * nb];
     const double *js = &T->fjs[(side * nqf + q) * nb * d];
     double factor = T->fw[side * nqf + q] * area;
     double b[MAXD] = {0, 0, 0};
-    if (!(co && co->active) && p->nmodes > 0) {
+    if (!act && have_velocity(p)) {
       double xg[MAXD];
       for (int j = 0; j < d; j++) xg[j] = (ix[j] + T->floc[(side * nqf + q) * d + j]) * h[j];
-      velocity(p, xg, b);
+      b_face(p, nqf, ix, side, q, xg, b);
     }
     double normalflux = 0.0;
     for (int j = 0; j < d; j++) normalflux += b[j] * nF[j];
@@ -1786,7 +2086,8 @@ int pdgo_eval_points(const pdgo_problem *p, const double *u, int m, double *xyz,
    proportional to H = 2 Ks Kn / (Ks + Kn + 1e-20) (:326-346), the volume
    term to K_e (:124-127) and the Dirichlet face terms to K_s (:720-734). */
 int pdgo_grad_logK(const pdgo_problem *p, const double *u, const double *lam, double *g) {
-  if (p->weights != PDGO_WEIGHTS_ON) return PDGO_EARG;
+  /* defined for A = K I with K per cell only */
+  if (p->weights != PDGO_WEIGHTS_ON || p->Acell || pointwise_A(p)) return PDGO_EARG;
   tables T;
   if (tables_init(p, &T)) return PDGO_EARG;
   int d = T.d, nb = T.nb;

@@ -89,6 +89,27 @@ typedef struct pdgo_problem {
      finiteelementmap/qkdg.hh:18): PDGO_LAGRANGE (default), PDGO_LEGENDRE,
      PDGO_LOBATTO */
   int basis;
+  /* Diffusion tensor beyond A = K I (ConvectionDiffusionModelProblem::A,
+     convectiondiffusionparameter.hh:148-157): Acell [ncell][d][d] row-major
+     is A(cell, centre) and replaces K.  With Aq_vol and Aq_face both set,
+     permeabilityIsConstantPerCell() is false and A is taken at every
+     quadrature point (convectiondiffusiondg.hh:141-146, 365-382, 750-761):
+     Aq_vol [ncell][nq^d][d][d] at the volume points, Aq_face
+     [ncell][2d][nq^(d-1)][d][d] at each cell's own points of its faces
+     -x,+x,-y,+y(,-z,+z), in the face-point order of the boundary points. */
+  const double *Acell;
+  const double *Aq_vol;
+  const double *Aq_face;
+  /* reaction c(cell, x) per volume quadrature point [ncell][nq^d] (added to
+     the per-cell c) */
+  const double *cq;
+  /* velocity b(cell, x) per point; both set replaces the Fourier modes.
+     bq_vol [ncell][nq^d][d]; bq_face [face lattice][nq^(d-1)][d], one value
+     per face point shared by both sides (the reference upwinds with b from
+     the inside cell and assumes an H(div) field, :425-426): see
+     pdgo_face_lattice_index for the face numbering. */
+  const double *bq_vol;
+  const double *bq_face;
 } pdgo_problem;
 
 typedef struct pdgo_result {
@@ -134,6 +155,23 @@ int pdgo_jacobian_apply(const pdgo_problem *p, const double *z, double *y);
    the cells sum to the full apply. */
 int pdgo_jacobian_apply_range(const pdgo_problem *p, const double *z, double *y,
                               long e_begin, long e_end);
+/* y += J^T z, matrix-free: the transposed local forms of jacobian_apply
+   over the same one-sided traversal (no reference counterpart; checked
+   against the transposed assembled blocks). */
+int pdgo_jacobian_apply_transpose(const pdgo_problem *p, const double *z, double *y);
+int pdgo_jacobian_apply_transpose_range(const pdgo_problem *p, const double *z, double *y,
+                                        long e_begin, long e_end);
+/* The face lattice of the grid: every face once.  Faces normal to x come
+   first, then y, then z; per direction the planes 0..nc[dir] in order, and
+   in a plane the faces lexicographic over the other directions (x
+   fastest).  Face (dir, cell ix, upper side hi) has index
+   pdgo_face_lattice_index(p, dir, ix[dir] + hi, ix). */
+long pdgo_nface_lattice(const pdgo_problem *p);
+long pdgo_face_lattice_index(const pdgo_problem *p, int dir, int plane, const int *ix);
+/* coordinates of every face-lattice point [faces][nq^(d-1)][dim] and of
+   every cell's own face points [ncell][2d][nq^(d-1)][dim] */
+int pdgo_face_lattice_points(const pdgo_problem *p, double *xyz);
+int pdgo_cell_face_points(const pdgo_problem *p, double *xyz);
 /* GridOperator::residual(x, r): r += R(x)  (gridoperator.hh:176-181) */
 int pdgo_residual(const pdgo_problem *p, const double *x, double *r);
 

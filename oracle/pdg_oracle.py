@@ -33,6 +33,8 @@ class _Problem(C.Structure):
         ("fq", _dp), ("fc", _dp), ("gq", _dp), ("jq", _dp), ("oq", _dp),
         ("nl_deg", C.c_int), ("nl_coef", C.c_double * 5), ("xlin", _dp),
         ("basis", C.c_int),
+        ("Acell", _dp), ("Aq_vol", _dp), ("Aq_face", _dp), ("cq", _dp),
+        ("bq_vol", _dp), ("bq_face", _dp),
     ]
 
 
@@ -123,6 +125,11 @@ def lib():
             "pdgo_jacobian_apply": (C.c_int, [P, _dp, _dp]),
             "pdgo_residual": (C.c_int, [P, _dp, _dp]),
             "pdgo_jacobian_apply_range": (C.c_int, [P, _dp, _dp, C.c_long, C.c_long]),
+            "pdgo_jacobian_apply_transpose": (C.c_int, [P, _dp, _dp]),
+            "pdgo_jacobian_apply_transpose_range": (C.c_int, [P, _dp, _dp, C.c_long, C.c_long]),
+            "pdgo_nface_lattice": (C.c_long, [P]),
+            "pdgo_face_lattice_points": (C.c_int, [P, _dp]),
+            "pdgo_cell_face_points": (C.c_int, [P, _dp]),
             "pdgo_assemble_jacobian": (C.c_int, [P, _dp]),
             "pdgo_blocks_apply": (C.c_int, [P, _dp, _dp, _dp]),
             "pdgo_blocks_apply_transpose": (C.c_int, [P, _dp, _dp, _dp]),
@@ -271,6 +278,37 @@ class Problem:
         y = np.zeros(self.ndof) if y is None else y
         _check(lib().pdgo_jacobian_apply(self.ref, _ptr(z), _ptr(y)))
         return y
+
+    def jacobian_apply_transpose(self, z, y=None):
+        """y += J^T z, matrix-free (the transposed local forms)."""
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        y = np.zeros(self.ndof) if y is None else y
+        _check(lib().pdgo_jacobian_apply_transpose(self.ref, _ptr(z), _ptr(y)))
+        return y
+
+    def jacobian_apply_transpose_range(self, z, y, e_begin, e_end):
+        _check(lib().pdgo_jacobian_apply_transpose_range(self.ref, _ptr(z), _ptr(y), e_begin,
+                                                         e_end))
+        return y
+
+    @property
+    def nq_face(self):
+        return (self.k + 1) ** (self.dim - 1)
+
+    def nface_lattice(self):
+        return lib().pdgo_nface_lattice(self.ref)
+
+    def face_lattice_points(self):
+        """[faces][nq_face][dim]: every face once (x-normal faces, then y, z)."""
+        out = np.zeros((self.nface_lattice(), self.nq_face, self.dim))
+        _check(lib().pdgo_face_lattice_points(self.ref, _ptr(out)))
+        return out
+
+    def cell_face_points(self):
+        """[ncell][2 dim][nq_face][dim]: each cell's own points of its faces."""
+        out = np.zeros((self.ncell, 2 * self.dim, self.nq_face, self.dim))
+        _check(lib().pdgo_cell_face_points(self.ref, _ptr(out)))
+        return out
 
     def jacobian_apply_range(self, z, y, e_begin, e_end):
         _check(lib().pdgo_jacobian_apply_range(self.ref, _ptr(z), _ptr(y), e_begin, e_end))
@@ -422,3 +460,73 @@ class OracleError(RuntimeError):
 def _check(st):
     if st != 0:
         raise OracleError(f"oracle status {st}")
+
+
+# --------------------------------------------------------------------------
+# full-size applies over all host cores (test and baseline infrastructure)
+# --------------------------------------------------------------------------
+_POOL_STATE = {}
+
+
+def _pool_init(spec, shm_x, ndof):
+    from multiprocessing import shared_memory
+    sx = shared_memory.SharedMemory(name=shm_x)
+    _POOL_STATE.update(P=Problem(**spec), sx=sx,
+                       x=np.ndarray((ndof,), dtype=np.float64, buffer=sx.buf))
+
+
+def _pool_apply(args):
+    from multiprocessing import shared_memory
+    b, e, shm_y, ndof, transpose = args
+    sy = shared_memory.SharedMemory(name=shm_y)
+    y = np.ndarray((ndof,), dtype=np.float64, buffer=sy.buf)
+    y[:] = 0.0
+    P = _POOL_STATE["P"]
+    if transpose:
+        P.jacobian_apply_transpose_range(_POOL_STATE["x"], y, b, e)
+    else:
+        P.jacobian_apply_range(_POOL_STATE["x"], y, b, e)
+    del y
+    sy.close()
+    return 0
+
+
+def parallel_apply(spec, x, transpose=False, workers=None):
+    """J x (or J^T x) of Problem(**spec), the cells split over `workers`
+    spawned processes (default: all host cores, at most 32); the partial
+    results of the cell ranges are summed.  Spawned, so it is safe after
+    CUDA was initialised in the calling process."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    from multiprocessing import shared_memory
+    build()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    ndof = x.size
+    probe = Problem(**spec)
+    ncell = probe.ncell
+    assert probe.ndof == ndof
+    workers = workers or min(32, os.cpu_count() or 1)
+    workers = max(1, min(workers, ncell))
+    sx = shared_memory.SharedMemory(create=True, size=ndof * 8)
+    sys_ = [shared_memory.SharedMemory(create=True, size=ndof * 8) for _ in range(workers)]
+    try:
+        np.ndarray((ndof,), dtype=np.float64, buffer=sx.buf)[:] = x
+        bounds = np.linspace(0, ncell, workers + 1).astype(int)
+        jobs = [(int(bounds[i]), int(bounds[i + 1]), sys_[i].name, ndof, bool(transpose))
+                for i in range(workers)]
+        # a process pool executor raises BrokenProcessPool when a worker
+        # dies, where multiprocessing.Pool would wait for it forever
+        with cf.ProcessPoolExecutor(workers, mp_context=mp.get_context("spawn"),
+                                    initializer=_pool_init,
+                                    initargs=(spec, sx.name, ndof)) as pool:
+            list(pool.map(_pool_apply, jobs))
+        y = np.zeros(ndof)
+        for s in sys_:
+            y += np.ndarray((ndof,), dtype=np.float64, buffer=s.buf)
+        return y
+    finally:
+        sx.close()
+        sx.unlink()
+        for s in sys_:
+            s.close()
+            s.unlink()

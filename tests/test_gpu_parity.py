@@ -56,6 +56,35 @@ def test_jacobian_apply_f64(pdg, oracle, dim, k, n):
     assert _rel(y, yref) <= TOL64
 
 
+@pytest.mark.parametrize("dim,k,n,conv", [(2, 2, 5, False), (3, 2, 3, False), (3, 3, 3, True)])
+def test_on_the_fly_operator_apply_and_applyscaleadd(pdg, oracle, dim, k, n, conv):
+    """OnTheFlyOperator (seqistlsolverbackend.hh:66-90): apply(x, y) sets
+    y = J x; applyscaleadd(alpha, x, y) adds alpha J x to y (the reference's
+    temp = J x; y += alpha temp)."""
+    go, P, rng = _pair(pdg, oracle, dim, k, n, seed=40 + dim * k, react=conv)
+    if conv:
+        m = pdg.fourier_velocity_modes(4)
+        go.set_velocity_modes(m)
+        P.set_modes(m)
+    op = pdg.OnTheFlyOperator(go)
+    x = rng.uniform(-1, 1, go.ndof)
+    Jx = P.jacobian_apply(x)
+    y = rng.uniform(-1, 1, go.ndof)
+    op.apply(x, y)                                # overwrites y
+    assert _rel(y, Jx) <= TOL64
+    for alpha in (-0.7, 2.5):
+        y0 = rng.uniform(-1, 1, go.ndof)
+        y = y0.copy()
+        op.applyscaleadd(alpha, x, y)
+        ref = y0 + alpha * Jx
+        assert float(np.max(np.abs(y - ref))) <= TOL64 * float(np.max(np.abs(alpha * Jx)))
+    # the transposed apply of the convection operator against the oracle's
+    # matrix-free transpose
+    yt = np.zeros(go.ndof)
+    go.jacobian_apply_transpose(x, yt)
+    assert _rel(yt, P.jacobian_apply_transpose(x)) <= TOL64
+
+
 @pytest.mark.parametrize("method", [0, 1, 2])
 @pytest.mark.parametrize("weights", [0, 1])
 def test_methods_and_weights(pdg, oracle, method, weights):
@@ -230,6 +259,33 @@ def test_matrix_free_linear_solve(pdg, oracle, solver):
     xyz, w, val = P.eval_points(u, 6)
     ce = (0.5 - xyz[..., 0]) ** 2 + (0.5 - xyz[..., 1]) ** 2
     assert np.sum(w * (val - np.exp(-ce)) ** 2) < 1e-6
+
+
+def test_c1_sin_source_solve(pdg, oracle):
+    """The 2D Q1 64^2 workload: K = 1, alpha = 3, homogeneous Dirichlet,
+    f = sin(2 pi x) sin(2 pi y) + eps_cell with eps_cell i.i.d. normal of
+    variance 0.01 (standard deviation 0.1, the N(mu, sigma^2) reading),
+    CG + cell-block Jacobi to 1e-10: iterations within one of the oracle's
+    CG and the solutions within 1e-8."""
+    import bench
+    go, fq = bench.c1_problem(pdg, np, 0)
+    P = oracle.Problem(2, 1, (64, 64), alpha=3.0, fq=fq)
+    uref, rres, st = P.solve(solver="cg", op=0, reduction=1e-10)
+    assert st == 0 and rres.converged
+    ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG, preconditioner=pdg.PREC_BJ_FDM)
+    u = np.zeros(go.ndof)
+    slp = pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10)
+    slp.apply()
+    res = slp.result()
+    assert res.converged
+    assert abs(res.iterations - rres.iterations) <= 1, (res.iterations, rres.iterations)
+    assert _rel(u, uref) <= 1e-8
+    # the true FP64 defect of the GPU solution
+    r, r0 = np.zeros(go.ndof), np.zeros(go.ndof)
+    go.residual(u, r)
+    go.residual(np.zeros(go.ndof), r0)
+    assert np.linalg.norm(r) <= 1.01e-10 * np.linalg.norm(r0)
+    go.close()
 
 
 def test_solve_3d_cg_fp64_and_mixed(pdg, oracle):

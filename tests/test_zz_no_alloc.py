@@ -63,3 +63,21 @@ def test_dot_noalloc_rejects_oversize(pdg):
                              r.data_ptr(), None)
     assert st == pdg.PDG_EINVAL
     assert b"PDG_DOT_NOALLOC_MAX_N" in lib.pdg_last_error()
+
+
+def test_dot_noalloc_empty_and_host_pointers(pdg):
+    import numpy as np
+    import torch
+    lib = pdg.load()
+    a = torch.ones(4, dtype=torch.float64, device="cuda")
+    r = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+    # n = 0: the sum over nothing is zero, written over the NaN
+    st = lib.pdg_dot_noalloc(ctypes.c_long(0), a.data_ptr(), a.data_ptr(), r.data_ptr(), None)
+    assert st == pdg.PDG_OK, lib.pdg_last_error()
+    torch.cuda.synchronize()
+    assert r.item() == 0.0
+    # host memory is refused before anything runs
+    h = np.ones(4)
+    st = lib.pdg_dot_noalloc(ctypes.c_long(4), h.ctypes.data, a.data_ptr(), r.data_ptr(), None)
+    assert st == pdg.PDG_EINVAL
+    assert b"device pointers" in lib.pdg_last_error()
