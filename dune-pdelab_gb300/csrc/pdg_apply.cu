@@ -598,6 +598,12 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
                  const T *tab) {
   if (ctx->basis == PDG_BASIS_LEGENDRE && !ctx->leg_nodal)
     return launch_apply_modal<T>(ctx, a, K, c, tab);
+  if (general_coefficients(ctx)) {
+    // tensor or per-point coefficients: the Gauss-point operator
+    PDG_TRY(launch_apply_general<T>(ctx, a));
+    if (convection_on(ctx)) PDG_TRY(launch_convection<T>(ctx, a));
+    return nl_apply<T>(ctx, a);
+  }
   OpParams<T> p = make_params<T>(ctx, K, c, tab);
   if constexpr (std::is_same<T, float>::value) {
     // the staged kernels (plane per thread) win for N <= 4: Q1, Q2 (78 vs
@@ -606,7 +612,7 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
     if (ctx->dim == 3 && ctx->N <= 4 && !a.cells && a.ncells == 0 && K == ctx->K32) {
       PDG_TRY(ensure_record32(ctx));
       PDG_TRY(launch_apply32_3d(ctx, a, p, ctx->rec32));
-      if (ctx->vel.nmodes > 0) PDG_TRY(launch_convection<T>(ctx, a));
+      if (convection_on(ctx)) PDG_TRY(launch_convection<T>(ctx, a));
       return nl_apply<T>(ctx, a);
     }
   }
@@ -633,7 +639,7 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
     case 34: st = launch_apply_dn<T, 3, 5>(ctx, a, p, rec); break;
     default: return set_error(PDG_EUNSUPPORTED, "dim/degree not compiled in");
   }
-  if (st == PDG_OK && ctx->vel.nmodes > 0) st = launch_convection<T>(ctx, a);
+  if (st == PDG_OK && convection_on(ctx)) st = launch_convection<T>(ctx, a);
   if (st == PDG_OK) st = nl_apply<T>(ctx, a);
   return st;
 }

@@ -148,6 +148,19 @@ struct pdg_context {
   int rec_valid;
   float *rec32;        // the same records rounded to FP32 (3D FP32 operator)
   int rec32_valid;
+  // parameter fields beyond A = K I (pdg_set_permeability_tensor / _points,
+  // pdg_set_reaction_points): the diffusion and reaction terms then run in
+  // the Gauss-point operator (pdg_general.cu).  gen_A: 0 = scalar K per cell,
+  // 1 = tensor per cell Ac [ncell][d*d], 2 = tensor per point Aqv
+  // [ncell][nqv][d*d] and Aqf [ncell][2d][nqf][d*d]; cq [ncell][nqv] a
+  // per-point reaction added to c.
+  int gen_A;
+  double *Ac64, *Aqv64, *Aqf64, *cq64;
+  float *Ac32, *Aqv32, *Aqf32, *cq32;
+  // velocity from point data (pdg_set_velocity_points) instead of Fourier
+  // modes: volume points [ncell][nqv][3], face lattice [faces][nqf][3]
+  int vel_points;
+  double *bqv64, *bqf64;
   double *conv64;      // per-cell weighted velocity at volume and face points (FP64)
   float *conv32;       // the same in FP32
   double *convtab64;   // B and D (basis values / derivatives at Gauss points)
@@ -310,6 +323,21 @@ int jacobian_rowptr(const pdg_context *ctx, long *rowptr, long *colind);
 int matrix_apply(pdg_context *ctx, const double *x, double *y, const double *add, double alpha,
                  int accumulate, int transpose, const int *skip);
 int matrix_export(pdg_context *ctx, const long *rowptr_dev, double *values_dev);
+
+// parameter fields beyond A = K I: true when the Gauss-point operator replaces
+// the Kronecker kernels; its launch (diffusion and reaction terms only)
+bool general_coefficients(const pdg_context *ctx);
+template <typename T>
+int launch_apply_general(pdg_context *ctx, const ApplyArgs<T> &a);
+// R(0)'s Dirichlet-data diffusion terms with the tensor (added to ctx->r0)
+int launch_rhs_general(pdg_context *ctx);
+// the face lattice (every face once: x-normal faces, then y, then z; planes
+// in order, faces in a plane lexicographic over the other directions)
+long face_lattice_count(const pdg_context *ctx);
+// true when convection terms are present (Fourier modes or point data)
+inline bool convection_on(const pdg_context *ctx) {
+  return ctx->vel.nmodes > 0 || ctx->vel_points;
+}
 
 // convection (3D): set-up of the per-cell velocity records, and the launch
 // that adds alpha * C x (or C^T x) to y after the diffusion operator
