@@ -318,7 +318,8 @@ struct KrylovOut {
 // (no convection, nonlinear term, modal basis or assembled matrix) and the
 // FDM block Jacobi.
 static bool cg_fusable(const pdg_context *ctx) {
-  return ctx->dim == 3 && ctx->N <= 4 && ctx->vel.nmodes == 0 && ctx->nl_deg == 0 &&
+  return ctx->dim == 3 && ctx->N <= 4 && !convection_on(ctx) && ctx->nl_deg == 0 &&
+         !general_coefficients(ctx) &&
          ctx->basis != PDG_BASIS_LEGENDRE && !ctx->use_matrix &&
          ctx->prec[PDG_F32].ready && ctx->prec[PDG_F32].kind == PDG_PREC_BJ_FDM;
 }
@@ -772,6 +773,30 @@ __global__ void k_perm(long n, const double *__restrict__ src, int is_log,
   K32[i] = (float)v;
 }
 
+// an FP64 upload and its FP32 copy (src null frees both)
+static int upload_dual(pdg_context *ctx, double **d64, float **d32, const double *src, size_t n) {
+  PDG_TRY(upload(ctx, d64, src, n));
+  if (!src) {
+    if (*d32) cudaFree(*d32);
+    *d32 = nullptr;
+    return PDG_OK;
+  }
+  if (!*d32) PDG_CUDA_TRY(cudaMalloc(d32, sizeof(float) * n));
+  PDG_TRY(vec_to_f32(ctx, (long)n, *d64, *d32));
+  PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return PDG_OK;
+}
+
+// drop the tensor fields (per cell and per point)
+static void free_tensors(pdg_context *ctx) {
+  double **d[] = {&ctx->Ac64, &ctx->Aqv64, &ctx->Aqf64};
+  float **f[] = {&ctx->Ac32, &ctx->Aqv32, &ctx->Aqf32};
+  for (double **p : d)
+    if (*p) { cudaFree(*p); *p = nullptr; }
+  for (float **p : f)
+    if (*p) { cudaFree(*p); *p = nullptr; }
+}
+
 static void invalidate(pdg_context *ctx, bool operator_changed) {
   ctx->r0_valid = 0;
   if (operator_changed) {
@@ -1000,7 +1025,8 @@ int pdg_destroy(pdg_context *c) {
                   c->A64, c->rec32, c->nlW64, c->nlW32, c->nlB64, c->nlB32,
                   c->massW, c->massWi, c->massB, c->massBiT, c->cstage64, c->cstage32,
                   c->leg64, c->leg32, c->legw64[0], c->legw64[1], c->legw32[0], c->legw32[1],
-                  c->fuse_part, c->fuse_cnt};
+                  c->fuse_part, c->fuse_cnt, c->Ac64, c->Aqv64, c->Aqf64, c->cq64, c->Ac32,
+                  c->Aqv32, c->Aqf32, c->cq32, c->bqv64, c->bqf64};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 10; i++)
@@ -1100,7 +1126,138 @@ int pdg_set_permeability(pdg_context *ctx, const double *K, int is_log) {
   PDG_CUDA_TRY(cudaGetLastError());
   PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   cudaFree(tmp);
+  // A = K I: a tensor set before is dropped
+  free_tensors(ctx);
+  ctx->gen_A = 0;
   invalidate(ctx, true);
+  return PDG_OK;
+}
+
+int pdg_set_permeability_tensor(pdg_context *ctx, const double *A) {
+  PDG_CHECK_CTX(ctx);
+  if (!A) {
+    if (ctx->gen_A == 1) {
+      free_tensors(ctx);
+      ctx->gen_A = 0;
+      invalidate(ctx, true);
+    }
+    return PDG_OK;
+  }
+  free_tensors(ctx);
+  PDG_TRY(upload_dual(ctx, &ctx->Ac64, &ctx->Ac32, A, (size_t)ctx->ncell * ctx->dim * ctx->dim));
+  ctx->gen_A = 1;
+  invalidate(ctx, true);
+  return PDG_OK;
+}
+
+int pdg_set_permeability_points(pdg_context *ctx, const double *Avol, const double *Aface) {
+  PDG_CHECK_CTX(ctx);
+  if (!Avol != !Aface)
+    return set_error(PDG_EINVAL, "give both the volume and the face tensors, or neither");
+  if (!Avol) {
+    if (ctx->gen_A == 2) {
+      free_tensors(ctx);
+      ctx->gen_A = 0;
+      invalidate(ctx, true);
+    }
+    return PDG_OK;
+  }
+  free_tensors(ctx);
+  const size_t dd = (size_t)ctx->dim * ctx->dim;
+  PDG_TRY(upload_dual(ctx, &ctx->Aqv64, &ctx->Aqv32, Avol, (size_t)ctx->ncell * ctx->nqv * dd));
+  PDG_TRY(upload_dual(ctx, &ctx->Aqf64, &ctx->Aqf32, Aface,
+                      (size_t)ctx->ncell * 2 * ctx->dim * ctx->nqf * dd));
+  ctx->gen_A = 2;
+  invalidate(ctx, true);
+  return PDG_OK;
+}
+
+int pdg_set_reaction_points(pdg_context *ctx, const double *cq) {
+  PDG_CHECK_CTX(ctx);
+  PDG_TRY(upload_dual(ctx, &ctx->cq64, &ctx->cq32, cq, (size_t)ctx->ncell * ctx->nqv));
+  invalidate(ctx, true);
+  return PDG_OK;
+}
+
+int pdg_set_velocity_points(pdg_context *ctx, const double *bvol, const double *bface) {
+  PDG_CHECK_CTX(ctx);
+  if (!bvol != !bface)
+    return set_error(PDG_EINVAL, "give both the volume and the face velocities, or neither");
+  if (bvol && ctx->dim != 3)
+    return set_error(PDG_EUNSUPPORTED, "convection is implemented for 3D grids");
+  if (!bvol) {
+    if (ctx->vel_points) {
+      PDG_TRY(upload(ctx, &ctx->bqv64, nullptr, 0));
+      PDG_TRY(upload(ctx, &ctx->bqf64, nullptr, 0));
+      ctx->vel_points = 0;
+      invalidate(ctx, true);
+    }
+    return PDG_OK;
+  }
+  PDG_TRY(upload(ctx, &ctx->bqv64, bvol, (size_t)ctx->ncell * ctx->nqv * 3));
+  PDG_TRY(upload(ctx, &ctx->bqf64, bface, (size_t)face_lattice_count(ctx) * ctx->nqf * 3));
+  ctx->vel.nmodes = 0;
+  ctx->vel_points = 1;
+  invalidate(ctx, true);
+  const int st = conv_setup(ctx);
+  if (st != PDG_OK) ctx->vel_points = 0;
+  return st;
+}
+
+int pdg_face_lattice_size(const pdg_context *ctx, long *nfaces) {
+  if (!ctx || !nfaces) return set_error(PDG_EINVAL, "null argument");
+  *nfaces = face_lattice_count(ctx);
+  return PDG_OK;
+}
+
+int pdg_face_lattice_points(const pdg_context *ctx, double *xyz) {
+  if (!ctx || !xyz) return set_error(PDG_EINVAL, "null argument");
+  const RhsTables t = make_rhs_tables(ctx);
+  const int d = ctx->dim, N = ctx->N;
+  int nc[3] = {ctx->cfg.cells[0], ctx->cfg.cells[1], d == 3 ? ctx->cfg.cells[2] : 1};
+  for (int dir = 0; dir < d; dir++) {
+    int od[2] = {0, 0}, no = 0;
+    for (int j = 0; j < d; j++)
+      if (j != dir) od[no++] = j;
+    int ix[3] = {0, 0, 0};
+    for (int pl = 0; pl <= nc[dir]; pl++)
+      for (int b = 0; b < (no > 1 ? nc[od[1]] : 1); b++)
+        for (int a = 0; a < nc[od[0]]; a++) {
+          ix[od[0]] = a;
+          if (no > 1) ix[od[1]] = b;
+          const long fi = face_lattice_index(nc, d, dir, pl, ix);
+          for (int q = 0; q < ctx->nqf; q++) {
+            double *pt = xyz + (fi * ctx->nqf + q) * d;
+            pt[dir] = pl * ctx->h[dir];
+            pt[od[0]] = (a + t.x[q % N]) * ctx->h[od[0]];
+            if (no > 1) pt[od[1]] = (b + t.x[q / N]) * ctx->h[od[1]];
+          }
+        }
+  }
+  return PDG_OK;
+}
+
+int pdg_cell_face_points(const pdg_context *ctx, double *xyz) {
+  if (!ctx || !xyz) return set_error(PDG_EINVAL, "null argument");
+  const RhsTables t = make_rhs_tables(ctx);
+  const int d = ctx->dim, N = ctx->N;
+  for (long e = 0; e < ctx->ncell; e++) {
+    int ix[3];
+    long r = e;
+    for (int j = 0; j < d; j++) { ix[j] = (int)(r % ctx->cfg.cells[j]); r /= ctx->cfg.cells[j]; }
+    for (int f = 0; f < 2 * d; f++) {
+      const int dir = f >> 1, hi = f & 1;
+      int od[2] = {0, 0}, no = 0;
+      for (int j = 0; j < d; j++)
+        if (j != dir) od[no++] = j;
+      for (int q = 0; q < ctx->nqf; q++) {
+        double *pt = xyz + ((e * 2 * d + f) * ctx->nqf + q) * d;
+        pt[dir] = (ix[dir] + hi) * ctx->h[dir];
+        pt[od[0]] = (ix[od[0]] + t.x[q % N]) * ctx->h[od[0]];
+        if (no > 1) pt[od[1]] = (ix[od[1]] + t.x[q / N]) * ctx->h[od[1]];
+      }
+    }
+  }
   return PDG_OK;
 }
 
@@ -1126,6 +1283,12 @@ int pdg_set_velocity_modes(pdg_context *ctx, int nmodes, const double *modes) {
   if (nmodes > 0 && ctx->dim != 3)
     return set_error(PDG_EUNSUPPORTED, "convection is implemented for 3D grids");
   ctx->vel.nmodes = nmodes;
+  if (nmodes > 0 && ctx->vel_points) {
+    // modes replace velocity point data
+    PDG_TRY(upload(ctx, &ctx->bqv64, nullptr, 0));
+    PDG_TRY(upload(ctx, &ctx->bqf64, nullptr, 0));
+    ctx->vel_points = 0;
+  }
   for (int m = 0; m < nmodes; m++)
     for (int j = 0; j < 7; j++) ctx->vel.m[m][j] = modes[7 * m + j];
   invalidate(ctx, true);
@@ -1970,9 +2133,10 @@ int pdg_adjoint_solve(pdg_context *ctx, const pdg_solver_options *opt, const dou
   else
     PDG_CUDA_TRY(cudaMemcpyAsync(r, rhs, sizeof(double) * ctx->ndof, cudaMemcpyHostToDevice,
                                  ctx->stream));
-  // SIPG diffusion-reaction is symmetric (J^T = J); NIPG/IIPG and upwind
-  // convection are not
-  const int transpose = (ctx->cfg.method == PDG_SIPG && ctx->vel.nmodes == 0) ? 0 : 1;
+  // SIPG diffusion-reaction with a scalar K is symmetric (J^T = J); NIPG/IIPG,
+  // upwind convection and general tensors (which need not be symmetric) are not
+  const int transpose =
+      (ctx->cfg.method == PDG_SIPG && !convection_on(ctx) && ctx->gen_A == 0) ? 0 : 1;
   pdg_solver_options o = *opt;
   if (transpose && (o.preconditioner & PDG_PREC_BLOCK_MASK) == PDG_PREC_BJ_FDM)
     o.preconditioner = (o.preconditioner & ~PDG_PREC_BLOCK_MASK) | PDG_PREC_BJ_DENSE;
@@ -1987,6 +2151,8 @@ int pdg_grad_logK(pdg_context *ctx, const double *u, const double *lambda, doubl
   if (!u || !lambda || !g) return set_error(PDG_EINVAL, "null argument");
   if (ctx->cfg.weights != PDG_WEIGHTS_ON)
     return set_error(PDG_EUNSUPPORTED, "log-K gradient needs weightsOn");
+  if (ctx->gen_A != 0)
+    return set_error(PDG_EUNSUPPORTED, "log-K gradient needs A = K I per cell (no tensor)");
   PDG_TRY(ensure_r0(ctx));
   PDG_TRY(ensure_stage(ctx));
   Staged<double> su, sl;

@@ -111,6 +111,55 @@ __global__ void k_conv_setup(const OpParams<double> p, const Velocity vel, const
   }
 }
 
+// The same record from velocity point data (pdg_set_velocity_points): b at
+// the volume points [ncell][N^3][3] and at the face-lattice points
+// [faces][N^2][3], one value per face point for both sides (the reference
+// upwinds with b of the inside cell and assumes an H(div) field,
+// convectiondiffusiondg.hh:425-426).
+template <int N>
+__global__ void k_conv_setup_points(const OpParams<double> p, const RhsTables tb,
+                                    const double *__restrict__ bqv, const double *__restrict__ bqf,
+                                    double *__restrict__ rec64, float *__restrict__ rec32,
+                                    int *__restrict__ bad) {
+  using C = CCfg<N>;
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.ncell) return;
+  int ix[3];
+  {
+    long r = e;
+    ix[0] = (int)(r % p.nc[0]); r /= p.nc[0];
+    ix[1] = (int)(r % p.nc[1]); r /= p.nc[1];
+    ix[2] = (int)r;
+  }
+  const double detJ = p.h[0] * p.h[1] * p.h[2];
+  double *r64 = rec64 + e * (C::VREC + C::FREC);
+  float *r32 = rec32 + e * (C::VREC + C::FREC);
+  for (int q = 0; q < C::NB; q++) {
+    const int qa[3] = {q % N, (q / N) % N, q / (N * N)};
+    const double w = tb.w[qa[0]] * tb.w[qa[1]] * tb.w[qa[2]] * detJ;
+    for (int d = 0; d < 3; d++) {
+      const double g = bqv[(e * C::NB + q) * 3 + d] * w / p.h[d];
+      r64[d * C::NB + q] = g;
+      r32[d * C::NB + q] = (float)g;
+    }
+  }
+  for (int f = 0; f < 6; f++) {
+    const int dir = f >> 1, hi = f & 1;
+    const double area = detJ / p.h[dir];
+    const double sgn = hi ? 1.0 : -1.0;
+    const bool bnd = hi ? ix[dir] == p.nc[dir] - 1 : ix[dir] == 0;
+    const long fi = face_lattice_index(p.nc, 3, dir, ix[dir] + hi, ix);
+    for (int q = 0; q < C::N2; q++) {
+      const int qt[2] = {q % N, q / N};
+      const double w = area * tb.w[qt[0]] * tb.w[qt[1]];
+      const double bn = sgn * bqf[(fi * C::N2 + q) * 3 + dir];
+      if (bnd && p.bc[f] == PDG_BC_OUTFLOW && bn < -1e-30) atomicExch(bad, 1);
+      r64[C::VREC + f * C::N2 + q] = bn * w;
+      r32[C::VREC + f * C::N2 + q] = (float)(bn * w);
+    }
+  }
+}
+
 template <typename T, int N>
 __global__ void __launch_bounds__(CCfg<N>::THREADS)
     k_conv(const OpParams<T> p, const ApplyArgs<T> a, const T *__restrict__ vrec,
@@ -463,8 +512,12 @@ static int conv_setup_n(pdg_context *ctx) {
   PDG_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
   OpParams<double> p = make_params<double>(ctx, ctx->K64, ctx->c64, ctx->tab64);
   RhsTables tb = make_rhs_tables(ctx);
-  k_conv_setup<N><<<(unsigned)((ctx->ncell + 127) / 128), 128, 0, ctx->stream>>>(
-      p, ctx->vel, tb, ctx->conv64, ctx->conv32, bad);
+  if (ctx->vel_points)
+    k_conv_setup_points<N><<<(unsigned)((ctx->ncell + 127) / 128), 128, 0, ctx->stream>>>(
+        p, tb, ctx->bqv64, ctx->bqf64, ctx->conv64, ctx->conv32, bad);
+  else
+    k_conv_setup<N><<<(unsigned)((ctx->ncell + 127) / 128), 128, 0, ctx->stream>>>(
+        p, ctx->vel, tb, ctx->conv64, ctx->conv32, bad);
   PDG_CUDA_TRY(cudaGetLastError());
   int hbad = 0;
   PDG_CUDA_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

@@ -605,6 +605,126 @@ static int launch_gp_dn(pdg_context *ctx, const ApplyArgs<T> &a, const OpParams<
   return PDG_OK;
 }
 
+// R(0)'s Dirichlet-data diffusion terms with a tensor A (residual_boundary_
+// integral with u = 0, :851-877): r_i += w [-pen g psi_i - theta g
+// (A_s n).grad psi_i], pen from delta = (A_s n).n at the point (per point
+// when A is) or per cell.  One thread per cell, dense loops (once per solve).
+template <int D, int N>
+__global__ void k_rhs_gp(const OpParams<double> p, const GenCoef<double> g, const GpTab<double, N> tb,
+                         const double *__restrict__ gq, double *__restrict__ r0) {
+  using C = GCfg<D, N>;
+  constexpr int NB = C::NB, NQF = C::NQF, DD = C::DD;
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.ncell) return;
+  int ix[3];
+  {
+    long r = e;
+    ix[0] = (int)(r % p.nc[0]); r /= p.nc[0];
+    ix[1] = (int)(r % p.nc[1]); r /= p.nc[1];
+    ix[2] = (int)r;
+  }
+  for (int f = 0; f < 2 * D; f++) {
+    const int dir = f >> 1, hi = f & 1;
+    const bool bnd = hi ? ix[dir] == p.nc[dir] - 1 : ix[dir] == 0;
+    if (!bnd || p.bc[f] != PDG_BC_DIRICHLET) continue;
+    int od[2] = {0, 0};
+    {
+      int c = 0;
+      for (int j = 0; j < D; j++)
+        if (j != dir) od[c++] = j;
+    }
+    // boundary points: sides in order, faces lexicographic over the other
+    // directions, NQF points per face
+    long base = 0;
+    for (int sd = 0; sd < f; sd++) {
+      long cnt = 1;
+      for (int j = 0; j < D; j++)
+        if (j != (sd >> 1)) cnt *= p.nc[j];
+      base += cnt * NQF;
+    }
+    long fidx = 0;
+    for (int j = D - 1; j >= 0; j--) {
+      if (j == dir) continue;
+      fidx = fidx * p.nc[j] + ix[j];
+    }
+    base += fidx * NQF;
+    const double sgn = hi ? 1.0 : -1.0;
+    double area = 1.0;
+    for (int j = 0; j < D; j++)
+      if (j != dir) area *= p.h[j];
+    for (int q = 0; q < NQF; q++) {
+      const double gv = gq[base + q];
+      if (gv == 0.0) continue;
+      const int qt[2] = {q % N, D == 3 ? q / N : 0};
+      double A[DD];
+      cell_tensor<double, D, N>(p, g, e, f, q, A);
+      double An[3];
+      for (int j = 0; j < D; j++) An[j] = A[j * D + dir] * sgn;
+      const double harm = p.weights == PDG_WEIGHTS_ON ? A[dir * D + dir] : 1.0;
+      const double pen = p.pen_fac / p.h[dir] * harm;
+      double w = area * tb.w[qt[0]] * (D == 3 ? tb.w[qt[1]] : 1.0);
+      for (int i = 0; i < NB; i++) {
+        const int ia[3] = {i % N, (i / N) % N, i / (N * N)};
+        // value and reference derivatives of psi_i at the point
+        double tv[2], td[2];
+        for (int t = 0; t < D - 1; t++) {
+          tv[t] = tb.B[qt[t] * N + ia[od[t]]];
+          td[t] = tb.D[qt[t] * N + ia[od[t]]];
+        }
+        const double vn = tb.v[hi][ia[dir]], dn = tb.d[hi][ia[dir]];
+        double tang = 1.0;
+        for (int t = 0; t < D - 1; t++) tang *= tv[t];
+        const double psi = vn * tang;
+        double agrad = An[dir] * dn / p.h[dir] * tang;
+        for (int t = 0; t < D - 1; t++) {
+          double gt = vn * td[t] / p.h[od[t]];
+          for (int s2 = 0; s2 < D - 1; s2++)
+            if (s2 != t) gt *= tv[s2];
+          agrad += An[od[t]] * gt;
+        }
+        r0[e * NB + i] += w * (-pen * gv * psi - p.theta * gv * agrad);
+      }
+    }
+  }
+}
+
+long face_lattice_count(const pdg_context *ctx) {
+  long n = 0;
+  for (int dir = 0; dir < ctx->dim; dir++) {
+    long c = ctx->cfg.cells[dir] + 1;
+    for (int j = 0; j < ctx->dim; j++)
+      if (j != dir) c *= ctx->cfg.cells[j];
+    n += c;
+  }
+  return n;
+}
+
+int launch_rhs_general(pdg_context *ctx) {
+  if (!ctx->gq || !ctx->gen_A) return PDG_OK;
+  OpParams<double> p = make_params<double>(ctx, ctx->K64, ctx->c64, ctx->tab64);
+  GenCoef<double> g{};
+  if (ctx->gen_A == 1) g.Ac = ctx->Ac64;
+  if (ctx->gen_A == 2) { g.Aqv = ctx->Aqv64; g.Aqf = ctx->Aqf64; }
+  const unsigned blocks = (unsigned)((ctx->ncell + 127) / 128);
+#define PDG_RGP(D, N)                                                            \
+  k_rhs_gp<D, N><<<blocks, 128, 0, ctx->stream>>>(p, g, make_gp_tab<double, N>(ctx), ctx->gq, \
+                                                  ctx->r0)
+  switch (ctx->dim * 10 + ctx->k) {
+    case 21: PDG_RGP(2, 2); break;
+    case 22: PDG_RGP(2, 3); break;
+    case 23: PDG_RGP(2, 4); break;
+    case 24: PDG_RGP(2, 5); break;
+    case 31: PDG_RGP(3, 2); break;
+    case 32: PDG_RGP(3, 3); break;
+    case 33: PDG_RGP(3, 4); break;
+    case 34: PDG_RGP(3, 5); break;
+    default: return set_error(PDG_EUNSUPPORTED, "dim/degree not compiled in");
+  }
+#undef PDG_RGP
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+
 bool general_coefficients(const pdg_context *ctx) {
   return ctx->gen_A != 0 || ctx->cq64 != nullptr;
 }

@@ -324,6 +324,29 @@ int matrix_apply(pdg_context *ctx, const double *x, double *y, const double *add
                  int accumulate, int transpose, const int *skip);
 int matrix_export(pdg_context *ctx, const long *rowptr_dev, double *values_dev);
 
+// Index of the face normal to `dir` in plane `plane` (0..nc[dir]) whose other
+// coordinates are those of ix, on the face lattice: faces normal to x first,
+// then y, then z; planes in order; faces of a plane lexicographic over the
+// other directions, x fastest.
+__host__ __device__ inline long face_lattice_index(const int *nc, int dim, int dir, int plane,
+                                                   const int *ix) {
+  long off = 0;
+  for (int j = 0; j < dir; j++) {
+    long n = nc[j] + 1;
+    for (int m = 0; m < dim; m++)
+      if (m != j) n *= nc[m];
+    off += n;
+  }
+  long inplane = 1, idx = 0;
+  for (int m = 0; m < dim; m++)
+    if (m != dir) inplane *= nc[m];
+  for (int j = dim - 1; j >= 0; j--) {
+    if (j == dir) continue;
+    idx = idx * nc[j] + ix[j];
+  }
+  return off + (long)plane * inplane + idx;
+}
+
 // parameter fields beyond A = K I: true when the Gauss-point operator replaces
 // the Kronecker kernels; its launch (diffusion and reaction terms only)
 bool general_coefficients(const pdg_context *ctx);

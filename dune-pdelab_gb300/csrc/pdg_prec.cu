@@ -926,6 +926,10 @@ int prec_setup_impl(pdg_context *ctx, int kind, int precision) {
     if (ctx->cfg.method != PDG_SIPG)
       return set_error(PDG_EUNSUPPORTED,
                        "FDM block Jacobi needs symmetric blocks (SIPG); use PDG_PREC_BJ_DENSE");
+    if (general_coefficients(ctx))
+      return set_error(PDG_EUNSUPPORTED,
+                       "FDM block Jacobi needs separable blocks (A = K I per cell, c per cell); "
+                       "use PDG_PREC_BJ_DENSE with a tensor or per-point coefficients");
     PDG_TRY(fdm_setup(ctx, precision));
   } else if (base == PDG_PREC_BJ_DENSE) {
     PDG_TRY(dense_setup(ctx, precision));

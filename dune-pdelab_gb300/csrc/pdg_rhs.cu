@@ -44,7 +44,7 @@ __global__ void k_rhs(const OpParams<double> p, const RhsTables tb, const Veloci
                       const double *__restrict__ fq, const double *__restrict__ fc,
                       const double *__restrict__ gq, const double *__restrict__ jq,
                       const double *__restrict__ oq, double *__restrict__ r0,
-                      double *__restrict__ r0K) {
+                      double *__restrict__ r0K, int skipK, const double *__restrict__ bqf) {
   constexpr int NB = D == 3 ? N * N * N : N * N;
   constexpr int NQF = D == 3 ? N * N : N;
   const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -127,15 +127,22 @@ __global__ void k_rhs(const OpParams<double> p, const RhsTables tb, const Veloci
       } else {
         const double g = gq ? gq[base + q] : 0.0;
         double bn = 0.0;
-        if (vel.nmodes > 0) {
+        if (bqf) {
+          // velocity given at the face-lattice points
+          const long fi = face_lattice_index(p.nc, D, dir, ix[dir] + hi, ix);
+          bn = sgn * bqf[(fi * NQF + q) * 3 + dir];
+        } else if (vel.nmodes > 0) {
           double xg[3], b[3];
           for (int j = 0; j < D; j++) xg[j] = (ix[j] + loc[j]) * p.h[j];
           velocity_at(vel, D, xg, b);
           bn = sgn * b[dir];
         }
         if (bn < 0.0) cv += g * bn;
-        cdK = -p.theta * Ke * g;
-        cvK = -pen * g;
+        if (!skipK) {
+          // with a tensor A these terms come from launch_rhs_general
+          cdK = -p.theta * Ke * g;
+          cvK = -pen * g;
+        }
       }
       for (int i = 0; i < NB; i++) {
         int ia[3] = {i % N, (i / N) % N, i / (N * N)};
@@ -360,10 +367,12 @@ int launch_rhs(pdg_context *ctx) {
   const unsigned blocks = (unsigned)((ctx->ncell + 127) / 128);
 #define PDG_RHS(D, N)                                                                       \
   k_rhs<D, N><<<blocks, 128, 0, ctx->stream>>>(p, tb, ctx->vel, ctx->fq, ctx->fc, ctx->gq, \
-                                               ctx->jq, ctx->oq, ctx->r0, r0K)
+                                               ctx->jq, ctx->oq, ctx->r0, r0K, ctx->gen_A != 0, \
+                                               ctx->vel_points ? ctx->bqf64 : nullptr)
   PDG_DISPATCH_DN(ctx, PDG_RHS);
 #undef PDG_RHS
   PDG_CUDA_TRY(cudaGetLastError());
+  if (ctx->gen_A) PDG_TRY(launch_rhs_general(ctx));
   return PDG_OK;
 }
 

@@ -174,6 +174,13 @@ _SIGS = {
     "pdg_jacobian_pattern": (C.c_int, [_vp, C.POINTER(C.c_long)]),
     "pdg_jacobian_export": (C.c_int, [_vp, _vp, _vp, _vp]),
     "pdg_matrix_apply": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_set_permeability_tensor": (C.c_int, [_vp, _vp]),
+    "pdg_set_permeability_points": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_set_reaction_points": (C.c_int, [_vp, _vp]),
+    "pdg_set_velocity_points": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_face_lattice_size": (C.c_int, [_vp, C.POINTER(C.c_long)]),
+    "pdg_face_lattice_points": (C.c_int, [_vp, _vp]),
+    "pdg_cell_face_points": (C.c_int, [_vp, _vp]),
 }
 
 _lib = None
@@ -359,11 +366,58 @@ class GridOperator:
         _check(load().pdg_boundary_points(self._h, out.ctypes.data))
         return out
 
+    @property
+    def nq_face(self):
+        return (self.degree + 1) ** (self.dim - 1)
+
+    def face_lattice_size(self):
+        n = C.c_long()
+        _check(load().pdg_face_lattice_size(self._h, C.byref(n)))
+        return n.value
+
+    def face_lattice_points(self):
+        """[faces][nq_face][dim]: every face once (x-normal faces, then y, z)."""
+        out = np.zeros((self.face_lattice_size(), self.nq_face, self.dim))
+        _check(load().pdg_face_lattice_points(self._h, out.ctypes.data))
+        return out
+
+    def cell_face_points(self):
+        """[ncell][2 dim][nq_face][dim]: each cell's own points of its faces."""
+        out = np.zeros((self.ncell, 2 * self.dim, self.nq_face, self.dim))
+        _check(load().pdg_cell_face_points(self._h, out.ctypes.data))
+        return out
+
     # -- parameters -------------------------------------------------------
     @_stream_ordered
     def set_permeability(self, K, is_log=False):
         K = np.ascontiguousarray(K, dtype=np.float64) if isinstance(K, (list, np.ndarray)) else K
         _check(load().pdg_set_permeability(self._h, _ptr(K), int(is_log)))
+
+    def set_permeability_tensor(self, A):
+        """A(cell) as a dim x dim tensor per cell ([ncell][dim][dim]); None
+        returns to A = K I."""
+        A = None if A is None else np.ascontiguousarray(A, dtype=np.float64)
+        _check(load().pdg_set_permeability_tensor(self._h, _ptr(A)))
+
+    def set_permeability_points(self, Avol, Aface):
+        """A per quadrature point: [ncell][nq_volume][dim][dim] and
+        [ncell][2 dim][nq_face][dim][dim] (permeabilityIsConstantPerCell()
+        false); both None return to A = K I."""
+        Av = None if Avol is None else np.ascontiguousarray(Avol, dtype=np.float64)
+        Af = None if Aface is None else np.ascontiguousarray(Aface, dtype=np.float64)
+        _check(load().pdg_set_permeability_points(self._h, _ptr(Av), _ptr(Af)))
+
+    def set_reaction_points(self, cq):
+        """c per volume quadrature point [ncell][nq_volume], added to the per-cell c."""
+        cq = None if cq is None else np.ascontiguousarray(cq, dtype=np.float64)
+        _check(load().pdg_set_reaction_points(self._h, _ptr(cq)))
+
+    def set_velocity_points(self, bvol, bface):
+        """b at the volume points [ncell][nq_volume][3] and at the face-lattice
+        points [faces][nq_face][3] (3D); both None remove the velocity."""
+        bv = None if bvol is None else np.ascontiguousarray(bvol, dtype=np.float64)
+        bf = None if bface is None else np.ascontiguousarray(bface, dtype=np.float64)
+        _check(load().pdg_set_velocity_points(self._h, _ptr(bv), _ptr(bf)))
 
     def set_reaction(self, c):
         c = None if c is None else np.ascontiguousarray(c, dtype=np.float64)

@@ -233,7 +233,8 @@ int pdg_boundary_points(const pdg_context *ctx, double *xyz);
 /* parameter.hh:134-209; permeabilityIsConstantPerCell() == true)     */
 /* ---------------------------------------------------------------- */
 
-/* A(cell) = K_e I per cell; is_log != 0 means the array holds log K. */
+/* A(cell) = K_e I per cell; is_log != 0 means the array holds log K.  Drops
+   a tensor of pdg_set_permeability_tensor / _points. */
 int pdg_set_permeability(pdg_context *ctx, const double *K, int is_log);
 /* c(cell) per cell (NULL = 0) */
 int pdg_set_reaction(pdg_context *ctx, const double *c);
@@ -248,6 +249,52 @@ int pdg_set_source(pdg_context *ctx, const double *fq, const double *fc);
    Neumann j, outflow o (convectiondiffusiondg.hh:770-879). */
 int pdg_set_boundary_data(pdg_context *ctx, const double *g, const double *j,
                           const double *o);
+
+/* Parameter fields beyond A = K I, as ConvectionDiffusionDG evaluates them
+   (convectiondiffusionparameter.hh:143-183: A(cell, x) a d x d tensor,
+   b(cell, x), c(cell, x) per point).  With any of these set the diffusion
+   and reaction terms are evaluated at the operator's Gauss points (order
+   2k) instead of in Kronecker form; the FDM block Jacobi (which needs
+   separable blocks) and the log-K gradient are then unavailable
+   (PDG_EUNSUPPORTED): use PDG_PREC_BJ_DENSE or PDG_PREC_BJ_ITERATIVE.
+   pdg_set_permeability drops a tensor set before. */
+
+/* A(cell) per cell [ncell][dim][dim], row-major (A[i][j] multiplies
+   d u/d x_j in row i), taken at the cell centre as the reference does
+   (convectiondiffusiondg.hh:124-127, 305-309, 710-713).  NULL returns to
+   A = K I. */
+int pdg_set_permeability_tensor(pdg_context *ctx, const double *A);
+/* permeabilityIsConstantPerCell() == false: A at every volume quadrature
+   point [ncell][(k+1)^d][dim][dim] (order of pdg_volume_points) and at
+   every cell's own points of its 2d faces [ncell][2d][(k+1)^(d-1)][dim][dim]
+   (sides -x,+x,-y,+y,-z,+z; points of pdg_cell_face_points), where
+   alpha_volume, alpha_skeleton and the boundary integral re-evaluate it
+   (convectiondiffusiondg.hh:141-146, 365-382, 750-761); weights and
+   penalty are then formed per point.  Both NULL returns to A = K I. */
+int pdg_set_permeability_points(pdg_context *ctx, const double *Avol, const double *Aface);
+/* c(cell, x) at the volume quadrature points [ncell][(k+1)^d], added to the
+   per-cell c of pdg_set_reaction (convectiondiffusiondg.hh:181).  NULL
+   removes it. */
+int pdg_set_reaction_points(pdg_context *ctx, const double *cq);
+/* b(cell, x) at the volume quadrature points [ncell][(k+1)^3][3] and at
+   the face-lattice points [nfaces][(k+1)^2][3] (pdg_face_lattice_points):
+   one value per face point serves both sides, as the reference upwinds
+   with the inside cell's b and assumes an H(div) field
+   (convectiondiffusiondg.hh:425-426, 796-797).  Replaces Fourier modes;
+   3D.  Both NULL removes the velocity. */
+int pdg_set_velocity_points(pdg_context *ctx, const double *bvol, const double *bface);
+/* The face lattice: every face of the grid once.  Faces normal to x come
+   first, then y, then z; per direction the planes 0..cells[dir] in order;
+   in a plane the faces are lexicographic over the other directions (x
+   fastest); (k+1)^(d-1) points per face, lexicographic over the other
+   directions.  No reference counterpart (the reference calls b(cell, x)
+   at these points). */
+int pdg_face_lattice_size(const pdg_context *ctx, long *nfaces);
+/* coordinates of the face-lattice points [nfaces][(k+1)^(d-1)][dim] and of
+   every cell's own face points [ncell][2d][(k+1)^(d-1)][dim] (host
+   outputs), for evaluating b and A where the operator integrates them */
+int pdg_face_lattice_points(const pdg_context *ctx, double *xyz);
+int pdg_cell_face_points(const pdg_context *ctx, double *xyz);
 
 /* ---------------------------------------------------------------- */
 /* operator (GridOperator, gridoperator/gridoperator.hh:176-205)      */
