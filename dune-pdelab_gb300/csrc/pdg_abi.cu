@@ -789,8 +789,8 @@ static int upload_dual(pdg_context *ctx, double **d64, float **d32, const double
 
 // drop the tensor fields (per cell and per point)
 static void free_tensors(pdg_context *ctx) {
-  double **d[] = {&ctx->Ac64, &ctx->Aqv64, &ctx->Aqf64};
-  float **f[] = {&ctx->Ac32, &ctx->Aqv32, &ctx->Aqf32};
+  double **d[] = {&ctx->Ac64, &ctx->Aqv64, &ctx->Aqf64, &ctx->Kd64};
+  float **f[] = {&ctx->Ac32, &ctx->Aqv32, &ctx->Aqf32, &ctx->Kd32};
   for (double **p : d)
     if (*p) { cudaFree(*p); *p = nullptr; }
   for (float **p : f)
@@ -1026,7 +1026,7 @@ int pdg_destroy(pdg_context *c) {
                   c->massW, c->massWi, c->massB, c->massBiT, c->cstage64, c->cstage32,
                   c->leg64, c->leg32, c->legw64[0], c->legw64[1], c->legw32[0], c->legw32[1],
                   c->fuse_part, c->fuse_cnt, c->Ac64, c->Aqv64, c->Aqf64, c->cq64, c->Ac32,
-                  c->Aqv32, c->Aqf32, c->cq32, c->bqv64, c->bqf64};
+                  c->Aqv32, c->Aqf32, c->cq32, c->bqv64, c->bqf64, c->Kd64, c->Kd32};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 10; i++)
@@ -1136,7 +1136,7 @@ int pdg_set_permeability(pdg_context *ctx, const double *K, int is_log) {
 int pdg_set_permeability_tensor(pdg_context *ctx, const double *A) {
   PDG_CHECK_CTX(ctx);
   if (!A) {
-    if (ctx->gen_A == 1) {
+    if (ctx->gen_A == 1 || ctx->gen_A == 3) {
       free_tensors(ctx);
       ctx->gen_A = 0;
       invalidate(ctx, true);
@@ -1144,8 +1144,27 @@ int pdg_set_permeability_tensor(pdg_context *ctx, const double *A) {
     return PDG_OK;
   }
   free_tensors(ctx);
-  PDG_TRY(upload_dual(ctx, &ctx->Ac64, &ctx->Ac32, A, (size_t)ctx->ncell * ctx->dim * ctx->dim));
-  ctx->gen_A = 1;
+  const int d = ctx->dim;
+  const size_t n = (size_t)ctx->ncell * d * d;
+  PDG_TRY(upload_dual(ctx, &ctx->Ac64, &ctx->Ac32, A, n));
+  // a diagonal tensor keeps the operator separable: K per direction in the
+  // Kronecker records (and the FDM block Jacobi stays exact)
+  std::vector<double> h(n);
+  PDG_CUDA_TRY(cudaMemcpy(h.data(), ctx->Ac64, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  bool diag = true;
+  for (long e = 0; e < ctx->ncell && diag; e++)
+    for (int i = 0; i < d; i++)
+      for (int j = 0; j < d; j++)
+        if (i != j && h[(size_t)e * d * d + i * d + j] != 0.0) diag = false;
+  if (diag) {
+    std::vector<double> kd((size_t)ctx->ncell * 3, 1.0);
+    for (long e = 0; e < ctx->ncell; e++)
+      for (int i = 0; i < d; i++) kd[(size_t)e * 3 + i] = h[(size_t)e * d * d + i * d + i];
+    PDG_TRY(upload_dual(ctx, &ctx->Kd64, &ctx->Kd32, kd.data(), kd.size()));
+    ctx->gen_A = 3;
+  } else {
+    ctx->gen_A = 1;
+  }
   invalidate(ctx, true);
   return PDG_OK;
 }

@@ -127,7 +127,6 @@ __global__ void k_cell_record(const OpParams<double> p, T *__restrict__ rec) {
   int ix[3];
   cell_coords(p, (unsigned)e, ix);
   const long stride[3] = {1, (long)p.nc[0], (long)p.nc[0] * p.nc[1]};
-  const double Ke = p.K[e];
   const double cc = p.c ? p.c[e] : 0.0;
   double raw[3 * 2 * D];
 #pragma unroll
@@ -136,7 +135,7 @@ __global__ void k_cell_record(const OpParams<double> p, T *__restrict__ rec) {
     long nb;
     if (f & 1) nb = ix[dir] + 1 < p.nc[dir] ? e + stride[dir] : -1;
     else nb = ix[dir] > 0 ? e - stride[dir] : -1;
-    face_coefficients(p, f, Ke, nb, raw + 3 * f);
+    face_coefficients(p, f, kdir(p, e, dir), nb, raw + 3 * f);
   }
   T *r = rec + e * (face_vectors<T, D>() ? C::RECW : C::REC);
 #pragma unroll
@@ -145,7 +144,8 @@ __global__ void k_cell_record(const OpParams<double> p, T *__restrict__ rec) {
     for (int i = 0; i < N; i++)
       for (int a = 0; a < N; a++)
         r[dir * N * N + i * N + a] =
-            (T)(hp * a_entry<double, N>(p, dir, i, a, Ke, cc, raw, tM, tS, td0, td1));
+            (T)(hp * a_entry<double, N>(p, dir, i, a, kdir(p, e, dir), cc, raw, tM, tS, td0,
+                                        td1));
   }
 #pragma unroll
   for (int f = 0; f < 2 * D; f++) {
@@ -246,11 +246,10 @@ __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
 #pragma unroll
   for (int z = 0; z < N; z++) ue[z * TPC + l] = col[z];
   if (!rec) {
-    const T Ke = p.K[ee];
 #pragma unroll
     for (int f = 0; f < NF; f++)
       if (f % TPC == l) {
-        face_coefficients(p, f, Ke, nbr[f], raw + 3 * f);
+        face_coefficients(p, f, kdir(p, ee, f >> 1), nbr[f], raw + 3 * f);
         scale_face<T, D>(p, f, raw + 3 * f, c5 + 5 * f);
       }
     __syncthreads();
@@ -259,15 +258,17 @@ __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
       const int i = l / N, aa = l % N;
 #pragma unroll
       for (int dir = 0; dir < D; dir++)
-        Am[dir * N2 + l] =
-            hperp<T, D>(p, dir) * a_entry<T, N>(p, dir, i, aa, Ke, cc, raw, tM, tS, td0, td1);
+        Am[dir * N2 + l] = hperp<T, D>(p, dir) *
+                           a_entry<T, N>(p, dir, i, aa, kdir(p, ee, dir), cc, raw, tM, tS, td0,
+                                         td1);
     } else {
 #pragma unroll
       for (int dir = 0; dir < D; dir++)
 #pragma unroll
         for (int aa = 0; aa < N; aa++)
           Am[dir * N2 + l * N + aa] =
-              hperp<T, D>(p, dir) * a_entry<T, N>(p, dir, l, aa, Ke, cc, raw, tM, tS, td0, td1);
+              hperp<T, D>(p, dir) *
+              a_entry<T, N>(p, dir, l, aa, kdir(p, ee, dir), cc, raw, tM, tS, td0, td1);
     }
   }
   __syncthreads();
@@ -474,6 +475,9 @@ OpParams<T> make_params(const pdg_context *ctx, const T *K, const T *c, const T 
   p.weights = ctx->cfg.weights;
   for (int j = 0; j < 6; j++) p.bc[j] = ctx->cfg.bctype[j];
   p.K = K;
+  p.Kd = nullptr;
+  if (ctx->gen_A == 3)
+    p.Kd = std::is_same<T, double>::value ? (const T *)ctx->Kd64 : (const T *)ctx->Kd32;
   p.c = c;
   p.tab = tab;
   return p;

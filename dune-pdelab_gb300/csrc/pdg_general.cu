@@ -700,7 +700,7 @@ long face_lattice_count(const pdg_context *ctx) {
 }
 
 int launch_rhs_general(pdg_context *ctx) {
-  if (!ctx->gq || !ctx->gen_A) return PDG_OK;
+  if (!ctx->gq || !(ctx->gen_A == 1 || ctx->gen_A == 2)) return PDG_OK;
   OpParams<double> p = make_params<double>(ctx, ctx->K64, ctx->c64, ctx->tab64);
   GenCoef<double> g{};
   if (ctx->gen_A == 1) g.Ac = ctx->Ac64;
@@ -726,7 +726,8 @@ int launch_rhs_general(pdg_context *ctx) {
 }
 
 bool general_coefficients(const pdg_context *ctx) {
-  return ctx->gen_A != 0 || ctx->cq64 != nullptr;
+  // a diagonal tensor per cell (gen_A 3) stays in Kronecker form
+  return ctx->gen_A == 1 || ctx->gen_A == 2 || ctx->cq64 != nullptr;
 }
 
 template <typename T>
@@ -737,7 +738,7 @@ int launch_apply_general(pdg_context *ctx, const ApplyArgs<T> &a) {
   const T *tab = dbl ? (const T *)ctx->tab64 : (const T *)ctx->tab32;
   OpParams<T> p = make_params<T>(ctx, K, c, tab);
   GenCoef<T> g{};
-  if (ctx->gen_A == 1) g.Ac = dbl ? (const T *)ctx->Ac64 : (const T *)ctx->Ac32;
+  if (ctx->gen_A == 1 || ctx->gen_A == 3) g.Ac = dbl ? (const T *)ctx->Ac64 : (const T *)ctx->Ac32;
   if (ctx->gen_A == 2) {
     g.Aqv = dbl ? (const T *)ctx->Aqv64 : (const T *)ctx->Aqv32;
     g.Aqf = dbl ? (const T *)ctx->Aqf64 : (const T *)ctx->Aqf32;

@@ -78,6 +78,7 @@ struct OpParams {
   int weights;    // PDG_WEIGHTS_ON / OFF
   int bc[6];
   const T *K;     // per cell
+  const T *Kd;    // diagonal tensor per cell [ncell][3] (K per direction), or null
   const T *c;     // per cell or nullptr
   const T *tab;   // 1D tables: Mhat[N*N], Shat[N*N], d0[N], d1[N]
 };
@@ -154,9 +155,12 @@ struct pdg_context {
   // 1 = tensor per cell Ac [ncell][d*d], 2 = tensor per point Aqv
   // [ncell][nqv][d*d] and Aqf [ncell][2d][nqf][d*d]; cq [ncell][nqv] a
   // per-point reaction added to c.
+  // gen_A = 3: a diagonal tensor per cell, kept in Kronecker form with K per
+  // direction Kd [ncell][3] (the records, the FDM block Jacobi and R(0) take
+  // K_dir for the terms of direction dir; no Gauss-point operator)
   int gen_A;
-  double *Ac64, *Aqv64, *Aqf64, *cq64;
-  float *Ac32, *Aqv32, *Aqf32, *cq32;
+  double *Ac64, *Aqv64, *Aqf64, *cq64, *Kd64;
+  float *Ac32, *Aqv32, *Aqf32, *cq32, *Kd32;
   // velocity from point data (pdg_set_velocity_points) instead of Fourier
   // modes: volume points [ncell][nqv][3], face lattice [faces][nqf][3]
   int vel_points;

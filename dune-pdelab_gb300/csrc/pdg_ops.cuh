@@ -18,6 +18,16 @@ __device__ __forceinline__ T over_h(const OpParams<T> &p, int dir, T x) {
   return x * p.inv_h[dir];
 }
 
+// K of cell e for the terms of direction dir: with a diagonal tensor per
+// cell A = diag(K_x, K_y, K_z), (A n).n = K_dir on a face normal to dir and
+// the volume term of direction dir is K_dir d_dir u d_dir psi
+// (convectiondiffusiondg.hh:124-127, 318-338)
+template <typename T>
+__device__ __forceinline__ T kdir(const OpParams<T> &p, long e, int dir) {
+  return p.Kd ? p.Kd[3 * e + dir] : p.K[e];
+}
+
+// Ke: K of this cell in the face's normal direction (kdir)
 template <typename T>
 __device__ __forceinline__ void face_coefficients(const OpParams<T> &p, int f, T Ke,
                                                   long nb, T *coef) {
@@ -25,7 +35,7 @@ __device__ __forceinline__ void face_coefficients(const OpParams<T> &p, int f, T
   const int dir = f >> 1;
   T kap_e = T(0), kap_o = T(0), pen = T(0);
   if (nb >= 0) {
-    const T Ko = p.K[nb];
+    const T Ko = kdir(p, nb, dir);
     if (p.weights == PDG_WEIGHTS_ON) {
       // convectiondiffusiondg.hh:326-332: delta = (A n).n = K
       const T S = Ke + Ko + T(1e-20);

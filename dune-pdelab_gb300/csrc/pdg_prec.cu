@@ -51,7 +51,7 @@ __global__ void k_fdm_setup(const OpParams<double> p, int dim, const double *__r
     ix[2] = (int)r;
   }
   const long stride[3] = {1, (long)p.nc[0], (long)p.nc[0] * p.nc[1]};
-  const double Ke = p.K[e];
+  const double Ke = kdir(p, e, dir);
   const double cc = p.c ? p.c[e] : 0.0;
   double cf[18];
   for (int f = 2 * dir; f < 2 * dir + 2; f++) {

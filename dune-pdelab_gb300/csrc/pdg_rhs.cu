@@ -79,11 +79,11 @@ __global__ void k_rhs(const OpParams<double> p, const RhsTables tb, const Veloci
     }
   }
   // boundary faces
-  const double Ke = p.K[e];
   for (int f = 0; f < 2 * D; f++) {
     const int dir = f >> 1, hi = f & 1;
     const bool bnd = hi ? ix[dir] == p.nc[dir] - 1 : ix[dir] == 0;
     if (!bnd) continue;
+    const double Ke = kdir(p, e, dir);   // (A n).n on this face
     const int bc = p.bc[f];
     if (bc == PDG_BC_NONE) continue;
     // boundary point base index: sides in order, faces lexicographic over the
@@ -367,12 +367,13 @@ int launch_rhs(pdg_context *ctx) {
   const unsigned blocks = (unsigned)((ctx->ncell + 127) / 128);
 #define PDG_RHS(D, N)                                                                       \
   k_rhs<D, N><<<blocks, 128, 0, ctx->stream>>>(p, tb, ctx->vel, ctx->fq, ctx->fc, ctx->gq, \
-                                               ctx->jq, ctx->oq, ctx->r0, r0K, ctx->gen_A != 0, \
+                                               ctx->jq, ctx->oq, ctx->r0, r0K,                   \
+                                               ctx->gen_A == 1 || ctx->gen_A == 2,       \
                                                ctx->vel_points ? ctx->bqf64 : nullptr)
   PDG_DISPATCH_DN(ctx, PDG_RHS);
 #undef PDG_RHS
   PDG_CUDA_TRY(cudaGetLastError());
-  if (ctx->gen_A) PDG_TRY(launch_rhs_general(ctx));
+  PDG_TRY(launch_rhs_general(ctx));
   return PDG_OK;
 }
 

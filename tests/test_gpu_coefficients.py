@@ -225,3 +225,35 @@ def test_scalar_permeability_drops_tensor(pdg, oracle):
     _check_apply(go, P, rng)
     pdg.GridOperatorPreconditioner(go, kind=pdg.PREC_BJ_FDM).pre()   # separable again
     go.close()
+
+
+def test_diagonal_tensor_keeps_fdm_and_mixed_solve(pdg, oracle):
+    """A diagonal tensor per cell stays separable (K per direction in the
+    Kronecker records): the FDM block Jacobi is exact for it, and the FP64 and
+    mixed-precision CG solves match the oracle's CG."""
+    go, P, rng = _pair(pdg, oracle, 3, 3, 4, seed=90)
+    A = _spd(rng, go.ncell, 3, full=False)
+    go.set_permeability_tensor(A)
+    go.set_source(fc=np.ones(go.ncell))
+    P.set(Acell=A, fc=np.ones(go.ncell))
+    # the FDM block inverse against the oracle's LU of the diagonal blocks
+    prec = pdg.GridOperatorPreconditioner(go, kind=pdg.PREC_BJ_FDM)
+    prec.pre()
+    d = rng.uniform(-1, 1, go.ndof)
+    v = np.zeros(go.ndof)
+    prec.apply(v, d)
+    lu, piv = P.lu(P.block_diagonal())
+    assert _rel(v, P.lu_apply(lu, piv, d)) <= 1e-10
+    uref, rres, st = P.solve(solver="cg", op=0, reduction=1e-10)
+    assert st == 0 and rres.converged
+    for mixed in (False, True):
+        ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG, preconditioner=pdg.PREC_BJ_FDM,
+                                                 mixed=mixed)
+        u = np.zeros(go.ndof)
+        slp = pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10)
+        slp.apply()
+        assert slp.result().converged
+        if not mixed:
+            assert abs(slp.result().iterations - rres.iterations) <= 1
+        assert _rel(u, uref) <= 1e-8
+    go.close()
