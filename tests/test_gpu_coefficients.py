@@ -72,10 +72,13 @@ def test_full_tensor_per_cell(pdg, oracle, dim, k, n):
     go.set_permeability_tensor(A)
     P.set(Acell=A)
     x = _check_apply(go, P, rng)
-    # FP32 operator (the inner operator of mixed-precision solves)
-    y32 = np.zeros(go.ndof, dtype=np.float32)
-    go.jacobian_apply_f32(x.astype(np.float32), y32)
-    assert _rel(y32.astype(np.float64), P.jacobian_apply(x)) <= TOL32
+    # FP32 operator (the inner operator of mixed-precision solves; device
+    # vectors only)
+    import torch
+    x32 = torch.tensor(x, dtype=torch.float32, device="cuda")
+    y32 = torch.zeros(go.ndof, dtype=torch.float32, device="cuda")
+    go.jacobian_apply_f32(x32, y32)
+    assert _rel(y32.double().cpu().numpy(), P.jacobian_apply(x)) <= TOL32
     go.close()
 
 
