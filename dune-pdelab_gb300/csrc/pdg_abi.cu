@@ -802,6 +802,7 @@ static void invalidate(pdg_context *ctx, bool operator_changed) {
   if (operator_changed) {
     ctx->op_gen++;
     ctx->rec_valid = 0;
+    ctx->recfp_valid = 0;
     ctx->rec32_valid = 0;
     ctx->A_valid = 0;
     ctx->prec[0].ready = 0;
@@ -1026,7 +1027,8 @@ int pdg_destroy(pdg_context *c) {
                   c->massW, c->massWi, c->massB, c->massBiT, c->cstage64, c->cstage32,
                   c->leg64, c->leg32, c->legw64[0], c->legw64[1], c->legw32[0], c->legw32[1],
                   c->fuse_part, c->fuse_cnt, c->Ac64, c->Aqv64, c->Aqf64, c->cq64, c->Ac32,
-                  c->Aqv32, c->Aqf32, c->cq32, c->bqv64, c->bqf64, c->Kd64, c->Kd32};
+                  c->Aqv32, c->Aqf32, c->cq32, c->bqv64, c->bqf64, c->Kd64, c->Kd32,
+                  c->recfp, c->tabfp};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 10; i++)
@@ -1221,6 +1223,17 @@ int pdg_set_velocity_points(pdg_context *ctx, const double *bvol, const double *
   const int st = conv_setup(ctx);
   if (st != PDG_OK) ctx->vel_points = 0;
   return st;
+}
+
+int pdg_set_f64_arithmetic(pdg_context *ctx, int mode) {
+  PDG_CHECK_CTX(ctx);
+  if (mode != PDG_F64_NATIVE && mode != PDG_F64_FLOAT_PAIR)
+    return set_error(PDG_EINVAL, "mode must be PDG_F64_NATIVE or PDG_F64_FLOAT_PAIR");
+  if (mode == PDG_F64_FLOAT_PAIR && ctx->dim != 3)
+    return set_error(PDG_EUNSUPPORTED, "float-pair arithmetic is implemented for 3D grids");
+  ctx->f64_pair = mode == PDG_F64_FLOAT_PAIR;
+  ctx->op_gen++;   // cached solver state (block-SOR graphs) follows the operator
+  return PDG_OK;
 }
 
 int pdg_face_lattice_size(const pdg_context *ctx, long *nfaces) {

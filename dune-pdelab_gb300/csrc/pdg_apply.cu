@@ -630,6 +630,14 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
     PDG_TRY(ensure_record32(ctx));
     rec = (const T *)ctx->rec32;
   }
+  if constexpr (std::is_same<T, double>::value) {
+    if (ctx->f64_pair && ctx->dim == 3 && rec) {
+      // FP64 applies in float-pair arithmetic on the FP32 pipe
+      PDG_TRY(launch_apply_float_pair(ctx, a));
+      if (convection_on(ctx)) PDG_TRY(launch_convection<T>(ctx, a));
+      return nl_apply<T>(ctx, a);
+    }
+  }
   const int key = ctx->dim * 10 + ctx->k;
   int st;
   switch (key) {

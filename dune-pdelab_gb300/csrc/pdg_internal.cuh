@@ -161,6 +161,11 @@ struct pdg_context {
   int gen_A;
   double *Ac64, *Aqv64, *Aqf64, *cq64, *Kd64;
   float *Ac32, *Aqv32, *Aqf32, *cq32, *Kd32;
+  // FP64 operator applies in float-pair arithmetic (pdg_set_f64_arithmetic):
+  // float-pair copies of rec64 and of the 1D tables
+  int f64_pair;
+  void *recfp, *tabfp;
+  int recfp_valid;
   // velocity from point data (pdg_set_velocity_points) instead of Fourier
   // modes: volume points [ncell][nqv][3], face lattice [faces][nqf][3]
   int vel_points;
@@ -350,6 +355,10 @@ __host__ __device__ inline long face_lattice_index(const int *nc, int dim, int d
   }
   return off + (long)plane * inplane + idx;
 }
+
+// the 3D FP64 operator in float-pair arithmetic (pdg_apply_fp.cu); rec64 must
+// be valid
+int launch_apply_float_pair(pdg_context *ctx, const ApplyArgs<double> &a);
 
 // parameter fields beyond A = K I: true when the Gauss-point operator replaces
 // the Kronecker kernels; its launch (diffusion and reaction terms only)

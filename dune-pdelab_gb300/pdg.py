@@ -48,6 +48,7 @@ CG, BICGSTAB, GMRES = 0, 1, 2
 PREC_NONE, PREC_BJ_FDM, PREC_BJ_DENSE, PREC_BJ_ITERATIVE = 0, 1, 2, 3
 PREC_SOR = 16          # OR-ed with a block kind: one block-SOR sweep
 F64, F32 = 0, 1
+F64_NATIVE, F64_FLOAT_PAIR = 0, 1          # arithmetic of the FP64 operator applies
 LAGRANGE, LEGENDRE, LOBATTO = 0, 1, 2     # QkDGBasisPolynomial
 
 
@@ -174,6 +175,7 @@ _SIGS = {
     "pdg_jacobian_pattern": (C.c_int, [_vp, C.POINTER(C.c_long)]),
     "pdg_jacobian_export": (C.c_int, [_vp, _vp, _vp, _vp]),
     "pdg_matrix_apply": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_set_f64_arithmetic": (C.c_int, [_vp, C.c_int]),
     "pdg_set_permeability_tensor": (C.c_int, [_vp, _vp]),
     "pdg_set_permeability_points": (C.c_int, [_vp, _vp, _vp]),
     "pdg_set_reaction_points": (C.c_int, [_vp, _vp]),
@@ -392,6 +394,11 @@ class GridOperator:
     def set_permeability(self, K, is_log=False):
         K = np.ascontiguousarray(K, dtype=np.float64) if isinstance(K, (list, np.ndarray)) else K
         _check(load().pdg_set_permeability(self._h, _ptr(K), int(is_log)))
+
+    def set_f64_arithmetic(self, mode):
+        """F64_NATIVE or F64_FLOAT_PAIR (the 3D operator's FP64 applies on the
+        FP32 pipe in float pairs)."""
+        _check(load().pdg_set_f64_arithmetic(self._h, int(mode)))
 
     def set_permeability_tensor(self, A):
         """A(cell) as a dim x dim tensor per cell ([ncell][dim][dim]); None

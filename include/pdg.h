@@ -318,6 +318,16 @@ int pdg_apply(pdg_context *ctx, const double *x, double *y);
    (seqistlsolverbackend.hh:78-90), without the full-vector temporary */
 int pdg_applyscaleadd(pdg_context *ctx, double alpha, const double *x, double *y);
 
+/* Arithmetic of the FP64 operator applies.  No reference counterpart (the
+   reference computes in RF = double).  PDG_F64_FLOAT_PAIR carries every FP64
+   value of the 3D operator kernel (scalar or diagonal-tensor K per cell) as
+   an unevaluated sum of two floats and runs the multiply-adds on the FP32
+   pipe (exact two-product and two-sum, 48 significant bits): results agree
+   with PDG_F64_NATIVE to about 1e-14 relative; every other kernel (convection,
+   tensor fields, preconditioners, vector updates) stays FP64.  3D only. */
+enum { PDG_F64_NATIVE = 0, PDG_F64_FLOAT_PAIR = 1 };
+int pdg_set_f64_arithmetic(pdg_context *ctx, int mode);
+
 /* ---------------------------------------------------------------- */
 /* preconditioner (GridOperatorPreconditioner over                    */
 /* AssembledBlockJacobiPreconditionerLocalOperator,                   */
