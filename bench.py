@@ -772,6 +772,25 @@ def c3_metrics(pdg, np, torch, stream, inner_reduction=1e-4):
     out["speedup_mixed_vs_fp64"] = out["fp64_s"] / out["mixed_s"]
     out["mixed_vs_fp64_rel_l2"] = float(torch.linalg.norm(e) / torch.linalg.norm(sols["fp64"]))
     out["mixed_vs_fp64_rel_max"] = float(e.abs().max() / sols["fp64"].abs().max())
+    # the FP64 solve again with the operator applies in float-pair arithmetic
+    # (a separately labelled mode; the FP64 baseline above stays native)
+    go.set_f64_arithmetic(pdg.F64_FLOAT_PAIR)
+    try:
+        ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG, maxiter=20000)
+        u = torch.zeros(go.ndof, dtype=torch.float64, device=stream.device)
+        slp = pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        slp.apply()
+        dt = time.perf_counter() - t0
+    finally:
+        go.set_f64_arithmetic(pdg.F64_NATIVE)
+    e = u - sols["fp64"]
+    out["fp64_float_pair_s"] = dt
+    out["fp64_float_pair_iterations"] = slp.result().iterations
+    out["fp64_float_pair_converged"] = bool(slp.result().converged)
+    out["fp64_float_pair_vs_fp64_rel_l2"] = float(torch.linalg.norm(e) /
+                                                  torch.linalg.norm(sols["fp64"]))
     go.close()
     return out
 
