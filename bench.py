@@ -234,13 +234,17 @@ def measured_peaks():
         return {}
 
 
-def profile_traffic(key):
-    """DRAM bytes per launch from the committed ncu summary, if present."""
+def profile_traffic(key, what=None):
+    """DRAM bytes per launch from the committed ncu summary, if present
+    (what="captured": when and from which capture)."""
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            return json.load(f).get(key)
+            d = json.load(f)
     except (OSError, ValueError):
         return None
+    if what == "captured":
+        return d.get("_captured", {}).get(key)
+    return d.get(key)
 
 
 def cpu_baseline_port(np, wl=WORKLOAD, applies=2):
@@ -464,6 +468,7 @@ def run_gb300(args, world, rank, local):
         "bound": "fp32" if f32 else "fp64", "achieved": achieved, "peak": pk,
         "unit": "TFLOP/s", "frac": achieved / pk if pk else None,
         "traffic": profile_traffic(wname),
+        "traffic_source": profile_traffic(wname, "captured"),
         "peak_source": "measured in this run: FMA throughput microbenchmark of the CUDA "
                        "cores (libpdg_probe.so); MEASURED_PEAKS.json has no FP64/FP32 "
                        "CUDA-core figure",
@@ -519,6 +524,12 @@ def run_gb300(args, world, rank, local):
         "cpu_baseline": cpu,
     }
     if float_pair:
+        # the same algorithmic flops, on the FP64 pipe's scale
+        float_pair["fp64_equivalent_tflops"] = fl / (float_pair["ms_per_apply"] * 1e-3) / 1e12
+        if peaks["fp64"]:
+            float_pair["fp64_equivalent_over_fp64_peak"] = (
+                float_pair["fp64_equivalent_tflops"] / peaks["fp64"])
+        float_pair["traffic"] = profile_traffic(wname.replace("_apply", "_float_pair_apply"))
         line["f64_float_pair"] = float_pair
     line.update(extras)
     print(json.dumps(line), flush=True)
