@@ -99,6 +99,24 @@ class GridOperator {
   void setPermeability(const std::vector<double> &K, bool is_log = false) {
     check(pdg_set_permeability(ctx_, K.data(), is_log ? 1 : 0));
   }
+  // A(cell, x) beyond K I: a dim x dim tensor per cell (row-major), or per
+  // quadrature point when the parameter class's permeabilityIsConstantPerCell()
+  // is false (convectiondiffusionparameter.hh:143-157)
+  void setPermeabilityTensor(const std::vector<double> &A) {
+    check(pdg_set_permeability_tensor(ctx_, A.data()));
+  }
+  void setPermeabilityPoints(const std::vector<double> &Avol, const std::vector<double> &Aface) {
+    check(pdg_set_permeability_points(ctx_, Avol.data(), Aface.data()));
+  }
+  // c(cell, x) at the volume points, b(cell, x) at the volume and face-lattice points
+  void setReactionPoints(const std::vector<double> &cq) {
+    check(pdg_set_reaction_points(ctx_, cq.data()));
+  }
+  void setVelocityPoints(const std::vector<double> &bvol, const std::vector<double> &bface) {
+    check(pdg_set_velocity_points(ctx_, bvol.data(), bface.data()));
+  }
+  // PDG_F64_NATIVE or PDG_F64_FLOAT_PAIR (no reference counterpart)
+  void setF64Arithmetic(int mode) { check(pdg_set_f64_arithmetic(ctx_, mode)); }
   void setSource(const double *fq, const double *fc) { check(pdg_set_source(ctx_, fq, fc)); }
   void setBoundaryData(const double *g, const double *j = nullptr, const double *o = nullptr) {
     check(pdg_set_boundary_data(ctx_, g, j, o));
