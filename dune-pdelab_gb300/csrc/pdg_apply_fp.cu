@@ -70,6 +70,14 @@ __device__ __forceinline__ void pmac(fpair &acc, fpair a, fpair b) {
   acc.lo += t + c;
 }
 
+// a * b as a pair: the exact product of the leading parts plus the cross
+// terms (the first term of a chain, 4 FP32 operations)
+__device__ __forceinline__ fpair pmul(fpair a, fpair b) {
+  const float p = a.hi * b.hi;
+  const float e = fmaf(a.hi, b.hi, -p);
+  return fpair{p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e))};
+}
+
 // acc += a
 __device__ __forceinline__ void padd(fpair &acc, fpair a) {
   const float s = acc.hi + a.hi;
@@ -102,10 +110,15 @@ struct FpCfg {
   static constexpr int TAB = 2 * N2 + 2 * N;            // Mhat, Shat, d0, d1
   // ue, Xs, Ys, Zs, face data (12 TPC), record part; padding per cell
   static constexpr int PER_CELL = 4 * NB + 12 * TPC + RECU + 1;
+  // blocks per SM the register allocation must allow: 6 for Q2 (at most 86
+  // registers; 0.262 against 0.287 ms per 64^3 apply with the compiler's 96),
+  // the compiler's choice otherwise (Q4 bounded to 6 blocks: 0.416 against
+  // 0.374 ms at 40^3)
+  static constexpr int MINB = N == 3 ? 6 : 1;
 };
 
 template <int N>
-__global__ void __launch_bounds__(FpCfg<N>::THREADS)
+__global__ void __launch_bounds__(FpCfg<N>::THREADS, FpCfg<N>::MINB)
     k_apply_fp(const OpParams<double> p, const ApplyArgs<double> a, const fpair *__restrict__ rec,
                const fpair *__restrict__ tab) {
   using C = FpCfg<N>;
@@ -187,9 +200,13 @@ __global__ void __launch_bounds__(FpCfg<N>::THREADS)
     fpair s1{0.f, 0.f}, s2{0.f, 0.f};
     if (nbr[f] >= 0 && !a.diag_only) {
       const fpair *w = W + f * (N + 1);
+      fpair vf[N];
 #pragma unroll
-      for (int q = 0; q < N; q++) pmac(s1, w[q], split_bits(vd[f][q]));
-      pmac(s2, w[N], split_bits(vd[f][hi ? 0 : N - 1]));
+      for (int q = 0; q < N; q++) vf[q] = split_bits(vd[f][q]);
+      s1 = pmul(w[0], vf[0]);
+#pragma unroll
+      for (int q = 1; q < N; q++) pmac(s1, w[q], vf[q]);
+      s2 = pmul(w[N], vf[hi ? 0 : N - 1]);
     }
     fa[(2 * f) * TPC + l] = norm(s1);
     fa[(2 * f + 1) * TPC + l] = norm(s2);
@@ -215,9 +232,11 @@ __global__ void __launch_bounds__(FpCfg<N>::THREADS)
   fpair X[N], Y[N], Z[N];
 #pragma unroll
   for (int z = 0; z < N; z++) {
-    fpair sx{0.f, 0.f}, sy{0.f, 0.f}, sz{0.f, 0.f};
+    fpair sx = pmul(Arx[0], ue[z * N2 + ty * N]);
+    fpair sy = pmul(Ary[0], ue[z * N2 + tx]);
+    fpair sz = pmul(Aat(2, z, 0), col[0]);
 #pragma unroll
-    for (int q = 0; q < N; q++) {
+    for (int q = 1; q < N; q++) {
       pmac(sx, Arx[q], ue[z * N2 + ty * N + q]);
       pmac(sy, Ary[q], ue[z * N2 + q * N + tx]);
       pmac(sz, Aat(2, z, q), col[q]);
@@ -250,9 +269,11 @@ __global__ void __launch_bounds__(FpCfg<N>::THREADS)
   fpair Wv[N];
 #pragma unroll
   for (int z = 0; z < N; z++) {
-    fpair w{0.f, 0.f}, t1{0.f, 0.f};
+    fpair w = pmul(Mty[0], Xs[z * N2 + tx]);
+    fpair t1 = pmul(Mtx[0], Zs[z * N2 + ty * N]);
+    pmac(w, Mtx[0], Ys[z * N2 + ty * N]);
 #pragma unroll
-    for (int q = 0; q < N; q++) {
+    for (int q = 1; q < N; q++) {
       pmac(w, Mty[q], Xs[z * N2 + q * N + tx]);
       pmac(w, Mtx[q], Ys[z * N2 + ty * N + q]);
       pmac(t1, Mtx[q], Zs[z * N2 + ty * N + q]);
@@ -268,9 +289,10 @@ __global__ void __launch_bounds__(FpCfg<N>::THREADS)
     const bool scale = a.alpha != 1.0;
 #pragma unroll
     for (int z = 0; z < N; z++) {
-      fpair s{0.f, 0.f};
+      fpair s = pmul(tM[z * N], Wv[0]);
+      pmac(s, Mty[0], ue[z * N2 + tx]);
 #pragma unroll
-      for (int q = 0; q < N; q++) {
+      for (int q = 1; q < N; q++) {
         pmac(s, tM[z * N + q], Wv[q]);
         pmac(s, Mty[q], ue[z * N2 + q * N + tx]);
       }
