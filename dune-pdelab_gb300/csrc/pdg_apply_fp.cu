@@ -112,9 +112,9 @@ struct FpCfg {
   static constexpr int PER_CELL = 4 * NB + 12 * TPC + RECU + 1;
   // blocks per SM the register allocation must allow: 6 for Q2 (at most 86
   // registers; 0.262 against 0.287 ms per 64^3 apply with the compiler's 96),
-  // the compiler's choice otherwise (Q4 bounded to 6 blocks: 0.416 against
-  // 0.374 ms at 40^3)
-  static constexpr int MINB = N == 3 ? 6 : 1;
+  // the compiler's choice otherwise (0: no bound; Q4 bounded to 6 blocks:
+  // 0.416 against 0.374 ms at 40^3)
+  static constexpr int MINB = N == 3 ? 6 : 0;
 };
 
 template <int N>
