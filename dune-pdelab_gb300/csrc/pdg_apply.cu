@@ -572,7 +572,12 @@ static int ensure_record(pdg_context *ctx) {
 
 // the FP64 operator's lazily built per-cell records, built now (before
 // launches are spread over several streams)
-int prepare_apply64(pdg_context *ctx) { return ensure_record(ctx); }
+int prepare_apply64(pdg_context *ctx) {
+  PDG_TRY(ensure_record(ctx));
+  if (ctx->f64_pair && ctx->dim == 3 && !general_coefficients(ctx))
+    PDG_TRY(prepare_float_pair(ctx));
+  return PDG_OK;
+}
 
 // Legendre basis: y = acc*y + alpha T^T J_nodal T x + add (pdg_basis.cu)
 template <typename T>

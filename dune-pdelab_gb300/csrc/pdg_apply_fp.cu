@@ -344,13 +344,26 @@ static int ensure_pairs(pdg_context *ctx, long rec_doubles) {
   return PDG_OK;
 }
 
+// the float-pair copies, built on the context stream (before a launch is
+// spread over several streams)
+int prepare_float_pair(pdg_context *ctx) {
+  switch (ctx->N) {
+    case 2: return ensure_pairs(ctx, (long)FpCfg<2>::RECW * ctx->ncell);
+    case 3: return ensure_pairs(ctx, (long)FpCfg<3>::RECW * ctx->ncell);
+    case 4: return ensure_pairs(ctx, (long)FpCfg<4>::RECW * ctx->ncell);
+    case 5: return ensure_pairs(ctx, (long)FpCfg<5>::RECW * ctx->ncell);
+    default: return set_error(PDG_EUNSUPPORTED, "degree not compiled in");
+  }
+}
+
 int launch_apply_float_pair(pdg_context *ctx, const ApplyArgs<double> &a) {
   OpParams<double> p = make_params<double>(ctx, ctx->K64, ctx->c64, ctx->tab64);
+  PDG_TRY(prepare_float_pair(ctx));
   switch (ctx->N) {
-    case 2: PDG_TRY(ensure_pairs(ctx, (long)FpCfg<2>::RECW * ctx->ncell)); return launch_fp_n<2>(ctx, a, p);
-    case 3: PDG_TRY(ensure_pairs(ctx, (long)FpCfg<3>::RECW * ctx->ncell)); return launch_fp_n<3>(ctx, a, p);
-    case 4: PDG_TRY(ensure_pairs(ctx, (long)FpCfg<4>::RECW * ctx->ncell)); return launch_fp_n<4>(ctx, a, p);
-    case 5: PDG_TRY(ensure_pairs(ctx, (long)FpCfg<5>::RECW * ctx->ncell)); return launch_fp_n<5>(ctx, a, p);
+    case 2: return launch_fp_n<2>(ctx, a, p);
+    case 3: return launch_fp_n<3>(ctx, a, p);
+    case 4: return launch_fp_n<4>(ctx, a, p);
+    case 5: return launch_fp_n<5>(ctx, a, p);
     default: return set_error(PDG_EUNSUPPORTED, "degree not compiled in");
   }
 }

@@ -359,6 +359,7 @@ __host__ __device__ inline long face_lattice_index(const int *nc, int dim, int d
 // the 3D FP64 operator in float-pair arithmetic (pdg_apply_fp.cu); rec64 must
 // be valid
 int launch_apply_float_pair(pdg_context *ctx, const ApplyArgs<double> &a);
+int prepare_float_pair(pdg_context *ctx);
 
 // parameter fields beyond A = K I: true when the Gauss-point operator replaces
 // the Kronecker kernels; its launch (diffusion and reaction terms only)
