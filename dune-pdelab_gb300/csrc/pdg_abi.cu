@@ -787,6 +787,50 @@ static int upload_dual(pdg_context *ctx, double **d64, float **d32, const double
   return PDG_OK;
 }
 
+// 2D grids: an outflow boundary side must not see inflow, b.n < -1e-30 at a
+// boundary quadrature point (convectiondiffusiondg.hh:802-806); b from the
+// Fourier modes or the velocity point data (face lattice)
+static int check_outflow_2d(pdg_context *ctx) {
+  const RhsTables t = make_rhs_tables(ctx);
+  const int nc[3] = {ctx->cfg.cells[0], ctx->cfg.cells[1], 1};
+  const int N = ctx->N;
+  std::vector<double> bf;
+  if (ctx->vel_points) {
+    bf.resize((size_t)face_lattice_count(ctx) * ctx->nqf * 3);
+    PDG_CUDA_TRY(cudaMemcpy(bf.data(), ctx->bqf64, sizeof(double) * bf.size(),
+                            cudaMemcpyDeviceToHost));
+  }
+  for (int side = 0; side < 4; side++) {
+    if (ctx->cfg.bctype[side] != PDG_BC_OUTFLOW) continue;
+    const int dir = side >> 1, hi = side & 1, o = 1 - dir;
+    int ix[3] = {0, 0, 0};
+    ix[dir] = hi ? nc[dir] - 1 : 0;
+    for (int a = 0; a < nc[o]; a++) {
+      ix[o] = a;
+      const long fi = face_lattice_index(nc, 2, dir, ix[dir] + hi, ix);
+      for (int q = 0; q < N; q++) {
+        double b[2] = {0.0, 0.0};
+        if (ctx->vel_points) {
+          b[dir] = bf[((size_t)fi * N + q) * 3 + dir];
+        } else {
+          double xg[2];
+          xg[dir] = (ix[dir] + hi) * ctx->h[dir];
+          xg[o] = (a + t.x[q]) * ctx->h[o];
+          for (int m = 0; m < ctx->vel.nmodes; m++) {
+            double arg = ctx->vel.m[m][3];
+            for (int j = 0; j < 2; j++) arg += 2.0 * M_PI * ctx->vel.m[m][j] * xg[j];
+            const double sv = std::sin(arg);
+            for (int j = 0; j < 2; j++) b[j] += ctx->vel.m[m][4 + j] * sv;
+          }
+        }
+        if ((hi ? b[dir] : -b[dir]) < -1e-30)
+          return set_error(PDG_EOUTFLOW, "outflow boundary condition on inflow");
+      }
+    }
+  }
+  return PDG_OK;
+}
+
 // drop the tensor fields (per cell and per point)
 static void free_tensors(pdg_context *ctx) {
   double **d[] = {&ctx->Ac64, &ctx->Aqv64, &ctx->Aqf64, &ctx->Kd64};
@@ -1204,8 +1248,6 @@ int pdg_set_velocity_points(pdg_context *ctx, const double *bvol, const double *
   PDG_CHECK_CTX(ctx);
   if (!bvol != !bface)
     return set_error(PDG_EINVAL, "give both the volume and the face velocities, or neither");
-  if (bvol && ctx->dim != 3)
-    return set_error(PDG_EUNSUPPORTED, "convection is implemented for 3D grids");
   if (!bvol) {
     if (ctx->vel_points) {
       PDG_TRY(upload(ctx, &ctx->bqv64, nullptr, 0));
@@ -1220,7 +1262,7 @@ int pdg_set_velocity_points(pdg_context *ctx, const double *bvol, const double *
   ctx->vel.nmodes = 0;
   ctx->vel_points = 1;
   invalidate(ctx, true);
-  const int st = conv_setup(ctx);
+  const int st = ctx->dim == 3 ? conv_setup(ctx) : check_outflow_2d(ctx);
   if (st != PDG_OK) ctx->vel_points = 0;
   return st;
 }
@@ -1312,8 +1354,6 @@ int pdg_set_velocity_modes(pdg_context *ctx, int nmodes, const double *modes) {
   PDG_CHECK_CTX(ctx);
   if (nmodes < 0 || nmodes > kMaxModes) return set_error(PDG_EINVAL, "nmodes must be 0..16");
   if (nmodes > 0 && !modes) return set_error(PDG_EINVAL, "null modes");
-  if (nmodes > 0 && ctx->dim != 3)
-    return set_error(PDG_EUNSUPPORTED, "convection is implemented for 3D grids");
   ctx->vel.nmodes = nmodes;
   if (nmodes > 0 && ctx->vel_points) {
     // modes replace velocity point data
@@ -1325,7 +1365,9 @@ int pdg_set_velocity_modes(pdg_context *ctx, int nmodes, const double *modes) {
     for (int j = 0; j < 7; j++) ctx->vel.m[m][j] = modes[7 * m + j];
   invalidate(ctx, true);
   if (nmodes > 0) {
-    const int st = conv_setup(ctx);
+    // 3D: the convection kernel's records; 2D: the Gauss-point operator
+    // evaluates b itself, so only the outflow sides are checked here
+    const int st = ctx->dim == 3 ? conv_setup(ctx) : check_outflow_2d(ctx);
     if (st != PDG_OK) {
       ctx->vel.nmodes = 0;
       return st;

@@ -608,9 +608,10 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
   if (ctx->basis == PDG_BASIS_LEGENDRE && !ctx->leg_nodal)
     return launch_apply_modal<T>(ctx, a, K, c, tab);
   if (general_coefficients(ctx)) {
-    // tensor or per-point coefficients: the Gauss-point operator
+    // tensor or per-point coefficients, or 2D convection: the Gauss-point
+    // operator (3D convection stays in its own kernel)
     PDG_TRY(launch_apply_general<T>(ctx, a));
-    if (convection_on(ctx)) PDG_TRY(launch_convection<T>(ctx, a));
+    if (convection_on(ctx) && ctx->dim == 3) PDG_TRY(launch_convection<T>(ctx, a));
     return nl_apply<T>(ctx, a);
   }
   OpParams<T> p = make_params<T>(ctx, K, c, tab);

@@ -32,6 +32,8 @@
 // Thread mapping: N^(d-1) threads per cell.  Line passes: one line per
 // thread.  Face steps: one face node or face point per thread.  Thread l
 // owns the output column (z-column in 3D, y-column in 2D) of k_apply.
+#include <cmath>
+
 #include "pdg_ops.cuh"
 #include "pdg_vec.cuh"
 
@@ -44,7 +46,28 @@ struct GpTab {
   T v[2][N];    // phi_a(0), phi_a(1)
   T d[2][N];    // phi_a'(0), phi_a'(1)
   T w[N];       // Gauss weights on [0,1]
+  double x[N];  // Gauss points on [0,1] (velocity evaluation)
 };
+
+// Convection inside this kernel (2D grids; 3D runs pdg_conv.cu): b from point
+// data (volume points [ncell][nqv][3], face lattice [faces][nqf][3]) or from
+// the Fourier modes at the point's coordinates
+struct GenConv {
+  int on;
+  const double *bqv, *bqf;
+  Velocity vel;
+};
+
+template <int D>
+__device__ __forceinline__ void velocity_modes(const Velocity &vel, const double *xg, double *b) {
+  b[0] = b[1] = b[2] = 0.0;
+  for (int m = 0; m < vel.nmodes; m++) {
+    double arg = vel.m[m][3];
+    for (int j = 0; j < D; j++) arg += 2.0 * M_PI * vel.m[m][j] * xg[j];
+    const double s = sin(arg);
+    for (int j = 0; j < D; j++) b[j] += vel.m[m][4 + j] * s;
+  }
+}
 
 template <typename T>
 struct GenCoef {
@@ -97,7 +120,7 @@ __device__ __forceinline__ void cell_tensor(const OpParams<T> &p, const GenCoef<
 template <typename T, int D, int N>
 __global__ void __launch_bounds__(GCfg<D, N>::THREADS)
     k_apply_gp(const OpParams<T> p, const ApplyArgs<T> a, const GenCoef<T> g,
-               const GpTab<T, N> tb) {
+               const GpTab<T, N> tb, const GenConv cv_) {
   using C = GCfg<D, N>;
   constexpr int NB = C::NB, NQF = C::NQF, TPC = C::TPC, CPB = C::CPB, DD = C::DD;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -208,12 +231,30 @@ __global__ void __launch_bounds__(GCfg<D, N>::THREADS)
           for (int j = 0; j < 3; j++) s += (tr ? A[j * 3 + i] : A[i * 3 + j]) * gr[j];
           F[i] = w * s;
         }
-        Fx[q] = over_h(p, 0, F[0]);
-        Fy[q] = over_h(p, 1, F[1]);
-        Fz[q] = over_h(p, 2, F[2]);
         T cc = p.c ? p.c[ee] : T(0);
         if (g.cq) cc += g.cq[(size_t)ee * NB + qi];
         R[q] = w * cc * uq;
+        if (cv_.on) {
+          // -u b.grad psi (:175-186); transposed: -psi b.grad z
+          double b[3];
+          if (cv_.bqv) {
+            for (int j = 0; j < 3; j++) b[j] = cv_.bqv[((size_t)ee * NB + qi) * 3 + j];
+          } else {
+            const double xg[3] = {(ix[0] + tb.x[q]) * (double)p.h[0],
+                                  (ix[1] + tb.x[q1]) * (double)p.h[1],
+                                  (ix[2] + tb.x[q2]) * (double)p.h[2]};
+            velocity_modes<3>(cv_.vel, xg, b);
+          }
+          if (!tr) {
+#pragma unroll
+            for (int j = 0; j < 3; j++) F[j] -= w * uq * (T)b[j];
+          } else {
+            R[q] -= w * ((T)b[0] * gr[0] + (T)b[1] * gr[1] + (T)b[2] * gr[2]);
+          }
+        }
+        Fx[q] = over_h(p, 0, F[0]);
+        Fy[q] = over_h(p, 1, F[1]);
+        Fz[q] = over_h(p, 2, F[2]);
       }
 #pragma unroll
       for (int k = 0; k < N; k++) {
@@ -296,11 +337,28 @@ __global__ void __launch_bounds__(GCfg<D, N>::THREADS)
           for (int j = 0; j < 2; j++) s += (tr ? A[j * 2 + i] : A[i * 2 + j]) * gr[j];
           F[i] = w * s;
         }
-        Fx[q] = over_h(p, 0, F[0]);
-        Fy[q] = over_h(p, 1, F[1]);
         T cc = p.c ? p.c[ee] : T(0);
         if (g.cq) cc += g.cq[(size_t)ee * NB + qi];
         R[q] = w * cc * uq;
+        if (cv_.on) {
+          // -u b.grad psi (:175-186); transposed: -psi b.grad z
+          double b[3];
+          if (cv_.bqv) {
+            for (int j = 0; j < 2; j++) b[j] = cv_.bqv[((size_t)ee * NB + qi) * 3 + j];
+          } else {
+            const double xg[2] = {(ix[0] + tb.x[q]) * (double)p.h[0],
+                                  (ix[1] + tb.x[q1]) * (double)p.h[1]};
+            velocity_modes<2>(cv_.vel, xg, b);
+          }
+          if (!tr) {
+            F[0] -= w * uq * (T)b[0];
+            F[1] -= w * uq * (T)b[1];
+          } else {
+            R[q] -= w * ((T)b[0] * gr[0] + (T)b[1] * gr[1]);
+          }
+        }
+        Fx[q] = over_h(p, 0, F[0]);
+        Fy[q] = over_h(p, 1, F[1]);
       }
       __syncthreads();   // the x pass read other threads' y-pass lines
 #pragma unroll
@@ -342,7 +400,8 @@ __global__ void __launch_bounds__(GCfg<D, N>::THREADS)
     else nb = ix[dir] > 0 ? (long)ee - gstride[dir] : -1;
     const bool interior = nb >= 0;
     const bool dirichlet = !interior && p.bc[f] == PDG_BC_DIRICHLET;
-    const bool live = interior || dirichlet;
+    const bool outflow = !interior && cv_.on && p.bc[f] == PDG_BC_OUTFLOW;
+    const bool live = interior || dirichlet || outflow;
     const bool coupled = interior && !a.diag_only;
 
     // step 1: value and normal-derivative layers at the face (thread l:
@@ -442,8 +501,30 @@ __global__ void __launch_bounds__(GCfg<D, N>::THREADS)
       if (D == 3) gs[o2] = over_h(p, o2, dt2s);
       T wq = tb.w[q1] * (D == 3 ? tb.w[q2] : T(1));
       wq *= p.h[o1] * (D == 3 ? p.h[o2] : T(1));
+      // convection: b.n_F at the face point (one value for both sides) and
+      // the upwind side (:425-443, 796-849)
+      T nflux = T(0);
+      if (cv_.on) {
+        double b[3];
+        if (cv_.bqf) {
+          const long fi = face_lattice_index(p.nc, D, dir, ix[dir] + hi, ix);
+          b[dir] = cv_.bqf[(fi * NQF + pq) * 3 + dir];
+        } else {
+          double xg[3];
+          xg[dir] = (ix[dir] + hi) * (double)p.h[dir];
+          xg[o1] = (ix[o1] + tb.x[q1]) * (double)p.h[o1];
+          if (D == 3) xg[o2] = (ix[o2] + tb.x[q2]) * (double)p.h[o2];
+          velocity_modes<D>(cv_.vel, xg, b);
+        }
+        nflux = (T)(hi ? b[dir] : -b[dir]);
+      }
+      const T up_s = nflux >= T(0) ? T(1) : T(0);
       T Cv, Cg;
-      if (interior) {
+      if (outflow) {
+        // u b.n psi (:799-820), symmetric in trial and test
+        Cv = us * nflux * wq;
+        Cg = T(0);
+      } else if (interior) {
         cell_tensor<T, D, N>(p, g, nb, f ^ 1, pq, An);
 #pragma unroll
         for (int j = 0; j < D; j++) AnN[j] = An[j * D + dir] * sgn;
@@ -469,9 +550,12 @@ __global__ void __launch_bounds__(GCfg<D, N>::THREADS)
         if (!tr) {
           Cv = (-(om_s * As_g + om_n * An_g) + pen * jump) * wq;
           Cg = p.theta * om_s * jump * wq;
+          // term 1: (up_s u_s + up_n u_n) b.n psi_s
+          if (cv_.on) Cv += (up_s * us + (T(1) - up_s) * un) * nflux * wq;
         } else {
           Cv = (pen * jump + p.theta * (om_s * As_g + om_n * An_g)) * wq;
           Cg = -om_s * jump * wq;
+          if (cv_.on) Cv += up_s * nflux * jump * wq;
         }
       } else {
         const T harm = p.weights == PDG_WEIGHTS_ON ? delta_s : T(1);
@@ -486,6 +570,8 @@ __global__ void __launch_bounds__(GCfg<D, N>::THREADS)
           Cv = (pen * us + p.theta * As_g) * wq;
           Cg = -us * wq;
         }
+        // Dirichlet inflow upwind term with g = 0 (:842-849), symmetric
+        if (cv_.on) Cv += up_s * us * nflux * wq;
       }
       // test: Cv psi + Cg (A_s n).grad psi, the gradient in reference
       // coordinates scaled by 1/h per direction
@@ -571,6 +657,7 @@ static GpTab<T, N> make_gp_tab(const pdg_context *ctx) {
   GpTab<T, N> tb{};
   for (int q = 0; q < N; q++) {
     tb.w[q] = (T)r.w[q];
+    tb.x[q] = r.x[q];
     for (int k = 0; k < N; k++) {
       tb.B[q * N + k] = (T)r.B[q * N + k];
       tb.D[q * N + k] = (T)lagrange_derivative(ctx, k, r.x[q]);
@@ -588,7 +675,7 @@ static GpTab<T, N> make_gp_tab(const pdg_context *ctx) {
 
 template <typename T, int D, int N>
 static int launch_gp_dn(pdg_context *ctx, const ApplyArgs<T> &a, const OpParams<T> &p,
-                        const GenCoef<T> &g) {
+                        const GenCoef<T> &g, const GenConv &cv) {
   using C = GCfg<D, N>;
   const size_t smem = sizeof(T) * C::CPB * C::PER_CELL;
   static int attr_dev = -1;
@@ -600,7 +687,8 @@ static int launch_gp_dn(pdg_context *ctx, const ApplyArgs<T> &a, const OpParams<
   const long work = (a.cells || a.ncells > 0) ? a.ncells : ctx->ncell;
   if (work <= 0) return PDG_OK;
   const unsigned blocks = (unsigned)((work + C::CPB - 1) / C::CPB);
-  k_apply_gp<T, D, N><<<blocks, C::THREADS, smem, ctx->stream>>>(p, a, g, make_gp_tab<T, N>(ctx));
+  k_apply_gp<T, D, N><<<blocks, C::THREADS, smem, ctx->stream>>>(p, a, g, make_gp_tab<T, N>(ctx),
+                                                                  cv);
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
 }
@@ -726,8 +814,10 @@ int launch_rhs_general(pdg_context *ctx) {
 }
 
 bool general_coefficients(const pdg_context *ctx) {
-  // a diagonal tensor per cell (gen_A 3) stays in Kronecker form
-  return ctx->gen_A == 1 || ctx->gen_A == 2 || ctx->cq64 != nullptr;
+  // a diagonal tensor per cell (gen_A 3) stays in Kronecker form; 2D
+  // convection runs here (3D convection has its own kernel)
+  return ctx->gen_A == 1 || ctx->gen_A == 2 || ctx->cq64 != nullptr ||
+         (ctx->dim == 2 && convection_on(ctx));
 }
 
 template <typename T>
@@ -744,15 +834,22 @@ int launch_apply_general(pdg_context *ctx, const ApplyArgs<T> &a) {
     g.Aqf = dbl ? (const T *)ctx->Aqf64 : (const T *)ctx->Aqf32;
   }
   g.cq = dbl ? (const T *)ctx->cq64 : (const T *)ctx->cq32;
+  GenConv cv{};
+  cv.on = ctx->dim == 2 && convection_on(ctx);
+  if (cv.on) {
+    cv.bqv = ctx->vel_points ? ctx->bqv64 : nullptr;
+    cv.bqf = ctx->vel_points ? ctx->bqf64 : nullptr;
+    cv.vel = ctx->vel;
+  }
   switch (ctx->dim * 10 + ctx->k) {
-    case 21: return launch_gp_dn<T, 2, 2>(ctx, a, p, g);
-    case 22: return launch_gp_dn<T, 2, 3>(ctx, a, p, g);
-    case 23: return launch_gp_dn<T, 2, 4>(ctx, a, p, g);
-    case 24: return launch_gp_dn<T, 2, 5>(ctx, a, p, g);
-    case 31: return launch_gp_dn<T, 3, 2>(ctx, a, p, g);
-    case 32: return launch_gp_dn<T, 3, 3>(ctx, a, p, g);
-    case 33: return launch_gp_dn<T, 3, 4>(ctx, a, p, g);
-    case 34: return launch_gp_dn<T, 3, 5>(ctx, a, p, g);
+    case 21: return launch_gp_dn<T, 2, 2>(ctx, a, p, g, cv);
+    case 22: return launch_gp_dn<T, 2, 3>(ctx, a, p, g, cv);
+    case 23: return launch_gp_dn<T, 2, 4>(ctx, a, p, g, cv);
+    case 24: return launch_gp_dn<T, 2, 5>(ctx, a, p, g, cv);
+    case 31: return launch_gp_dn<T, 3, 2>(ctx, a, p, g, cv);
+    case 32: return launch_gp_dn<T, 3, 3>(ctx, a, p, g, cv);
+    case 33: return launch_gp_dn<T, 3, 4>(ctx, a, p, g, cv);
+    case 34: return launch_gp_dn<T, 3, 5>(ctx, a, p, g, cv);
     default: return set_error(PDG_EUNSUPPORTED, "dim/degree not compiled in");
   }
 }

@@ -239,7 +239,8 @@ int pdg_set_permeability(pdg_context *ctx, const double *K, int is_log);
 /* c(cell) per cell (NULL = 0) */
 int pdg_set_reaction(pdg_context *ctx, const double *c);
 /* b(x) = sum_m coef_m sin(2 pi kv_m . x + phase_m); modes [n][7] =
-   kx ky kz phase cx cy cz (n = 0 clears the velocity). */
+   kx ky kz phase cx cy cz (n = 0 clears the velocity; in 2D the z entries are
+   ignored).  PDG_EOUTFLOW if an outflow side sees inflow. */
 int pdg_set_velocity_modes(pdg_context *ctx, int nmodes, const double *modes);
 /* f at volume quadrature points [ncell][(k+1)^d] (NULL = 0) plus a per-cell
    constant fc [ncell] (NULL = 0).  Used by lambda_volume
@@ -280,8 +281,8 @@ int pdg_set_reaction_points(pdg_context *ctx, const double *cq);
    the face-lattice points [nfaces][(k+1)^2][3] (pdg_face_lattice_points):
    one value per face point serves both sides, as the reference upwinds
    with the inside cell's b and assumes an H(div) field
-   (convectiondiffusiondg.hh:425-426, 796-797).  Replaces Fourier modes;
-   3D.  Both NULL removes the velocity. */
+   (convectiondiffusiondg.hh:425-426, 796-797); in 2D the third component
+   is ignored.  Replaces Fourier modes.  Both NULL removes the velocity. */
 int pdg_set_velocity_points(pdg_context *ctx, const double *bvol, const double *bface);
 /* The face lattice: every face of the grid once.  Faces normal to x come
    first, then y, then z; per direction the planes 0..cells[dir] in order;
