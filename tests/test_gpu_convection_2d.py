@@ -80,7 +80,8 @@ def test_convection_2d_point_velocity_and_residual(pdg, oracle):
         return b
     bv, bf = b_at(go.volume_points()), b_at(go.face_lattice_points())
     go.set_velocity_points(bv, bf)
-    P.set(K=K, bq_vol=bv, bq_face=bf)
+    # the oracle holds dim components per point, the C ABI three
+    P.set(K=K, bq_vol=bv[..., :2], bq_face=bf[..., :2])
     f = rng.uniform(-1, 1, (go.ncell, P.nq_volume))
     g = rng.uniform(-1, 1, P.nbpts_total())
     o = rng.uniform(-1, 1, P.nbpts_total())
