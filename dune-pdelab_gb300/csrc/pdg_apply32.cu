@@ -427,11 +427,13 @@ __device__ __forceinline__ float4 ld4(const float *p, bool vec) {
   return make_float4(p[0], p[1], p[2], p[3]);
 }
 
-// 6 blocks of 128 threads per SM (35 KB of shared memory each): 333 us at
-// 96^3 Q3, against 351 us with the compiler's free register choice (96
-// registers, 5 blocks per SM) and 378 us without the aliased runs
+// 5 blocks of 128 threads per SM (96 registers; 35 KB of shared memory each):
+// with the z-neighbour rows loaded before the staging wait, 325 us at 96^3 Q3,
+// against 334 us with those loads after stage 1 at 6 blocks per SM (80
+// registers), 350 us at 4 blocks and 351 us with the compiler's free register
+// choice; 378 us without the aliased runs
 template <bool kTma>
-__global__ void __launch_bounds__(Q3Cfg::THREADS, 6)
+__global__ void __launch_bounds__(Q3Cfg::THREADS, 5)
     k_apply32_q3(const OpParams<float> p, const ApplyArgs<float> a, const float *__restrict__ rec,
                  const EdgeTab tb, const __grid_constant__ CUtensorMap map_own,
                  const __grid_constant__ CUtensorMap map_run, int *tma_err) {
@@ -455,6 +457,27 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS, 6)
   const float *__restrict__ x = a.x;
   const bool coupled = !a.diag_only;
   const bool vec = (reinterpret_cast<uintptr_t>(x) & 15) == 0;
+  const int t = threadIdx.x, cs = t >> 2, z = t & 3;
+  const long e = e0 + cs;
+  const bool active = e < ncell;
+  const long ee = active ? e : 0;
+  int ix[3];
+  coords32(p, (unsigned)ee, ix);
+  const bool has[6] = {coupled && ix[0] > 0, coupled && ix[0] + 1 < p.nc[0],
+                       coupled && ix[1] > 0, coupled && ix[1] + 1 < p.nc[1],
+                       coupled && ix[2] > 0, coupled && ix[2] + 1 < p.nc[2]};
+  const bool tr = a.transpose != 0;
+  // the z-neighbour rows (plane q, row y = z of each z neighbour) come straight
+  // from global memory; issued before the staging wait so that their latency
+  // overlaps the staging copies and stage 1
+  float4 zl[N], zh[N];
+#pragma unroll
+  for (int q = 0; q < N; q++) {
+    zl[q] = has[4] ? ld4(x + (ee - sxy) * NB + q * N2 + z * N, vec)
+                   : make_float4(0.f, 0.f, 0.f, 0.f);
+    zh[q] = has[5] ? ld4(x + (ee + sxy) * NB + q * N2 + z * N, vec)
+                   : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
 
   // rows of cells [c0, c0 + ncells) into dst (swizzled); absent cells read 0
   auto stage_rows = [&](float4 *dst, long c0, int ncells, bool on) {
@@ -530,16 +553,6 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS, 6)
   asm volatile("cp.async.commit_group;\n" ::: "memory");
   }
 
-  const int t = threadIdx.x, cs = t >> 2, z = t & 3;
-  const long e = e0 + cs;
-  const bool active = e < ncell;
-  const long ee = active ? e : 0;
-  int ix[3];
-  coords32(p, (unsigned)ee, ix);
-  const bool has[6] = {coupled && ix[0] > 0, coupled && ix[0] + 1 < p.nc[0],
-                       coupled && ix[1] > 0, coupled && ix[1] + 1 < p.nc[1],
-                       coupled && ix[2] > 0, coupled && ix[2] + 1 < p.nc[2]};
-  const bool tr = a.transpose != 0;
 
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();
@@ -602,14 +615,6 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS, 6)
   // ---- z faces of the face points of row z ----
   {
     // z-neighbour rows (plane q, row z) straight from global memory
-    float4 zl[N], zh[N];
-#pragma unroll
-    for (int q = 0; q < N; q++) {
-      zl[q] = has[4] ? ld4(x + (ee - sxy) * NB + q * N2 + z * N, vec)
-                     : make_float4(0.f, 0.f, 0.f, 0.f);
-      zh[q] = has[5] ? ld4(x + (ee + sxy) * NB + q * N2 + z * N, vec)
-                     : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
     float s1l[N], s2l[N], s1h[N], s2h[N];
 #pragma unroll
     for (int xx = 0; xx < N; xx++) {
