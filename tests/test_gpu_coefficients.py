@@ -260,3 +260,28 @@ def test_diagonal_tensor_keeps_fdm_and_mixed_solve(pdg, oracle):
             assert abs(slp.result().iterations - rres.iterations) <= 1
         assert _rel(u, uref) <= 1e-8
     go.close()
+
+
+@pytest.mark.parametrize("dim,k,nc", [(3, 2, (3, 2, 4)), (3, 1, (1, 1, 1)), (2, 3, (1, 5)),
+                                      (2, 2, (4, 1))])
+def test_tensor_non_cubic_and_single_cell(pdg, oracle, dim, k, nc):
+    rng = np.random.default_rng(sum(nc) + 10 * k)
+    go = pdg.GridOperator(dim, k, nc, alpha=3.0, bctype=[1, -1, 1, 1, -1, 1])
+    P = oracle.Problem(dim, k, nc, alpha=3.0, bctype=[1, -1, 1, 1, -1, 1])
+    A = _spd(rng, go.ncell, dim)
+    go.set_permeability_tensor(A)
+    P.set(Acell=A)
+    _check_apply(go, P, rng)
+    go.close()
+
+
+@pytest.mark.parametrize("basis", [1, 2])
+def test_tensor_with_legendre_and_lobatto(pdg, oracle, basis):
+    rng = np.random.default_rng(120 + basis)
+    go = pdg.GridOperator(3, 2, (3, 3, 2), alpha=3.0, basis=basis)
+    P = oracle.Problem(3, 2, (3, 3, 2), alpha=3.0, basis=basis)
+    A = _spd(rng, go.ncell, 3)
+    go.set_permeability_tensor(A)
+    P.set(Acell=A)
+    _check_apply(go, P, rng)
+    go.close()

@@ -108,3 +108,18 @@ def test_float_pair_host_buffers_match_device(pdg):
     go.jacobian_apply(x, yh)
     assert np.array_equal(yh, yd.cpu().numpy())
     go.close()
+
+
+@pytest.mark.parametrize("nc", [(1, 1, 1), (2, 1, 3)])
+def test_float_pair_small_grids(pdg, oracle, nc):
+    rng = np.random.default_rng(sum(nc))
+    K = np.exp(rng.standard_normal(int(np.prod(nc))))
+    go = pdg.GridOperator(3, 3, nc, alpha=3.0)
+    go.set_permeability(K)
+    go.set_f64_arithmetic(pdg.F64_FLOAT_PAIR)
+    P = oracle.Problem(3, 3, nc, alpha=3.0, K=K)
+    x = rng.uniform(-1, 1, go.ndof)
+    y = np.zeros(go.ndof)
+    go.jacobian_apply(x, y)
+    assert _rel(y, P.jacobian_apply(x)) <= TOL64
+    go.close()
