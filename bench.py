@@ -490,11 +490,12 @@ def run_gb300(args, world, rank, local):
     # convection-diffusion-reaction solves and gradients) are on the default
     # line; --legs picks a subset, --extended adds the block-preconditioner
     # and assembled-matrix legs
-    legs = set(args.legs.split(","))
+    if args.legs is not None:
+        legs = set(args.legs.split(","))          # explicit legs run regardless
+    else:
+        legs = set() if args.no_solves else {"c1", "c3", "c4", "c5"}
     if args.extended:
         legs |= {"prec", "asm"}
-    if args.no_solves:
-        legs = set()
     if legs:
         for leg, key, fn in (("c1", "solve_q1_2d_64", c1_metrics),
                              ("c3", "solve_q3_96", c3_metrics), ("c4", "adjoint_q2_64", c4_metrics),
@@ -1038,15 +1039,17 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--no-solves", action="store_true", help="skip solve/adjoint metrics")
+    ap.add_argument("--no-solves", action="store_true",
+                    help="skip the 64^3 Q2 solve/adjoint metrics and the default legs")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--extended", action="store_true",
                     help="also run the block-preconditioner (prec) and assembled-matrix (asm) "
                          "legs")
-    ap.add_argument("--legs", default="c1,c3,c4,c5",
-                    help="configuration legs to run: c1 (2D Q1 64^2 solve and its CPU "
-                         "solve), c3 (96^3 Q3 mixed vs FP64), c4 (64^3 Q2 adjoint checks), c5 "
-                         "(48^3 Q4 convection-diffusion-reaction); prec, asm")
+    ap.add_argument("--legs", default=None,
+                    help="configuration legs to run (default c1,c3,c4,c5, none with "
+                         "--no-solves): c1 (2D Q1 64^2 solve and its CPU solve), c3 (96^3 Q3 "
+                         "mixed vs FP64), c4 (64^3 Q2 adjoint checks), c5 (48^3 Q4 "
+                         "convection-diffusion-reaction); prec, asm")
     ap.add_argument("--no-probe", action="store_true",
                     help="skip the FMA peak probe (profiling runs); roofline frac is then null")
     ap.add_argument("--solves-only", action="store_true",
