@@ -309,8 +309,6 @@ struct KrylovOut {
   int state;       // 0 running/maxit, 1 converged, 2 non-finite, 3 breakdown
   int iterations;
   double def0, def;
-  double rho_last; // fused CG: the rho of the last iteration (for a continuation)
-  bool fused;      // the solve ran the fused FP32 CG
 };
 
 // The inner FP32 CG can fuse its two dot products into the kernels that
@@ -340,31 +338,18 @@ static int ensure_fuse(pdg_context *ctx) {
 
 // dune-istl CGSolver::apply restated on the device.  x: initial guess and
 // result; b: right-hand side, overwritten by the defect.  w0, w1: work.
-// cont > 0 continues a previous solve whose last direction is still in p (a
-// reliable update, Sleijpen & van der Vorst 1996): b holds the true residual
-// scaled as this solve's right-hand side, and the first direction is
-// p = M^{-1} b + cont <M^{-1} b, b> p_old, with cont = s / rho_old for the
-// rho of the previous solve's last iteration and s the ratio of this
-// right-hand side's scale to the previous one's.
 template <typename T>
 static int cg_device(pdg_context *ctx, T *x, T *b, T *p, T *q, double reduction, int maxit,
-                     int transpose, KrylovOut *out, double cont = 0.0) {
+                     int transpose, KrylovOut *out) {
   const RedCtx rc = red_ctx(ctx);
   const int *skip = ctx->d_flag + F_STATE;
   k_init_solve<<<1, 1, 0, ctx->stream>>>(rc.scal, rc.flags, reduction);
   // b -= A x   (applyscaleadd(-1, x, b))
   PDG_TRY(op_launch<T>(ctx, x, b, nullptr, T(-1), 1, transpose, nullptr));
   PDG_TRY(dot<T>(ctx, rc, b, b, nullptr, nullptr, FIN_DEF0, -1, -1, false));
-  if (cont > 0.0) {
-    // z = M^{-1} b ; rholast = <z, b> ; p = z + cont rholast p_old
-    PDG_TRY(prec_op<T>(ctx, b, q, transpose, skip));
-    PDG_TRY(dot<T>(ctx, rc, q, b, nullptr, nullptr, FIN_STORE, S_RHO, -1, true));
-    PDG_TRY(cg_continue_p<T>(ctx, rc, ctx->ndof, p, q, cont));
-  } else {
-    // p = M^{-1} b ; rholast = <p, b>
-    PDG_TRY(prec_op<T>(ctx, b, p, transpose, skip));
-    PDG_TRY(dot<T>(ctx, rc, p, b, nullptr, nullptr, FIN_STORE, S_RHO, -1, true));
-  }
+  // p = M^{-1} b ; rholast = <p, b>
+  PDG_TRY(prec_op<T>(ctx, b, p, transpose, skip));
+  PDG_TRY(dot<T>(ctx, rc, p, b, nullptr, nullptr, FIN_STORE, S_RHO, -1, true));
   double scal[S_COUNT];
   int flags[F_COUNT];
   int i = 1;
@@ -408,8 +393,6 @@ static int cg_device(pdg_context *ctx, T *x, T *b, T *p, T *q, double reduction,
   out->def0 = scal[S_DEF0];
   out->def = scal[S_DEF];
   out->iterations = (int)scal[S_ITER];
-  out->fused = fuse;
-  out->rho_last = scal[S_RHONEW];
   return PDG_OK;
 }
 
@@ -470,9 +453,8 @@ static int bicgstab_device(pdg_context *ctx, T *x, T *b, T *w[8], double reducti
 template <typename T>
 static int krylov_device(pdg_context *ctx, int method, T *x, T *b, T **w, double reduction,
                          int maxit, int transpose, KrylovOut *out, double guard = 0.0,
-                         int restart = 30, int replace = 0, double cont = 0.0) {
-  if (method == PDG_CG)
-    return cg_device<T>(ctx, x, b, w[0], w[1], reduction, maxit, transpose, out, cont);
+                         int restart = 30, int replace = 0) {
+  if (method == PDG_CG) return cg_device<T>(ctx, x, b, w[0], w[1], reduction, maxit, transpose, out);
   if (method == PDG_BICGSTAB)
     return bicgstab_device<T>(ctx, x, b, w, reduction, maxit, transpose, out, guard, replace);
   if (method == PDG_GMRES) {
@@ -649,10 +631,6 @@ static int solve_correction(pdg_context *ctx, const pdg_solver_options *opt, dou
   const double target = opt->reduction * def0;
   int total_inner = 0, outer = 0, weak = 0;
   int st = PDG_OK;
-  // reliable updates of the FP32 CG (inner_continue): the defect of the last
-  // inner solve's scale and its last rho, so that the next inner solve
-  // continues that solve's last direction instead of restarting
-  double prev_scale = 0.0, prev_rho = 0.0;
   while (def >= target && def >= 1e-30 && outer < opt->max_outer) {
     if (!std::isfinite(def)) { st = set_error(PDG_ENONFINITE, "non-finite defect"); break; }
     KrylovOut o{};
@@ -664,18 +642,9 @@ static int solve_correction(pdg_context *ctx, const pdg_solver_options *opt, dou
       k_set_scal<<<1, 1, 0, ctx->stream>>>(rc.scal, S_SCALE, def);
       PDG_TRY(vec_to_f32_scaled(ctx, n, d, d32, rc.scal));
       PDG_TRY(vec_fill<float>(ctx, n, c32, 0.f));
-      double cont = 0.0;
-      if (opt->inner_continue && inner == PDG_CG && prev_scale > 0.0 && prev_rho > 0.0 &&
-          std::isfinite(prev_rho))
-        cont = (def / prev_scale) / prev_rho;
       PDG_TRY(krylov_device<float>(ctx, inner, c32, d32, ctx->w32, opt->inner_reduction,
                                    opt->inner_maxit, transpose, &o, opt->inner_breakdown,
-                                   opt->restart, opt->inner_replace, cont));
-      // a later inner solve may continue this one (fused FP32 CG: its last
-      // direction is in w32[0] and its last rho is known)
-      const bool can = inner == PDG_CG && o.fused && (o.state == 0 || o.state == 1);
-      prev_scale = can ? def : 0.0;
-      prev_rho = can ? o.rho_last : 0.0;
+                                   opt->restart, opt->inner_replace));
     } else {
       // FP64 Krylov vectors, FP32 operator and block Jacobi (ctx->ops32)
       double *c64 = ctx->w64[8], *d64 = ctx->w64[9];
@@ -916,7 +885,6 @@ void pdg_default_solver_options(pdg_solver_options *o) {
   o->restart = 30;
   o->inner_replace = 25;
   o->inner_vectors = -1;
-  o->inner_continue = 1;
   o->assembled = 0;
 }
 
@@ -1679,8 +1647,6 @@ static int check_opts(const pdg_solver_options *o) {
     return set_error(PDG_EINVAL, "GMRES restart length must be 1..64");
   if (o->mixed < 0 || o->mixed > 3) return set_error(PDG_EINVAL, "mixed must be 0..3");
   if (o->assembled != 0 && o->assembled != 1) return set_error(PDG_EINVAL, "bad assembled flag");
-  if (o->inner_continue != 0 && o->inner_continue != 1)
-    return set_error(PDG_EINVAL, "bad inner_continue flag");
   if ((o->preconditioner & ~(PDG_PREC_BLOCK_MASK | PDG_PREC_SOR)) != 0 ||
       (o->preconditioner & PDG_PREC_BLOCK_MASK) > PDG_PREC_BJ_ITERATIVE)
     return set_error(PDG_EINVAL, "bad preconditioner kind");

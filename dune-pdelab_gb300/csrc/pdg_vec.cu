@@ -155,18 +155,6 @@ __global__ void k_cg_xfin(long n, T *__restrict__ x, const T *__restrict__ p, Re
     x[i] += lambda * p[i];
 }
 
-// first direction of a CG continued after its residual was replaced by the
-// true one (reliable update): p = z + gamma p with gamma = factor rho
-template <typename T>
-__global__ void k_cg_continue_p(long n, T *__restrict__ p, const T *__restrict__ z, RedCtx rc,
-                                double factor) {
-  if (rc.flags[F_STATE]) return;
-  const T gamma = (T)(factor * rc.scal[S_RHO]);
-  const long stride = (long)gridDim.x * blockDim.x;
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    p[i] = z[i] + gamma * p[i];
-}
-
 // BiCGSTABSolver: p = r (first half step) or p = beta (p - omega v) + r
 template <typename T>
 __global__ void k_bi_p(long n, T *__restrict__ p, const T *__restrict__ r,
@@ -260,12 +248,6 @@ int cg_finish_x(pdg_context *ctx, const RedCtx &rc, long n, T *x, const T *p) {
   return PDG_OK;
 }
 template <typename T>
-int cg_continue_p(pdg_context *ctx, const RedCtx &rc, long n, T *p, const T *z, double factor) {
-  k_cg_continue_p<T><<<ew_grid(n), 256, 0, ctx->stream>>>(n, p, z, rc, factor);
-  PDG_CUDA_TRY(cudaGetLastError());
-  return PDG_OK;
-}
-template <typename T>
 int bi_update_p(pdg_context *ctx, const RedCtx &rc, long n, T *p, const T *r, const T *v,
                 int first) {
   k_bi_p<T><<<ew_grid(n), 256, 0, ctx->stream>>>(n, p, r, v, rc, first);
@@ -298,7 +280,6 @@ int set_iter(pdg_context *ctx, const RedCtx &rc, double it) {
   template int cg_update_p<T>(pdg_context *, const RedCtx &, long, T *, const T *);         \
   template int cg_update_px<T>(pdg_context *, const RedCtx &, long, T *, T *, const T *);   \
   template int cg_finish_x<T>(pdg_context *, const RedCtx &, long, T *, const T *);         \
-  template int cg_continue_p<T>(pdg_context *, const RedCtx &, long, T *, const T *, double); \
   template int bi_update_p<T>(pdg_context *, const RedCtx &, long, T *, const T *,          \
                               const T *, int);                                              \
   template int bi_update_half<T>(pdg_context *, const RedCtx &, long, T *, T *, const T *,  \

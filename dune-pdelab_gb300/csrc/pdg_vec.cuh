@@ -23,7 +23,7 @@ enum Slot {
   S_DEF = 1,      // current defect (two-norm)
   S_RED = 2,      // requested reduction
   S_RHO = 3,      // CG rholast / BiCGStab rho
-  S_RHONEW = 4,   // BiCGStab rho_new; fused CG: the rho of the last iteration
+  S_RHONEW = 4,   // BiCGStab rho_new
   S_ALPHA = 5,    // CG lambda / BiCGStab alpha
   S_BETA = 6,
   S_OMEGA = 7,
@@ -111,7 +111,6 @@ __device__ inline void run_finisher(const RedCtx &rc, int fin, int slot0, int sl
       else if (def < s[S_DEF0] * s[S_RED] || def < 1e-30) fl[F_STATE] = 1;
       if (fl[F_STATE]) fl[F_XPEND] = 1;
       s[S_BETA] = d1 / s[S_RHO];
-      s[S_RHONEW] = s[S_RHO];   // kept for a continued solve (reliable update)
       s[S_RHO] = d1;
       break;
     }
@@ -268,9 +267,6 @@ template <typename T>
 int cg_update_px(pdg_context *ctx, const RedCtx &rc, long n, T *x, T *p, const T *z);
 template <typename T>
 int cg_finish_x(pdg_context *ctx, const RedCtx &rc, long n, T *x, const T *p);
-// p = z + factor * scal[S_RHO] * p (the first direction of a continued CG)
-template <typename T>
-int cg_continue_p(pdg_context *ctx, const RedCtx &rc, long n, T *p, const T *z, double factor);
 template <typename T>
 int bi_update_p(pdg_context *ctx, const RedCtx &rc, long n, T *p, const T *r, const T *v,
                 int first);   // p = r (first) or p = beta (p - omega v) + r

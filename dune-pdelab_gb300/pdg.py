@@ -72,7 +72,7 @@ class SolverOptions(C.Structure):
                 ("inner_maxit", C.c_int), ("max_outer", C.c_int), ("verbose", C.c_int),
                 ("inner_breakdown", C.c_double), ("inner_method", C.c_int),
                 ("restart", C.c_int), ("inner_replace", C.c_int), ("inner_vectors", C.c_int),
-                ("assembled", C.c_int), ("inner_continue", C.c_int)]
+                ("assembled", C.c_int)]
 
 
 class PrecOptions(C.Structure):

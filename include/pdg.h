@@ -166,13 +166,6 @@ typedef struct pdg_solver_options {
                               (pdg_jacobian_assemble; assembled on first use),
                               the matrix-based path of the reference's
                               matrix-free tests; FP64 only */
-  int inner_continue;      /* mixed, CG with FP32 inner vectors: 1 (default)
-                              continues the last inner solve's search
-                              direction after each FP64 defect update (a
-                              reliable update: the residual is replaced by the
-                              true one, the Krylov recurrence goes on); 0
-                              restarts CG at every defect correction.  No
-                              reference counterpart. */
 } pdg_solver_options;
 
 /* LinearSolverResult (backend/solver.hh:29-51) +

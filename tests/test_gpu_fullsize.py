@@ -217,26 +217,3 @@ def test_q2_64_adjoint_gradient_vs_central_difference(env):
         ad = float((logK.grad * d).sum())
         assert abs(fd - ad) <= 1e-4 * abs(ad), (fd, ad)
     go.close()
-
-
-def test_q2_64_mixed_cg_reliable_update_vs_restart(env):
-    """The FP32 inner CG continued across the FP64 defect updates (reliable
-    updates, the default) against restarting it at every update: both reach
-    the true FP64 defect bound, the continued one in fewer inner iterations."""
-    pdg, torch, bench = env
-    go, logK = bench.make_problem(pdg, np, 0)
-    go.set_source(fc=np.ones(go.ncell))
-    its = {}
-    for cont in (0, 1):
-        ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG, mixed=True, maxiter=20000,
-                                                 inner_reduction=1e-4)
-        ls.opts.inner_continue = cont
-        u = torch.zeros(go.ndof, dtype=torch.float64, device="cuda")
-        slp = pdg.StationaryLinearProblemSolver(go, ls, u, 1e-10)
-        slp.apply()
-        assert slp.result().converged
-        assert _true_defect_ratio(go, torch, u) <= 1.01e-10
-        its[cont] = slp.result().iterations
-    print(f"64^3 Q2 mixed CG inner iterations: restart {its[0]}, continued {its[1]}")
-    assert its[1] <= its[0]
-    go.close()
