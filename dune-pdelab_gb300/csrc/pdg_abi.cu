@@ -848,6 +848,7 @@ static void invalidate(pdg_context *ctx, bool operator_changed) {
     ctx->rec_valid = 0;
     ctx->recfp_valid = 0;
     ctx->rec32_valid = 0;
+    ctx->rec32q_valid = 0;
     ctx->A_valid = 0;
     ctx->prec[0].ready = 0;
     ctx->prec[1].ready = 0;
@@ -1072,7 +1073,7 @@ int pdg_destroy(pdg_context *c) {
                   c->leg64, c->leg32, c->legw64[0], c->legw64[1], c->legw32[0], c->legw32[1],
                   c->fuse_part, c->fuse_cnt, c->Ac64, c->Aqv64, c->Aqf64, c->cq64, c->Ac32,
                   c->Aqv32, c->Aqf32, c->cq32, c->bqv64, c->bqf64, c->Kd64, c->Kd32,
-                  c->recfp, c->tabfp};
+                  c->recfp, c->tabfp, c->rec32q};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 10; i++)
@@ -1581,6 +1582,13 @@ int pdg_jacobian_apply_f32(pdg_context *ctx, const float *z, float *y) {
   if (!is_device_ptr(z) || !is_device_ptr(y))
     return set_error(PDG_EINVAL, "pdg_jacobian_apply_f32 takes device pointers");
   return op_launch<float>(ctx, z, y, nullptr, 1.f, 1, 0, nullptr);
+}
+int pdg_jacobian_apply_transpose_f32(pdg_context *ctx, const float *z, float *y) {
+  PDG_CHECK_CTX(ctx);
+  if (!z || !y) return set_error(PDG_EINVAL, "null vector");
+  if (!is_device_ptr(z) || !is_device_ptr(y))
+    return set_error(PDG_EINVAL, "pdg_jacobian_apply_transpose_f32 takes device pointers");
+  return op_launch<float>(ctx, z, y, nullptr, 1.f, 1, 1, nullptr);
 }
 
 int pdg_prec_setup(pdg_context *ctx, int kind, int precision) {

@@ -804,6 +804,423 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS, 5)
         (double)part, 0.0, a.dot_fin, -1, -1, reinterpret_cast<double *>(YH));
 }
 
+// ---------------------------------------------------------------------------
+// Q3 kernel with phase-aliased shared memory (the TMA path of coupled
+// applies).  Same staging and the same arithmetic as k_apply32_q3, with the
+// address arithmetic and the data exchanges reorganised:
+//  * record of 84 floats per cell (A'_x, A'_y, A'_z row-major, the five
+//    coupling coefficients of each face, zero where the face has no
+//    neighbour, 6 floats of padding) read as 16-byte vectors; the neighbour
+//    couplings need no per-face predicates;
+//  * the swizzled row of (cell c, plane z, row y) is
+//      16c + 8(z>>1) + 4((z&1) ^ ((c>>1)&1)) + ((2(c&1) | (z>>1)) ^ y)
+//    (the 128-byte pattern written out), so a thread forms each of its
+//    stage-1 addresses once from its cell and plane;
+//  * after stage 1 the staged runs are dead and their space holds three
+//    unswizzled arrays [cell][plane][row]: the cell values U, the P planes,
+//    and the z-face terms already combined per plane (thread y of a cell
+//    forms the terms of the face points of row y for all four planes);
+//  * the odd strides (21 rows of 16 bytes per cell, in the arrays and the
+//    records; 5 rows per plane) put the 8 cells of a warp on 8 different
+//    16-byte bank groups: the loads that the 4 threads of a cell share are
+//    one wavefront, and the plane-per-thread accesses four;
+//  * each thread stores its own plane (64 contiguous bytes) with two 32-byte
+//    vector stores, so no staging of the result;
+//  * operator direction as a template parameter.
+// ---------------------------------------------------------------------------
+struct Q3T {
+  static constexpr int N = 4, N2 = 16, NB = 64, CPB = 32, THREADS = 128, REC = 84;
+  // phase 1 (TMA): own run with one halo cell each side, the y-neighbour
+  // runs (128-byte swizzle, 1024-byte aligned), the records
+  static constexpr int OWN_B = 0, YL_B = 9216, YH_B = YL_B + CPB * 256,
+                       REC_B = YH_B + CPB * 256, P1_END = REC_B + CPB * REC * 4;
+  // phase 2: [cell][plane][row] float4 arrays, 21 rows per cell, 5 per plane
+  static constexpr int CR = 21, PR = 5, ARR = CPB * CR * 16;
+  static constexpr int U_B = 0, PS_B = ARR, FS_B = 2 * ARR, P2_END = 3 * ARR;
+  static constexpr int SMEM = 1024 + P1_END;
+  static constexpr int LINES_OWN = (CPB + 2) * 2, LINES_RUN = CPB * 2;
+  static_assert((CPB + 2) * 256 <= YL_B, "own run overlaps the y runs");
+  static_assert(P2_END + 2 * THREADS * 8 <= P1_END,
+                "phase-2 arrays and the block-sum scratch must fit the phase-1 space");
+  static_assert(LINES_OWN == Q3Cfg::LINES_OWN && LINES_RUN == Q3Cfg::LINES_RUN,
+                "tensor maps are shared with k_apply32_q3");
+};
+
+// byte offset of row y of plane z of cell c in a swizzled run buffer
+__device__ __forceinline__ unsigned q3_swz_row(int c, int z, int y) {
+  return 16u * (unsigned)(16 * c + 8 * (z >> 1) + 4 * ((z & 1) ^ ((c >> 1) & 1)) +
+                          ((2 * (c & 1) | (z >> 1)) ^ y));
+}
+// byte offset of row y of plane q of cell c in a phase-2 array
+__device__ __forceinline__ unsigned q3_pad_row(int c, int q, int y) {
+  return 16u * (unsigned)(Q3T::CR * c + Q3T::PR * q + y);
+}
+__device__ __forceinline__ float4 sh4(const unsigned char *b, unsigned off) {
+  return *reinterpret_cast<const float4 *>(b + off);
+}
+__device__ __forceinline__ void st4(unsigned char *b, unsigned off, float4 v) {
+  *reinterpret_cast<float4 *>(b + off) = v;
+}
+__device__ __forceinline__ float f4c(const float4 &v, int i) {
+  return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+// 32-byte global vector accesses (32-byte aligned addresses)
+__device__ __forceinline__ void ld8(const float *p, float *w) {
+  asm volatile("ld.global.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(w[0]), "=f"(w[1]), "=f"(w[2]), "=f"(w[3]), "=f"(w[4]), "=f"(w[5]),
+                 "=f"(w[6]), "=f"(w[7])
+               : "l"(p));
+}
+__device__ __forceinline__ void st8(float *p, const float *w) {
+  asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(w[0]),
+               "f"(w[1]), "f"(w[2]), "f"(w[3]), "f"(w[4]), "f"(w[5]), "f"(w[6]), "f"(w[7])
+               : "memory");
+}
+
+// coupling of a neighbour trace (val, dv) on a lower (hi = false) or upper
+// face; cf = {hp ke, hp ko, hp pen, th hp ke, th hp ko} (zero without a
+// neighbour)
+template <bool kTr>
+__device__ __forceinline__ void q3_face(const float *cf, bool hi, float val, float dv, float &s1,
+                                        float &s2) {
+  if constexpr (!kTr) {
+    s1 = (hi ? -cf[1] : cf[1]) * dv - cf[2] * val;
+    s2 = (hi ? -cf[3] : cf[3]) * val;
+  } else {
+    s1 = (hi ? cf[4] : -cf[4]) * dv - cf[2] * val;
+    s2 = (hi ? cf[0] : -cf[0]) * val;
+  }
+}
+
+// records of k_apply32_q3t from the 78-float records: padded to 84 floats,
+// the coupling coefficients of faces without a neighbour zeroed
+__global__ void k_record_q3t(const OpParams<float> p, const float *__restrict__ rec,
+                             float *__restrict__ out) {
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.ncell) return;
+  int ix[3];
+  coords32(p, (unsigned)e, ix);
+  const float *r = rec + e * Q3Cfg::REC;
+  float *o = out + e * Q3T::REC;
+  for (int i = 0; i < 3 * Q3T::N2; i++) o[i] = r[i];
+  for (int f = 0; f < 6; f++) {
+    const int d = f >> 1;
+    const bool has = (f & 1) ? ix[d] + 1 < p.nc[d] : ix[d] > 0;
+    for (int j = 0; j < 5; j++) o[3 * Q3T::N2 + 5 * f + j] = has ? r[3 * Q3T::N2 + 5 * f + j] : 0.f;
+  }
+  for (int i = 78; i < Q3T::REC; i++) o[i] = 0.f;
+}
+
+// blocks per SM the register allocation is sized for
+#ifndef Q3T_MINB
+#define Q3T_MINB 5
+#endif
+template <bool kTr>
+__global__ void __launch_bounds__(Q3T::THREADS, Q3T_MINB)
+    k_apply32_q3t(const OpParams<float> p, const ApplyArgs<float> a, const float *__restrict__ rec,
+                  const EdgeTab tb, const __grid_constant__ CUtensorMap map_own,
+                  const __grid_constant__ CUtensorMap map_run, int *tma_err) {
+  using C = Q3T;
+  constexpr int N = 4, NB = 64, CPB = C::CPB, REC = C::REC;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ __align__(8) unsigned long long stage_bar;
+  if (a.skip && *a.skip) return;
+  // 1024-byte aligned base, kept in the shared window
+  unsigned char *base = smraw + ((1024u - (smem_u32(smraw) & 1023u)) & 1023u);
+
+  const long e0 = (long)blockIdx.x * CPB;
+  const long ncell = p.ncell;
+  const long sx = p.nc[0], sxy = (long)p.nc[0] * p.nc[1];
+  const float *__restrict__ x = a.x;
+  const int t = threadIdx.x, cs = t >> 2, z = t & 3;
+  const long e = e0 + cs;
+  const long ee = e < ncell ? e : 0;
+  int ix[3];
+  coords32(p, (unsigned)ee, ix);
+  // z-neighbour rows (plane q, row y = z) straight from global memory, issued
+  // before the staging wait; zero where the cell has no z neighbour
+  float4 zl[N], zh[N];
+  {
+    const bool lo = ix[2] > 0, hi = ix[2] + 1 < p.nc[2];
+    const float4 *pl = reinterpret_cast<const float4 *>(x + (ee - (lo ? sxy : 0)) * NB + z * N);
+    const float4 *ph = reinterpret_cast<const float4 *>(x + (ee + (hi ? sxy : 0)) * NB + z * N);
+#pragma unroll
+    for (int q = 0; q < N; q++) {
+      zl[q] = lo ? pl[q * 4] : make_float4(0.f, 0.f, 0.f, 0.f);
+      zh[q] = hi ? ph[q * 4] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+
+  {
+    const unsigned bar = smem_u32(&stage_bar);
+    const long ncp = ncell - e0 < CPB ? ncell - e0 : CPB;
+    const unsigned rbytes = (unsigned)(ncp * REC * 4);
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_expect_tx(bar, (unsigned)(C::LINES_OWN + 2 * C::LINES_RUN) * 128u + rbytes);
+      tma_load_2d(smem_u32(base + C::OWN_B), &map_own, 0, (int)((e0 - 1) * 2), bar);
+      tma_load_2d(smem_u32(base + C::YL_B), &map_run, 0, (int)((e0 - sx) * 2), bar);
+      tma_load_2d(smem_u32(base + C::YH_B), &map_run, 0, (int)((e0 + sx) * 2), bar);
+      bulk_load(smem_u32(base + C::REC_B), rec + e0 * REC, rbytes, bar);
+    }
+    if (!mbar_wait(bar, 0, kTmaPolls)) {
+      if (threadIdx.x == 0) atomicExch(tma_err, 1);
+      mbar_wait(bar, 0, kTmaPolls);
+      return;
+    }
+  }
+
+  const unsigned char *R = base + C::REC_B + cs * REC * 4;
+  auto rec4 = [&](int i) -> float4 { return sh4(R, 16u * i); };
+  // coupling coefficients: floats 48..77 of the record
+  float cf[32];
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const float4 v = rec4(12 + i);
+    cf[4 * i] = v.x; cf[4 * i + 1] = v.y; cf[4 * i + 2] = v.z; cf[4 * i + 3] = v.w;
+  }
+  // row z (column z for the transpose) of A'_z, for stage 2
+  float az[N];
+  if constexpr (!kTr) {
+    const float4 v = sh4(R, 128u + 16u * z);
+    az[0] = v.x; az[1] = v.y; az[2] = v.z; az[3] = v.w;
+  } else {
+#pragma unroll
+    for (int q = 0; q < N; q++) az[q] = *reinterpret_cast<const float *>(R + 128u + 16u * q + 4u * z);
+  }
+
+  // ---- stage 1: plane z ----
+  const unsigned char *OWN = base + C::OWN_B;
+  float u[N][N];
+#pragma unroll
+  for (int y = 0; y < N; y++) {
+    const float4 v = sh4(OWN, q3_swz_row(cs + 1, z, y));
+    u[y][0] = v.x; u[y][1] = v.y; u[y][2] = v.z; u[y][3] = v.w;
+  }
+  float P[N][N];
+  {
+    // x: X = A'_x u + x-face terms, P = Mhat_y X
+    float X[N][N];
+    float4 A[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) A[i] = rec4(i);
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      const float4 l = sh4(OWN, q3_swz_row(cs, z, y));
+      const float4 h = sh4(OWN, q3_swz_row(cs + 2, z, y));
+      const float dvl = tb.d1[0] * l.x + tb.d1[1] * l.y + tb.d1[2] * l.z + tb.d1[3] * l.w;
+      const float dvh = tb.d0[0] * h.x + tb.d0[1] * h.y + tb.d0[2] * h.z + tb.d0[3] * h.w;
+      float s1l, s2l, s1h, s2h;
+      q3_face<kTr>(cf + 0, false, l.w, dvl, s1l, s2l);
+      q3_face<kTr>(cf + 5, true, h.x, dvh, s1h, s2h);
+#pragma unroll
+      for (int xx = 0; xx < N; xx++) {
+        float s = tb.d0[xx] * s2l + tb.d1[xx] * s2h;
+        if (xx == 0) s += s1l;
+        if (xx == N - 1) s += s1h;
+#pragma unroll
+        for (int q = 0; q < N; q++)
+          s += (kTr ? f4c(A[q], xx) : f4c(A[xx], q)) * u[y][q];
+        X[y][xx] = s;
+      }
+    }
+#pragma unroll
+    for (int y = 0; y < N; y++)
+#pragma unroll
+      for (int xx = 0; xx < N; xx++) {
+        float s = 0.f;
+#pragma unroll
+        for (int r = 0; r < N; r++) s += tb.M[y * N + r] * X[r][xx];
+        P[y][xx] = s;
+      }
+  }
+  {
+    // y: Y = A'_y u + y-face terms, P += Mhat_x Y
+    float Y[N][N];
+    float4 A[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) A[i] = rec4(4 + i);
+    float s1l[N], s2l[N], s1h[N], s2h[N];
+    {
+      float4 yl[N], yh[N];
+#pragma unroll
+      for (int y = 0; y < N; y++) {
+        yl[y] = sh4(base + C::YL_B, q3_swz_row(cs, z, y));
+        yh[y] = sh4(base + C::YH_B, q3_swz_row(cs, z, y));
+      }
+#pragma unroll
+      for (int xx = 0; xx < N; xx++) {
+        float dvl = 0.f, dvh = 0.f;
+#pragma unroll
+        for (int q = 0; q < N; q++) {
+          dvl += tb.d1[q] * f4c(yl[q], xx);
+          dvh += tb.d0[q] * f4c(yh[q], xx);
+        }
+        q3_face<kTr>(cf + 10, false, f4c(yl[N - 1], xx), dvl, s1l[xx], s2l[xx]);
+        q3_face<kTr>(cf + 15, true, f4c(yh[0], xx), dvh, s1h[xx], s2h[xx]);
+      }
+    }
+#pragma unroll
+    for (int y = 0; y < N; y++)
+#pragma unroll
+      for (int xx = 0; xx < N; xx++) {
+        float s = tb.d0[y] * s2l[xx] + tb.d1[y] * s2h[xx];
+        if (y == 0) s += s1l[xx];
+        if (y == N - 1) s += s1h[xx];
+#pragma unroll
+        for (int q = 0; q < N; q++)
+          s += (kTr ? f4c(A[q], y) : f4c(A[y], q)) * u[q][xx];
+        Y[y][xx] = s;
+      }
+#pragma unroll
+    for (int y = 0; y < N; y++)
+#pragma unroll
+      for (int xx = 0; xx < N; xx++) {
+        float s = P[y][xx];
+#pragma unroll
+        for (int r = 0; r < N; r++) s += tb.M[xx * N + r] * Y[y][r];
+        P[y][xx] = s;
+      }
+  }
+  // z faces at the face points of row y = z, combined for each plane w:
+  //   F_w = [w = 0] s1 lo + d0[w] s2 lo + [w = N-1] s1 hi + d1[w] s2 hi
+  float F[N][N];
+  {
+    float s1l[N], s2l[N], s1h[N], s2h[N];
+#pragma unroll
+    for (int xx = 0; xx < N; xx++) {
+      float dvl = 0.f, dvh = 0.f;
+#pragma unroll
+      for (int q = 0; q < N; q++) {
+        dvl += tb.d1[q] * f4c(zl[q], xx);
+        dvh += tb.d0[q] * f4c(zh[q], xx);
+      }
+      q3_face<kTr>(cf + 20, false, f4c(zl[N - 1], xx), dvl, s1l[xx], s2l[xx]);
+      q3_face<kTr>(cf + 25, true, f4c(zh[0], xx), dvh, s1h[xx], s2h[xx]);
+    }
+#pragma unroll
+    for (int w = 0; w < N; w++)
+#pragma unroll
+      for (int xx = 0; xx < N; xx++) {
+        float s = tb.d0[w] * s2l[xx] + tb.d1[w] * s2h[xx];
+        if (w == 0) s += s1l[xx];
+        if (w == N - 1) s += s1h[xx];
+        F[w][xx] = s;
+      }
+  }
+  // every thread has read the staged runs and records: phase-2 arrays
+  __syncthreads();
+  unsigned char *U = base + C::U_B, *PS = base + C::PS_B, *FS = base + C::FS_B;
+#pragma unroll
+  for (int y = 0; y < N; y++) {
+    st4(U, q3_pad_row(cs, z, y), make_float4(u[y][0], u[y][1], u[y][2], u[y][3]));
+    st4(PS, q3_pad_row(cs, z, y), make_float4(P[y][0], P[y][1], P[y][2], P[y][3]));
+  }
+#pragma unroll
+  for (int w = 0; w < N; w++)
+    st4(FS, q3_pad_row(cs, w, z), make_float4(F[w][0], F[w][1], F[w][2], F[w][3]));
+  __syncthreads();
+
+  // ---- stage 2: z contractions of plane z ----
+  float out[N][N];
+  {
+    float Zp[N][N];
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      float4 acc = sh4(FS, q3_pad_row(cs, z, y));
+#pragma unroll
+      for (int q = 0; q < N; q++) {
+        const float4 v = sh4(U, q3_pad_row(cs, q, y));
+        acc.x += az[q] * v.x; acc.y += az[q] * v.y; acc.z += az[q] * v.z; acc.w += az[q] * v.w;
+      }
+      Zp[y][0] = acc.x; Zp[y][1] = acc.y; Zp[y][2] = acc.z; Zp[y][3] = acc.w;
+    }
+    float T1[N][N];   // Mhat_x along x
+#pragma unroll
+    for (int y = 0; y < N; y++)
+#pragma unroll
+      for (int xx = 0; xx < N; xx++) {
+        float s = 0.f;
+#pragma unroll
+        for (int r = 0; r < N; r++) s += tb.M[xx * N + r] * Zp[y][r];
+        T1[y][xx] = s;
+      }
+    float mz[N];
+#pragma unroll
+    for (int q = 0; q < N; q++) mz[q] = tb.M[z * N + q];
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < N; q++) {
+        const float4 v = sh4(PS, q3_pad_row(cs, q, y));
+        acc.x += mz[q] * v.x; acc.y += mz[q] * v.y; acc.z += mz[q] * v.z; acc.w += mz[q] * v.w;
+      }
+#pragma unroll
+      for (int r = 0; r < N; r++) {
+        const float m = tb.M[y * N + r];
+        acc.x += m * T1[r][0]; acc.y += m * T1[r][1]; acc.z += m * T1[r][2]; acc.w += m * T1[r][3];
+      }
+      out[y][0] = acc.x; out[y][1] = acc.y; out[y][2] = acc.z; out[y][3] = acc.w;
+    }
+  }
+
+  // ---- write-back: the thread's plane, 64 contiguous bytes ----
+  float part = 0.f;
+  if (e < ncell) {
+    const float alpha = a.alpha;
+    float v[NB / N];
+#pragma unroll
+    for (int y = 0; y < N; y++)
+#pragma unroll
+      for (int xx = 0; xx < N; xx++) v[y * N + xx] = alpha * out[y][xx];
+    float *yp = a.y + e * NB + z * 16;
+    const float *ap = a.add ? a.add + e * NB + z * 16 : nullptr;
+    if (((reinterpret_cast<uintptr_t>(yp) | reinterpret_cast<uintptr_t>(ap)) & 31) == 0) {
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        float *d = yp + 8 * h;
+        if (a.accumulate) {
+          float w[8];
+          ld8(d, w);
+#pragma unroll
+          for (int j = 0; j < 8; j++) v[8 * h + j] += w[j];
+        }
+        if (ap) {
+          float w[8];
+          ld8(ap + 8 * h, w);
+#pragma unroll
+          for (int j = 0; j < 8; j++) v[8 * h + j] += w[j];
+        }
+        st8(d, v + 8 * h);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        float r = v[j];
+        if (a.accumulate) r += yp[j];
+        if (ap) r += ap[j];
+        yp[j] = r;
+        v[j] = r;
+      }
+    }
+    if (a.dot_part) {
+#pragma unroll
+      for (int y = 0; y < N; y++) {
+        const float4 pin = sh4(U, q3_pad_row(cs, z, y));
+        part += pin.x * v[4 * y] + pin.y * v[4 * y + 1] + pin.z * v[4 * y + 2] + pin.w * v[4 * y + 3];
+      }
+    }
+  }
+  // block sums in the phase-1 space past the phase-2 arrays (record space,
+  // dead since stage 1; other warps may still read the arrays)
+  if (a.dot_part)
+    reduce_tail_grouped<Q3T::THREADS, true>(
+        a.dot_part, a.dot_max_blocks, a.dot_cnt, RedCtx{nullptr, a.dot_scal, a.dot_flags},
+        (double)part, 0.0, a.dot_fin, -1, -1, reinterpret_cast<double *>(base + C::P2_END));
+}
+
 static EdgeTab make_edge_tab_uncached(const pdg_context *ctx) {
   EdgeTab t{};
   const RhsTables r = make_rhs_tables(ctx);
@@ -939,6 +1356,33 @@ static int launch32_q3(pdg_context *ctx, const ApplyArgs<float> &a, const OpPara
   // TMA needs a 16-byte aligned vector (and records, from cudaMalloc)
   if ((reinterpret_cast<uintptr_t>(a.x) & 15) == 0 && (reinterpret_cast<uintptr_t>(rec) & 15) == 0 &&
       lines_maps(a.x, ctx->ndof, &own, &run)) {
+    if (!a.diag_only) {
+      static_assert(Q3T::CPB == Q3Cfg::CPB, "one block per run of CPB cells");
+      if (!ctx->rec32q_valid) {
+        if (!ctx->rec32q)
+          PDG_CUDA_TRY(cudaMalloc(&ctx->rec32q, sizeof(float) * Q3T::REC * ctx->ncell));
+        k_record_q3t<<<(unsigned)((ctx->ncell + 127) / 128), 128, 0, ctx->stream>>>(p, rec,
+                                                                                   ctx->rec32q);
+        PDG_CUDA_TRY(cudaGetLastError());
+        ctx->rec32q_valid = 1;
+      }
+      static int attr_t = -1;
+      if (attr_t != ctx->device) {
+        PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply32_q3t<false>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, Q3T::SMEM));
+        PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply32_q3t<true>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, Q3T::SMEM));
+        attr_t = ctx->device;
+      }
+      if (a.transpose)
+        k_apply32_q3t<true><<<blocks, Q3T::THREADS, Q3T::SMEM, ctx->stream>>>(
+            p, a, ctx->rec32q, tb, *own, *run, err);
+      else
+        k_apply32_q3t<false><<<blocks, Q3T::THREADS, Q3T::SMEM, ctx->stream>>>(
+            p, a, ctx->rec32q, tb, *own, *run, err);
+      PDG_CUDA_TRY(cudaGetLastError());
+      return PDG_OK;
+    }
     k_apply32_q3<true><<<blocks, Q3Cfg::THREADS, smem, ctx->stream>>>(p, a, rec, tb, *own, *run,
                                                                       err);
   } else {

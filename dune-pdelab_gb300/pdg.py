@@ -139,6 +139,7 @@ _SIGS = {
     "pdg_residual": (C.c_int, [_vp, _vp, _vp]),
     "pdg_jacobian_apply": (C.c_int, [_vp, _vp, _vp]),
     "pdg_jacobian_apply_f32": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_jacobian_apply_transpose_f32": (C.c_int, [_vp, _vp, _vp]),
     "pdg_jacobian_apply_transpose": (C.c_int, [_vp, _vp, _vp]),
     "pdg_apply": (C.c_int, [_vp, _vp, _vp]),
     "pdg_applyscaleadd": (C.c_int, [_vp, C.c_double, _vp, _vp]),
@@ -462,6 +463,13 @@ class GridOperator:
     def jacobian_apply_f32(self, z, y):
         """y += J z in FP32 (device tensors)"""
         _check(load().pdg_jacobian_apply_f32(self._h, _ptr(z, np.float32), _ptr(y, np.float32)))
+        return y
+
+    @_stream_ordered
+    def jacobian_apply_transpose_f32(self, z, y):
+        """y += J^T z in FP32 (device tensors)"""
+        _check(load().pdg_jacobian_apply_transpose_f32(self._h, _ptr(z, np.float32),
+                                                       _ptr(y, np.float32)))
         return y
 
     @_stream_ordered

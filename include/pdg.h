@@ -312,6 +312,9 @@ int pdg_jacobian_apply_f32(pdg_context *ctx, const float *z, float *y);
 /* Transposed apply y += J^T z (adjoint; no reference counterpart, derived
    from jacobian_skeleton's sn/ns blocks, convectiondiffusiondg.hh:483-669) */
 int pdg_jacobian_apply_transpose(pdg_context *ctx, const double *z, double *y);
+/* Same in FP32, device pointers (the transposed inner operator of the
+   mixed-precision adjoint solve) */
+int pdg_jacobian_apply_transpose_f32(pdg_context *ctx, const float *z, float *y);
 /* OnTheFlyOperator::apply(x, y): y = J x
    (backend/istl/seqistlsolverbackend.hh:66-76) */
 int pdg_apply(pdg_context *ctx, const double *x, double *y);

@@ -158,6 +158,31 @@ def test_jacobian_apply_f32_staged(pdg, oracle, k, nc, method, weights, react, b
     assert _rel(yt.cpu().double().numpy(), ref) <= TOL32
 
 
+@pytest.mark.parametrize("k,nc,method,weights,react,bct", [
+    (1, (7, 6, 5), 1, 0, True, None),
+    (2, (9, 5, 4), 2, 1, True, [1, -1, 1, -2, -1, 1]),
+    (3, (11, 4, 3), 0, 1, False, None),
+    (3, (13, 7, 5), 1, 0, True, [1, -1, -2, 1, 1, -1]),
+    (3, (33, 2, 3), 2, 1, False, None),
+    (3, (1, 1, 1), 1, 0, False, None),
+    (3, (5, 9, 11), 0, 0, True, None),
+])
+def test_jacobian_apply_transpose_f32_staged(pdg, oracle, k, nc, method, weights, react, bct):
+    # the transposed FP32 operator (inner operator of the mixed adjoint solve)
+    # against the oracle's matrix-free transpose
+    import torch
+    go, P, rng = _pair(pdg, oracle, 3, k, nc, seed=57 + k, method=method, weights=weights,
+                       bctype=bct, react=react)
+    x = rng.uniform(-1, 1, go.ndof)
+    y0 = rng.uniform(-1, 1, go.ndof)
+    xt = torch.tensor(x, dtype=torch.float32, device="cuda")
+    yt = torch.tensor(y0, dtype=torch.float32, device="cuda")
+    go.jacobian_apply_transpose_f32(xt, yt)     # accumulates: y0 + J^T x
+    torch.cuda.synchronize()
+    ref = y0 + P.jacobian_apply_transpose(x)
+    assert _rel(yt.cpu().double().numpy(), ref) <= TOL32
+
+
 def test_device_pointers_match_host(pdg, oracle):
     import torch
     go, P, rng = _pair(pdg, oracle, 3, 3, 3, seed=4)
