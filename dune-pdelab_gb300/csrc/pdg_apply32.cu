@@ -27,6 +27,7 @@
 // The output is staged in shared memory and written back coalesced.
 #include <cuda.h>
 
+#include <cstddef>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -808,7 +809,7 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS, 5)
 // Q3 kernel with phase-aliased shared memory (the TMA path of coupled
 // applies).  Same staging and the same arithmetic as k_apply32_q3, with the
 // address arithmetic and the data exchanges reorganised:
-//  * record of 84 floats per cell (A'_x, A'_y, A'_z row-major, the five
+//  * record of 84 floats per cell (A'_x column-major, A'_y, A'_z row-major, the five
 //    coupling coefficients of each face, zero where the face has no
 //    neighbour, 6 floats of padding) read as 16-byte vectors; the neighbour
 //    couplings need no per-face predicates;
@@ -826,6 +827,11 @@ __global__ void __launch_bounds__(Q3Cfg::THREADS, 5)
 //    one wavefront, and the plane-per-thread accesses four;
 //  * each thread stores its own plane (64 contiguous bytes) with two 32-byte
 //    vector stores, so no staging of the result;
+//  * rows are held as pairs (x0, x1), (x2, x3) and every contraction runs as
+//    paired FP32 multiply-adds (one instruction for two lanes, the scalar
+//    factor broadcast): along x the pair is a column pair of the 1D matrix,
+//    along y and z a row pair of the data.  The FP32 instructions per thread
+//    fall from about 830 to 430 (ncu instruction counts at 80^3 Q3);
 //  * operator direction as a template parameter.
 // ---------------------------------------------------------------------------
 struct Q3T {
@@ -877,6 +883,23 @@ __device__ __forceinline__ void st8(float *p, const float *w) {
                : "memory");
 }
 
+// paired FP32 arithmetic (one instruction for two lanes; a scalar operand
+// is broadcast to both)
+__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+
+// 1D tables of the Q3 kernel (kernel parameter space), with the pairs its
+// paired multiply-adds take as operands
+struct Q3Tab {
+  float M[16];         // Mhat row-major
+  float d0[4], d1[4];  // basis derivatives at 0 and 1
+  float2 MTp[4][2];    // MTp[c][h] = (Mhat[2h][c], Mhat[2h+1][c])
+  float2 d0p[2], d1p[2];
+};
+static_assert(offsetof(Q3Tab, MTp) % 8 == 0, "pairs must be 8-byte aligned");
+
 // coupling of a neighbour trace (val, dv) on a lower (hi = false) or upper
 // face; cf = {hp ke, hp ko, hp pen, th hp ke, th hp ko} (zero without a
 // neighbour)
@@ -892,8 +915,26 @@ __device__ __forceinline__ void q3_face(const float *cf, bool hi, float val, flo
   }
 }
 
-// records of k_apply32_q3t from the 78-float records: padded to 84 floats,
-// the coupling coefficients of faces without a neighbour zeroed
+// the same for two face points at once
+template <bool kTr>
+__device__ __forceinline__ void q3_face2(const float *cf, bool hi, float2 val, float2 dv, float2 &s1,
+                                         float2 &s2) {
+  if constexpr (!kTr) {
+    s1 = ffma2(bc2(hi ? -cf[1] : cf[1]), dv, fmul2(bc2(-cf[2]), val));
+    s2 = fmul2(bc2(hi ? -cf[3] : cf[3]), val);
+  } else {
+    s1 = ffma2(bc2(hi ? cf[4] : -cf[4]), dv, fmul2(bc2(-cf[2]), val));
+    s2 = fmul2(bc2(hi ? cf[0] : -cf[0]), val);
+  }
+}
+
+// records of k_apply32_q3t from the 78-float records (computed in FP64,
+// rounded): padded to 84 floats, A'_x transposed (its columns are the pairs
+// of the x contraction), the coupling coefficients of faces without a
+// neighbour zeroed.  Records built in the kernel from K in FP32 instead cost
+// more time than their copy (272 against 217 us at 96^3) and, less
+// accurate, took the mixed solve of the 96^3 Q3 problem from 5,533 to 7,885
+// inner iterations.
 __global__ void k_record_q3t(const OpParams<float> p, const float *__restrict__ rec,
                              float *__restrict__ out) {
   const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -902,7 +943,9 @@ __global__ void k_record_q3t(const OpParams<float> p, const float *__restrict__ 
   coords32(p, (unsigned)e, ix);
   const float *r = rec + e * Q3Cfg::REC;
   float *o = out + e * Q3T::REC;
-  for (int i = 0; i < 3 * Q3T::N2; i++) o[i] = r[i];
+  for (int i = 0; i < 4; i++)
+    for (int q = 0; q < 4; q++) o[q * 4 + i] = r[i * 4 + q];
+  for (int i = Q3T::N2; i < 3 * Q3T::N2; i++) o[i] = r[i];
   for (int f = 0; f < 6; f++) {
     const int d = f >> 1;
     const bool has = (f & 1) ? ix[d] + 1 < p.nc[d] : ix[d] > 0;
@@ -918,7 +961,7 @@ __global__ void k_record_q3t(const OpParams<float> p, const float *__restrict__ 
 template <bool kTr>
 __global__ void __launch_bounds__(Q3T::THREADS, Q3T_MINB)
     k_apply32_q3t(const OpParams<float> p, const ApplyArgs<float> a, const float *__restrict__ rec,
-                  const EdgeTab tb, const __grid_constant__ CUtensorMap map_own,
+                  const Q3Tab tb, const __grid_constant__ CUtensorMap map_own,
                   const __grid_constant__ CUtensorMap map_run, int *tma_err) {
   using C = Q3T;
   constexpr int N = 4, NB = 64, CPB = C::CPB, REC = C::REC;
@@ -990,19 +1033,20 @@ __global__ void __launch_bounds__(Q3T::THREADS, Q3T_MINB)
     for (int q = 0; q < N; q++) az[q] = *reinterpret_cast<const float *>(R + 128u + 16u * q + 4u * z);
   }
 
-  // ---- stage 1: plane z ----
+  // ---- stage 1: plane z, rows as pairs (x0, x1), (x2, x3) ----
   const unsigned char *OWN = base + C::OWN_B;
-  float u[N][N];
+  float2 u[N][2];
 #pragma unroll
   for (int y = 0; y < N; y++) {
     const float4 v = sh4(OWN, q3_swz_row(cs + 1, z, y));
-    u[y][0] = v.x; u[y][1] = v.y; u[y][2] = v.z; u[y][3] = v.w;
+    u[y][0] = make_float2(v.x, v.y);
+    u[y][1] = make_float2(v.z, v.w);
   }
-  float P[N][N];
+  float2 P[N][2];
   {
     // x: X = A'_x u + x-face terms, P = Mhat_y X
-    float X[N][N];
-    float4 A[N];
+    float2 X[N][2];
+    float4 A[N];   // A[i] = column i of A'_x
 #pragma unroll
     for (int i = 0; i < N; i++) A[i] = rec4(i);
 #pragma unroll
@@ -1014,99 +1058,112 @@ __global__ void __launch_bounds__(Q3T::THREADS, Q3T_MINB)
       float s1l, s2l, s1h, s2h;
       q3_face<kTr>(cf + 0, false, l.w, dvl, s1l, s2l);
       q3_face<kTr>(cf + 5, true, h.x, dvh, s1h, s2h);
+      // [xx = 0] s1l + d0[xx] s2l + [xx = N-1] s1h + d1[xx] s2h
+      X[y][0] = ffma2(tb.d1p[0], bc2(s2h), ffma2(tb.d0p[0], bc2(s2l), make_float2(s1l, 0.f)));
+      X[y][1] = ffma2(tb.d1p[1], bc2(s2h), ffma2(tb.d0p[1], bc2(s2l), make_float2(0.f, s1h)));
 #pragma unroll
-      for (int xx = 0; xx < N; xx++) {
-        float s = tb.d0[xx] * s2l + tb.d1[xx] * s2h;
-        if (xx == 0) s += s1l;
-        if (xx == N - 1) s += s1h;
-#pragma unroll
-        for (int q = 0; q < N; q++)
-          s += (kTr ? f4c(A[q], xx) : f4c(A[xx], q)) * u[y][q];
-        X[y][xx] = s;
+      for (int q = 0; q < N; q++) {
+        const float uq = q < 2 ? (q == 0 ? u[y][0].x : u[y][0].y) : (q == 2 ? u[y][1].x : u[y][1].y);
+        if constexpr (!kTr) {
+          X[y][0] = ffma2(make_float2(A[q].x, A[q].y), bc2(uq), X[y][0]);
+          X[y][1] = ffma2(make_float2(A[q].z, A[q].w), bc2(uq), X[y][1]);
+        } else {
+          X[y][0] = ffma2(make_float2(f4c(A[0], q), f4c(A[1], q)), bc2(uq), X[y][0]);
+          X[y][1] = ffma2(make_float2(f4c(A[2], q), f4c(A[3], q)), bc2(uq), X[y][1]);
+        }
       }
     }
 #pragma unroll
     for (int y = 0; y < N; y++)
 #pragma unroll
-      for (int xx = 0; xx < N; xx++) {
-        float s = 0.f;
+      for (int hh = 0; hh < 2; hh++) {
+        float2 s = fmul2(bc2(tb.M[y * N]), X[0][hh]);
 #pragma unroll
-        for (int r = 0; r < N; r++) s += tb.M[y * N + r] * X[r][xx];
-        P[y][xx] = s;
+        for (int r = 1; r < N; r++) s = ffma2(bc2(tb.M[y * N + r]), X[r][hh], s);
+        P[y][hh] = s;
       }
   }
   {
     // y: Y = A'_y u + y-face terms, P += Mhat_x Y
-    float Y[N][N];
-    float4 A[N];
-#pragma unroll
-    for (int i = 0; i < N; i++) A[i] = rec4(4 + i);
-    float s1l[N], s2l[N], s1h[N], s2h[N];
+    float2 s1l[2], s2l[2], s1h[2], s2h[2];
     {
-      float4 yl[N], yh[N];
+      float2 yl[N][2], yh[N][2];
 #pragma unroll
       for (int y = 0; y < N; y++) {
-        yl[y] = sh4(base + C::YL_B, q3_swz_row(cs, z, y));
-        yh[y] = sh4(base + C::YH_B, q3_swz_row(cs, z, y));
+        const float4 l = sh4(base + C::YL_B, q3_swz_row(cs, z, y));
+        const float4 h = sh4(base + C::YH_B, q3_swz_row(cs, z, y));
+        yl[y][0] = make_float2(l.x, l.y); yl[y][1] = make_float2(l.z, l.w);
+        yh[y][0] = make_float2(h.x, h.y); yh[y][1] = make_float2(h.z, h.w);
       }
 #pragma unroll
-      for (int xx = 0; xx < N; xx++) {
-        float dvl = 0.f, dvh = 0.f;
+      for (int hh = 0; hh < 2; hh++) {
+        float2 dvl = fmul2(bc2(tb.d1[0]), yl[0][hh]), dvh = fmul2(bc2(tb.d0[0]), yh[0][hh]);
 #pragma unroll
-        for (int q = 0; q < N; q++) {
-          dvl += tb.d1[q] * f4c(yl[q], xx);
-          dvh += tb.d0[q] * f4c(yh[q], xx);
+        for (int q = 1; q < N; q++) {
+          dvl = ffma2(bc2(tb.d1[q]), yl[q][hh], dvl);
+          dvh = ffma2(bc2(tb.d0[q]), yh[q][hh], dvh);
         }
-        q3_face<kTr>(cf + 10, false, f4c(yl[N - 1], xx), dvl, s1l[xx], s2l[xx]);
-        q3_face<kTr>(cf + 15, true, f4c(yh[0], xx), dvh, s1h[xx], s2h[xx]);
+        q3_face2<kTr>(cf + 10, false, yl[N - 1][hh], dvl, s1l[hh], s2l[hh]);
+        q3_face2<kTr>(cf + 15, true, yh[0][hh], dvh, s1h[hh], s2h[hh]);
       }
     }
+    const float4 A0 = rec4(4), A1 = rec4(5), A2 = rec4(6), A3 = rec4(7);
 #pragma unroll
-    for (int y = 0; y < N; y++)
+    for (int y = 0; y < N; y++) {
+      float2 Y[2];
 #pragma unroll
-      for (int xx = 0; xx < N; xx++) {
-        float s = tb.d0[y] * s2l[xx] + tb.d1[y] * s2h[xx];
-        if (y == 0) s += s1l[xx];
-        if (y == N - 1) s += s1h[xx];
+      for (int hh = 0; hh < 2; hh++) {
+        float2 s = ffma2(bc2(tb.d1[y]), s2h[hh], fmul2(bc2(tb.d0[y]), s2l[hh]));
+        if (y == 0) s = fadd2(s, s1l[hh]);
+        if (y == N - 1) s = fadd2(s, s1h[hh]);
 #pragma unroll
-        for (int q = 0; q < N; q++)
-          s += (kTr ? f4c(A[q], y) : f4c(A[y], q)) * u[q][xx];
-        Y[y][xx] = s;
+        for (int q = 0; q < N; q++) {
+          // A'_y(y, q), or A'_y(q, y) for the transpose
+          const float4 &Ar = kTr ? (q == 0 ? A0 : q == 1 ? A1 : q == 2 ? A2 : A3)
+                                 : (y == 0 ? A0 : y == 1 ? A1 : y == 2 ? A2 : A3);
+          s = ffma2(bc2(f4c(Ar, kTr ? y : q)), u[q][hh], s);
+        }
+        Y[hh] = s;
       }
+      // P[y][xx] += sum_r Mhat[xx][r] Y[r]
 #pragma unroll
-    for (int y = 0; y < N; y++)
-#pragma unroll
-      for (int xx = 0; xx < N; xx++) {
-        float s = P[y][xx];
-#pragma unroll
-        for (int r = 0; r < N; r++) s += tb.M[xx * N + r] * Y[y][r];
-        P[y][xx] = s;
+      for (int r = 0; r < N; r++) {
+        const float yr = r < 2 ? (r == 0 ? Y[0].x : Y[0].y) : (r == 2 ? Y[1].x : Y[1].y);
+        P[y][0] = ffma2(tb.MTp[r][0], bc2(yr), P[y][0]);
+        P[y][1] = ffma2(tb.MTp[r][1], bc2(yr), P[y][1]);
       }
+    }
   }
   // z faces at the face points of row y = z, combined for each plane w:
   //   F_w = [w = 0] s1 lo + d0[w] s2 lo + [w = N-1] s1 hi + d1[w] s2 hi
-  float F[N][N];
+  float2 F[N][2];
   {
-    float s1l[N], s2l[N], s1h[N], s2h[N];
+    float2 s1l[2], s2l[2], s1h[2], s2h[2];
 #pragma unroll
-    for (int xx = 0; xx < N; xx++) {
-      float dvl = 0.f, dvh = 0.f;
+    for (int hh = 0; hh < 2; hh++) {
+      float2 zl2[N], zh2[N];
 #pragma unroll
       for (int q = 0; q < N; q++) {
-        dvl += tb.d1[q] * f4c(zl[q], xx);
-        dvh += tb.d0[q] * f4c(zh[q], xx);
+        zl2[q] = hh ? make_float2(zl[q].z, zl[q].w) : make_float2(zl[q].x, zl[q].y);
+        zh2[q] = hh ? make_float2(zh[q].z, zh[q].w) : make_float2(zh[q].x, zh[q].y);
       }
-      q3_face<kTr>(cf + 20, false, f4c(zl[N - 1], xx), dvl, s1l[xx], s2l[xx]);
-      q3_face<kTr>(cf + 25, true, f4c(zh[0], xx), dvh, s1h[xx], s2h[xx]);
+      float2 dvl = fmul2(bc2(tb.d1[0]), zl2[0]), dvh = fmul2(bc2(tb.d0[0]), zh2[0]);
+#pragma unroll
+      for (int q = 1; q < N; q++) {
+        dvl = ffma2(bc2(tb.d1[q]), zl2[q], dvl);
+        dvh = ffma2(bc2(tb.d0[q]), zh2[q], dvh);
+      }
+      q3_face2<kTr>(cf + 20, false, zl2[N - 1], dvl, s1l[hh], s2l[hh]);
+      q3_face2<kTr>(cf + 25, true, zh2[0], dvh, s1h[hh], s2h[hh]);
     }
 #pragma unroll
     for (int w = 0; w < N; w++)
 #pragma unroll
-      for (int xx = 0; xx < N; xx++) {
-        float s = tb.d0[w] * s2l[xx] + tb.d1[w] * s2h[xx];
-        if (w == 0) s += s1l[xx];
-        if (w == N - 1) s += s1h[xx];
-        F[w][xx] = s;
+      for (int hh = 0; hh < 2; hh++) {
+        float2 s = ffma2(bc2(tb.d1[w]), s2h[hh], fmul2(bc2(tb.d0[w]), s2l[hh]));
+        if (w == 0) s = fadd2(s, s1l[hh]);
+        if (w == N - 1) s = fadd2(s, s1h[hh]);
+        F[w][hh] = s;
       }
   }
   // every thread has read the staged runs and records: phase-2 arrays
@@ -1114,55 +1171,68 @@ __global__ void __launch_bounds__(Q3T::THREADS, Q3T_MINB)
   unsigned char *U = base + C::U_B, *PS = base + C::PS_B, *FS = base + C::FS_B;
 #pragma unroll
   for (int y = 0; y < N; y++) {
-    st4(U, q3_pad_row(cs, z, y), make_float4(u[y][0], u[y][1], u[y][2], u[y][3]));
-    st4(PS, q3_pad_row(cs, z, y), make_float4(P[y][0], P[y][1], P[y][2], P[y][3]));
+    st4(U, q3_pad_row(cs, z, y), make_float4(u[y][0].x, u[y][0].y, u[y][1].x, u[y][1].y));
+    st4(PS, q3_pad_row(cs, z, y), make_float4(P[y][0].x, P[y][0].y, P[y][1].x, P[y][1].y));
   }
 #pragma unroll
   for (int w = 0; w < N; w++)
-    st4(FS, q3_pad_row(cs, w, z), make_float4(F[w][0], F[w][1], F[w][2], F[w][3]));
+    st4(FS, q3_pad_row(cs, w, z), make_float4(F[w][0].x, F[w][0].y, F[w][1].x, F[w][1].y));
   __syncthreads();
 
   // ---- stage 2: z contractions of plane z ----
-  float out[N][N];
+  float2 out[N][2];
   {
-    float Zp[N][N];
+    float2 Zp[N][2];
 #pragma unroll
     for (int y = 0; y < N; y++) {
-      float4 acc = sh4(FS, q3_pad_row(cs, z, y));
+      const float4 f = sh4(FS, q3_pad_row(cs, z, y));
+      float2 a0 = make_float2(f.x, f.y), a1 = make_float2(f.z, f.w);
 #pragma unroll
       for (int q = 0; q < N; q++) {
         const float4 v = sh4(U, q3_pad_row(cs, q, y));
-        acc.x += az[q] * v.x; acc.y += az[q] * v.y; acc.z += az[q] * v.z; acc.w += az[q] * v.w;
+        a0 = ffma2(bc2(az[q]), make_float2(v.x, v.y), a0);
+        a1 = ffma2(bc2(az[q]), make_float2(v.z, v.w), a1);
       }
-      Zp[y][0] = acc.x; Zp[y][1] = acc.y; Zp[y][2] = acc.z; Zp[y][3] = acc.w;
+      Zp[y][0] = a0;
+      Zp[y][1] = a1;
     }
-    float T1[N][N];   // Mhat_x along x
-#pragma unroll
-    for (int y = 0; y < N; y++)
-#pragma unroll
-      for (int xx = 0; xx < N; xx++) {
-        float s = 0.f;
-#pragma unroll
-        for (int r = 0; r < N; r++) s += tb.M[xx * N + r] * Zp[y][r];
-        T1[y][xx] = s;
-      }
     float mz[N];
 #pragma unroll
     for (int q = 0; q < N; q++) mz[q] = tb.M[z * N + q];
 #pragma unroll
     for (int y = 0; y < N; y++) {
-      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      // Mhat_z P
+      float2 a0, a1;
+      {
+        const float4 v = sh4(PS, q3_pad_row(cs, 0, y));
+        a0 = fmul2(bc2(mz[0]), make_float2(v.x, v.y));
+        a1 = fmul2(bc2(mz[0]), make_float2(v.z, v.w));
+      }
 #pragma unroll
-      for (int q = 0; q < N; q++) {
+      for (int q = 1; q < N; q++) {
         const float4 v = sh4(PS, q3_pad_row(cs, q, y));
-        acc.x += mz[q] * v.x; acc.y += mz[q] * v.y; acc.z += mz[q] * v.z; acc.w += mz[q] * v.w;
+        a0 = ffma2(bc2(mz[q]), make_float2(v.x, v.y), a0);
+        a1 = ffma2(bc2(mz[q]), make_float2(v.z, v.w), a1);
+      }
+      out[y][0] = a0;
+      out[y][1] = a1;
+    }
+    // (Mhat_y (x) Mhat_x) Zp: T1 = Mhat_x along x, then Mhat_y across rows
+#pragma unroll
+    for (int r = 0; r < N; r++) {
+      float2 t0 = make_float2(0.f, 0.f), t1 = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int c = 0; c < N; c++) {
+        const float zc = c < 2 ? (c == 0 ? Zp[r][0].x : Zp[r][0].y)
+                               : (c == 2 ? Zp[r][1].x : Zp[r][1].y);
+        t0 = ffma2(tb.MTp[c][0], bc2(zc), t0);
+        t1 = ffma2(tb.MTp[c][1], bc2(zc), t1);
       }
 #pragma unroll
-      for (int r = 0; r < N; r++) {
-        const float m = tb.M[y * N + r];
-        acc.x += m * T1[r][0]; acc.y += m * T1[r][1]; acc.z += m * T1[r][2]; acc.w += m * T1[r][3];
+      for (int y = 0; y < N; y++) {
+        out[y][0] = ffma2(bc2(tb.M[y * N + r]), t0, out[y][0]);
+        out[y][1] = ffma2(bc2(tb.M[y * N + r]), t1, out[y][1]);
       }
-      out[y][0] = acc.x; out[y][1] = acc.y; out[y][2] = acc.z; out[y][3] = acc.w;
     }
   }
 
@@ -1174,7 +1244,11 @@ __global__ void __launch_bounds__(Q3T::THREADS, Q3T_MINB)
 #pragma unroll
     for (int y = 0; y < N; y++)
 #pragma unroll
-      for (int xx = 0; xx < N; xx++) v[y * N + xx] = alpha * out[y][xx];
+      for (int hh = 0; hh < 2; hh++) {
+        const float2 o = fmul2(bc2(alpha), out[y][hh]);
+        v[y * N + 2 * hh] = o.x;
+        v[y * N + 2 * hh + 1] = o.y;
+      }
     float *yp = a.y + e * NB + z * 16;
     const float *ap = a.add ? a.add + e * NB + z * 16 : nullptr;
     if (((reinterpret_cast<uintptr_t>(yp) | reinterpret_cast<uintptr_t>(ap)) & 31) == 0) {
@@ -1374,12 +1448,24 @@ static int launch32_q3(pdg_context *ctx, const ApplyArgs<float> &a, const OpPara
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, Q3T::SMEM));
         attr_t = ctx->device;
       }
+      Q3Tab qt;
+      for (int i = 0; i < 16; i++) qt.M[i] = tb.M[i];
+      for (int i = 0; i < 4; i++) {
+        qt.d0[i] = tb.d0[i];
+        qt.d1[i] = tb.d1[i];
+      }
+      for (int c = 0; c < 4; c++)
+        for (int h = 0; h < 2; h++) qt.MTp[c][h] = make_float2(qt.M[2 * h * 4 + c], qt.M[(2 * h + 1) * 4 + c]);
+      for (int h = 0; h < 2; h++) {
+        qt.d0p[h] = make_float2(qt.d0[2 * h], qt.d0[2 * h + 1]);
+        qt.d1p[h] = make_float2(qt.d1[2 * h], qt.d1[2 * h + 1]);
+      }
       if (a.transpose)
         k_apply32_q3t<true><<<blocks, Q3T::THREADS, Q3T::SMEM, ctx->stream>>>(
-            p, a, ctx->rec32q, tb, *own, *run, err);
+            p, a, ctx->rec32q, qt, *own, *run, err);
       else
         k_apply32_q3t<false><<<blocks, Q3T::THREADS, Q3T::SMEM, ctx->stream>>>(
-            p, a, ctx->rec32q, tb, *own, *run, err);
+            p, a, ctx->rec32q, qt, *own, *run, err);
       PDG_CUDA_TRY(cudaGetLastError());
       return PDG_OK;
     }

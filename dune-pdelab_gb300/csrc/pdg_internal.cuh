@@ -149,7 +149,7 @@ struct pdg_context {
   int rec_valid;
   float *rec32;        // the same records rounded to FP32 (3D FP32 operator)
   int rec32_valid;
-  float *rec32q;       // Q3: the FP32 records padded to 80 floats, couplings of
+  float *rec32q;       // Q3: the FP32 records padded to 84 floats, couplings of
   int rec32q_valid;    // faces without a neighbour zeroed (k_apply32_q3t)
   // parameter fields beyond A = K I (pdg_set_permeability_tensor / _points,
   // pdg_set_reaction_points): the diffusion and reaction terms then run in
