@@ -27,6 +27,7 @@
 // The output is staged in shared memory and written back coalesced.
 #include <cuda.h>
 
+#include <algorithm>
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
@@ -954,66 +955,18 @@ __global__ void k_record_q3t(const OpParams<float> p, const float *__restrict__ 
   for (int i = 78; i < Q3T::REC; i++) o[i] = 0.f;
 }
 
-// blocks per SM the register allocation is sized for
-#ifndef Q3T_MINB
-#define Q3T_MINB 5
-#endif
+// One run of CPB cells (first cell e0) from a staged phase-1 region `base`
+// (own run with halo, y-neighbour runs, records); zl / zh: the thread's
+// z-neighbour rows.  Returns the thread's part of <x, y_out>.
 template <bool kTr>
-__global__ void __launch_bounds__(Q3T::THREADS, Q3T_MINB)
-    k_apply32_q3t(const OpParams<float> p, const ApplyArgs<float> a, const float *__restrict__ rec,
-                  const Q3Tab tb, const __grid_constant__ CUtensorMap map_own,
-                  const __grid_constant__ CUtensorMap map_run, int *tma_err) {
+__device__ __forceinline__ float q3_run(const OpParams<float> &p, const ApplyArgs<float> &a,
+                                        const Q3Tab &tb, unsigned char *base, long e0,
+                                        const float4 *zl, const float4 *zh) {
   using C = Q3T;
-  constexpr int N = 4, NB = 64, CPB = C::CPB, REC = C::REC;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ __align__(8) unsigned long long stage_bar;
-  if (a.skip && *a.skip) return;
-  // 1024-byte aligned base, kept in the shared window
-  unsigned char *base = smraw + ((1024u - (smem_u32(smraw) & 1023u)) & 1023u);
-
-  const long e0 = (long)blockIdx.x * CPB;
+  constexpr int N = 4, NB = 64, REC = C::REC;
   const long ncell = p.ncell;
-  const long sx = p.nc[0], sxy = (long)p.nc[0] * p.nc[1];
-  const float *__restrict__ x = a.x;
-  const int t = threadIdx.x, cs = t >> 2, z = t & 3;
+  const int cs = threadIdx.x >> 2, z = threadIdx.x & 3;
   const long e = e0 + cs;
-  const long ee = e < ncell ? e : 0;
-  int ix[3];
-  coords32(p, (unsigned)ee, ix);
-  // z-neighbour rows (plane q, row y = z) straight from global memory, issued
-  // before the staging wait; zero where the cell has no z neighbour
-  float4 zl[N], zh[N];
-  {
-    const bool lo = ix[2] > 0, hi = ix[2] + 1 < p.nc[2];
-    const float4 *pl = reinterpret_cast<const float4 *>(x + (ee - (lo ? sxy : 0)) * NB + z * N);
-    const float4 *ph = reinterpret_cast<const float4 *>(x + (ee + (hi ? sxy : 0)) * NB + z * N);
-#pragma unroll
-    for (int q = 0; q < N; q++) {
-      zl[q] = lo ? pl[q * 4] : make_float4(0.f, 0.f, 0.f, 0.f);
-      zh[q] = hi ? ph[q * 4] : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-  }
-
-  {
-    const unsigned bar = smem_u32(&stage_bar);
-    const long ncp = ncell - e0 < CPB ? ncell - e0 : CPB;
-    const unsigned rbytes = (unsigned)(ncp * REC * 4);
-    if (threadIdx.x == 0) mbar_init(bar, 1);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      mbar_expect_tx(bar, (unsigned)(C::LINES_OWN + 2 * C::LINES_RUN) * 128u + rbytes);
-      tma_load_2d(smem_u32(base + C::OWN_B), &map_own, 0, (int)((e0 - 1) * 2), bar);
-      tma_load_2d(smem_u32(base + C::YL_B), &map_run, 0, (int)((e0 - sx) * 2), bar);
-      tma_load_2d(smem_u32(base + C::YH_B), &map_run, 0, (int)((e0 + sx) * 2), bar);
-      bulk_load(smem_u32(base + C::REC_B), rec + e0 * REC, rbytes, bar);
-    }
-    if (!mbar_wait(bar, 0, kTmaPolls)) {
-      if (threadIdx.x == 0) atomicExch(tma_err, 1);
-      mbar_wait(bar, 0, kTmaPolls);
-      return;
-    }
-  }
-
   const unsigned char *R = base + C::REC_B + cs * REC * 4;
   auto rec4 = [&](int i) -> float4 { return sh4(R, 16u * i); };
   // coupling coefficients: floats 48..77 of the record
@@ -1287,12 +1240,176 @@ __global__ void __launch_bounds__(Q3T::THREADS, Q3T_MINB)
       }
     }
   }
+  return part;
+}
+
+// blocks per SM the register allocation is sized for
+#ifndef Q3T_MINB
+#define Q3T_MINB 5
+#endif
+template <bool kTr>
+__global__ void __launch_bounds__(Q3T::THREADS, Q3T_MINB)
+    k_apply32_q3t(const OpParams<float> p, const ApplyArgs<float> a, const float *__restrict__ rec,
+                  const Q3Tab tb, const __grid_constant__ CUtensorMap map_own,
+                  const __grid_constant__ CUtensorMap map_run, int *tma_err) {
+  using C = Q3T;
+  constexpr int N = 4, NB = 64, CPB = C::CPB, REC = C::REC;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ __align__(8) unsigned long long stage_bar;
+  if (a.skip && *a.skip) return;
+  // 1024-byte aligned base, kept in the shared window
+  unsigned char *base = smraw + ((1024u - (smem_u32(smraw) & 1023u)) & 1023u);
+
+  const long e0 = (long)blockIdx.x * CPB;
+  const long ncell = p.ncell;
+  const long sx = p.nc[0], sxy = (long)p.nc[0] * p.nc[1];
+  const float *__restrict__ x = a.x;
+  const int t = threadIdx.x, cs = t >> 2, z = t & 3;
+  const long e = e0 + cs;
+  const long ee = e < ncell ? e : 0;
+  int ix[3];
+  coords32(p, (unsigned)ee, ix);
+  // z-neighbour rows (plane q, row y = z) straight from global memory, issued
+  // before the staging wait; zero where the cell has no z neighbour
+  float4 zl[N], zh[N];
+  {
+    const bool lo = ix[2] > 0, hi = ix[2] + 1 < p.nc[2];
+    const float4 *pl = reinterpret_cast<const float4 *>(x + (ee - (lo ? sxy : 0)) * NB + z * N);
+    const float4 *ph = reinterpret_cast<const float4 *>(x + (ee + (hi ? sxy : 0)) * NB + z * N);
+#pragma unroll
+    for (int q = 0; q < N; q++) {
+      zl[q] = lo ? pl[q * 4] : make_float4(0.f, 0.f, 0.f, 0.f);
+      zh[q] = hi ? ph[q * 4] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+
+  {
+    const unsigned bar = smem_u32(&stage_bar);
+    const long ncp = ncell - e0 < CPB ? ncell - e0 : CPB;
+    const unsigned rbytes = (unsigned)(ncp * REC * 4);
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_expect_tx(bar, (unsigned)(C::LINES_OWN + 2 * C::LINES_RUN) * 128u + rbytes);
+      tma_load_2d(smem_u32(base + C::OWN_B), &map_own, 0, (int)((e0 - 1) * 2), bar);
+      tma_load_2d(smem_u32(base + C::YL_B), &map_run, 0, (int)((e0 - sx) * 2), bar);
+      tma_load_2d(smem_u32(base + C::YH_B), &map_run, 0, (int)((e0 + sx) * 2), bar);
+      bulk_load(smem_u32(base + C::REC_B), rec + e0 * REC, rbytes, bar);
+    }
+    if (!mbar_wait(bar, 0, kTmaPolls)) {
+      if (threadIdx.x == 0) atomicExch(tma_err, 1);
+      mbar_wait(bar, 0, kTmaPolls);
+      return;
+    }
+  }
+
+  const float part = q3_run<kTr>(p, a, tb, base, e0, zl, zh);
   // block sums in the phase-1 space past the phase-2 arrays (record space,
   // dead since stage 1; other warps may still read the arrays)
   if (a.dot_part)
     reduce_tail_grouped<Q3T::THREADS, true>(
         a.dot_part, a.dot_max_blocks, a.dot_cnt, RedCtx{nullptr, a.dot_scal, a.dot_flags},
         (double)part, 0.0, a.dot_fin, -1, -1, reinterpret_cast<double *>(base + C::P2_END));
+}
+
+// Persistent form: a block runs the runs blockIdx.x, + gridDim.x, ... with
+// two phase-1 regions; the copies of run i + 2 are issued as soon as run i
+// has released its region, and the z-neighbour rows of run i + 1 are loaded
+// into registers while run i computes, so the staging latency of a run
+// overlaps the computation of the one before.
+struct Q3P {
+  static constexpr int STAGE = (Q3T::P1_END + 1023) / 1024 * 1024;
+  static constexpr int SMEM = 1024 + 2 * STAGE;
+};
+__device__ __forceinline__ void q3_zrows(const OpParams<float> &p, const float *x, long run,
+                                         float4 *zl, float4 *zh) {
+  constexpr int N = 4, NB = 64;
+  const int cs = threadIdx.x >> 2, z = threadIdx.x & 3;
+  const long e = run * Q3T::CPB + cs;
+  const long ee = e < p.ncell ? e : 0;
+  const long sxy = (long)p.nc[0] * p.nc[1];
+  int ix[3];
+  coords32(p, (unsigned)ee, ix);
+  const bool lo = ix[2] > 0, hi = ix[2] + 1 < p.nc[2];
+  const float4 *pl = reinterpret_cast<const float4 *>(x + (ee - (lo ? sxy : 0)) * NB + z * N);
+  const float4 *ph = reinterpret_cast<const float4 *>(x + (ee + (hi ? sxy : 0)) * NB + z * N);
+#pragma unroll
+  for (int q = 0; q < N; q++) {
+    zl[q] = lo ? pl[q * 4] : make_float4(0.f, 0.f, 0.f, 0.f);
+    zh[q] = hi ? ph[q * 4] : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+template <bool kTr>
+__global__ void __launch_bounds__(Q3T::THREADS, 3)
+    k_apply32_q3p(const OpParams<float> p, const ApplyArgs<float> a, const float *__restrict__ rec,
+                  const Q3Tab tb, const __grid_constant__ CUtensorMap map_own,
+                  const __grid_constant__ CUtensorMap map_run, int *tma_err) {
+  using C = Q3T;
+  constexpr int N = 4, CPB = C::CPB, REC = C::REC;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ __align__(8) unsigned long long stage_bar[2];
+  if (a.skip && *a.skip) return;
+  unsigned char *base = smraw + ((1024u - (smem_u32(smraw) & 1023u)) & 1023u);
+  const long ncell = p.ncell;
+  const long nruns = (ncell + CPB - 1) / CPB;
+  const long sx = p.nc[0];
+  const long G = gridDim.x;
+  const unsigned bar0 = smem_u32(&stage_bar[0]), bar1 = smem_u32(&stage_bar[1]);
+  // thread 0: the copies of run r into region b
+  auto issue = [&](long r, int b) {
+    const long e0 = r * CPB;
+    const long ncp = ncell - e0 < CPB ? ncell - e0 : CPB;
+    const unsigned rbytes = (unsigned)(ncp * REC * 4);
+    unsigned char *st = base + b * Q3P::STAGE;
+    const unsigned bar = b ? bar1 : bar0;
+    // the region was last written by ordinary stores (phase-2 arrays)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(bar, (unsigned)(C::LINES_OWN + 2 * C::LINES_RUN) * 128u + rbytes);
+    tma_load_2d(smem_u32(st + C::OWN_B), &map_own, 0, (int)((e0 - 1) * 2), bar);
+    tma_load_2d(smem_u32(st + C::YL_B), &map_run, 0, (int)((e0 - sx) * 2), bar);
+    tma_load_2d(smem_u32(st + C::YH_B), &map_run, 0, (int)((e0 + sx) * 2), bar);
+    bulk_load(smem_u32(st + C::REC_B), rec + e0 * REC, rbytes, bar);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar1, 1);
+  }
+  __syncthreads();
+  const long r0 = blockIdx.x;
+  if (threadIdx.x == 0) {
+    if (r0 < nruns) issue(r0, 0);
+    if (r0 + G < nruns) issue(r0 + G, 1);
+  }
+  float4 zl[N], zh[N];
+  if (r0 < nruns) q3_zrows(p, a.x, r0, zl, zh);
+  double part = 0.0;   // a block runs up to nruns / gridDim.x runs
+  int it = 0;
+  for (long r = r0; r < nruns; r += G, it++) {
+    const int b = it & 1;
+    float4 nzl[N], nzh[N];
+    if (r + G < nruns) q3_zrows(p, a.x, r + G, nzl, nzh);
+    if (!mbar_wait(b ? bar1 : bar0, (unsigned)((it >> 1) & 1), kTmaPolls)) {
+      if (threadIdx.x == 0) atomicExch(tma_err, 1);
+      mbar_wait(b ? bar1 : bar0, (unsigned)((it >> 1) & 1), kTmaPolls);
+      return;
+    }
+    part += (double)q3_run<kTr>(p, a, tb, base + b * Q3P::STAGE, r * CPB, zl, zh);
+    // every thread is done with region b: stage run r + 2G there
+    __syncthreads();
+    if (threadIdx.x == 0 && r + 2 * G < nruns) issue(r + 2 * G, b);
+#pragma unroll
+    for (int q = 0; q < N; q++) {
+      zl[q] = nzl[q];
+      zh[q] = nzh[q];
+    }
+  }
+  // block sums in region 0's scratch space (free: the last sync above, or
+  // no run at all)
+  if (a.dot_part)
+    reduce_tail_grouped<Q3T::THREADS, true>(
+        a.dot_part, a.dot_max_blocks, a.dot_cnt, RedCtx{nullptr, a.dot_scal, a.dot_flags},
+        part, 0.0, a.dot_fin, -1, -1, reinterpret_cast<double *>(base + C::P2_END));
 }
 
 static EdgeTab make_edge_tab_uncached(const pdg_context *ctx) {
@@ -1440,12 +1557,17 @@ static int launch32_q3(pdg_context *ctx, const ApplyArgs<float> &a, const OpPara
         PDG_CUDA_TRY(cudaGetLastError());
         ctx->rec32q_valid = 1;
       }
-      static int attr_t = -1;
+      static int attr_t = -1, sms = 0;
       if (attr_t != ctx->device) {
         PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply32_q3t<false>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, Q3T::SMEM));
         PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply32_q3t<true>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, Q3T::SMEM));
+        PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply32_q3p<false>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, Q3P::SMEM));
+        PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply32_q3p<true>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, Q3P::SMEM));
+        PDG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
         attr_t = ctx->device;
       }
       Q3Tab qt;
@@ -1460,12 +1582,27 @@ static int launch32_q3(pdg_context *ctx, const ApplyArgs<float> &a, const OpPara
         qt.d0p[h] = make_float2(qt.d0[2 * h], qt.d0[2 * h + 1]);
         qt.d1p[h] = make_float2(qt.d1[2 * h], qt.d1[2 * h + 1]);
       }
-      if (a.transpose)
+#ifndef Q3_PERSIST
+#define Q3_PERSIST 1
+#endif
+      if (Q3_PERSIST && !a.accumulate && !a.add) {
+        // three resident blocks per SM (two phase-1 regions each); the
+        // accumulating forms stay with one run per block, whose read of y
+        // other resident blocks cover (96^3 Q3, y += J x: 220 us against 253)
+        const unsigned pblocks = (unsigned)std::min<long>(blocks, 3L * sms);
+        if (a.transpose)
+          k_apply32_q3p<true><<<pblocks, Q3T::THREADS, Q3P::SMEM, ctx->stream>>>(
+              p, a, ctx->rec32q, qt, *own, *run, err);
+        else
+          k_apply32_q3p<false><<<pblocks, Q3T::THREADS, Q3P::SMEM, ctx->stream>>>(
+              p, a, ctx->rec32q, qt, *own, *run, err);
+      } else if (a.transpose) {
         k_apply32_q3t<true><<<blocks, Q3T::THREADS, Q3T::SMEM, ctx->stream>>>(
             p, a, ctx->rec32q, qt, *own, *run, err);
-      else
+      } else {
         k_apply32_q3t<false><<<blocks, Q3T::THREADS, Q3T::SMEM, ctx->stream>>>(
             p, a, ctx->rec32q, qt, *own, *run, err);
+      }
       PDG_CUDA_TRY(cudaGetLastError());
       return PDG_OK;
     }
