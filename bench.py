@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import functools
 import json
 import os
 import statistics
@@ -503,6 +504,8 @@ def run_gb300(args, world, rank, local):
                              ("asm", "assembled_q2_32", assembled_metrics)):
             if leg not in legs:
                 continue
+            if leg == "c3" and (args.c3_cells or args.c3_mixed_only):
+                fn = functools.partial(fn, n=args.c3_cells or 96, mixed_only=args.c3_mixed_only)
             try:
                 extras[key] = fn(pdg, np, torch, stream)
             except Exception as exc:   # report the failing leg, keep the others
@@ -750,19 +753,21 @@ def smoothed_logK(np, n, seed=3, sigma=1.5):
     return np.ascontiguousarray(s.ravel())
 
 
-def c3_metrics(pdg, np, torch, stream, inner_reduction=1e-4):
+def c3_metrics(pdg, np, torch, stream, inner_reduction=1e-4, n=96, mixed_only=False):
     """96^3 Q3 (56.6M DoF): FP64 CG + block Jacobi vs FP32-apply / FP64
     defect correction, both to 1e-10, f = 1; errors of the mixed solution
-    against the FP64 one."""
-    n = 96
+    against the FP64 one.  Profiling runs may size the grid (n) and run the
+    mixed solve alone."""
     go = pdg.GridOperator(3, 3, (n, n, n), alpha=3.0, device=stream.device.index or 0)
     go.set_stream(stream)
     go.set_permeability(smoothed_logK(np, n), is_log=True)
     go.set_source(fc=np.ones(go.ncell))
     out = {"workload": "sipg3d_q3_96^3 (56.6M DoF), log-normal K box-filtered, sigma_g=1.5, "
                        "f=1, CG + cell-block Jacobi (FDM), reduction 1e-10"}
+    if n != 96:
+        out["workload"] = out["workload"].replace("96^3 (56.6M DoF)", f"{n}^3")
     sols = {}
-    for mixed in (True, False):
+    for mixed in ((True,) if mixed_only else (True, False)):
         ls = pdg.ISTLBackend_SEQ_MatrixFree_Base(go, method=pdg.CG, mixed=mixed, maxiter=20000,
                                                  inner_reduction=inner_reduction)
         u = torch.zeros(go.ndof, dtype=torch.float64, device=stream.device)
@@ -780,6 +785,9 @@ def c3_metrics(pdg, np, torch, stream, inner_reduction=1e-4):
         out[f"{key}_converged"] = bool(r.converged)
         if mixed:
             out["mixed_outer_iterations"] = r.outer_iterations
+    if mixed_only:
+        go.close()
+        return out
     e = sols["mixed"] - sols["fp64"]
     out["speedup_mixed_vs_fp64"] = out["fp64_s"] / out["mixed_s"]
     out["mixed_vs_fp64_rel_l2"] = float(torch.linalg.norm(e) / torch.linalg.norm(sols["fp64"]))
@@ -1061,6 +1069,10 @@ def main():
     ap.add_argument("--step", choices=["apply", "prec"], default="apply",
                     help="profiling runs: time the FDM block-Jacobi apply instead of the "
                          "operator (the roofline fields then describe the operator only)")
+    ap.add_argument("--c3-cells", type=int, default=None,
+                    help="profiling runs: the C3 leg on an N^3 grid instead of 96^3")
+    ap.add_argument("--c3-mixed-only", action="store_true",
+                    help="profiling runs: the C3 leg's mixed-precision solve alone")
     ap.add_argument("--convection", action="store_true",
                     help="time the convection-diffusion-reaction operator (upwind velocity "
                          "and reaction of the 48^3 Q4 leg) instead of pure diffusion")
