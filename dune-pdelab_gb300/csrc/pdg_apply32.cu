@@ -33,6 +33,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "pdg_tma.cuh"
 #include "pdg_vec.cuh"
 
 namespace pdg {
@@ -379,50 +380,6 @@ struct Q3Cfg {
   static_assert((RUN * 16) % 1024 == 0, "runs must keep the 1024-byte alignment");
 };
 
-// ---- TMA / mbarrier helpers (inline PTX) ------------------------------------
-__device__ __forceinline__ unsigned smem_u32(const void *p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-// true once phase `parity` of the barrier completed; at most `limit` polls
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int limit) {
-  for (int it = 0; it < limit; it++) {
-    unsigned done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-__device__ __forceinline__ void tma_load_2d(unsigned dst, const CUtensorMap *map, int c0, int c1,
-                                            unsigned bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
-      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(bar)
-      : "memory");
-}
-__device__ __forceinline__ void bulk_load(unsigned dst, const void *src, unsigned bytes,
-                                          unsigned bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-          "r"(dst), "l"(src), "r"(bytes), "r"(bar)
-      : "memory");
-}
-// polls of the staging barrier before a launch gives up (far above any
-// real copy time); the kernel then records the failure and returns
-constexpr int kTmaPolls = 1 << 22;
 
 __device__ __forceinline__ float4 ld4(const float *p, bool vec) {
   if (vec) return *reinterpret_cast<const float4 *>(p);
@@ -849,47 +806,15 @@ struct Q3T {
   static_assert((CPB + 2) * 256 <= YL_B, "own run overlaps the y runs");
   static_assert(P2_END + 2 * THREADS * 8 <= P1_END,
                 "phase-2 arrays and the block-sum scratch must fit the phase-1 space");
-  static_assert(LINES_OWN == Q3Cfg::LINES_OWN && LINES_RUN == Q3Cfg::LINES_RUN,
+  static_assert(LINES_OWN == Q3Cfg::LINES_OWN && LINES_RUN == Q3Cfg::LINES_RUN &&
+                    LINES_OWN == (int)kLinesOwn && LINES_RUN == (int)kLinesRun,
                 "tensor maps are shared with k_apply32_q3");
 };
 
-// byte offset of row y of plane z of cell c in a swizzled run buffer
-__device__ __forceinline__ unsigned q3_swz_row(int c, int z, int y) {
-  return 16u * (unsigned)(16 * c + 8 * (z >> 1) + 4 * ((z & 1) ^ ((c >> 1) & 1)) +
-                          ((2 * (c & 1) | (z >> 1)) ^ y));
-}
 // byte offset of row y of plane q of cell c in a phase-2 array
 __device__ __forceinline__ unsigned q3_pad_row(int c, int q, int y) {
   return 16u * (unsigned)(Q3T::CR * c + Q3T::PR * q + y);
 }
-__device__ __forceinline__ float4 sh4(const unsigned char *b, unsigned off) {
-  return *reinterpret_cast<const float4 *>(b + off);
-}
-__device__ __forceinline__ void st4(unsigned char *b, unsigned off, float4 v) {
-  *reinterpret_cast<float4 *>(b + off) = v;
-}
-__device__ __forceinline__ float f4c(const float4 &v, int i) {
-  return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
-}
-// 32-byte global vector accesses (32-byte aligned addresses)
-__device__ __forceinline__ void ld8(const float *p, float *w) {
-  asm volatile("ld.global.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=f"(w[0]), "=f"(w[1]), "=f"(w[2]), "=f"(w[3]), "=f"(w[4]), "=f"(w[5]),
-                 "=f"(w[6]), "=f"(w[7])
-               : "l"(p));
-}
-__device__ __forceinline__ void st8(float *p, const float *w) {
-  asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(w[0]),
-               "f"(w[1]), "f"(w[2]), "f"(w[3]), "f"(w[4]), "f"(w[5]), "f"(w[6]), "f"(w[7])
-               : "memory");
-}
-
-// paired FP32 arithmetic (one instruction for two lanes; a scalar operand
-// is broadcast to both)
-__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
-__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fadd2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 
 // 1D tables of the Q3 kernel (kernel parameter space), with the pairs its
 // paired multiply-adds take as operands
@@ -1504,8 +1429,8 @@ struct LinesMaps {
   long ndof;
   CUtensorMap own, run;
 };
-static bool lines_maps(const float *x, long ndof, const CUtensorMap **own,
-                       const CUtensorMap **run) {
+bool q3_lines_maps(const float *x, long ndof, const CUtensorMap **own,
+                   const CUtensorMap **run) {
   constexpr int kSlots = 8;
   thread_local LinesMaps cache[kSlots];
   thread_local int next = 0;
@@ -1516,8 +1441,7 @@ static bool lines_maps(const float *x, long ndof, const CUtensorMap **own,
       return true;
     }
   LinesMaps &c = cache[next];
-  if (!encode_lines(&c.own, x, ndof, Q3Cfg::LINES_OWN) ||
-      !encode_lines(&c.run, x, ndof, Q3Cfg::LINES_RUN)) {
+  if (!encode_lines(&c.own, x, ndof, kLinesOwn) || !encode_lines(&c.run, x, ndof, kLinesRun)) {
     c.x = nullptr;
     return false;
   }
@@ -1546,7 +1470,7 @@ static int launch32_q3(pdg_context *ctx, const ApplyArgs<float> &a, const OpPara
   const CUtensorMap *own = nullptr, *run = nullptr;
   // TMA needs a 16-byte aligned vector (and records, from cudaMalloc)
   if ((reinterpret_cast<uintptr_t>(a.x) & 15) == 0 && (reinterpret_cast<uintptr_t>(rec) & 15) == 0 &&
-      lines_maps(a.x, ctx->ndof, &own, &run)) {
+      q3_lines_maps(a.x, ctx->ndof, &own, &run)) {
     if (!a.diag_only) {
       static_assert(Q3T::CPB == Q3Cfg::CPB, "one block per run of CPB cells");
       if (!ctx->rec32q_valid) {

@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "pdg_ops.cuh"
+#include "pdg_tma.cuh"
 #include "pdg_vec.cuh"
 
 namespace pdg {
@@ -763,6 +764,235 @@ __global__ void __launch_bounds__(FdmQ3Cfg::THREADS)
 }
 
 // ---------------------------------------------------------------------------
+// The same FDM apply with TMA staging and paired FP32 arithmetic (16-byte
+// aligned d and q): the runs of d and q arrive as 128-byte-swizzled tensor
+// copies and the factors as bulk copies, all on one mbarrier (bounded wait);
+// each thread reads its plane rows at closed-form swizzled addresses, keeps
+// b = d - lambda q in registers, writes b and its own plane of v with 32-byte
+// stores, and runs every contraction as paired multiply-adds (one issue for
+// two lanes).  The two z exchanges reuse the q run's swizzled rows: a thread
+// rewrites exactly the rows it read.
+// ---------------------------------------------------------------------------
+struct FdmQ3T {
+  static constexpr int CPB = 32, THREADS = 128;
+  static constexpr int DR_B = 0, QR_B = 8192, QS_B = 16384, LS_B = QS_B + CPB * 192,
+                       END = LS_B + CPB * 48;
+  static constexpr int SMEM = 1024 + END;
+};
+
+__global__ void __launch_bounds__(FdmQ3T::THREADS)
+    k_fdm32_q3t(long ncell, const float *__restrict__ Q, const float *__restrict__ L, float *d,
+                float *v, const int *__restrict__ skip, float scale, double *dot_part,
+                long dot_max_blocks, int *dot_cnt, double *dot_scal, int *dot_flags, int dot_fin,
+                const float *rq, const __grid_constant__ CUtensorMap map_d,
+                const __grid_constant__ CUtensorMap map_q, int *tma_err) {
+  using C = FdmQ3T;
+  constexpr int N = 4, NB = 64, CPB = C::CPB;
+  extern __shared__ __align__(16) unsigned char fsraw[];
+  __shared__ __align__(8) unsigned long long fbar;
+  if (skip && *skip) return;
+  unsigned char *base = fsraw + ((1024u - (smem_u32(fsraw) & 1023u)) & 1023u);
+  const long e0 = (long)blockIdx.x * CPB;
+  const long cmax = ncell - e0 < CPB ? ncell - e0 : CPB;
+  {
+    const unsigned bar = smem_u32(&fbar);
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const unsigned fb = (unsigned)(cmax * 240);
+      mbar_expect_tx(bar, (rq ? 2u : 1u) * kLinesRun * 128u + fb);
+      tma_load_2d(smem_u32(base + C::DR_B), &map_d, 0, (int)(e0 * 2), bar);
+      if (rq) tma_load_2d(smem_u32(base + C::QR_B), &map_q, 0, (int)(e0 * 2), bar);
+      bulk_load(smem_u32(base + C::QS_B), Q + e0 * 48, (unsigned)(cmax * 192), bar);
+      bulk_load(smem_u32(base + C::LS_B), L + e0 * 12, (unsigned)(cmax * 48), bar);
+    }
+    if (!mbar_wait(bar, 0, kTmaPolls)) {
+      if (threadIdx.x == 0) atomicExch(tma_err, 1);
+      mbar_wait(bar, 0, kTmaPolls);
+      return;
+    }
+  }
+  const int cs = threadIdx.x >> 2, z = threadIdx.x & 3;
+  const long e = e0 + cs;
+  const bool active = cs < cmax;
+  const unsigned char *F = base + C::QS_B + cs * 192;   // Qx rows 0..3, Qy 4..7, Qz 8..11
+  const float4 lx = sh4(base + C::LS_B, cs * 48u), ly = sh4(base + C::LS_B, cs * 48u + 16u);
+  const float lz = f4c(sh4(base + C::LS_B, cs * 48u + 32u), z);
+  unsigned char *X = base + C::QR_B;
+
+  // b (= d, or d - lambda q with the fused residual update), own plane
+  float2 b[N][2];
+#pragma unroll
+  for (int y = 0; y < N; y++) {
+    const float4 w = sh4(base + C::DR_B, q3_swz_row(cs, z, y));
+    b[y][0] = make_float2(w.x, w.y);
+    b[y][1] = make_float2(w.z, w.w);
+  }
+  float part2 = 0.f;   // |b - lambda q|^2
+  const bool v32 = ((reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(v)) & 31) == 0;
+  if (rq) {
+    const float2 ml = bc2(-(float)dot_scal[S_ALPHA]);
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      const float4 q = sh4(X, q3_swz_row(cs, z, y));
+      b[y][0] = ffma2(ml, make_float2(q.x, q.y), b[y][0]);
+      b[y][1] = ffma2(ml, make_float2(q.z, q.w), b[y][1]);
+    }
+    float w[16];
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      w[4 * y] = b[y][0].x; w[4 * y + 1] = b[y][0].y;
+      w[4 * y + 2] = b[y][1].x; w[4 * y + 3] = b[y][1].y;
+    }
+#pragma unroll
+    for (int j = 0; j < 16; j++) part2 += w[j] * w[j];
+    if (active) {
+      float *dp = d + e * NB + z * 16;
+      if (v32) {
+        st8(dp, w);
+        st8(dp + 8, w + 8);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; j++) dp[j] = w[j];
+      }
+    } else {
+      part2 = 0.f;
+    }
+  }
+
+  float2 u[N][2];
+  {
+    // forward x then y: w[y'][x'] = sum_y Qy[y][y'] sum_x Qx[x][x'] b[y][x]
+    float2 t1[N][2];
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int x = 0; x < N; x++) {
+        const float4 qx = sh4(F, 16u * x);
+        const float bx = f4c(make_float4(b[y][0].x, b[y][0].y, b[y][1].x, b[y][1].y), x);
+        a0 = ffma2(make_float2(qx.x, qx.y), bc2(bx), a0);
+        a1 = ffma2(make_float2(qx.z, qx.w), bc2(bx), a1);
+      }
+      t1[y][0] = a0;
+      t1[y][1] = a1;
+    }
+#pragma unroll
+    for (int yp = 0; yp < N; yp++) {
+      float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int y = 0; y < N; y++) {
+        const float qy = f4c(sh4(F, 64u + 16u * y), yp);
+        a0 = ffma2(bc2(qy), t1[y][0], a0);
+        a1 = ffma2(bc2(qy), t1[y][1], a1);
+      }
+      u[yp][0] = a0;
+      u[yp][1] = a1;
+    }
+  }
+#pragma unroll
+  for (int y = 0; y < N; y++)
+    st4(X, q3_swz_row(cs, z, y), make_float4(u[y][0].x, u[y][0].y, u[y][1].x, u[y][1].y));
+  __syncthreads();
+  // forward z and scaling: c_z'[y][x] = sum_z Qz[z][z'] w_z[y][x] / (Lx[x] + Ly[y] + Lz[z'])
+  {
+    float qzc[N];
+#pragma unroll
+    for (int zz = 0; zz < N; zz++) qzc[zz] = f4c(sh4(F, 128u + 16u * zz), z);
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int zz = 0; zz < N; zz++) {
+        const float4 w = sh4(X, q3_swz_row(cs, zz, y));
+        a0 = ffma2(bc2(qzc[zz]), make_float2(w.x, w.y), a0);
+        a1 = ffma2(bc2(qzc[zz]), make_float2(w.z, w.w), a1);
+      }
+      const float lyz = f4c(ly, y) + lz;
+      u[y][0] = make_float2(__fdividef(a0.x, lx.x + lyz), __fdividef(a0.y, lx.y + lyz));
+      u[y][1] = make_float2(__fdividef(a1.x, lx.z + lyz), __fdividef(a1.y, lx.w + lyz));
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int y = 0; y < N; y++)
+    st4(X, q3_swz_row(cs, z, y), make_float4(u[y][0].x, u[y][0].y, u[y][1].x, u[y][1].y));
+  __syncthreads();
+  // backward z: e_z[y][x] = sum_z' Qz[z][z'] c_z'[y][x]
+  {
+    const float4 qzr = sh4(F, 128u + 16u * z);
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int zz = 0; zz < N; zz++) {
+        const float4 w = sh4(X, q3_swz_row(cs, zz, y));
+        a0 = ffma2(bc2(f4c(qzr, zz)), make_float2(w.x, w.y), a0);
+        a1 = ffma2(bc2(f4c(qzr, zz)), make_float2(w.z, w.w), a1);
+      }
+      u[y][0] = a0;
+      u[y][1] = a1;
+    }
+  }
+  // backward y then x: g[y][x] = sum_x' Qx[x][x'] sum_y' Qy[y][y'] e[y'][x']
+  float g[16];
+  {
+    float2 t1[N][2];
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      const float4 qy = sh4(F, 64u + 16u * y);
+      float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int yp = 0; yp < N; yp++) {
+        a0 = ffma2(bc2(f4c(qy, yp)), u[yp][0], a0);
+        a1 = ffma2(bc2(f4c(qy, yp)), u[yp][1], a1);
+      }
+      t1[y][0] = a0;
+      t1[y][1] = a1;
+    }
+    const float4 q0 = sh4(F, 0u), q1 = sh4(F, 16u), q2 = sh4(F, 32u), q3 = sh4(F, 48u);
+#pragma unroll
+    for (int y = 0; y < N; y++) {
+      float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int xp = 0; xp < N; xp++) {
+        const float tv = xp < 2 ? (xp == 0 ? t1[y][0].x : t1[y][0].y)
+                                : (xp == 2 ? t1[y][1].x : t1[y][1].y);
+        a0 = ffma2(make_float2(f4c(q0, xp), f4c(q1, xp)), bc2(tv), a0);
+        a1 = ffma2(make_float2(f4c(q2, xp), f4c(q3, xp)), bc2(tv), a1);
+      }
+      const float2 s0 = fmul2(bc2(scale), a0), s1 = fmul2(bc2(scale), a1);
+      g[4 * y] = s0.x; g[4 * y + 1] = s0.y; g[4 * y + 2] = s1.x; g[4 * y + 3] = s1.y;
+    }
+  }
+  // own plane of v; fused <b, v>
+  float part = 0.f;
+  if (active) {
+    float *vp = v + e * NB + z * 16;
+    if (v32) {
+      st8(vp, g);
+      st8(vp + 8, g + 8);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 16; j++) vp[j] = g[j];
+    }
+#pragma unroll
+    for (int y = 0; y < N; y++)
+      part += b[y][0].x * g[4 * y] + b[y][0].y * g[4 * y + 1] + b[y][1].x * g[4 * y + 2] +
+              b[y][1].y * g[4 * y + 3];
+  }
+  if (dot_part) {
+    double s0 = (double)part, s1 = 0.0;
+    if (rq) {
+      s0 = (double)part2;
+      s1 = (double)part;
+    }
+    reduce_tail_grouped<C::THREADS>(dot_part, dot_max_blocks, dot_cnt,
+                                    RedCtx{nullptr, dot_scal, dot_flags}, s0, s1, dot_fin, -1, -1);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 static int fdm_setup(pdg_context *ctx, int precision) {
@@ -957,6 +1187,28 @@ static int fdm_apply_dn(pdg_context *ctx, const T *d, T *v, const int *skip, con
       }
       const bool fuse = ctx->fuse_fin != 0;
       const unsigned blocks = (unsigned)((ctx->ncell + Q::CPB - 1) / Q::CPB);
+      const float *rq = (fuse && ctx->fuse_fin == FIN_CG_DEF_BETA) ? (const float *)ctx->fuse_q
+                                                                   : nullptr;
+      const CUtensorMap *md = nullptr, *mq = nullptr, *unused = nullptr;
+      const bool aligned = ((reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(rq) |
+                             reinterpret_cast<uintptr_t>(ctx->prec[PDG_F32].Q) |
+                             reinterpret_cast<uintptr_t>(ctx->prec[PDG_F32].L)) & 15) == 0;
+      if (aligned && q3_lines_maps(d, ctx->ndof, &unused, &md) &&
+          (!rq || q3_lines_maps(rq, ctx->ndof, &unused, &mq))) {
+        static int attr_t = -1;
+        if (attr_t != ctx->device) {
+          PDG_CUDA_TRY(cudaFuncSetAttribute(
+              k_fdm32_q3t, cudaFuncAttributeMaxDynamicSharedMemorySize, FdmQ3T::SMEM));
+          attr_t = ctx->device;
+        }
+        k_fdm32_q3t<<<blocks, FdmQ3T::THREADS, FdmQ3T::SMEM, ctx->stream>>>(
+            ctx->ncell, (const float *)ctx->prec[PDG_F32].Q, (const float *)ctx->prec[PDG_F32].L,
+            const_cast<float *>(d), v, skip, scale, fuse ? ctx->fuse_part : nullptr,
+            ctx->fuse_max_blocks, ctx->fuse_cnt, ctx->red_out, ctx->d_flag, ctx->fuse_fin, rq,
+            *md, rq ? *mq : *md, ctx->d_flag + F_TMA);
+        PDG_CUDA_TRY(cudaGetLastError());
+        return PDG_OK;
+      }
       k_fdm32_q3<<<blocks, Q::THREADS, smem, ctx->stream>>>(
           ctx->ncell, (const float *)ctx->prec[PDG_F32].Q, (const float *)ctx->prec[PDG_F32].L,
           const_cast<float *>(d), v, skip, scale, fuse ? ctx->fuse_part : nullptr,
