@@ -20,7 +20,7 @@ PROBE_LIB = os.path.join(OUT, "libpdg_probe.so")   # bench-only FMA peak probe
 SOURCES = ["pdg_abi.cu", "pdg_apply.cu", "pdg_prec.cu", "pdg_rhs.cu", "pdg_vec.cu",
            "pdg_noalloc.cu", "pdg_conv.cu", "pdg_assemble.cu",
            "pdg_blocksolve.cu", "pdg_apply32.cu",
-           "pdg_nonlinear.cu", "pdg_basis.cu", "pdg_general.cu", "pdg_apply_fp.cu"]
+           "pdg_nonlinear.cu", "pdg_basis.cu", "pdg_general.cu", "pdg_apply_fp.cu", "pdg_apply_m.cu"]
 PROBE_SOURCES = ["probe_peak.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",

@@ -846,6 +846,7 @@ static void invalidate(pdg_context *ctx, bool operator_changed) {
   if (operator_changed) {
     ctx->op_gen++;
     ctx->rec_valid = 0;
+    ctx->rec64m_valid = 0;
     ctx->recfp_valid = 0;
     ctx->rec32_valid = 0;
     ctx->rec32q_valid = 0;
@@ -1027,6 +1028,53 @@ int pdg_create(const pdg_config *cfg, pdg_context **out) {
       cudaMallocHost(&c->h_red, sizeof(double) * S_COUNT + sizeof(int) * F_COUNT) != cudaSuccess)
     return fail(set_error(PDG_ECUDA, "device allocation failed"));
   cudaMemcpy(c->tab64, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice);
+  if (c->dim == 3) {
+    // the mass-factored operator's tables: Mhat, Mhat^-1 applied to the face
+    // vectors e0, e_{N-1}, d0, d1, and Mhat^-1 (Gauss-Jordan, partial pivoting)
+    std::vector<double> a(tab.begin(), tab.begin() + N * N), inv(N * N, 0.0);
+    for (int i = 0; i < N; i++) inv[i * N + i] = 1.0;
+    for (int col = 0; col < N; col++) {
+      int piv = col;
+      for (int r = col + 1; r < N; r++)
+        if (std::fabs(a[r * N + col]) > std::fabs(a[piv * N + col])) piv = r;
+      for (int j = 0; j < N; j++) {
+        std::swap(a[col * N + j], a[piv * N + j]);
+        std::swap(inv[col * N + j], inv[piv * N + j]);
+      }
+      const double d = a[col * N + col];
+      for (int j = 0; j < N; j++) {
+        a[col * N + j] /= d;
+        inv[col * N + j] /= d;
+      }
+      for (int r = 0; r < N; r++)
+        if (r != col) {
+          const double f = a[r * N + col];
+          for (int j = 0; j < N; j++) {
+            a[r * N + j] -= f * a[col * N + j];
+            inv[r * N + j] -= f * inv[col * N + j];
+          }
+        }
+    }
+    std::vector<double> tm(2 * N * N + 4 * N);
+    for (int i = 0; i < N * N; i++) {
+      tm[i] = tab[i];
+      tm[N * N + 4 * N + i] = inv[i];
+    }
+    for (int i = 0; i < N; i++) {
+      double m0 = inv[i * N], m1 = inv[i * N + N - 1], md0 = 0.0, md1 = 0.0;
+      for (int k = 0; k < N; k++) {
+        md0 += inv[i * N + k] * tab[2 * N * N + k];
+        md1 += inv[i * N + k] * tab[2 * N * N + N + k];
+      }
+      tm[N * N + i] = m0;
+      tm[N * N + N + i] = m1;
+      tm[N * N + 2 * N + i] = md0;
+      tm[N * N + 3 * N + i] = md1;
+    }
+    if (cudaMalloc(&c->tabm64, sizeof(double) * tm.size()) != cudaSuccess)
+      return fail(set_error(PDG_ECUDA, "device allocation failed"));
+    cudaMemcpy(c->tabm64, tm.data(), sizeof(double) * tm.size(), cudaMemcpyHostToDevice);
+  }
   cudaMemcpy(c->tab32, tab32.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice);
   cudaMemcpy(c->K64, ones.data(), sizeof(double) * c->ncell, cudaMemcpyHostToDevice);
   cudaMemcpy(c->K32, ones32.data(), sizeof(float) * c->ncell, cudaMemcpyHostToDevice);
@@ -1073,7 +1121,7 @@ int pdg_destroy(pdg_context *c) {
                   c->leg64, c->leg32, c->legw64[0], c->legw64[1], c->legw32[0], c->legw32[1],
                   c->fuse_part, c->fuse_cnt, c->Ac64, c->Aqv64, c->Aqf64, c->cq64, c->Ac32,
                   c->Aqv32, c->Aqf32, c->cq32, c->bqv64, c->bqf64, c->Kd64, c->Kd32,
-                  c->recfp, c->tabfp, c->rec32q};
+                  c->recfp, c->tabfp, c->rec32q, c->rec64m, c->tabm64};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 10; i++)

@@ -574,6 +574,7 @@ static int ensure_record(pdg_context *ctx) {
 // launches are spread over several streams)
 int prepare_apply64(pdg_context *ctx) {
   PDG_TRY(ensure_record(ctx));
+  if (ctx->dim == 3 && ctx->tabm64 && !general_coefficients(ctx)) PDG_TRY(prepare_apply_m(ctx));
   if (ctx->f64_pair && ctx->dim == 3 && !general_coefficients(ctx))
     PDG_TRY(prepare_float_pair(ctx));
   return PDG_OK;
@@ -636,7 +637,17 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
     PDG_TRY(ensure_record32(ctx));
     rec = (const T *)ctx->rec32;
   }
+#ifndef PDG_MFORM
+#define PDG_MFORM 1
+#endif
   if constexpr (std::is_same<T, double>::value) {
+    if (PDG_MFORM && !ctx->f64_pair && ctx->dim == 3 && rec && ctx->tabm64 && !a.transpose &&
+        !a.diag_only && !a.cells) {
+      // the mass-factored form (fewer FP64 operations; non-transposed only)
+      PDG_TRY(launch_apply_m(ctx, a, p));
+      if (convection_on(ctx)) PDG_TRY(launch_convection<T>(ctx, a));
+      return nl_apply<T>(ctx, a);
+    }
     if (ctx->f64_pair && ctx->dim == 3 && rec) {
       // FP64 applies in float-pair arithmetic on the FP32 pipe
       PDG_TRY(launch_apply_float_pair(ctx, a));

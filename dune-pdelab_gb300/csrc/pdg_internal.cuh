@@ -147,6 +147,9 @@ struct pdg_context {
   int r0_valid;
   double *rec64;       // FP64 per-cell operator records (scaled A'_dir + face coefficients)
   int rec_valid;
+  double *rec64m;      // 3D: Mhat^-1 A'_dir and the operator's line coefficients (k_apply_m)
+  int rec64m_valid;
+  double *tabm64;      // 3D: Mhat, Mhat^-1 e0, Mhat^-1 e_{N-1}, Mhat^-1 d0, Mhat^-1 d1, Mhat^-1
   float *rec32;        // the same records rounded to FP32 (3D FP32 operator)
   int rec32_valid;
   float *rec32q;       // Q3: the FP32 records padded to 84 floats, couplings of
@@ -362,6 +365,10 @@ __host__ __device__ inline long face_lattice_index(const int *nc, int dim, int d
 // be valid
 int launch_apply_float_pair(pdg_context *ctx, const ApplyArgs<double> &a);
 int prepare_float_pair(pdg_context *ctx);
+// the 3D FP64 operator with the mass matrix factored out (pdg_apply_m.cu;
+// non-transposed, coupled, all cells or a cell range); rec64 must be valid
+int launch_apply_m(pdg_context *ctx, const ApplyArgs<double> &a, const OpParams<double> &p);
+int prepare_apply_m(pdg_context *ctx);
 
 // parameter fields beyond A = K I: true when the Gauss-point operator replaces
 // the Kronecker kernels; its launch (diffusion and reaction terms only)
