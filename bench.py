@@ -229,6 +229,15 @@ def fma_peaks(pdg):
         if lib.pdg_probe_dmma_peak(1000, ctypes.byref(v)) == 0:
             best = max(best, v.value)
     out["fp64_tensor_mma"] = best
+    # both at once: the sum of the two rates if the tensor path were a second
+    # FP64 unit, either one's rate if they share it
+    lib.pdg_probe_fp64_mixed.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    best = 0.0
+    for _ in range(3):
+        v = ctypes.c_double()
+        if lib.pdg_probe_fp64_mixed(1000, ctypes.byref(v)) == 0:
+            best = max(best, v.value)
+    out["fp64_mma_plus_fma"] = best
     return out
 
 
@@ -487,6 +496,7 @@ def run_gb300(args, world, rank, local):
         "hbm_frac": (alg_bytes / (ms * 1e-3) / 1e9) / mp_["hbm_gbs"] if mp_.get("hbm_gbs") else None,
         "fp32_fma_peak_tflops": peaks["fp32"],
         "fp64_tensor_mma_peak_tflops": peaks.get("fp64_tensor_mma"),
+        "fp64_mma_plus_fma_tflops": peaks.get("fp64_mma_plus_fma"),
     }
 
     extras = {}
