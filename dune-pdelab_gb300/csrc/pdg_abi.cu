@@ -1631,6 +1631,13 @@ int pdg_jacobian_apply_f32(pdg_context *ctx, const float *z, float *y) {
     return set_error(PDG_EINVAL, "pdg_jacobian_apply_f32 takes device pointers");
   return op_launch<float>(ctx, z, y, nullptr, 1.f, 1, 0, nullptr);
 }
+int pdg_apply_f32(pdg_context *ctx, const float *x, float *y) {
+  PDG_CHECK_CTX(ctx);
+  if (!x || !y) return set_error(PDG_EINVAL, "null vector");
+  if (!is_device_ptr(x) || !is_device_ptr(y))
+    return set_error(PDG_EINVAL, "pdg_apply_f32 takes device pointers");
+  return op_launch<float>(ctx, x, y, nullptr, 1.f, 0, 0, nullptr);
+}
 int pdg_jacobian_apply_transpose_f32(pdg_context *ctx, const float *z, float *y) {
   PDG_CHECK_CTX(ctx);
   if (!z || !y) return set_error(PDG_EINVAL, "null vector");

@@ -140,6 +140,7 @@ _SIGS = {
     "pdg_jacobian_apply": (C.c_int, [_vp, _vp, _vp]),
     "pdg_jacobian_apply_f32": (C.c_int, [_vp, _vp, _vp]),
     "pdg_jacobian_apply_transpose_f32": (C.c_int, [_vp, _vp, _vp]),
+    "pdg_apply_f32": (C.c_int, [_vp, _vp, _vp]),
     "pdg_jacobian_apply_transpose": (C.c_int, [_vp, _vp, _vp]),
     "pdg_apply": (C.c_int, [_vp, _vp, _vp]),
     "pdg_applyscaleadd": (C.c_int, [_vp, C.c_double, _vp, _vp]),
@@ -463,6 +464,12 @@ class GridOperator:
     def jacobian_apply_f32(self, z, y):
         """y += J z in FP32 (device tensors)"""
         _check(load().pdg_jacobian_apply_f32(self._h, _ptr(z, np.float32), _ptr(y, np.float32)))
+        return y
+
+    @_stream_ordered
+    def apply_f32(self, x, y):
+        """y = J x in FP32 (device tensors)"""
+        _check(load().pdg_apply_f32(self._h, _ptr(x, np.float32), _ptr(y, np.float32)))
         return y
 
     @_stream_ordered

@@ -315,6 +315,9 @@ int pdg_jacobian_apply_transpose(pdg_context *ctx, const double *z, double *y);
 /* Same in FP32, device pointers (the transposed inner operator of the
    mixed-precision adjoint solve) */
 int pdg_jacobian_apply_transpose_f32(pdg_context *ctx, const float *z, float *y);
+/* y = J x in FP32, device pointers: the operator apply of the inner CG of the
+   mixed-precision solve (OnTheFlyOperator::apply in FP32) */
+int pdg_apply_f32(pdg_context *ctx, const float *x, float *y);
 /* OnTheFlyOperator::apply(x, y): y = J x
    (backend/istl/seqistlsolverbackend.hh:66-76) */
 int pdg_apply(pdg_context *ctx, const double *x, double *y);

@@ -183,6 +183,29 @@ def test_jacobian_apply_transpose_f32_staged(pdg, oracle, k, nc, method, weights
     assert _rel(yt.cpu().double().numpy(), ref) <= TOL32
 
 
+@pytest.mark.parametrize("k,nc,method,weights,react,bct", [
+    (3, (11, 4, 3), 0, 1, False, None),
+    (3, (13, 7, 5), 1, 0, True, [1, -1, -2, 1, 1, -1]),
+    (3, (33, 2, 3), 2, 1, False, None),
+    (3, (1, 1, 1), 1, 0, False, None),
+    (3, (5, 9, 11), 0, 0, True, None),
+    (3, (40, 37, 12), 1, 0, True, None),
+    (2, (9, 5, 4), 1, 0, True, [1, -1, 1, -2, -1, 1]),
+])
+def test_apply_f32_overwrites(pdg, oracle, k, nc, method, weights, react, bct):
+    # y = J x in FP32 (the inner CG's operator; at Q3 the persistent kernel with
+    # two staging regions per block, several runs per block on the larger grid)
+    import torch
+    go, P, rng = _pair(pdg, oracle, 3, k, nc, seed=71 + k, method=method, weights=weights,
+                       bctype=bct, react=react)
+    x = rng.uniform(-1, 1, go.ndof)
+    xt = torch.tensor(x, dtype=torch.float32, device="cuda")
+    yt = torch.full((go.ndof,), 7.0, dtype=torch.float32, device="cuda")
+    go.apply_f32(xt, yt)
+    torch.cuda.synchronize()
+    assert _rel(yt.cpu().double().numpy(), P.jacobian_apply(x)) <= TOL32
+
+
 def test_device_pointers_match_host(pdg, oracle):
     import torch
     go, P, rng = _pair(pdg, oracle, 3, 3, 3, seed=4)
