@@ -118,6 +118,7 @@ struct PrecData {
   int *iters;      // block-solve iteration counts of the last apply [ncell]
   void *inv16;     // FP16 dense inverses (dense_fp16), scaled by invscale [ncell]
   float *invscale;
+  double *Lsum_inv;  // FP64 FDM: 1 / (sum of the directions' eigenvalues) per DOF [ncell][N^d]
 };
 
 }  // namespace pdg

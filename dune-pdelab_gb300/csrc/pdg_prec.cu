@@ -162,12 +162,26 @@ constexpr int fdm_pad() {
   return N == 2 ? 2 : N == 3 ? 2 : N == 5 ? 5 : 0;
 }
 
+// 1 / (Lx[x] + Ly[y] (+ Lz[z])) per DOF (local index x fastest), FP64
+__global__ void k_fdm_lsum_inv(long ndof, int dim, int N, const double *__restrict__ L,
+                               double *__restrict__ out) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ndof) return;
+  const int nb = dim == 3 ? N * N * N : N * N;
+  const long e = i / nb;
+  const int k = (int)(i - e * nb);
+  const double *l = L + e * dim * N;
+  double s = l[k % N] + l[N + (k / N) % N];
+  if (dim == 3) s += l[2 * N + k / (N * N)];
+  out[i] = 1.0 / s;
+}
+
 template <typename T, int D, int N>
 __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
     k_fdm_apply(long ncell, const T *__restrict__ Q, const T *__restrict__ L, T *d, T *v,
                 const int *__restrict__ skip, const int *__restrict__ cells, int ncells, T scale,
                 double *dot_part, long dot_max_blocks, int *dot_cnt, double *dot_scal,
-                int *dot_flags, int dot_fin, const T *rq) {
+                int *dot_flags, int dot_fin, const T *rq, const T *__restrict__ Linv) {
   // rq != null (fused CG): first d -= lambda rq (lambda = dot_scal[S_ALPHA]),
   // written back; the fused dot then carries |d|^2 and <d, v>.  d, v and rq
   // may alias element-wise: every entry is read and written by one thread.
@@ -232,7 +246,8 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
       T s = T(0);
 #pragma unroll
       for (int x = 0; x < N; x++) s += Qx[x * N + tx] * S1[z * N2 + ty * N + x];
-      a[z] = qdiv(s, Ls[tx] + Ls[N + ty] + Ls[2 * N + z]);
+      a[z] = Linv ? s * Linv[(size_t)ee * NB + z * N2 + l]
+                  : qdiv(s, Ls[tx] + Ls[N + ty] + Ls[2 * N + z]);
     }
     __syncthreads();
 #pragma unroll
@@ -285,7 +300,7 @@ __global__ void __launch_bounds__(PCfg<D, N>::THREADS)
       T s = T(0);
 #pragma unroll
       for (int x = 0; x < N; x++) s += Qx[x * N + tx] * S0[y * N + x];
-      a[y] = qdiv(s, Ls[tx] + Ls[N + y]);
+      a[y] = Linv ? s * Linv[(size_t)ee * NB + y * N + tx] : qdiv(s, Ls[tx] + Ls[N + y]);
     }
 #pragma unroll
     for (int y = 0; y < N; y++) S1[y * N + tx] = a[y];
@@ -1043,6 +1058,15 @@ static int fdm_setup(pdg_context *ctx, int precision) {
     default: cudaFree(dLi); return set_error(PDG_EUNSUPPORTED, "degree not compiled in");
   }
   PDG_CUDA_TRY(cudaGetLastError());
+  if (precision == PDG_F64) {
+    // the scaling of the FP64 apply as one multiply per DOF: FP64 division is a
+    // multi-instruction sequence on the FP64 pipe that bounds the apply
+    PDG_CUDA_TRY(cudaMalloc(&pd.Lsum_inv, sizeof(double) * ctx->ndof));
+    const unsigned b2 = (unsigned)((ctx->ndof + 255) / 256);
+    k_fdm_lsum_inv<<<b2, 256, 0, ctx->stream>>>(ctx->ndof, dim, N, (const double *)pd.L,
+                                                   pd.Lsum_inv);
+    PDG_CUDA_TRY(cudaGetLastError());
+  }
   PDG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   cudaFree(dLi);
   return PDG_OK;
@@ -1136,7 +1160,8 @@ void prec_free(pdg_context *ctx, int precision) {
   if (pd.iters) cudaFree(pd.iters);
   if (pd.inv16) cudaFree(pd.inv16);
   if (pd.invscale) cudaFree(pd.invscale);
-  pd = PrecData{0, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  if (pd.Lsum_inv) cudaFree(pd.Lsum_inv);
+  pd = PrecData{0, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 }
 
 int prec_setup_impl(pdg_context *ctx, int kind, int precision) {
@@ -1229,7 +1254,8 @@ static int fdm_apply_dn(pdg_context *ctx, const T *d, T *v, const int *skip, con
       (const T *)ctx->prec[std::is_same<T, double>::value ? 0 : 1].L, const_cast<T *>(d), v, skip,
       cells, ncells, scale, fuse ? ctx->fuse_part : nullptr, ctx->fuse_max_blocks, ctx->fuse_cnt,
       ctx->red_out, ctx->d_flag, ctx->fuse_fin,
-      (fuse && ctx->fuse_fin == FIN_CG_DEF_BETA) ? (const T *)ctx->fuse_q : nullptr);
+      (fuse && ctx->fuse_fin == FIN_CG_DEF_BETA) ? (const T *)ctx->fuse_q : nullptr,
+      std::is_same<T, double>::value ? (const T *)ctx->prec[0].Lsum_inv : nullptr);
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
 }
