@@ -847,7 +847,6 @@ static void invalidate(pdg_context *ctx, bool operator_changed) {
     ctx->op_gen++;
     ctx->rec_valid = 0;
     ctx->rec64m_valid = 0;
-    ctx->recfpm_valid = 0;
     ctx->recfp_valid = 0;
     ctx->rec32_valid = 0;
     ctx->rec32q_valid = 0;
@@ -1122,7 +1121,7 @@ int pdg_destroy(pdg_context *c) {
                   c->leg64, c->leg32, c->legw64[0], c->legw64[1], c->legw32[0], c->legw32[1],
                   c->fuse_part, c->fuse_cnt, c->Ac64, c->Aqv64, c->Aqf64, c->cq64, c->Ac32,
                   c->Aqv32, c->Aqf32, c->cq32, c->bqv64, c->bqf64, c->Kd64, c->Kd32,
-                  c->recfp, c->tabfp, c->rec32q, c->rec64m, c->tabm64, c->recfpm, c->tabfpm};
+                  c->recfp, c->tabfp, c->rec32q, c->rec64m, c->tabm64};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 10; i++)

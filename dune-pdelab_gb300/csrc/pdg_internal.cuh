@@ -172,8 +172,6 @@ struct pdg_context {
   int f64_pair;
   void *recfp, *tabfp;
   int recfp_valid;
-  void *recfpm, *tabfpm;   // float-pair copies of rec64m and of the mass-factored tables
-  int recfpm_valid;
   // velocity from point data (pdg_set_velocity_points) instead of Fourier
   // modes: volume points [ncell][nqv][3], face lattice [faces][nqf][3]
   int vel_points;
