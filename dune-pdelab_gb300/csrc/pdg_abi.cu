@@ -357,8 +357,9 @@ static int cg_device(pdg_context *ctx, T *x, T *b, T *p, T *q, double reduction,
   bool done = false;
   const bool fuse = std::is_same<T, float>::value && cg_fusable(ctx);
   if (fuse) PDG_TRY(ensure_fuse(ctx));
-  for (; i <= maxit && !done; i++) {
-    PDG_TRY(set_iter(ctx, rc, (double)i));
+  // one iteration's launches (the iteration count advances on the device)
+  auto body = [&]() -> int {
+    PDG_TRY(inc_iter(ctx, rc, 1.0));
     if (fuse) {
       // q = A p with lambda = rholast / <p, q> in the same launch
       ctx->fuse_fin = FIN_CG_LAMBDA;
@@ -382,11 +383,50 @@ static int cg_device(pdg_context *ctx, T *x, T *b, T *p, T *q, double reduction,
       PDG_TRY(dot<T>(ctx, rc, q, b, nullptr, nullptr, FIN_CG_BETA, -1, -1, true));   // beta
       PDG_TRY(cg_update_p<T>(ctx, rc, ctx->ndof, p, q));                           // p = q + beta p
     }
-    if (i % batch == 0 || i == maxit || i == 1) {
-      PDG_TRY(fetch_state(ctx, scal, flags));
+    return PDG_OK;
+  };
+  // After two batches run one by one (lazy set-up done, the solve not yet
+  // converged), a batch of iterations is captured once into a CUDA graph and
+  // replayed: one launch per batch instead of one per kernel, which is what
+  // small grids are bound by.  Launches after convergence skip their work.
+  cudaGraphExec_t gexec = nullptr;
+  const bool graphs = ctx->stream != nullptr && ctx->stream != cudaStreamLegacy &&
+                      ctx->stream != cudaStreamPerThread && !ctx->use_matrix;
+  int st = PDG_OK;
+  while (i <= maxit && !done) {
+    if (graphs && i > 2 * batch && i + batch - 1 <= maxit && (i - 1) % batch == 0) {
+      if (!gexec) {
+        cudaGraph_t g = nullptr;
+        PDG_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < batch && st == PDG_OK; k++) st = body();
+        const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+        if (st != PDG_OK || ce != cudaSuccess || !g ||
+            cudaGraphInstantiate(&gexec, g, 0) != cudaSuccess) {
+          if (g) cudaGraphDestroy(g);
+          if (gexec) cudaGraphExecDestroy(gexec);
+          cudaGetLastError();
+          return st != PDG_OK ? st : set_error(PDG_ECUDA, "CUDA graph capture of the CG batch failed");
+        }
+        cudaGraphDestroy(g);
+      }
+      if (cudaGraphLaunch(gexec, ctx->stream) != cudaSuccess) {
+        cudaGraphExecDestroy(gexec);
+        return set_error(PDG_ECUDA, "CUDA graph launch failed");
+      }
+      i += batch;
+    } else {
+      st = body();
+      if (st != PDG_OK) break;
+      i++;
+    }
+    if ((i - 1) % batch == 0 || i > maxit || i == 2) {
+      st = fetch_state(ctx, scal, flags);
+      if (st != PDG_OK) break;
       if (flags[F_STATE]) done = true;
     }
   }
+  if (gexec) cudaGraphExecDestroy(gexec);
+  PDG_TRY(st);
   if (fuse) PDG_TRY(cg_finish_x<T>(ctx, rc, ctx->ndof, x, p));
   PDG_TRY(fetch_state(ctx, scal, flags));
   out->state = flags[F_STATE];

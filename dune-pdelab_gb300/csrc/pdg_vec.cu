@@ -188,6 +188,11 @@ __global__ void k_set_iter(RedCtx rc, double it) {
   if (rc.flags[F_STATE]) return;
   rc.scal[S_ITER] = it;
 }
+// the same, counting on the device (launches replayed from a graph)
+__global__ void k_inc_iter(RedCtx rc, double step) {
+  if (rc.flags[F_STATE]) return;
+  rc.scal[S_ITER] += step;
+}
 
 static unsigned ew_grid(long n) {
   long g = (n + 255) / 256;
@@ -270,6 +275,11 @@ int bi_update_full(pdg_context *ctx, const RedCtx &rc, long n, T *x, T *r, const
 }
 int set_iter(pdg_context *ctx, const RedCtx &rc, double it) {
   k_set_iter<<<1, 1, 0, ctx->stream>>>(rc, it);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+int inc_iter(pdg_context *ctx, const RedCtx &rc, double step) {
+  k_inc_iter<<<1, 1, 0, ctx->stream>>>(rc, step);
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
 }

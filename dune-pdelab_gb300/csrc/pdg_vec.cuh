@@ -277,6 +277,7 @@ template <typename T>
 int bi_update_full(pdg_context *ctx, const RedCtx &rc, long n, T *x, T *r, const T *y,
                    const T *t);   // x += omega y; r -= omega t; def check; rho = rho_new
 int set_iter(pdg_context *ctx, const RedCtx &rc, double it);
+int inc_iter(pdg_context *ctx, const RedCtx &rc, double step);
 
 // plain vector kernels
 template <typename T>
