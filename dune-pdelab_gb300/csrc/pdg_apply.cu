@@ -637,11 +637,8 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
     PDG_TRY(ensure_record32(ctx));
     rec = (const T *)ctx->rec32;
   }
-#ifndef PDG_MFORM
-#define PDG_MFORM 1
-#endif
   if constexpr (std::is_same<T, double>::value) {
-    if (PDG_MFORM && !ctx->f64_pair && ctx->dim == 3 && rec && ctx->tabm64 && !a.transpose &&
+    if (!ctx->f64_pair && ctx->dim == 3 && rec && ctx->tabm64 && !a.transpose &&
         !a.diag_only && !a.cells) {
       // the mass-factored form (fewer FP64 operations; non-transposed only)
       PDG_TRY(launch_apply_m(ctx, a, p));

@@ -1168,12 +1168,9 @@ __device__ __forceinline__ float q3_run(const OpParams<float> &p, const ApplyArg
   return part;
 }
 
-// blocks per SM the register allocation is sized for
-#ifndef Q3T_MINB
-#define Q3T_MINB 5
-#endif
+// 5 blocks per SM (4: the same time at 96^3; 6: 254 against 227 us, spills)
 template <bool kTr>
-__global__ void __launch_bounds__(Q3T::THREADS, Q3T_MINB)
+__global__ void __launch_bounds__(Q3T::THREADS, 5)
     k_apply32_q3t(const OpParams<float> p, const ApplyArgs<float> a, const float *__restrict__ rec,
                   const Q3Tab tb, const __grid_constant__ CUtensorMap map_own,
                   const __grid_constant__ CUtensorMap map_run, int *tma_err) {
@@ -1506,10 +1503,7 @@ static int launch32_q3(pdg_context *ctx, const ApplyArgs<float> &a, const OpPara
         qt.d0p[h] = make_float2(qt.d0[2 * h], qt.d0[2 * h + 1]);
         qt.d1p[h] = make_float2(qt.d1[2 * h], qt.d1[2 * h + 1]);
       }
-#ifndef Q3_PERSIST
-#define Q3_PERSIST 1
-#endif
-      if (Q3_PERSIST && !a.accumulate && !a.add) {
+      if (!a.accumulate && !a.add) {
         // three resident blocks per SM (two phase-1 regions each); the
         // accumulating forms stay with one run per block, whose read of y
         // other resident blocks cover (96^3 Q3, y += J x: 220 us against 253)
