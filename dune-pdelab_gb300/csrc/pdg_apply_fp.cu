@@ -101,39 +101,107 @@ __global__ void k_to_pairs(long n, const double *__restrict__ src, fpair *__rest
 
 template <int N>
 struct FpCfg {
-  static constexpr int N2 = N * N, NB = N * N * N, TPC = N * N, NF = 6;
-  static constexpr int CPB = (128 / TPC) > 0 ? (128 / TPC) : 1;
-  static constexpr int THREADS = CPB * TPC;
+  static constexpr int N2 = N * N, NF = 6;
   static constexpr int NW = NF * (N + 1);               // neighbour-line coefficients
   static constexpr int RECW = 3 * N2 + 2 * NW;          // FP64 record (both forms)
-  static constexpr int RECU = 3 * N2 + NW;              // the part one launch uses
-  static constexpr int TAB = 2 * N2 + 2 * N;            // Mhat, Shat, d0, d1
-  // ue, Xs, Ys, Zs, face data (12 TPC), record part; padding per cell
-  static constexpr int PER_CELL = 4 * NB + 12 * TPC + RECU + 1;
-  // blocks per SM the register allocation must allow: 6 for Q2 (at most 86
-  // registers; 0.262 against 0.287 ms per 64^3 apply with the compiler's 96),
-  // the compiler's choice otherwise (0: no bound; Q4 bounded to 6 blocks:
+  // blocks per SM the register allocation must allow: 6 for Q2 (0.262 against
+  // 0.287 ms per 64^3 apply with the compiler's free choice, one z-level per
+  // instruction), the compiler's choice otherwise (Q4 bounded to 6 blocks:
   // 0.416 against 0.374 ms at 40^3)
   static constexpr int MINB = N == 3 ? 6 : 0;
 };
 
+// ---- the kernel: two z-levels per paired FP32 instruction ---------------------
+// Thread mapping and records of k_apply<double, 3, N>: N*N threads per cell,
+// each holding a z-column.  Each thread's chains for the z-levels z0 = 2 zp and
+// z1 = 2 zp + 1 run in the two lanes of FFMA2 / FADD2 / FMUL2 (one issue for
+// two lanes; a factor common to both levels is broadcast); every lane performs
+// the scalar float-pair operations (pmul / pmac / padd / norm) on its chain in
+// the scalar order, a lane-wise condition as the addition of an exact zero.
+// The shared arrays hold per z-pair (hi_z0, hi_z1, lo_z0, lo_z1) as one
+// 16-byte vector; with N odd the second lane of the last pair repeats the
+// first and is not stored.  (0.252 against 0.262 ms per 64^3 Q2 apply for the
+// same arithmetic one level per instruction, identical results.)
+struct f2p {
+  float2 hi, lo;
+};
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+__device__ __forceinline__ float2 bcf(float s) { return make_float2(s, s); }
+// acc += a * b, lane-wise pmac
+__device__ __forceinline__ void pmac2(f2p &acc, const f2p &a, const f2p &b) {
+  const float2 p = __fmul2_rn(a.hi, b.hi);
+  const float2 e = __ffma2_rn(a.hi, b.hi, neg2(p));
+  const float2 c = __ffma2_rn(a.hi, b.lo, __ffma2_rn(a.lo, b.hi, e));
+  const float2 s = __fadd2_rn(acc.hi, p);
+  const float2 bb = sub2(s, acc.hi);
+  const float2 t = __fadd2_rn(sub2(acc.hi, sub2(s, bb)), sub2(p, bb));
+  acc.hi = s;
+  acc.lo = __fadd2_rn(acc.lo, __fadd2_rn(t, c));
+}
+// acc += a, lane-wise padd
+__device__ __forceinline__ void padd2(f2p &acc, const f2p &a) {
+  const float2 s = __fadd2_rn(acc.hi, a.hi);
+  const float2 bb = sub2(s, acc.hi);
+  const float2 t = __fadd2_rn(sub2(acc.hi, sub2(s, bb)), sub2(a.hi, bb));
+  acc.hi = s;
+  acc.lo = __fadd2_rn(acc.lo, __fadd2_rn(t, a.lo));
+}
+__device__ __forceinline__ f2p pmul2(const f2p &a, const f2p &b) {
+  const float2 p = __fmul2_rn(a.hi, b.hi);
+  const float2 e = __ffma2_rn(a.hi, b.hi, neg2(p));
+  return f2p{p, __ffma2_rn(a.hi, b.lo, __ffma2_rn(a.lo, b.hi, e))};
+}
+__device__ __forceinline__ f2p norm2(const f2p &a) {
+  const float2 s = __fadd2_rn(a.hi, a.lo);
+  return f2p{s, sub2(a.lo, sub2(s, a.hi))};
+}
+__device__ __forceinline__ f2p bcp(fpair a) { return f2p{bcf(a.hi), bcf(a.lo)}; }
+__device__ __forceinline__ f2p two(fpair a, fpair b) {
+  return f2p{make_float2(a.hi, b.hi), make_float2(a.lo, b.lo)};
+}
+__device__ __forceinline__ f2p from4(float4 v) {
+  return f2p{make_float2(v.x, v.y), make_float2(v.z, v.w)};
+}
+__device__ __forceinline__ float4 to4(const f2p &a) {
+  return make_float4(a.hi.x, a.hi.y, a.lo.x, a.lo.y);
+}
+__device__ __forceinline__ fpair lane(const f2p &a, int k) {
+  return k ? fpair{a.hi.y, a.lo.y} : fpair{a.hi.x, a.lo.x};
+}
+
 template <int N>
-__global__ void __launch_bounds__(FpCfg<N>::THREADS, FpCfg<N>::MINB)
-    k_apply_fp(const OpParams<double> p, const ApplyArgs<double> a, const fpair *__restrict__ rec,
-               const fpair *__restrict__ tab) {
-  using C = FpCfg<N>;
-  constexpr int N2 = C::N2, NB = C::NB, TPC = C::TPC, CPB = C::CPB, NF = C::NF;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  fpair *tM = reinterpret_cast<fpair *>(smem_raw);
+struct Fp2Cfg {
+  static constexpr int N2 = N * N, NB = N * N * N, TPC = N * N, NF = 6, NZP = (N + 1) / 2;
+  static constexpr int CPB = (128 / TPC) > 0 ? (128 / TPC) : 1;
+  static constexpr int THREADS = CPB * TPC;
+  static constexpr int NW = NF * (N + 1);
+  static constexpr int RECW = 3 * N2 + 2 * NW;
+  static constexpr int RECU = 3 * N2 + NW;
+  static constexpr int TAB = 2 * N2 + 2 * N;            // Mhat, Shat, d0, d1
+  // per cell in 16-byte units: U, X, Y, Z as z-pairs (4 NZP N2), face data
+  // (12 TPC fpairs), record part (RECU fpairs); one unit of padding
+  static constexpr int PER_CELL = 4 * NZP * N2 + 6 * TPC + (RECU + 1) / 2 + 1;
+  static constexpr int TAB16 = (TAB + 1) / 2;
+  static constexpr int MINB = FpCfg<N>::MINB;
+};
+
+template <int N>
+__global__ void __launch_bounds__(Fp2Cfg<N>::THREADS, Fp2Cfg<N>::MINB)
+    k_apply_fp2(const OpParams<double> p, const ApplyArgs<double> a,
+                const fpair *__restrict__ rec, const fpair *__restrict__ tab) {
+  using C = Fp2Cfg<N>;
+  constexpr int N2 = C::N2, NB = C::NB, TPC = C::TPC, CPB = C::CPB, NF = C::NF, NZP = C::NZP;
+  extern __shared__ __align__(16) float4 fp2_raw[];
+  fpair *tM = reinterpret_cast<fpair *>(fp2_raw);
   fpair *td0 = tM + 2 * N2;          // (Shat is not needed: it is folded into the record)
   fpair *td1 = td0 + N;
   const int t = threadIdx.x;
   const int cs = t / TPC;
   const int l = t - cs * TPC;
-  fpair *cellmem = tM + C::TAB + cs * C::PER_CELL;
-  fpair *ue = cellmem;
-  fpair *Xs = ue + NB, *Ys = Xs + NB, *Zs = Ys + NB;
-  fpair *fa = Zs + NB;               // [2 NF][TPC]
+  float4 *UP = fp2_raw + C::TAB16 + cs * C::PER_CELL;   // [NZP][N2]
+  float4 *XP = UP + NZP * N2, *YP = XP + NZP * N2, *ZP = YP + NZP * N2;
+  fpair *fa = reinterpret_cast<fpair *>(ZP + NZP * N2);  // [2 NF][TPC]
   fpair *Am = fa + 2 * NF * TPC;     // A'_dir [3][N2], then the line coefficients [NF][N+1]
   fpair *W = Am + 3 * N2;
 
@@ -187,9 +255,11 @@ __global__ void __launch_bounds__(FpCfg<N>::THREADS, FpCfg<N>::MINB)
   }
   fpair col[N];
 #pragma unroll
-  for (int z = 0; z < N; z++) {
-    col[z] = split_bits(cold[z]);
-    ue[z * TPC + l] = col[z];
+  for (int z = 0; z < N; z++) col[z] = split_bits(cold[z]);
+#pragma unroll
+  for (int zp = 0; zp < NZP; zp++) {
+    const fpair c0 = col[2 * zp], c1 = col[2 * zp + 1 < N ? 2 * zp + 1 : 2 * zp];
+    UP[zp * N2 + l] = make_float4(c0.hi, c1.hi, c0.lo, c1.lo);
   }
   __syncthreads();
 
@@ -226,60 +296,60 @@ __global__ void __launch_bounds__(FpCfg<N>::THREADS, FpCfg<N>::MINB)
     Mtx[q] = tM[tx * N + q];
     Mty[q] = tM[ty * N + q];
   }
-  const fpair d0x = td0[tx], d1x = td1[tx], d0y = td0[ty], d1y = td1[ty];
+  const f2p d0x = bcp(td0[tx]), d1x = bcp(td1[tx]), d0y = bcp(td0[ty]), d1y = bcp(td1[ty]);
   const fpair zf0 = fa[8 * TPC + l], zf1 = fa[9 * TPC + l];
   const fpair zf2 = fa[10 * TPC + l], zf3 = fa[11 * TPC + l];
-  fpair X[N], Y[N], Z[N];
+  const fpair zero{0.f, 0.f};
+  // ---- X, Y, Z: the directional operators with the face terms ----
 #pragma unroll
-  for (int z = 0; z < N; z++) {
-    fpair sx = pmul(Arx[0], ue[z * N2 + ty * N]);
-    fpair sy = pmul(Ary[0], ue[z * N2 + tx]);
-    fpair sz = pmul(Aat(2, z, 0), col[0]);
+  for (int zp = 0; zp < NZP; zp++) {
+    const int z0 = 2 * zp, z1 = 2 * zp + 1 < N ? 2 * zp + 1 : 2 * zp;
+    f2p sx = pmul2(bcp(Arx[0]), from4(UP[zp * N2 + ty * N]));
+    f2p sy = pmul2(bcp(Ary[0]), from4(UP[zp * N2 + tx]));
+    f2p sz = pmul2(two(Aat(2, z0, 0), Aat(2, z1, 0)), bcp(col[0]));
 #pragma unroll
     for (int q = 1; q < N; q++) {
-      pmac(sx, Arx[q], ue[z * N2 + ty * N + q]);
-      pmac(sy, Ary[q], ue[z * N2 + q * N + tx]);
-      pmac(sz, Aat(2, z, q), col[q]);
+      pmac2(sx, bcp(Arx[q]), from4(UP[zp * N2 + ty * N + q]));
+      pmac2(sy, bcp(Ary[q]), from4(UP[zp * N2 + q * N + tx]));
+      pmac2(sz, two(Aat(2, z0, q), Aat(2, z1, q)), bcp(col[q]));
     }
-    const int lx = z * N + ty, ly = z * N + tx;
-    if (tx == 0) padd(sx, fa[0 * TPC + lx]);
-    pmac(sx, d0x, fa[1 * TPC + lx]);
-    if (tx == N - 1) padd(sx, fa[2 * TPC + lx]);
-    pmac(sx, d1x, fa[3 * TPC + lx]);
-    if (ty == 0) padd(sy, fa[4 * TPC + ly]);
-    pmac(sy, d0y, fa[5 * TPC + ly]);
-    if (ty == N - 1) padd(sy, fa[6 * TPC + ly]);
-    pmac(sy, d1y, fa[7 * TPC + ly]);
-    if (z == 0) padd(sz, zf0);
-    pmac(sz, td0[z], zf1);
-    if (z == N - 1) padd(sz, zf2);
-    pmac(sz, td1[z], zf3);
-    X[z] = norm(sx);
-    Y[z] = norm(sy);
-    Z[z] = norm(sz);
-  }
-#pragma unroll
-  for (int z = 0; z < N; z++) {
-    Xs[z * N2 + l] = X[z];
-    Ys[z * N2 + l] = Y[z];
-    Zs[z * N2 + l] = Z[z];
+    const int lx0 = z0 * N + ty, lx1 = z1 * N + ty, ly0 = z0 * N + tx, ly1 = z1 * N + tx;
+    auto fp2 = [&](int arr, int i0, int i1) -> f2p {
+      return two(fa[arr * TPC + i0], fa[arr * TPC + i1]);
+    };
+    if (tx == 0) padd2(sx, fp2(0, lx0, lx1));
+    pmac2(sx, d0x, fp2(1, lx0, lx1));
+    if (tx == N - 1) padd2(sx, fp2(2, lx0, lx1));
+    pmac2(sx, d1x, fp2(3, lx0, lx1));
+    if (ty == 0) padd2(sy, fp2(4, ly0, ly1));
+    pmac2(sy, d0y, fp2(5, ly0, ly1));
+    if (ty == N - 1) padd2(sy, fp2(6, ly0, ly1));
+    pmac2(sy, d1y, fp2(7, ly0, ly1));
+    // z faces: the lower-face value enters level 0 only, the upper one level N-1
+    padd2(sz, two(z0 == 0 ? zf0 : zero, z1 == 0 ? zf0 : zero));
+    pmac2(sz, two(td0[z0], td0[z1]), bcp(zf1));
+    padd2(sz, two(z0 == N - 1 ? zf2 : zero, z1 == N - 1 ? zf2 : zero));
+    pmac2(sz, two(td1[z0], td1[z1]), bcp(zf3));
+    XP[zp * N2 + l] = to4(norm2(sx));
+    YP[zp * N2 + l] = to4(norm2(sy));
+    ZP[zp * N2 + l] = to4(norm2(sz));
   }
   __syncthreads();
   // W = M_y X + M_x Y ; T1 = M_x Z   (tangential masses; scales are in A')
-  fpair Wv[N];
+  f2p Wv[NZP];
 #pragma unroll
-  for (int z = 0; z < N; z++) {
-    fpair w = pmul(Mty[0], Xs[z * N2 + tx]);
-    fpair t1 = pmul(Mtx[0], Zs[z * N2 + ty * N]);
-    pmac(w, Mtx[0], Ys[z * N2 + ty * N]);
+  for (int zp = 0; zp < NZP; zp++) {
+    f2p w = pmul2(bcp(Mty[0]), from4(XP[zp * N2 + tx]));
+    f2p t1 = pmul2(bcp(Mtx[0]), from4(ZP[zp * N2 + ty * N]));
+    pmac2(w, bcp(Mtx[0]), from4(YP[zp * N2 + ty * N]));
 #pragma unroll
     for (int q = 1; q < N; q++) {
-      pmac(w, Mty[q], Xs[z * N2 + q * N + tx]);
-      pmac(w, Mtx[q], Ys[z * N2 + ty * N + q]);
-      pmac(t1, Mtx[q], Zs[z * N2 + ty * N + q]);
+      pmac2(w, bcp(Mty[q]), from4(XP[zp * N2 + q * N + tx]));
+      pmac2(w, bcp(Mtx[q]), from4(YP[zp * N2 + ty * N + q]));
+      pmac2(t1, bcp(Mtx[q]), from4(ZP[zp * N2 + ty * N + q]));
     }
-    Wv[z] = norm(w);
-    ue[z * N2 + l] = norm(t1);   // ue is free: all reads finished before the sync
+    Wv[zp] = norm2(w);
+    UP[zp * N2 + l] = to4(norm2(t1));   // UP is free: all reads finished before the sync
   }
   __syncthreads();
   // out = M_z W + M_y T1, joined to FP64
@@ -288,38 +358,44 @@ __global__ void __launch_bounds__(FpCfg<N>::THREADS, FpCfg<N>::MINB)
     const double *ad = a.add ? a.add + (size_t)e * NB : nullptr;
     const bool scale = a.alpha != 1.0;
 #pragma unroll
-    for (int z = 0; z < N; z++) {
-      fpair s = pmul(tM[z * N], Wv[0]);
-      pmac(s, Mty[0], ue[z * N2 + tx]);
+    for (int zp = 0; zp < NZP; zp++) {
+      const int z0 = 2 * zp, z1 = 2 * zp + 1 < N ? 2 * zp + 1 : 2 * zp;
+      f2p s = pmul2(two(tM[z0 * N], tM[z1 * N]), bcp(lane(Wv[0], 0)));
+      pmac2(s, bcp(Mty[0]), from4(UP[zp * N2 + tx]));
 #pragma unroll
       for (int q = 1; q < N; q++) {
-        pmac(s, tM[z * N + q], Wv[q]);
-        pmac(s, Mty[q], ue[z * N2 + q * N + tx]);
+        pmac2(s, two(tM[z0 * N + q], tM[z1 * N + q]), bcp(lane(Wv[q >> 1], q & 1)));
+        pmac2(s, bcp(Mty[q]), from4(UP[zp * N2 + q * N + tx]));
       }
-      const int idx = z * TPC + l;
-      double r = join(s);
-      if (scale) r *= a.alpha;
-      if (a.accumulate) r += ye[idx];
-      if (ad) r += ad[idx];
-      ye[idx] = r;
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const int z = 2 * zp + k;
+        if (z >= N) break;
+        const int idx = z * TPC + l;
+        double r = join(lane(s, k));
+        if (scale) r *= a.alpha;
+        if (a.accumulate) r += ye[idx];
+        if (ad) r += ad[idx];
+        ye[idx] = r;
+      }
     }
   }
 }
 
 template <int N>
-static int launch_fp_n(pdg_context *ctx, const ApplyArgs<double> &a, const OpParams<double> &p) {
-  using C = FpCfg<N>;
-  const size_t smem = sizeof(fpair) * (C::TAB + C::CPB * C::PER_CELL);
+static int launch_fp2_n(pdg_context *ctx, const ApplyArgs<double> &a, const OpParams<double> &p) {
+  using C = Fp2Cfg<N>;
+  const size_t smem = 16 * (C::TAB16 + C::CPB * C::PER_CELL);
   static int attr_dev = -1;
   if (attr_dev != ctx->device) {
-    PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply_fp<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    PDG_CUDA_TRY(cudaFuncSetAttribute(k_apply_fp2<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
     attr_dev = ctx->device;
   }
   const long work = (a.cells || a.ncells > 0) ? a.ncells : ctx->ncell;
   if (work <= 0) return PDG_OK;
   const unsigned blocks = (unsigned)((work + C::CPB - 1) / C::CPB);
-  k_apply_fp<N><<<blocks, C::THREADS, smem, ctx->stream>>>(
+  k_apply_fp2<N><<<blocks, C::THREADS, smem, ctx->stream>>>(
       p, a, reinterpret_cast<const fpair *>(ctx->recfp),
       reinterpret_cast<const fpair *>(ctx->tabfp));
   PDG_CUDA_TRY(cudaGetLastError());
@@ -360,10 +436,10 @@ int launch_apply_float_pair(pdg_context *ctx, const ApplyArgs<double> &a) {
   OpParams<double> p = make_params<double>(ctx, ctx->K64, ctx->c64, ctx->tab64);
   PDG_TRY(prepare_float_pair(ctx));
   switch (ctx->N) {
-    case 2: return launch_fp_n<2>(ctx, a, p);
-    case 3: return launch_fp_n<3>(ctx, a, p);
-    case 4: return launch_fp_n<4>(ctx, a, p);
-    case 5: return launch_fp_n<5>(ctx, a, p);
+    case 2: return launch_fp2_n<2>(ctx, a, p);
+    case 3: return launch_fp2_n<3>(ctx, a, p);
+    case 4: return launch_fp2_n<4>(ctx, a, p);
+    case 5: return launch_fp2_n<5>(ctx, a, p);
     default: return set_error(PDG_EUNSUPPORTED, "degree not compiled in");
   }
 }
