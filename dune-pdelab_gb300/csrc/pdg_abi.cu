@@ -324,10 +324,20 @@ static bool cg_fusable(const pdg_context *ctx) {
          ctx->prec[PDG_F32].ready && ctx->prec[PDG_F32].kind == PDG_PREC_BJ_FDM;
 }
 
+// FP64 CG with three launches per iteration on 2D grids (<p, A p> in the
+// operator, the residual update and <M^-1 r, r> in the FDM block Jacobi): 2D
+// grids are small and launch-bound.  In 3D the FP64 kernels are bound by the
+// FP64 pipe, and the fused products made the 64^3 Q2 iteration slower.
+static bool cg_fusable64(const pdg_context *ctx, int transpose) {
+  return !transpose && ctx->dim == 2 && !convection_on(ctx) && ctx->nl_deg == 0 &&
+         !general_coefficients(ctx) && ctx->basis != PDG_BASIS_LEGENDRE && !ctx->use_matrix &&
+         !ctx->ops32 && ctx->prec[PDG_F64].ready && ctx->prec[PDG_F64].kind == PDG_PREC_BJ_FDM;
+}
+
 static int ensure_fuse(pdg_context *ctx) {
   if (ctx->fuse_part) return PDG_OK;
-  // the fused kernels run at least 8 cells per block
-  const long maxb = ctx->ncell / 8 + 2;
+  // the fused kernels run at least 5 cells per block
+  const long maxb = ctx->ncell / 5 + 2;
   const long ngroups = (maxb + kFuseGroup - 1) / kFuseGroup;
   PDG_CUDA_TRY(cudaMalloc(&ctx->fuse_part, sizeof(double) * 2 * (maxb + ngroups)));
   PDG_CUDA_TRY(cudaMalloc(&ctx->fuse_cnt, sizeof(int) * ngroups));
@@ -355,7 +365,8 @@ static int cg_device(pdg_context *ctx, T *x, T *b, T *p, T *q, double reduction,
   int i = 1;
   const int batch = 8;
   bool done = false;
-  const bool fuse = std::is_same<T, float>::value && cg_fusable(ctx);
+  const bool fuse = std::is_same<T, float>::value ? cg_fusable(ctx)
+                                                  : cg_fusable64(ctx, transpose);
   if (fuse) PDG_TRY(ensure_fuse(ctx));
   // one iteration's launches (the iteration count advances on the device)
   auto body = [&]() -> int {

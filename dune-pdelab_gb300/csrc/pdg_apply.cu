@@ -36,6 +36,7 @@
 // memory.  d = 2: N threads per cell holding y-columns.  All neighbour
 // lines are loaded before any arithmetic so that 2dN loads are in flight.
 #include "pdg_ops.cuh"
+#include "pdg_vec.cuh"
 
 namespace pdg {
 
@@ -444,6 +445,7 @@ __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
     }
   }
 
+  double part = 0.0;   // <x, y_out> of this thread's entries (fused CG dot)
   if (active) {
     T *ye = a.y + (size_t)e * NB;
     const T *ad = a.add ? a.add + (size_t)e * NB : nullptr;
@@ -455,7 +457,17 @@ __global__ void __launch_bounds__(Cfg<D, N>::THREADS)
       if (a.accumulate) r += ye[idx];
       if (ad) r += ad[idx];
       ye[idx] = r;
+      part += (double)col[z] * (double)r;
     }
+  }
+  // (compiled for the 2D FP64 operator only, the one fused CG that uses it)
+  if constexpr (D == 2 && sizeof(T) == 8) if (a.dot_part) {
+    // block sums in the cell memory, free once every thread is past its reads
+    __syncthreads();
+    reduce_tail_grouped<C::THREADS, true>(a.dot_part, a.dot_max_blocks, a.dot_cnt,
+                                          RedCtx{nullptr, a.dot_scal, a.dot_flags}, part, 0.0,
+                                          a.dot_fin, -1, -1,
+                                          reinterpret_cast<double *>(smem_raw));
   }
 }
 
@@ -504,7 +516,17 @@ static int launch_apply_dn(pdg_context *ctx, const ApplyArgs<T> &a, const OpPara
   const long work = (a.cells || a.ncells > 0) ? a.ncells : ctx->ncell;
   if (work <= 0) return PDG_OK;
   const long blocks = (work + C::CPB - 1) / C::CPB;
-  k_apply<T, D, N><<<(unsigned)blocks, C::THREADS, smem, ctx->stream>>>(p, a, rec);
+  ApplyArgs<T> af = a;
+  if (ctx->fuse_fin && !a.cells && a.ncells == 0) {
+    // the fused CG: <p, A p> -> lambda in the same launch
+    af.dot_part = ctx->fuse_part;
+    af.dot_max_blocks = ctx->fuse_max_blocks;
+    af.dot_cnt = ctx->fuse_cnt;
+    af.dot_scal = ctx->red_out;
+    af.dot_flags = ctx->d_flag;
+    af.dot_fin = ctx->fuse_fin;
+  }
+  k_apply<T, D, N><<<(unsigned)blocks, C::THREADS, smem, ctx->stream>>>(p, af, rec);
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
 }
