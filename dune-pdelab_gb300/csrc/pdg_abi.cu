@@ -1512,7 +1512,9 @@ static int ensure_stage(pdg_context *ctx) {
 // copies out overlap, ordered by events.  Consecutive slabs are applied on
 // two alternating streams: they write disjoint ranges of y, and the last,
 // partly filled wave of one slab's grid overlaps the first of the next.
-constexpr int kMaxSlabs = 16;
+constexpr int kMaxSlabs = kPipeMaxSlabs;
+static_assert(sizeof(pdg_context::pipe_ev) / sizeof(cudaEvent_t) == 2 * kMaxSlabs + 3,
+              "one event per slab each way, plus start, end and the second stream's");
 constexpr long kMinSlabCells = 16384;
 
 static int cuda_status(cudaError_t e) {

@@ -16,6 +16,8 @@ namespace pdg {
 constexpr int kMaxDim = 3;
 constexpr int kMaxDeg = 4;
 constexpr int kMaxN1 = kMaxDeg + 1;
+// most slabs a host-vector apply is pipelined over (sizes the context's events)
+constexpr int kPipeMaxSlabs = 16;
 constexpr int kMaxModes = 16;
 
 // Records a message for pdg_last_error() and returns the status code.
@@ -256,7 +258,7 @@ struct pdg_context {
   double *stage_a, *stage_b;
   // host-buffer applies pipelined over slabs: copy streams and their events
   cudaStream_t pipe_h2d, pipe_d2h, pipe_k2;
-  cudaEvent_t pipe_ev[35];
+  cudaEvent_t pipe_ev[2 * pdg::kPipeMaxSlabs + 3];   // per slab in / out, start, end, k2
 
   // solver work vectors (lazily allocated)
   double *w64[10];
