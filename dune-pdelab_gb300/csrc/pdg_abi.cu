@@ -898,6 +898,7 @@ static void invalidate(pdg_context *ctx, bool operator_changed) {
     ctx->op_gen++;
     ctx->rec_valid = 0;
     ctx->rec64m_valid = 0;
+    ctx->rec64mT_valid = 0;
     ctx->recfp_valid = 0;
     ctx->rec32_valid = 0;
     ctx->rec32q_valid = 0;
@@ -1172,7 +1173,7 @@ int pdg_destroy(pdg_context *c) {
                   c->leg64, c->leg32, c->legw64[0], c->legw64[1], c->legw32[0], c->legw32[1],
                   c->fuse_part, c->fuse_cnt, c->Ac64, c->Aqv64, c->Aqf64, c->cq64, c->Ac32,
                   c->Aqv32, c->Aqf32, c->cq32, c->bqv64, c->bqf64, c->Kd64, c->Kd32,
-                  c->recfp, c->tabfp, c->rec32q, c->rec64m, c->tabm64};
+                  c->recfp, c->tabfp, c->rec32q, c->rec64m, c->rec64mT, c->tabm64};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 10; i++)
@@ -1551,7 +1552,7 @@ static int apply_pipelined(pdg_context *ctx, const double *x, double *y, const d
                            double *ydev, bool hx, bool hy, const double *add, double alpha,
                            int acc, int transpose, int nslab, long pps) {
   PDG_TRY(pipe_ready(ctx));
-  PDG_TRY(prepare_apply64(ctx));
+  PDG_TRY(prepare_apply64(ctx, transpose));
   const long plane = ctx->ncell / ctx->cfg.cells[ctx->dim - 1];
   const long nb = ctx->nb;
   cudaEvent_t *ev_in = ctx->pipe_ev, *ev_out = ctx->pipe_ev + kMaxSlabs;

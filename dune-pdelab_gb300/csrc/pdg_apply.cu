@@ -594,9 +594,10 @@ static int ensure_record(pdg_context *ctx) {
 
 // the FP64 operator's lazily built per-cell records, built now (before
 // launches are spread over several streams)
-int prepare_apply64(pdg_context *ctx) {
+int prepare_apply64(pdg_context *ctx, int transpose) {
   PDG_TRY(ensure_record(ctx));
-  if (ctx->dim == 3 && ctx->tabm64 && !general_coefficients(ctx)) PDG_TRY(prepare_apply_m(ctx));
+  if (ctx->dim == 3 && ctx->tabm64 && !general_coefficients(ctx))
+    PDG_TRY(prepare_apply_m(ctx, transpose));
   if (ctx->f64_pair && ctx->dim == 3 && !general_coefficients(ctx))
     PDG_TRY(prepare_float_pair(ctx));
   return PDG_OK;
@@ -660,9 +661,9 @@ int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c
     rec = (const T *)ctx->rec32;
   }
   if constexpr (std::is_same<T, double>::value) {
-    if (!ctx->f64_pair && ctx->dim == 3 && rec && ctx->tabm64 && !a.transpose &&
-        !a.diag_only && !a.cells) {
-      // the mass-factored form (fewer FP64 operations; non-transposed only)
+    if (!ctx->f64_pair && ctx->dim == 3 && rec && ctx->tabm64 && !a.diag_only && !a.cells) {
+      // the mass-factored form (fewer FP64 operations), the operator or its
+      // transpose
       PDG_TRY(launch_apply_m(ctx, a, p));
       if (convection_on(ctx)) PDG_TRY(launch_convection<T>(ctx, a));
       return nl_apply<T>(ctx, a);

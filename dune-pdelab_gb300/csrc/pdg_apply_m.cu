@@ -1,5 +1,5 @@
 // pdg_apply_m.cu -- the 3D FP64 cell operator with the mass matrix factored
-// out (the form of the non-transposed coupled applies).
+// out (the form of the coupled applies, of the operator and of its transpose).
 //
 // Same operator as k_apply<double, 3, N> (pdg_apply.cu; reference:
 // ConvectionDiffusionDG::jacobian_apply_volume / _skeleton / _boundary,
@@ -42,23 +42,31 @@ struct MCfg {
 };
 
 // B_dir = Mhat^-1 A'_dir from the FP64 record, with the operator's line
-// coefficients
+// coefficients.  For the transposed operator the kernel below runs unchanged
+// on B_dir = Mhat^-1 A'_dir^T and the transpose's line coefficients: the
+// transposed block row of a cell has the same form (directional matrices
+// A'_dir^T, face couplings (e0 s1 + d0 s2) (x) Mhat (x) Mhat with the
+// transpose's neighbour-line terms).
 template <int N>
 __global__ void k_record_m(long ncell, const double *__restrict__ rec,
-                           const double *__restrict__ minv, double *__restrict__ out) {
+                           const double *__restrict__ minv, double *__restrict__ out,
+                           int transpose) {
   using C = MCfg<N>;
   const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= ncell) return;
   const double *r = rec + e * C::RECW;
   double *o = out + e * C::RECM;
+  // A'_dir[k][q] at r[k * N + q]; its transpose's entry [k][q] at r[q * N + k]
+  const int sk = transpose ? 1 : N, sq = transpose ? N : 1;
   for (int d = 0; d < 3; d++)
     for (int i = 0; i < N; i++)
       for (int q = 0; q < N; q++) {
         double s = 0.0;
-        for (int k = 0; k < N; k++) s += minv[i * N + k] * r[d * C::N2 + k * N + q];
+        for (int k = 0; k < N; k++) s += minv[i * N + k] * r[d * C::N2 + k * sk + q * sq];
         o[d * C::N2 + i * N + q] = s;
       }
-  for (int j = 0; j < C::NW; j++) o[3 * C::N2 + j] = r[3 * C::N2 + j];
+  const double *w = r + 3 * C::N2 + (transpose ? C::NW : 0);
+  for (int j = 0; j < C::NW; j++) o[3 * C::N2 + j] = w[j];
 }
 
 template <int N>
@@ -228,30 +236,33 @@ __global__ void __launch_bounds__(MCfg<N>::THREADS)
 }
 
 template <int N>
-static int record_m_n(pdg_context *ctx) {
+static int record_m_n(pdg_context *ctx, int transpose) {
   using C = MCfg<N>;
-  if (!ctx->rec64m)
-    PDG_CUDA_TRY(cudaMalloc(&ctx->rec64m, sizeof(double) * C::RECM * ctx->ncell));
+  double *&out = transpose ? ctx->rec64mT : ctx->rec64m;
+  if (!out) PDG_CUDA_TRY(cudaMalloc(&out, sizeof(double) * C::RECM * ctx->ncell));
   const unsigned blocks = (unsigned)((ctx->ncell + 127) / 128);
-  k_record_m<N><<<blocks, 128, 0, ctx->stream>>>(ctx->ncell, ctx->rec64,
-                                                 ctx->tabm64 + C::TAB, ctx->rec64m);
+  k_record_m<N><<<blocks, 128, 0, ctx->stream>>>(ctx->ncell, ctx->rec64, ctx->tabm64 + C::TAB,
+                                                 out, transpose);
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
 }
 
-int prepare_apply_m(pdg_context *ctx) {
-  if (ctx->rec64m_valid) return PDG_OK;
+// the records of the operator (transpose 0) or of its transpose (1), built
+// once per coefficient field
+int prepare_apply_m(pdg_context *ctx, int transpose) {
+  int &valid = transpose ? ctx->rec64mT_valid : ctx->rec64m_valid;
+  if (valid) return PDG_OK;
   if (!ctx->rec_valid || !ctx->tabm64)
     return set_error(PDG_EINVAL, "mass-factored records need the FP64 records and tables");
   int st;
   switch (ctx->N) {
-    case 2: st = record_m_n<2>(ctx); break;
-    case 3: st = record_m_n<3>(ctx); break;
-    case 4: st = record_m_n<4>(ctx); break;
-    case 5: st = record_m_n<5>(ctx); break;
+    case 2: st = record_m_n<2>(ctx, transpose); break;
+    case 3: st = record_m_n<3>(ctx, transpose); break;
+    case 4: st = record_m_n<4>(ctx, transpose); break;
+    case 5: st = record_m_n<5>(ctx, transpose); break;
     default: return set_error(PDG_EUNSUPPORTED, "degree not compiled in");
   }
-  if (st == PDG_OK) ctx->rec64m_valid = 1;
+  if (st == PDG_OK) valid = 1;
   return st;
 }
 
@@ -268,13 +279,14 @@ static int launch_m_n(pdg_context *ctx, const ApplyArgs<double> &a, const OpPara
   const long work = a.ncells > 0 ? a.ncells : ctx->ncell;
   if (work <= 0) return PDG_OK;
   const unsigned blocks = (unsigned)((work + C::CPB - 1) / C::CPB);
-  k_apply_m<N><<<blocks, C::THREADS, smem, ctx->stream>>>(p, a, ctx->rec64m, ctx->tabm64);
+  k_apply_m<N><<<blocks, C::THREADS, smem, ctx->stream>>>(
+      p, a, a.transpose ? ctx->rec64mT : ctx->rec64m, ctx->tabm64);
   PDG_CUDA_TRY(cudaGetLastError());
   return PDG_OK;
 }
 
 int launch_apply_m(pdg_context *ctx, const ApplyArgs<double> &a, const OpParams<double> &p) {
-  PDG_TRY(prepare_apply_m(ctx));
+  PDG_TRY(prepare_apply_m(ctx, a.transpose));
   switch (ctx->N) {
     case 2: return launch_m_n<2>(ctx, a, p);
     case 3: return launch_m_n<3>(ctx, a, p);

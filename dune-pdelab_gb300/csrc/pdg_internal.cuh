@@ -152,6 +152,8 @@ struct pdg_context {
   int rec_valid;
   double *rec64m;      // 3D: Mhat^-1 A'_dir and the operator's line coefficients (k_apply_m)
   int rec64m_valid;
+  double *rec64mT;     // 3D: Mhat^-1 A'_dir^T and the transpose's line coefficients
+  int rec64mT_valid;
   double *tabm64;      // 3D: Mhat, Mhat^-1 e0, Mhat^-1 e_{N-1}, Mhat^-1 d0, Mhat^-1 d1, Mhat^-1
   float *rec32;        // the same records rounded to FP32 (3D FP32 operator)
   int rec32_valid;
@@ -277,7 +279,7 @@ template <typename T>
 int launch_apply(pdg_context *ctx, const ApplyArgs<T> &a, const T *K, const T *c,
                  const T *tab);
 int launch_rhs(pdg_context *ctx);
-int prepare_apply64(pdg_context *ctx);
+int prepare_apply64(pdg_context *ctx, int transpose);
 // per-cell change of basis out = acc*out + alpha (M (x) M (x) M) in + add with
 // M = T (which 0) or T^{-1} (which 1), transposed if `transpose`
 template <typename T>
@@ -369,9 +371,10 @@ __host__ __device__ inline long face_lattice_index(const int *nc, int dim, int d
 int launch_apply_float_pair(pdg_context *ctx, const ApplyArgs<double> &a);
 int prepare_float_pair(pdg_context *ctx);
 // the 3D FP64 operator with the mass matrix factored out (pdg_apply_m.cu;
-// non-transposed, coupled, all cells or a cell range); rec64 must be valid
+// the operator or its transpose, coupled, all cells or a cell range); rec64
+// must be valid
 int launch_apply_m(pdg_context *ctx, const ApplyArgs<double> &a, const OpParams<double> &p);
-int prepare_apply_m(pdg_context *ctx);
+int prepare_apply_m(pdg_context *ctx, int transpose);
 
 // parameter fields beyond A = K I: true when the Gauss-point operator replaces
 // the Kronecker kernels; its launch (diffusion and reaction terms only)

@@ -117,6 +117,22 @@ def test_transpose_apply(pdg, oracle, method):
     assert _rel(y, P.blocks_apply(A, x, transpose=True)) <= TOL64
 
 
+@pytest.mark.parametrize("dim,k,n", CASES)
+def test_transpose_apply_every_degree(pdg, oracle, dim, k, n):
+    # the transposed operator of the non-symmetric method (NIPG, weights on)
+    # with reaction and mixed boundary types, accumulated onto y0, against the
+    # oracle's matrix-free transpose (convectiondiffusiondg.hh:191-195,
+    # 474-481, 892-899 with the roles of trial and test functions exchanged)
+    bct = [1, -1, -3, 1, -1, 1][:2 * dim]
+    go, P, rng = _pair(pdg, oracle, dim, k, n, seed=40 + dim * 10 + k, method=0, weights=1,
+                       react=True, bctype=bct)
+    x = rng.uniform(-1, 1, go.ndof)
+    y0 = rng.uniform(-1, 1, go.ndof)
+    y = y0.copy()
+    go.jacobian_apply_transpose(x, y)
+    assert _rel(y, y0 + P.jacobian_apply_transpose(x)) <= TOL64
+
+
 @pytest.mark.parametrize("dim,k,n", [(2, 1, 6), (3, 2, 3), (3, 3, 3), (3, 4, 2)])
 def test_jacobian_apply_f32(pdg, oracle, dim, k, n):
     import torch
