@@ -106,6 +106,26 @@ def test_matrix_free_equals_assembled(oracle, dim, k, n):
     assert np.max(np.abs(y3 - y)) <= 1e-12 * np.max(np.abs(y))
 
 
+@pytest.mark.parametrize("dim,k,n", [(2, 1, 5), (2, 4, 3), (3, 1, 3), (3, 2, 3), (3, 3, 2),
+                                     (3, 4, 2)])
+def test_matrix_free_transpose_equals_assembled(oracle, dim, k, n):
+    # the checker of the GPU transposed applies: the oracle's matrix-free
+    # transpose (NIPG, weights on, reaction, mixed boundary types) equals the
+    # transpose of its assembled blocks, and the operator is not symmetric
+    rng = np.random.default_rng(30 + dim * 10 + k)
+    nc = (n,) * dim
+    ncell = n ** dim
+    P = oracle.Problem(dim, k, nc, method=0, weights=1, alpha=3.0,
+                       bctype=[1, -1, -3, 1, -1, 1][:2 * dim],
+                       K=np.exp(rng.standard_normal(ncell)), c=rng.uniform(0.5, 2.0, ncell))
+    x = rng.uniform(-1, 1, P.ndof)
+    A = P.assemble_jacobian()
+    yt = P.jacobian_apply_transpose(x)
+    assert np.max(np.abs(yt - P.blocks_apply(A, x, transpose=True))) <= 1e-13 * np.max(np.abs(yt))
+    y = P.jacobian_apply(x)
+    assert np.max(np.abs(yt - y)) > 1e-6 * np.max(np.abs(y))
+
+
 @pytest.mark.parametrize("dim,k,ns", [
     (2, 1, (4, 8, 16)), (2, 2, (4, 8, 16)), (2, 3, (2, 4, 8)), (2, 4, (2, 4, 8)),
     (3, 1, (3, 6, 12)), (3, 2, (2, 4, 8)), (3, 3, (2, 4, 6)), (3, 4, (2, 3, 4))])
