@@ -12,6 +12,14 @@
 //                                        (dune/pdelab/backend/istl/matrixfree/backends.hh:62-143)
 //   pdg::StationaryLinearProblemSolver   apply, result
 //                                        (dune/pdelab/stationary/linearproblem.hh:59-338)
+//   pdg::NewtonMethod                    apply, result, set* of the method, its
+//                                        DefaultTerminate and line search
+//                                        (dune/pdelab/solver/newton.hh:63-669,
+//                                        terminate.hh:20-76, linesearch.hh:71-209)
+//   pdg::OneStepMethod                   apply(time, dt, xold, xnew), setMethod, result
+//                                        (dune/pdelab/instationary/implicitonestep.hh:56-275)
+//   pdg::Adjoint                         adjoint solve and gradients (no reference
+//                                        counterpart)
 //
 // Vectors are any contiguous double container with data()/size() (for a
 // PDELab ISTL BlockVector of FieldVector<double,n>, pass
@@ -95,9 +103,58 @@ class GridOperator {
   void jacobian_apply(span z, span y) const {
     check(pdg_jacobian_apply(ctx_, z.data(), y.data()));
   }
+  // y += J(x) z  (gridoperator.hh:200-205; sets x as the linearization point)
+  void jacobian_apply(span x, span z, span y) const {
+    check(pdg_jacobian_apply_nonlinear(ctx_, x.data(), z.data(), y.data()));
+  }
+  // y += J^T z  (the adjoint's operator; no reference counterpart)
+  void jacobian_apply_transpose(span z, span y) const {
+    check(pdg_jacobian_apply_transpose(ctx_, z.data(), y.data()));
+  }
+  // y = M x with the DG mass matrix (the L2 temporal operator, localoperator/l2.hh)
+  void mass_apply(span x, span y) const { check(pdg_mass_apply(ctx_, x.data(), y.data())); }
+
+  // GridOperator::jacobian(x, A) (gridoperator.hh:184-189) into an ISTL-shaped
+  // BCRS matrix: block rows in cell order, column blocks ascending, each
+  // block block x block, row-major
+  struct BCRSMatrix {
+    long rows = 0;
+    int block = 0;
+    std::vector<long> rowptr, colind;
+    std::vector<double> values;
+  };
+  void jacobian(BCRSMatrix &A) const {
+    long nc = 0, nnz = 0;
+    int nb = 0;
+    check(pdg_sizes(ctx_, &nc, &nb, nullptr, nullptr, nullptr));
+    check(pdg_jacobian_assemble(ctx_));
+    check(pdg_jacobian_pattern(ctx_, &nnz));
+    A.rows = nc;
+    A.block = nb;
+    A.rowptr.assign(nc + 1, 0);
+    A.colind.assign(nnz, 0);
+    A.values.assign((std::size_t)nnz * nb * nb, 0.0);
+    check(pdg_jacobian_export(ctx_, A.rowptr.data(), A.colind.data(), A.values.data()));
+  }
 
   void setPermeability(const std::vector<double> &K, bool is_log = false) {
     check(pdg_set_permeability(ctx_, K.data(), is_log ? 1 : 0));
+  }
+  // c per cell (an empty vector: c = 0)
+  void setReaction(const std::vector<double> &c) {
+    check(pdg_set_reaction(ctx_, c.empty() ? nullptr : c.data()));
+  }
+  // b(x) as Fourier modes [n][7] = kx ky kz phase cx cy cz (empty: b = 0)
+  void setVelocityModes(const std::vector<double> &modes) {
+    check(pdg_set_velocity_modes(ctx_, (int)(modes.size() / 7),
+                                 modes.empty() ? nullptr : modes.data()));
+  }
+  // the nonlinear volume term q(u) = sum_m coef[m] u^m of
+  // NonlinearConvectionDiffusionDG (coef.size() - 1 = degree, 1..4; empty
+  // removes it)
+  void setNonlinearity(const std::vector<double> &coef) {
+    check(pdg_set_nonlinearity(ctx_, coef.empty() ? 0 : (int)coef.size() - 1,
+                               coef.empty() ? nullptr : coef.data()));
   }
   // A(cell, x) beyond K I: a dim x dim tensor per cell (row-major), or per
   // quadrature point when the parameter class's permeabilityIsConstantPerCell()
@@ -134,6 +191,10 @@ class OnTheFlyOperator {
   void applyscaleadd(double alpha, span x, span y) const {
     check(pdg_applyscaleadd(go_.handle(), alpha, x.data(), y.data()));
   }
+  // backends.hh:129-135
+  void setLinearizationPoint(span x) {
+    check(pdg_set_linearization_point(go_.handle(), x.data()));
+  }
 
  private:
   const GridOperator &go_;
@@ -153,6 +214,11 @@ class GridOperatorPreconditioner {
   }
   void apply(span v, span d) { check(pdg_prec_apply(go_.handle(), d.data(), v.data())); }
   void post(span) {}
+  // gridoperatorpreconditioner.hh:38-42: the blocks are rebuilt at the new point
+  void setLinearizationPoint(span x) {
+    check(pdg_set_linearization_point(go_.handle(), x.data()));
+    ready_ = false;
+  }
 
  private:
   const GridOperator &go_;
@@ -216,6 +282,97 @@ class StationaryLinearProblemSolver {
   ISTLBackend_SEQ_MatrixFree_Base &ls_;
   span x_;
   double reduction_, min_defect_;
+  pdg_solver_result res_{};
+};
+
+// NewtonMethod<GridOperator, LinearSolver>: apply(u) solves R(u) = 0 from the
+// initial guess in u.  Reaching the iteration limit throws, as the reference's
+// DefaultTerminate does (TerminateError); a failed line search throws with
+// PDG_ELINESEARCH (LineSearchError).
+class NewtonMethod {
+ public:
+  NewtonMethod(const GridOperator &go, ISTLBackend_SEQ_MatrixFree_Base &ls) : go_(go), ls_(ls) {
+    pdg_default_newton_options(&opt_);
+  }
+  void apply(span u) {
+    check(pdg_newton_solve(go_.handle(), &opt_, &ls_.options(), u.data(), &res_));
+  }
+  const pdg_newton_result &result() const { return res_; }
+
+  void setVerbosityLevel(unsigned v) { opt_.verbose = (int)v; }
+  void setReduction(double r) { opt_.reduction = r; }
+  void setAbsoluteLimit(double a) { opt_.absolute_limit = a; }
+  void setMinLinearReduction(double r) { opt_.min_linear_reduction = r; }
+  void setFixedLinearReduction(bool b) { opt_.fixed_linear_reduction = b ? 1 : 0; }
+  // DefaultTerminate (terminate.hh:20-76)
+  void setMaxIterations(unsigned n) { opt_.max_iterations = (int)n; }
+  void setForceIteration(bool b) { opt_.force_iteration = b ? 1 : 0; }
+  // line search: Hackbusch-Reusken (true) or full Newton steps (false),
+  // HackbuschReuskenLineSearch's settings (linesearch.hh:71-209)
+  void setLineSearch(bool hackbusch_reusken) { opt_.line_search = hackbusch_reusken ? 1 : 0; }
+  void setLineSearchMaxIterations(unsigned n) { opt_.line_search_max_iterations = (int)n; }
+  void setLineSearchDampingFactor(double d) { opt_.line_search_damping = d; }
+  void setLineSearchAcceptBest(bool b) { opt_.line_search_accept_best = b ? 1 : 0; }
+  pdg_newton_options &options() { return opt_; }
+
+ private:
+  const GridOperator &go_;
+  ISTLBackend_SEQ_MatrixFree_Base &ls_;
+  pdg_newton_options opt_;
+  pdg_newton_result res_{};
+};
+
+// OneStepMethod with one of the TimeSteppingParameterInterface methods
+// (PDG_ONESTEP_*, instationary/onestepparameter.hh); the spatial data are
+// time-independent, so `time` only labels the step
+class OneStepMethod {
+ public:
+  OneStepMethod(const GridOperator &go, ISTLBackend_SEQ_MatrixFree_Base &ls, int method,
+                double theta = 1.0)
+      : go_(go), ls_(ls) {
+    setMethod(method, theta);
+  }
+  void setMethod(int method, double theta = 1.0) {
+    check(pdg_onestep_table(method, theta, &stages_, A_, B_, D_));
+  }
+  // implicitonestep.hh:144: xnew holds the initial guess on entry; returns dt
+  double apply(double /*time*/, double dt, span xold, span xnew) {
+    check(pdg_onestep_apply(go_.handle(), stages_, A_, B_, D_, dt, &ls_.options(), xold.data(),
+                            xnew.data(), &res_));
+    return dt;
+  }
+  const pdg_onestep_result &result() const { return res_; }
+
+ private:
+  const GridOperator &go_;
+  ISTLBackend_SEQ_MatrixFree_Base &ls_;
+  int stages_ = 0;
+  double A_[20] = {}, B_[20] = {}, D_[5] = {};
+  pdg_onestep_result res_{};
+};
+
+// Adjoint solve J^T lambda = rhs and the fused gradients dJ/dlog K and
+// dJ/d(per-cell source) from the primal u and the adjoint lambda (no
+// reference counterpart).  Non-convergence is reported through result().
+class Adjoint {
+ public:
+  Adjoint(const GridOperator &go, ISTLBackend_SEQ_MatrixFree_Base &ls) : go_(go), ls_(ls) {}
+  void solve(span rhs, span lambda, double reduction) {
+    pdg_solver_options o = ls_.options();
+    o.reduction = reduction;
+    check(pdg_adjoint_solve(go_.handle(), &o, rhs.data(), lambda.data(), &res_), true);
+  }
+  void gradLogK(span u, span lambda, span g) const {
+    check(pdg_grad_logK(go_.handle(), u.data(), lambda.data(), g.data()));
+  }
+  void gradSource(span lambda, span g) const {
+    check(pdg_grad_source(go_.handle(), lambda.data(), g.data()));
+  }
+  const pdg_solver_result &result() const { return res_; }
+
+ private:
+  const GridOperator &go_;
+  ISTLBackend_SEQ_MatrixFree_Base &ls_;
   pdg_solver_result res_{};
 };
 
