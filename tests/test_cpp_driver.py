@@ -117,3 +117,38 @@ def test_cpp_adapters_compile_and_link(tmp_path):
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert exe.exists()
+
+
+EXE2 = os.path.join(PKG, "_build", "adjoint_newton_onestep")
+
+
+def _build_adapters_driver():
+    import __graft_entry__
+    __graft_entry__.build()
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I",
+           os.path.join(ROOT, "include"), os.path.join(PKG, "examples", "adjoint_newton_onestep.cc"),
+           "-L", os.path.join(PKG, "_build"), "-lpdg",
+           "-Wl,-rpath," + os.path.join(PKG, "_build"), "-o", EXE2]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_cpp_adjoint_newton_onestep_builds():
+    _build_adapters_driver()
+    assert os.path.exists(EXE2)
+
+
+@pytest.mark.gpu
+def test_cpp_adjoint_newton_onestep():
+    # the adjoint, BCRS export, Newton and one-step adapters from C++ on the
+    # GPU, each against its own identity (central differences, A x = J x,
+    # R(u) = 0, the implicit Euler equation)
+    _build_adapters_driver()
+    r = subprocess.run([EXE2], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["adjoint_fd_rel_logK"] < 1e-5 and out["adjoint_fd_rel_source"] < 1e-5
+    assert out["bcrs_rel"] < 1e-12 and out["bcrs_transpose_rel"] < 1e-12
+    assert out["nipg_asymmetry"] > 1e-6
+    assert out["newton_converged"] == 1 and out["newton_residual_rel"] < 1e-9
+    assert out["implicit_euler_rel"] < 1e-10
