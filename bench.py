@@ -446,6 +446,10 @@ def run_gb300(args, world, rank, local):
     float_pair = None
     if not f32 and args.step == "apply" and WORKLOAD["dim"] == 3:
         float_pair = float_pair_metrics(pdg, torch, go, op, xs, ys, stream, args, npairs)
+    # the transposed apply (the operator of the adjoint solves)
+    transpose = None
+    if not f32 and args.step == "apply":
+        transpose = transpose_metrics(torch, go, xs, ys, stream, args, npairs)
 
     # end to end through the public API with host (pinned) buffers
     xh = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
@@ -553,6 +557,8 @@ def run_gb300(args, world, rank, local):
                 float_pair["fp64_equivalent_tflops"] / peaks["fp64"])
         float_pair["traffic"] = profile_traffic(wname.replace("_apply", "_float_pair_apply"))
         line["f64_float_pair"] = float_pair
+    if transpose:
+        line["transpose_apply"] = transpose
     line.update(extras)
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -588,6 +594,35 @@ def float_pair_metrics(pdg, torch, go, op, xs, ys, stream, args, npairs):
     return {"mode": "float pairs (hi + lo floats, 48 bits) on the FP32 pipe; not the headline",
             "ms_per_apply": ms, "gdofs": ndof / (ms * 1e-3) / 1e9,
             "rel_diff_vs_native_f64": float((yfp - ref).abs().max() / ref.abs().max())}
+
+
+def transpose_metrics(torch, go, xs, ys, stream, args, npairs):
+    """The transposed FP64 apply y += J^T x over the same rotating buffers and
+    step count (CUDA events), and the transpose identity <J^T x, w> = <x, J w>
+    at full size, relative to |J^T x| |w|."""
+    ndof = go.ndof
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            go.jacobian_apply_transpose(xs[i % npairs], ys[i % npairs])
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(args.steps):
+            go.jacobian_apply_transpose(xs[i % npairs], ys[i % npairs])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        x, w = xs[0], xs[1]
+        jtx = torch.zeros_like(x)
+        jw = torch.zeros_like(x)
+        go.jacobian_apply_transpose(x, jtx)
+        go.jacobian_apply(w, jw)
+        torch.cuda.synchronize()
+    a, b = float(torch.dot(jtx, w)), float(torch.dot(x, jw))
+    return {"form": "y += J^T x (accumulating), the adjoint solves' operator",
+            "ms_per_apply": ms, "gdofs": ndof / (ms * 1e-3) / 1e9,
+            "identity_rel": abs(a - b) / float(jtx.norm() * w.norm())}
 
 
 def _event_ms(torch, stream, fn, reps=5):
