@@ -61,14 +61,58 @@ __device__ __forceinline__ void reduce_tail(const RedCtx &rc, double s0, double 
   }
 }
 
+// 16-byte vector of T and the sum of its lane products, in lane order
+template <typename T> struct Vec16;
+template <> struct Vec16<double> {
+  using type = double2;
+  static __device__ __forceinline__ double dot(double s, double2 x, double2 y) {
+    s = fma(x.x, y.x, s);
+    return fma(x.y, y.y, s);
+  }
+};
+template <> struct Vec16<float> {
+  using type = float4;
+  static __device__ __forceinline__ float dot(float s, float4 x, float4 y) {
+    s = fmaf(x.x, y.x, s);
+    s = fmaf(x.y, y.y, s);
+    s = fmaf(x.z, y.z, s);
+    return fmaf(x.w, y.w, s);
+  }
+};
+
+// <a, b> (and <c, d> when c is given).  With vec set (every pointer 16-byte
+// aligned) the first n - n % W elements are read as 16-byte vectors, W per
+// load, the rest one by one.  The order of the sums is fixed by n, the grid
+// and vec, so results repeat bit for bit.
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads)
     k_dot(long n, const T *__restrict__ a, const T *__restrict__ b, const T *__restrict__ c,
-          const T *__restrict__ d, RedCtx rc, int fin, int slot0, int slot1, int respect) {
+          const T *__restrict__ d, RedCtx rc, int fin, int slot0, int slot1, int respect,
+          int vec) {
   if (respect && rc.flags[F_STATE]) return;
+  using V = typename Vec16<T>::type;
+  constexpr int W = 16 / sizeof(T);
   T s0 = T(0), s1 = T(0);
+  const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long stride = (long)gridDim.x * blockDim.x;
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+  long i0 = 0;
+  if (vec) {
+    const long nv = n / W;
+    const V *av = reinterpret_cast<const V *>(a), *bv = reinterpret_cast<const V *>(b);
+    if (c) {
+      const V *cv = reinterpret_cast<const V *>(c), *dv = reinterpret_cast<const V *>(d);
+#pragma unroll 4
+      for (long j = tid; j < nv; j += stride) {
+        s0 = Vec16<T>::dot(s0, av[j], bv[j]);
+        s1 = Vec16<T>::dot(s1, cv[j], dv[j]);
+      }
+    } else {
+#pragma unroll 4
+      for (long j = tid; j < nv; j += stride) s0 = Vec16<T>::dot(s0, av[j], bv[j]);
+    }
+    i0 = nv * W;
+  }
+  for (long i = i0 + tid; i < n; i += stride) {
     s0 += a[i] * b[i];
     if (c) s1 += c[i] * d[i];
   }
@@ -82,22 +126,28 @@ static unsigned red_grid(long n) {
   return (unsigned)g;
 }
 
+static int aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+template <typename T>
+static int launch_dot(pdg_context *ctx, const RedCtx &rc, long n, const T *a, const T *b,
+                      const T *c, const T *d, int fin, int slot0, int slot1, bool respect_flag) {
+  const int vec = aligned16(a) && aligned16(b) && (!c || (aligned16(c) && aligned16(d)));
+  k_dot<T><<<red_grid(n), kRedThreads, 0, ctx->stream>>>(n, a, b, c, d, rc, fin, slot0, slot1,
+                                                          respect_flag, vec);
+  PDG_CUDA_TRY(cudaGetLastError());
+  return PDG_OK;
+}
+
 int red_dot(pdg_context *ctx, const RedCtx &rc, long n, const double *a, const double *b,
             const double *c, const double *d, int fin, int slot0, int slot1,
             bool respect_flag) {
-  k_dot<double><<<red_grid(n), kRedThreads, 0, ctx->stream>>>(n, a, b, c, d, rc, fin, slot0,
-                                                               slot1, respect_flag);
-  PDG_CUDA_TRY(cudaGetLastError());
-  return PDG_OK;
+  return launch_dot<double>(ctx, rc, n, a, b, c, d, fin, slot0, slot1, respect_flag);
 }
 
 int red_dot_f32(pdg_context *ctx, const RedCtx &rc, long n, const float *a, const float *b,
                 const float *c, const float *d, int fin, int slot0, int slot1,
                 bool respect_flag) {
-  k_dot<float><<<red_grid(n), kRedThreads, 0, ctx->stream>>>(n, a, b, c, d, rc, fin, slot0,
-                                                              slot1, respect_flag);
-  PDG_CUDA_TRY(cudaGetLastError());
-  return PDG_OK;
+  return launch_dot<float>(ctx, rc, n, a, b, c, d, fin, slot0, slot1, respect_flag);
 }
 
 // ---- fused Krylov updates ------------------------------------------------
