@@ -49,7 +49,9 @@ inline void check(int st, bool allow_not_converged = false) {
   throw Error(st, std::string("pdg: ") + pdg_last_error());
 }
 
-// non-owning view of contiguous doubles (host or device memory)
+// non-owning view of contiguous doubles (host or device memory): span for
+// vectors a call writes, cspan for vectors it only reads (PDELab's
+// `const Domain&` arguments)
 struct span {
   double *p;
   std::size_t n;
@@ -57,6 +59,16 @@ struct span {
   template <class V>
   span(V &v) : p(v.data()), n(v.size()) {}
   double *data() const { return p; }
+  std::size_t size() const { return n; }
+};
+
+struct cspan {
+  const double *p;
+  std::size_t n;
+  cspan(const double *ptr, std::size_t size) : p(ptr), n(size) {}
+  template <class V>
+  cspan(const V &v) : p(v.data()), n(v.size()) {}
+  const double *data() const { return p; }
   std::size_t size() const { return n; }
 };
 
@@ -98,21 +110,21 @@ class GridOperator {
   }
 
   // r += R(x)
-  void residual(span x, span r) const { check(pdg_residual(ctx_, x.data(), r.data())); }
+  void residual(cspan x, span r) const { check(pdg_residual(ctx_, x.data(), r.data())); }
   // y += J z  (linear problem: the linearization point is not needed)
-  void jacobian_apply(span z, span y) const {
+  void jacobian_apply(cspan z, span y) const {
     check(pdg_jacobian_apply(ctx_, z.data(), y.data()));
   }
   // y += J(x) z  (gridoperator.hh:200-205; sets x as the linearization point)
-  void jacobian_apply(span x, span z, span y) const {
+  void jacobian_apply(cspan x, cspan z, span y) const {
     check(pdg_jacobian_apply_nonlinear(ctx_, x.data(), z.data(), y.data()));
   }
   // y += J^T z  (the adjoint's operator; no reference counterpart)
-  void jacobian_apply_transpose(span z, span y) const {
+  void jacobian_apply_transpose(cspan z, span y) const {
     check(pdg_jacobian_apply_transpose(ctx_, z.data(), y.data()));
   }
   // y = M x with the DG mass matrix (the L2 temporal operator, localoperator/l2.hh)
-  void mass_apply(span x, span y) const { check(pdg_mass_apply(ctx_, x.data(), y.data())); }
+  void mass_apply(cspan x, span y) const { check(pdg_mass_apply(ctx_, x.data(), y.data())); }
 
   // GridOperator::jacobian(x, A) (gridoperator.hh:184-189) into an ISTL-shaped
   // BCRS matrix: block rows in cell order, column blocks ascending, each
@@ -187,12 +199,12 @@ class GridOperator {
 class OnTheFlyOperator {
  public:
   explicit OnTheFlyOperator(const GridOperator &go) : go_(go) {}
-  void apply(span x, span y) const { check(pdg_apply(go_.handle(), x.data(), y.data())); }
-  void applyscaleadd(double alpha, span x, span y) const {
+  void apply(cspan x, span y) const { check(pdg_apply(go_.handle(), x.data(), y.data())); }
+  void applyscaleadd(double alpha, cspan x, span y) const {
     check(pdg_applyscaleadd(go_.handle(), alpha, x.data(), y.data()));
   }
   // backends.hh:129-135
-  void setLinearizationPoint(span x) {
+  void setLinearizationPoint(cspan x) {
     check(pdg_set_linearization_point(go_.handle(), x.data()));
   }
 
@@ -212,10 +224,10 @@ class GridOperatorPreconditioner {
       ready_ = true;
     }
   }
-  void apply(span v, span d) { check(pdg_prec_apply(go_.handle(), d.data(), v.data())); }
+  void apply(span v, cspan d) { check(pdg_prec_apply(go_.handle(), d.data(), v.data())); }
   void post(span) {}
   // gridoperatorpreconditioner.hh:38-42: the blocks are rebuilt at the new point
-  void setLinearizationPoint(span x) {
+  void setLinearizationPoint(cspan x) {
     check(pdg_set_linearization_point(go_.handle(), x.data()));
     ready_ = false;
   }
@@ -249,7 +261,7 @@ class ISTLBackend_SEQ_MatrixFree_Base {
     opt_.reduction = reduction;
     check(pdg_krylov_solve(go_.handle(), &opt_, z.data(), r.data(), &res_), true);
   }
-  double norm(span v) const {
+  double norm(cspan v) const {
     double out = 0.0;
     check(pdg_norm(go_.handle(), v.data(), &out));
     return out;
@@ -336,7 +348,7 @@ class OneStepMethod {
     check(pdg_onestep_table(method, theta, &stages_, A_, B_, D_));
   }
   // implicitonestep.hh:144: xnew holds the initial guess on entry; returns dt
-  double apply(double /*time*/, double dt, span xold, span xnew) {
+  double apply(double /*time*/, double dt, cspan xold, span xnew) {
     check(pdg_onestep_apply(go_.handle(), stages_, A_, B_, D_, dt, &ls_.options(), xold.data(),
                             xnew.data(), &res_));
     return dt;
@@ -357,15 +369,15 @@ class OneStepMethod {
 class Adjoint {
  public:
   Adjoint(const GridOperator &go, ISTLBackend_SEQ_MatrixFree_Base &ls) : go_(go), ls_(ls) {}
-  void solve(span rhs, span lambda, double reduction) {
+  void solve(cspan rhs, span lambda, double reduction) {
     pdg_solver_options o = ls_.options();
     o.reduction = reduction;
     check(pdg_adjoint_solve(go_.handle(), &o, rhs.data(), lambda.data(), &res_), true);
   }
-  void gradLogK(span u, span lambda, span g) const {
+  void gradLogK(cspan u, cspan lambda, span g) const {
     check(pdg_grad_logK(go_.handle(), u.data(), lambda.data(), g.data()));
   }
-  void gradSource(span lambda, span g) const {
+  void gradSource(cspan lambda, span g) const {
     check(pdg_grad_source(go_.handle(), lambda.data(), g.data()));
   }
   const pdg_solver_result &result() const { return res_; }

@@ -53,8 +53,9 @@ int drive(int n) {
   go.setNonlinearity({0.0, 0.0, 1.0});
   go.setNonlinearity({});
   go.setF64Arithmetic(PDG_F64_NATIVE);
-  go.residual(x, y);
-  go.jacobian_apply(x, y);
+  const std::vector<double> &cx = x;   // read-only inputs bind to const vectors
+  go.residual(cx, y);
+  go.jacobian_apply(cx, y);
   go.jacobian_apply(x, z, y);
   go.jacobian_apply_transpose(x, y);
   go.mass_apply(x, y);
@@ -94,6 +95,7 @@ int drive(int n) {
   nrm += osm.apply(0.0, 0.1, x, z) + osm.result().stages;
   pdg::Adjoint adj(go, ls);
   adj.solve(y, z, 1e-10);
+  adj.gradLogK(cx, cx, g);
   adj.gradLogK(x, z, g);
   adj.gradSource(z, g);
   return (int)(nrm + adj.result().iterations + A.rows);
