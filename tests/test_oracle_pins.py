@@ -206,6 +206,26 @@ def test_block_sor_and_iterative_jacobi_oracle(oracle):
     assert its.min() >= 1 and its.max() <= 100
 
 
+@pytest.mark.parametrize("dim,k,nc", [(2, 2, (4, 3)), (3, 1, (3, 3, 2)), (3, 3, (2, 2, 2))])
+def test_nonlinear_jacobian_central_differences(oracle, dim, k, nc):
+    # the checker of the GPU jacobian_apply(x, z, y): the oracle's Jacobian of
+    # the operator with the volume term int q(u) psi (NIPG, reaction) against
+    # central differences of its own residual
+    rng = np.random.default_rng(70 + dim * 10 + k)
+    ncell = int(np.prod(nc))
+    P = oracle.Problem(dim, k, nc, alpha=3.0, method=0, K=np.exp(rng.standard_normal(ncell)),
+                       c=rng.uniform(0.5, 1.5, ncell))
+    P.set_nonlinearity([0.3, -0.5, 2.0, 1.0])
+    x = rng.uniform(-1, 1, P.ndof)
+    z = rng.uniform(-1, 1, P.ndof)
+    P.set_linearization_point(x)
+    jz = P.jacobian_apply(z)
+    h = 1e-5
+    fd = (P.residual(x + h * z) - P.residual(x - h * z)) / (2 * h)
+    assert np.max(np.abs(fd - jz)) <= 1e-7 * np.max(np.abs(jz))
+    P.set_linearization_point(None)
+
+
 def test_nonlinear_reference_problem_oracle(oracle):
     """matrix_free_nonlinear.cc:386-405: Newton on q(u) = 2 u^2, g = |x|^2
     (2D Q1 16^2, SIPG, weightsOn, alpha 3) reaches L2 error^2 < 1e-6; the
