@@ -206,6 +206,27 @@ def test_block_sor_and_iterative_jacobi_oracle(oracle):
     assert its.min() >= 1 and its.max() <= 100
 
 
+@pytest.mark.parametrize("dim,k,method", [(2, 1, 1), (2, 3, 0), (3, 2, 2), (3, 1, 1)])
+def test_residual_is_affine_with_jacobian(oracle, dim, k, method):
+    # R(x) - R(0) = J x for the linear operator with source, Dirichlet, Neumann
+    # and outflow data on mixed sides: the residual's data terms (lambda_*)
+    # and the Jacobian's forms (alpha_* / jacobian_apply_*) are consistent
+    rng = np.random.default_rng(90 + dim * 10 + k)
+    nc = (3,) * dim
+    ncell = 3 ** dim
+    P = oracle.Problem(dim, k, nc, alpha=3.0, method=method, bctype=[1, -1, -2, 1, -1, 1][:2 * dim],
+                       K=np.exp(rng.standard_normal(ncell)), c=rng.uniform(0.5, 1.5, ncell))
+    nbp = P.nbpts_total()
+    P.set(fq=rng.standard_normal(ncell * (k + 1) ** dim), gq=rng.standard_normal(nbp),
+          jq=rng.standard_normal(nbp), oq=rng.standard_normal(nbp))
+    x = rng.uniform(-1, 1, P.ndof)
+    r0 = P.residual(np.zeros(P.ndof))
+    assert np.max(np.abs(r0)) > 0.1
+    lhs = P.residual(x) - r0
+    jx = P.jacobian_apply(x)
+    assert np.max(np.abs(lhs - jx)) <= 1e-13 * np.max(np.abs(jx))
+
+
 @pytest.mark.parametrize("dim,k,nc", [(2, 2, (4, 3)), (3, 1, (3, 3, 2)), (3, 3, (2, 2, 2))])
 def test_nonlinear_jacobian_central_differences(oracle, dim, k, nc):
     # the checker of the GPU jacobian_apply(x, z, y): the oracle's Jacobian of
