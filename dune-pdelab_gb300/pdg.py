@@ -669,8 +669,9 @@ def onestep_table(method, theta=1.0):
 
 class OneStepMethod:
     """OneStepMethod(method, igos, pdesolver) (instationary/implicitonestep.hh):
-    apply(time, dt, xold, xnew) advances one step; `method` is a scheme id
-    (IMPLICIT_EULER, ALEXANDER2, ...) or explicit (A, B, D) tables."""
+    apply(time, dt, xold, xnew) advances one step and returns the step size
+    taken (implicitonestep.hh:144); `method` is a scheme id (IMPLICIT_EULER,
+    ALEXANDER2, ...) or explicit (A, B, D) tables."""
 
     def __init__(self, method, go: GridOperator, ls: "ISTLBackend_SEQ_MatrixFree_Base",
                  theta=1.0):
@@ -688,7 +689,7 @@ class OneStepMethod:
         _check(load().pdg_onestep_apply(self.go.handle, s, A.ctypes.data, B.ctypes.data,
                                         D.ctypes.data, float(dt), C.byref(self.ls.opts),
                                         _ptr(xold), _ptr(xnew), C.byref(self.res)))
-        return time + dt
+        return dt
 
     def result(self):
         return self.res

@@ -64,7 +64,7 @@ def test_onestep_matches_oracle(pdg, oracle, name):
     t = 0.0
     for _ in range(3):
         xn = np.zeros(go.ndof)
-        t = osm.apply(t, dt, x, xn)
+        t += osm.apply(t, dt, x, xn)
         x = xn
         xo, _ = P.onestep(A, B, dt, xo, oracle.prec_config(2), reduction=1e-13)
     assert _rel(x, xo) <= 1e-9
